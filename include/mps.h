@@ -1,0 +1,245 @@
+/*
+ * mps.h - C ABI of the GB300-native MPS (Moving Particle Semi-implicit) time step.
+ *
+ * This is the drop-in boundary for OpenMps's compute class
+ * `Computer<POSITION_WALL, POSITION_WALL_PRE>` (src/OpenMps/Computer.hpp:434-1790).
+ * Particle arrays go in, one time step is advanced on one GPU, and the same
+ * fields (Type, x, z, u, w, p, n) come back in the caller's original order.
+ *
+ * Every entry point returns an int status (MPS_OK == 0).  Nothing throws across
+ * this boundary; the message of the last failure is kept per handle
+ * (mps_last_error).  One handle owns one CUDA stream and all device buffers of
+ * one scene; handles share no global state, so separate host threads may drive
+ * separate handles.  A handle is not re-entrant (like Computer::ForwardTime).
+ *
+ * Arrays passed with a `_host` meaning are plain host memory of `n` elements;
+ * the library copies them (the caller keeps ownership), as AddParticles copies
+ * the particles into Computer::particles (Computer.hpp:1754-1777).
+ */
+#ifndef OPENMPS_GB300_MPS_H
+#define OPENMPS_GB300_MPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define MPS_OK 0
+#define MPS_ERR_INVALID_ARGUMENT 1
+#define MPS_ERR_CUDA 2
+#define MPS_ERR_OUT_OF_MEMORY 3
+/* Grid::Exception "Too many particle in a block" (src/OpenMps/Grid.hpp:314-318) */
+#define MPS_ERR_CELL_OVERFLOW 4
+/* Computer::Exception "Conjugate Gradient method couldn't solve ..." (Computer.hpp:1424-1428) */
+#define MPS_ERR_CG_NOT_CONVERGED 5
+#define MPS_ERR_NOT_SUPPORTED 6
+#define MPS_ERR_STATE 7
+#define MPS_ERR_NONFINITE 8
+/* a bounded device-side wait ran out of iterations (never a hang) */
+#define MPS_ERR_TIMEOUT 9
+/* a device-side bounds check fired (index recorded, access skipped) */
+#define MPS_ERR_DEVICE_CHECK 10
+
+/* ------------------------------------------------- particle types (Particle.hpp:16-29) */
+#define MPS_TYPE_FLUID 0    /* Particle::Type::IncompressibleNewton */
+#define MPS_TYPE_WALL 1     /* Particle::Type::Wall */
+#define MPS_TYPE_DUMMY 2    /* Particle::Type::Dummy */
+#define MPS_TYPE_DISABLED 3 /* Particle::Type::Disabled */
+
+/* ------------------------------------- method flags: runtime form of defines.hpp:9-56 */
+#define MPS_FLAG_HS 0x01u  /* MPS_HS   higher-order source term        (defines.hpp:31) */
+#define MPS_FLAG_HL 0x02u  /* MPS_HL   higher-order Laplacian          (defines.hpp:36) */
+#define MPS_FLAG_ECS 0x04u /* MPS_ECS  error-compensating source       (defines.hpp:41) */
+#define MPS_FLAG_DS 0x08u  /* MPS_DS   dynamic stabilisation           (defines.hpp:51) */
+#define MPS_FLAG_SPP 0x10u /* MPS_SPP  space-potential (surface) particle (defines.hpp:56) */
+/* PRESSURE_GRADIENT_MIDPOINT (defines.hpp:21) is always on: the other branch does
+ * not compile in the reference (Computer.hpp:1522-1537). */
+/* The stock build of the reference (defines.hpp as shipped). */
+#define MPS_PRESET_REFERENCE (MPS_FLAG_HS | MPS_FLAG_HL | MPS_FLAG_ECS | MPS_FLAG_DS | MPS_FLAG_SPP)
+/* Plain MPS: standard source/Laplacian, free-surface flag n/n0 < surface_ratio. */
+#define MPS_PRESET_PLAIN 0u
+
+/* ----------------------------------------------------------- PPE solver */
+#define MPS_SOLVER_CG64 0   /* FP64 CG, the reference algorithm (Computer.hpp:1359-1429) */
+#define MPS_SOLVER_MIXED 1  /* FP32 inner CG + FP64 true residual / iterative refinement */
+#define MPS_SOLVER_LEARNED 2 /* MIXED with the learned initial guess + preconditioner scale */
+
+/* CG stopping rule */
+#define MPS_CRIT_INITIAL_RESIDUAL 0 /* reference: r_k.r_k < eps^2 r_0.r_0 (Computer.hpp:1386, :1408) */
+#define MPS_CRIT_RHS 1              /* |b - A x| <= eps |b| */
+
+/*
+ * Parameters of Environment (src/OpenMps/Environment.hpp:101-128) and
+ * ComputingCondition::Eps (src/OpenMps/ComputingCondition.hpp:13-16), plus the
+ * runtime method flags and solver controls.
+ */
+typedef struct mps_params {
+    double max_dt;        /* Environment(maxDt, ...) */
+    double courant;       /* courant */
+    double g;             /* gravity magnitude, G = (0, -g) (Environment.hpp:149) */
+    double rho;           /* density */
+    double nu;            /* kinematic viscosity */
+    double surface_ratio; /* free-surface threshold beta; used only without MPS_FLAG_SPP */
+    double re_by_l0;      /* r_eByl_0: radius of density, source and gradient */
+    double re_lap_by_l0;  /* Laplacian radius / l0 (viscosity, PPE matrix); <= 0 means re_by_l0.
+                             A second radius is an extension: the reference has one R_e. */
+    double l0;            /* l_0 */
+    double min_x, min_z, max_x, max_z; /* computational domain */
+    double eps;           /* CG allowable residual (ComputingCondition::Eps) */
+    uint32_t flags;       /* MPS_FLAG_* */
+    int32_t solver;       /* MPS_SOLVER_* */
+    int32_t criterion;    /* MPS_CRIT_* */
+    int32_t max_cg_iters; /* <= 0: number of unknowns, as the reference (Computer.hpp:1392) */
+    double inner_tol;     /* MIXED: relative residual reduction of one FP32 inner solve */
+    int32_t max_refinements; /* MIXED: maximum FP64 refinement passes */
+    int32_t reserved0;
+    double reserved[6];
+} mps_params;
+
+/* Derived constants of Environment (Environment.hpp:129-216) and Grid (Grid.hpp:137-150). */
+typedef struct mps_environment {
+    double t, dt;
+    double n0, lambda;         /* at r_e (Environment::N0, ::Lambda) */
+    double n0_lap, lambda_lap; /* at the Laplacian radius (equal to the above with one radius) */
+    double max_dt, max_dx, l0, re, re_lap, neighbor_length;
+    double rho, nu, g;
+    double min_x, min_z, max_x, max_z;
+    int64_t grid_nx, grid_nz, grid_max_per_cell;
+} mps_environment;
+
+/* Per-step solver statistics and counters. */
+typedef struct mps_stats {
+    int64_t steps;            /* ForwardTime calls completed */
+    int64_t kernel_launches;  /* cumulative kernels launched by this handle */
+    int64_t neighbor_total;   /* neighbour-list entries of the last search */
+    int64_t ppe_nnz;          /* nonzeros of the last PPE matrix */
+    int32_t cg_iterations;    /* inner iterations of the last solve (all passes) */
+    int32_t cg_refinements;   /* FP64 outer passes of the last solve (1 for CG64) */
+    int32_t disabled;         /* particles of type Disabled after the last search */
+    int32_t fallback;         /* 1 if the last learned solve fell back to plain CG64 */
+    double cg_rr0;            /* r_0.r_0 of the last solve */
+    double cg_rr;             /* final (recursive) r.r of the last solve */
+    double cg_true_relres;    /* |b - A x| / |b| recomputed in FP64 after the last solve */
+    double stage_ms[12];      /* last step, if stage timing is enabled: search, density,
+                                 ecs, explicit, density2, ppe, solve, pressure, gradient,
+                                 ds, other, total */
+} mps_stats;
+
+typedef struct mps_handle mps_handle;
+
+/* ------------------------------------------------------------ lifecycle */
+/* Fills the defaults: the stock reference preset and Sample.xml constants. */
+void mps_default_params(mps_params* prm);
+size_t mps_params_size(void);
+size_t mps_stats_size(void);
+size_t mps_environment_size(void);
+const char* mps_status_string(int status);
+/* Message of the last failure on `h` ("" if none).  Valid until the next call on h. */
+const char* mps_last_error(const mps_handle* h);
+/* Version string of the library build. */
+const char* mps_version(void);
+
+/* CreateComputer(allowableResidual, env, posWall, posWallPre) (Computer.hpp:1800-1815)
+ * and the Environment constructor (Environment.hpp:101-216). Selects CUDA device
+ * `device` (the caller's current device if < 0). */
+int mps_create(const mps_params* prm, int device, mps_handle** out);
+int mps_destroy(mps_handle* h);
+
+/* AddParticles(std::vector<Particle>&&) (Computer.hpp:1754-1777): appends particles.
+ * The wall target of each added particle is its position here, as the reference
+ * driver's static-wall callback returns the initial position (Main.cpp:303-318). */
+int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const double* x,
+                      const double* z, const double* u, const double* w, const double* p,
+                      const double* nd);
+int64_t mps_particle_count(const mps_handle* h);
+
+/* Particles() (Computer.hpp:1780-1783): copies the state to host arrays (any may be NULL). */
+int mps_get_particles(mps_handle* h, int32_t* type, double* x, double* z, double* u, double* w,
+                      double* p, double* nd);
+/* Overwrites the state of all particles from host arrays (count unchanged). */
+int mps_set_particles(mps_handle* h, const int32_t* type, const double* x, const double* z,
+                      const double* u, const double* w, const double* p, const double* nd);
+/* Same, with device pointers (stream-ordered on the handle's stream). */
+int mps_get_particles_device(mps_handle* h, int32_t* type, double* x, double* z, double* u,
+                             double* w, double* p, double* nd);
+int mps_set_particles_device(mps_handle* h, const int32_t* type, const double* x,
+                             const double* z, const double* u, const double* w,
+                             const double* p, const double* nd);
+
+/* positionWall(i, t, dt) targets (Computer.hpp:1015): the position every non-fluid
+ * particle takes in the explicit step.  Host arrays of n elements. */
+int mps_set_wall_positions(mps_handle* h, const double* wx, const double* wz);
+
+/* ForwardTime(double dt) (Computer.hpp:1700-1742); dt <= 0 selects ForwardTime()
+ * (Computer.hpp:1745-1751) with the CFL time step of DetermineDt (:759-777). */
+int mps_forward_time(mps_handle* h, double dt);
+/* nsteps calls of mps_forward_time(h, dt). */
+int mps_forward_steps(mps_handle* h, double dt, int32_t nsteps);
+
+/* GetEnvironment() (Computer.hpp:1786-1789). */
+int mps_get_environment(const mps_handle* h, mps_environment* env);
+int mps_get_stats(const mps_handle* h, mps_stats* st);
+/* Solver controls may change between steps. */
+int mps_set_solver(mps_handle* h, int32_t solver, int32_t criterion, double eps);
+/* Enables per-stage CUDA-event timing (stats.stage_ms). */
+int mps_set_stage_timing(mps_handle* h, int32_t enable);
+
+/* ------------------------------------------------- timing on the handle's stream */
+int mps_synchronize(mps_handle* h);
+/* Records CUDA event `slot` (0..15) on the handle's stream. */
+int mps_event_record(mps_handle* h, int32_t slot);
+/* Milliseconds between two recorded events (synchronizes on `end`). */
+int mps_event_elapsed(mps_handle* h, int32_t begin, int32_t end, float* ms);
+/* Writes `bytes` of scratch on the handle's stream (evicts L2 between timed runs). */
+int mps_flush_l2(mps_handle* h, int64_t bytes);
+
+/* ------------------------------------------------------------------------
+ * Stage hooks.  They mirror the reference's friend-class test access to the
+ * private stages of Computer (Computer.hpp:437-460) and run exactly one stage.
+ * ---------------------------------------------------------------------- */
+int mps_stage_search_neighbor(mps_handle* h);        /* SearchNeighbor          :698-756 */
+int mps_stage_density(mps_handle* h);                /* ComputeNeighborDensities :780-833 */
+int mps_stage_error_correction(mps_handle* h);       /* ComputeErrorCorrection  :877-910 */
+int mps_stage_explicit(mps_handle* h);               /* ComputeExplicitForces   :914-1021 */
+int mps_stage_save_x(mps_handle* h);                 /* SaveX                   :1025-1039 */
+int mps_stage_set_ppe(mps_handle* h);                /* SetPressurePoissonEquation :1145-1356 */
+int mps_stage_solve_ppe(mps_handle* h);              /* SolvePressurePoissonEquation :1359-1429 */
+int mps_stage_assign_pressure(mps_handle* h);        /* ComputeImplicitForces   :1076-1097 */
+int mps_stage_pressure_gradient(mps_handle* h);      /* ModifyByPressureGradient :1433-1564 */
+int mps_stage_dynamic_stabilize(mps_handle* h);      /* DynamicStabilize        :1568-1656 */
+/* Sets t and dt as ForwardTime does before its stages (Computer.hpp:1703-1706). */
+int mps_stage_begin_step(mps_handle* h, double dt);
+/* NeighborDensityVariationSpeed(i) for every particle (Computer.hpp:838-872). */
+int mps_stage_density_variation(mps_handle* h, double* speed_host);
+
+/* Neighbour lists of the last search in reference order (Computer.hpp:720-755):
+ * counts[n]; list receives the concatenated rows (capacity entries).  *total gets
+ * the number of entries. */
+int mps_debug_get_neighbors(mps_handle* h, int32_t* counts, int32_t* list, int64_t capacity,
+                            int64_t* total);
+/* PPE system of the last assembly: CSR with ascending columns (uBLAS compressed_matrix
+ * semantics, Computer.hpp:1330-1354), b and x.  Any pointer may be NULL. */
+int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val, double* b,
+                      double* x, int64_t capacity, int64_t* nnz);
+/* Auxiliary per-particle state: nWithoutSpp (:553-556), ecs (:543-546),
+ * originalX (:548-551).  Any pointer may be NULL. */
+int mps_debug_get_aux(mps_handle* h, double* n_without_spp, double* ecs, double* ox, double* oz);
+int mps_debug_set_aux(mps_handle* h, const double* n_without_spp, const double* ecs,
+                      const double* ox, const double* oz);
+
+/* SolvePressurePoissonEquation on a caller-supplied CSR system (host arrays), the
+ * entry the reference's CG tests drive (test_ComputerConjugateGradient.cpp).
+ * x holds the initial guess on entry and the solution on return. */
+int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int32_t* col,
+                     const double* val, const double* b, double* x, double eps,
+                     int32_t criterion, int32_t max_iters, int32_t solver, int32_t* iterations,
+                     double* true_relres);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENMPS_GB300_MPS_H */

@@ -1,0 +1,142 @@
+// grid.cu - cell-list neighbour search (Computer::SearchNeighbor, Computer.hpp:698-756;
+// Grid::Store / Grid::Iterator, Grid.hpp:276-559).
+//
+// The reference stores particles serially (ascending index) into dense cells and
+// then walks the nine surrounding cells in a fixed order.  Here every particle
+// claims a slot of its cell with one atomic, each cell is then sorted back to
+// ascending index (so the slot order equals the serial insertion order), and one
+// thread per particle walks the nine cells and writes its list into the
+// transposed ELL array.  The output equals the reference's list element for
+// element: same candidates, same order, same distance test.
+//
+// Compiled with -fmad=false: the distance test must round exactly like the
+// reference's sqrt(inner_prod(r, r)) < NeighborLength.
+#include "common.cuh"
+
+namespace mpsgb {
+
+// Grid::Block (Grid.hpp:250-254) + Grid::Store (:276-331): out-of-domain particles
+// are disabled (Computer.hpp:710-715); a cell beyond maxPerCell is the reference's
+// "Too many particle in a block" error.
+__global__ void k_bucket(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (st.type[i] == MPS_TYPE_DISABLED) {
+        atomicAdd(&st.status->disabled, 1);
+        return;
+    }
+    const double fx = floor(__ddiv_rn(__dadd_rn(st.x[i], -sc.min_x), sc.nl));
+    const double fz = floor(__ddiv_rn(__dadd_rn(st.z[i], -sc.min_z), sc.nl));
+    if (!(fx >= 0.0 && fx < static_cast<double>(sc.gnx) && fz >= 0.0 &&
+          fz < static_cast<double>(sc.gnz))) {
+        st.type[i] = MPS_TYPE_DISABLED;
+        atomicAdd(&st.status->disabled, 1);
+        return;
+    }
+    const int cell = static_cast<int>(fx) * sc.gnz + static_cast<int>(fz);
+    const int slot = atomicAdd(&st.cell_count[cell], 1);
+    if (slot < sc.max_per_cell) {
+        st.cell_slot[static_cast<int64_t>(cell) * sc.max_per_cell + slot] = i;
+    } else {
+        atomicOr(&st.status->flags, kStatusCellOverflow);
+    }
+}
+
+// Restores the serial insertion order of each cell (ascending particle index).
+__global__ void k_cell_sort(SceneConst sc, DeviceState st) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= sc.gnx * sc.gnz) return;
+    const int cnt = min(st.cell_count[c], sc.max_per_cell);
+    if (cnt < 2) return;
+    int32_t* s = st.cell_slot + static_cast<int64_t>(c) * sc.max_per_cell;
+    int buf[64];
+    const int m = min(cnt, 64);
+    for (int a = 0; a < m; a++) buf[a] = s[a];
+    for (int a = 1; a < m; a++) {
+        const int v = buf[a];
+        int b = a - 1;
+        while (b >= 0 && buf[b] > v) {
+            buf[b + 1] = buf[b];
+            b--;
+        }
+        buf[b + 1] = v;
+    }
+    if (cnt > 64) {  // maxPerCell > 64 only for r_e/l0 beyond 6: fall back to in-place sort
+        for (int a = 1; a < cnt; a++) {
+            const int v = s[a];
+            int b = a - 1;
+            while (b >= 0 && s[b] > v) {
+                s[b + 1] = s[b];
+                b--;
+            }
+            s[b + 1] = v;
+        }
+        return;
+    }
+    for (int a = 0; a < m; a++) s[a] = buf[a];
+}
+
+// Neighbour rows: the nine cells in Grid::Iterator order (Grid.hpp:393-401), each in
+// slot order, keeping j != i with R(x_i, x_j) < NeighborLength (Computer.hpp:740-749).
+__global__ void k_neighbors(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (st.type[i] == MPS_TYPE_DISABLED) {
+        st.nb_count[i] = 0;
+        return;
+    }
+    const double xi = st.x[i], zi = st.z[i];
+    const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
+    const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
+    int cnt = 0;
+    for (int di = -1; di <= 1; di++) {
+        const int cx = bx + di;
+        if (cx < 0 || cx >= sc.gnx) continue;
+        for (int dk = -1; dk <= 1; dk++) {
+            const int cz = bz + dk;
+            if (cz < 0 || cz >= sc.gnz) continue;
+            const int cell = cx * sc.gnz + cz;
+            const int m = min(st.cell_count[cell], sc.max_per_cell);
+            const int32_t* slots = st.cell_slot + static_cast<int64_t>(cell) * sc.max_per_cell;
+            for (int l = 0; l < m; l++) {
+                const int j = slots[l];
+                if (j == i) continue;
+                const double dx = __dadd_rn(xi, -st.x[j]);
+                const double dz = __dadd_rn(zi, -st.z[j]);
+                const double r2 = dot2(dx, dz, dx, dz);
+                bool inside;
+                if (r2 < sc.nl2_lo) {
+                    inside = true;
+                } else if (r2 > sc.nl2_hi) {
+                    inside = false;
+                } else {
+                    inside = __dsqrt_rn(r2) < sc.nl;
+                }
+                if (inside) {
+                    if (cnt < sc.nb_stride) {
+                        st.nb[ell(cnt, sc.n, i)] = j;
+                    } else {
+                        atomicOr(&st.status->flags, kStatusDeviceCheck);
+                        st.status->check_index = i;
+                    }
+                    cnt++;
+                }
+            }
+        }
+    }
+    st.nb_count[i] = min(cnt, sc.nb_stride);
+}
+
+void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_bucket<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_cell_sort<<<grid_for(static_cast<int64_t>(sc.gnx) * sc.gnz), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_neighbors<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+}  // namespace mpsgb

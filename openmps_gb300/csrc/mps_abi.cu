@@ -1,0 +1,974 @@
+// mps_abi.cu - the C ABI of include/mps.h: handle, device buffers, step orchestration.
+//
+// One handle = one scene on one GPU with its own CUDA stream.  A step is the stage
+// sequence of Computer::ForwardTime (Computer.hpp:1700-1742) issued on that stream
+// (the CG loop as one graph), followed by a single read of a small status block.
+// Errors of the reference become status codes: a cell overflow stops the step after
+// the search (Grid.hpp:314-318), a CG failure stops it before the pressure is
+// assigned (Computer.hpp:1424-1428); later stages check the device status word and
+// skip themselves, so no partial update happens past the failing stage.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "cg.cuh"
+#include "common.cuh"
+
+using namespace mpsgb;
+
+namespace {
+
+const char* kVersion = "openmps_gb300 0.1 (sm_103a)";
+
+struct StatusError {
+    int code;
+    std::string msg;
+};
+
+// Per-stage event slots used when stage timing is enabled.
+enum Stage { kSearch, kDensity, kEcs, kExplicit, kDensity2, kPpe, kSolve, kPressure, kGradient,
+             kDs, kNumStages };
+
+}  // namespace
+
+struct mps_handle {
+    mps_params prm{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t user_events[16] = {};
+    cudaEvent_t stage_events[kNumStages + 1] = {};
+    bool stage_timing = false;
+
+    SceneConst sc{};
+    DeviceState st{};
+    int64_t n = 0;
+    int64_t cap = 0;  // particles the buffers hold
+    double t = 0, dt = 0;
+
+    // CG buffers
+    CgScalars* S = nullptr;
+    double* partials = nullptr;
+    double *r = nullptr, *p = nullptr, *Ap = nullptr;
+    float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *d32 = nullptr;
+    CgGraph cg;
+
+    // pinned host mirrors of the status block
+    DevStatus* h_status = nullptr;
+    CgScalars* h_S = nullptr;
+    StepScalars* h_step = nullptr;
+
+    void* flush_buf = nullptr;
+    size_t flush_bytes = 0;
+
+    mps_stats stats{};
+    std::string err;
+    std::vector<void*> allocations;
+};
+
+namespace {
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        throw StatusError{e == cudaErrorMemoryAllocation ? MPS_ERR_OUT_OF_MEMORY : MPS_ERR_CUDA,
+                          std::string(what) + ": " + cudaGetErrorString(e)};
+    }
+}
+
+template <class F>
+int guarded(mps_handle* h, F f) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    try {
+        if (cudaSetDevice(h->device) != cudaSuccess)
+            throw StatusError{MPS_ERR_CUDA, "cudaSetDevice failed"};
+        f();
+        h->err.clear();
+        return MPS_OK;
+    } catch (const StatusError& e) {
+        h->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        h->err = "host out of memory";
+        return MPS_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return MPS_ERR_STATE;
+    }
+}
+
+template <class T>
+T* dalloc(mps_handle* h, int64_t count) {
+    void* ptr = nullptr;
+    const size_t bytes = static_cast<size_t>(std::max<int64_t>(count, 1)) * sizeof(T);
+    check(cudaMalloc(&ptr, bytes), "cudaMalloc");
+    h->allocations.push_back(ptr);
+    return static_cast<T*>(ptr);
+}
+
+void dfree_all(mps_handle* h) {
+    for (void* ptr : h->allocations) cudaFree(ptr);
+    h->allocations.clear();
+}
+
+void lattice_constants(double re_by_l0, double l0, double& n0, double& lambda) {
+    // Environment.hpp:163-215, same loop order and expression order as the reference
+    const double re = re_by_l0 * l0;
+    const int range = static_cast<int>(std::ceil(re_by_l0));
+    n0 = 0;
+    lambda = 0;
+    volatile double t0, t1;  // keep each product rounded (no contraction on the host)
+    for (int i = -range; i < range; i++) {
+        for (int j = -range; j < range; j++) {
+            if (!((i == 0) && (j == 0))) {
+                const double x0 = i * l0;
+                const double x1 = j * l0;
+                t0 = x0 * x0;
+                t1 = x1 * x1;
+                const double r = std::sqrt((0.0 + t0) + t1);
+                if (r < re) {
+                    const double w = ((0 < r) && (r < re)) ? (re / r - 1) : 0;
+                    n0 += w;
+                    t0 = r * r;
+                    t1 = t0 * w;
+                    lambda += t1;
+                }
+            }
+        }
+    }
+    lambda /= n0;
+}
+
+void validate(const mps_params& p) {
+    auto bad = [](const char* m) { throw StatusError{MPS_ERR_INVALID_ARGUMENT, m}; };
+    if (!(p.l0 > 0)) bad("l0 must be positive");
+    if (!(p.re_by_l0 > 0)) bad("re_by_l0 must be positive");
+    if (!(p.g > 0)) bad("g must be positive (MaxDt uses sqrt(2 courant l0 / g))");
+    if (!(p.rho > 0)) bad("rho must be positive");
+    if (!(p.courant > 0)) bad("courant must be positive");
+    if (!(p.max_x > p.min_x) || !(p.max_z > p.min_z)) bad("empty domain");
+    if (p.solver < MPS_SOLVER_CG64 || p.solver > MPS_SOLVER_LEARNED) bad("unknown solver");
+    if (p.solver == MPS_SOLVER_LEARNED)
+        throw StatusError{MPS_ERR_NOT_SUPPORTED, "learned solver needs mps_learned_* setup"};
+    if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
+        bad("unknown criterion");
+    if (p.flags & ~static_cast<uint32_t>(MPS_PRESET_REFERENCE)) bad("unknown method flag");
+}
+
+void setup_constants(mps_handle* h) {
+    const mps_params& p = h->prm;
+    SceneConst& sc = h->sc;
+    const double re_by = p.re_by_l0;
+    const double rl_by = p.re_lap_by_l0 > 0 ? p.re_lap_by_l0 : p.re_by_l0;
+    sc.flags = p.flags;
+    sc.l0 = p.l0;
+    sc.re = re_by * p.l0;
+    sc.re2 = sc.re * sc.re;
+    sc.re_lap = rl_by * p.l0;
+    sc.rl2 = sc.re_lap * sc.re_lap;
+    sc.nl = std::max(re_by, rl_by) * p.l0 * (1 + p.courant * 2);  // Environment.hpp:161
+    sc.nl2_lo = (sc.nl * (1.0 - 1e-12)) * (sc.nl * (1.0 - 1e-12));
+    sc.nl2_hi = (sc.nl * (1.0 + 1e-12)) * (sc.nl * (1.0 + 1e-12));
+    lattice_constants(re_by, p.l0, sc.n0, sc.lambda);
+    lattice_constants(rl_by, p.l0, sc.n0_lap, sc.lambda_lap);
+    sc.rho = p.rho;
+    sc.nu = p.nu;
+    sc.g = p.g;
+    sc.surface_ratio = p.surface_ratio;
+    sc.max_dt = std::min(p.max_dt, std::sqrt(2 * (p.courant * p.l0) / p.g));  // :138
+    sc.max_dx = p.courant * p.l0;                                             // :143
+    sc.min_x = p.min_x;
+    sc.min_z = p.min_z;
+    // Grid.hpp:137-150
+    const double cx = std::ceil((p.max_x - p.min_x) / sc.nl);
+    const double cz = std::ceil((p.max_z - p.min_z) / sc.nl);
+    if (!(cx < 1e6 && cz < 1e6 && cx * cz < 2e8))
+        throw StatusError{MPS_ERR_INVALID_ARGUMENT, "domain has too many cells"};
+    sc.gnx = static_cast<int32_t>(cx) + 2;
+    sc.gnz = static_cast<int32_t>(cz) + 2;
+    const int c = static_cast<int>(std::ceil(sc.nl / p.l0));
+    sc.max_per_cell = (c + 1) * (c + 1);
+    sc.nb_stride = sc.max_per_cell * 9;
+    sc.ppe_stride = sc.nb_stride + 1;
+}
+
+// (Re)allocates every per-particle buffer for n particles, preserving the first
+// `keep` entries of the persistent per-particle arrays.
+void allocate(mps_handle* h, int64_t n, int64_t keep) {
+    const SceneConst& sc = h->sc;
+    DeviceState old = h->st;
+    std::vector<void*> old_allocs;
+    old_allocs.swap(h->allocations);
+    DeviceState& st = h->st;
+    const int64_t cells = static_cast<int64_t>(sc.gnx) * sc.gnz;
+    st.type = dalloc<int32_t>(h, n);
+    double** dbl[] = {&st.x, &st.z, &st.u, &st.w, &st.p, &st.nd, &st.wall_x, &st.wall_z,
+                      &st.n_wo_spp, &st.ecs, &st.ox, &st.oz, &st.dux, &st.duz};
+    double* const* old_dbl[] = {&old.x, &old.z, &old.u, &old.w, &old.p, &old.nd, &old.wall_x,
+                                &old.wall_z, &old.n_wo_spp, &old.ecs, &old.ox, &old.oz,
+                                &old.dux, &old.duz};
+    for (double** a : dbl) *a = dalloc<double>(h, n);
+    st.cell_count = dalloc<int32_t>(h, cells);
+    st.cell_slot = dalloc<int32_t>(h, cells * sc.max_per_cell);
+    st.nb_count = dalloc<int32_t>(h, n);
+    st.nb = dalloc<int32_t>(h, n * sc.nb_stride);
+    st.ppe_len = dalloc<int32_t>(h, n);
+    st.ppe_col = dalloc<int32_t>(h, n * sc.ppe_stride);
+    st.ppe_col_tmp = dalloc<int32_t>(h, n * sc.ppe_stride);
+    st.ppe_val = dalloc<double>(h, n * sc.ppe_stride);
+    st.ppe_val_tmp = dalloc<double>(h, n * sc.ppe_stride);
+    st.ppe_val32 = dalloc<float>(h, n * sc.ppe_stride);
+    st.ppe_b = dalloc<double>(h, n);
+    st.ppe_x = dalloc<double>(h, n);
+    st.step = dalloc<StepScalars>(h, 1);
+    st.status = dalloc<DevStatus>(h, 1);
+    h->S = dalloc<CgScalars>(h, 1);
+    st.solve_ok = &h->S->converged;
+    h->partials = dalloc<double>(h, 2 * static_cast<int64_t>(grid_for(n)) + 64);
+    h->r = dalloc<double>(h, n);
+    h->p = dalloc<double>(h, n);
+    h->Ap = dalloc<double>(h, n);
+    h->r32 = dalloc<float>(h, n);
+    h->p32 = dalloc<float>(h, n);
+    h->q32 = dalloc<float>(h, n);
+    h->d32 = dalloc<float>(h, n);
+    cudaStream_t s = h->stream;
+    // zero everything persistent, then carry the old contents over
+    check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
+    for (double** a : dbl) check(cudaMemsetAsync(*a, 0, sizeof(double) * n, s), "memset");
+    check(cudaMemsetAsync(st.step, 0, sizeof(StepScalars), s), "memset");
+    check(cudaMemsetAsync(st.status, 0, sizeof(DevStatus), s), "memset");
+    check(cudaMemsetAsync(h->S, 0, sizeof(CgScalars), s), "memset");
+    check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
+    check(cudaMemsetAsync(st.nb_count, 0, sizeof(int32_t) * n, s), "memset");
+    check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * n, s), "memset");
+    check(cudaMemsetAsync(st.cell_count, 0, sizeof(int32_t) * cells, s), "memset");
+    if (keep > 0) {
+        check(cudaMemcpyAsync(st.type, old.type, sizeof(int32_t) * keep, cudaMemcpyDeviceToDevice, s),
+              "copy");
+        for (size_t k = 0; k < sizeof(dbl) / sizeof(dbl[0]); k++)
+            check(cudaMemcpyAsync(*dbl[k], *old_dbl[k], sizeof(double) * keep,
+                                  cudaMemcpyDeviceToDevice, s),
+                  "copy");
+        check(cudaMemcpyAsync(st.step, old.step, sizeof(StepScalars), cudaMemcpyDeviceToDevice, s),
+              "copy");
+    } else {
+        StepScalars init{h->t, h->dt, 0ull, 0.0};
+        check(cudaMemcpyAsync(st.step, &init, sizeof(init), cudaMemcpyHostToDevice, s), "copy");
+    }
+    check(cudaStreamSynchronize(s), "allocate");
+    for (void* ptr : old_allocs) cudaFree(ptr);
+    h->cap = n;
+    h->cg.reset();
+}
+
+CgOperands cg_operands(mps_handle* h) {
+    CgOperands o{};
+    o.n = static_cast<int32_t>(h->n);
+    o.len = h->st.ppe_len;
+    o.col = h->st.ppe_col;
+    o.val = h->st.ppe_val;
+    o.val32 = h->st.ppe_val32;
+    o.b = h->st.ppe_b;
+    o.x = h->st.ppe_x;
+    o.r = h->r;
+    o.p = h->p;
+    o.Ap = h->Ap;
+    o.r32 = h->r32;
+    o.p32 = h->p32;
+    o.q32 = h->q32;
+    o.d32 = h->d32;
+    o.partials = h->partials;
+    o.S = h->S;
+    o.status = h->st.status;
+    return o;
+}
+
+void require_particles(mps_handle* h) {
+    if (h->n <= 0) throw StatusError{MPS_ERR_STATE, "no particles: call mps_add_particles first"};
+}
+
+void launched(mps_handle* h, int k) { h->stats.kernel_launches += k; }
+
+void after_launch(const char* what) { check(cudaGetLastError(), what); }
+
+// Reads the status block and converts device flags into the reference's errors.
+void read_status(mps_handle* h, bool solve_done) {
+    cudaStream_t s = h->stream;
+    check(cudaMemcpyAsync(h->h_status, h->st.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s),
+          "status");
+    check(cudaMemcpyAsync(h->h_step, h->st.step, sizeof(StepScalars), cudaMemcpyDeviceToHost, s),
+          "status");
+    if (solve_done)
+        check(cudaMemcpyAsync(h->h_S, h->S, sizeof(CgScalars), cudaMemcpyDeviceToHost, s), "status");
+    check(cudaStreamSynchronize(s), "step");
+    h->t = h->h_step->t;
+    h->dt = h->h_step->dt;
+    h->stats.disabled = h->h_status->disabled;
+    if (solve_done) {
+        const CgScalars& S = *h->h_S;
+        h->stats.cg_iterations = S.iter;
+        h->stats.cg_refinements = (h->prm.solver == MPS_SOLVER_CG64) ? 1 : S.updates + 1;
+        h->stats.cg_rr0 = S.rr0;
+        h->stats.cg_rr = S.rr_new;
+        h->stats.cg_true_relres = (S.bb > 0) ? std::sqrt(S.true_rr / S.bb) : std::sqrt(S.true_rr);
+        launched(h, 2 + (h->prm.solver == MPS_SOLVER_CG64 ? 0 : 1) +
+                        S.iter * h->cg.kernels_per_iteration());
+    }
+    const int f = h->h_status->flags;
+    if (f & kStatusCellOverflow) throw StatusError{MPS_ERR_CELL_OVERFLOW, "Too many particle in a block"};
+    if (f & kStatusDeviceCheck) {
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), "device bounds check fired at particle %d",
+                      h->h_status->check_index);
+        throw StatusError{MPS_ERR_DEVICE_CHECK, buf};
+    }
+    if (solve_done && !h->h_S->converged)
+        throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
+                          "Conjugate Gradient method couldn't solve Pressure Poison Equation"};
+}
+
+void stage_mark(mps_handle* h, int k) {
+    if (h->stage_timing) check(cudaEventRecord(h->stage_events[k], h->stream), "event");
+}
+
+// ---- individual stages (stream-ordered, no sync)
+void do_search(mps_handle* h) {
+    cudaStream_t s = h->stream;
+    const int64_t cells = static_cast<int64_t>(h->sc.gnx) * h->sc.gnz;
+    check(cudaMemsetAsync(h->st.cell_count, 0, sizeof(int32_t) * cells, s), "memset");
+    check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
+    launch_bucket(h->sc, h->st, s);
+    launch_cell_sort(h->sc, h->st, s);
+    launch_neighbors(h->sc, h->st, s);
+    after_launch("search");
+    launched(h, kLaunchesSearch);
+}
+
+void do_solve(mps_handle* h) {
+    cudaStream_t s = h->stream;
+    const int max_iter = h->prm.max_cg_iters > 0 ? h->prm.max_cg_iters : static_cast<int>(h->n);
+    launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter, 0.01, s);
+    after_launch("cg configure");
+    launched(h, 1);
+    const int solver = h->prm.solver == MPS_SOLVER_CG64 ? MPS_SOLVER_CG64 : MPS_SOLVER_MIXED;
+    if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
+        check(h->cg.build(solver, cg_operands(h), s), "CG graph build");
+    }
+    check(h->cg.launch(s), "CG graph launch");
+}
+
+void forward(mps_handle* h, double dt) {
+    require_particles(h);
+    cudaStream_t s = h->stream;
+    const uint32_t flags = h->prm.flags;
+    SceneConst sc = h->sc;
+    sc.guard = 1;  // inside a step, stages skip themselves after a failure
+    stage_mark(h, kSearch);
+    if (dt > 0) {
+        launch_set_dt(sc, h->st, dt, s);
+        launched(h, kLaunchesDt);
+    } else {
+        launch_cfl_dt(sc, h->st, s);
+        launched(h, kLaunchesCfl);
+    }
+    do_search(h);
+    stage_mark(h, kDensity);
+    launch_density(sc, h->st, s);
+    launched(h, kLaunchesDensity);
+    stage_mark(h, kEcs);
+    if (flags & MPS_FLAG_ECS) {
+        launch_error_correction(sc, h->st, s);
+        launched(h, kLaunchesEcs);
+    }
+    stage_mark(h, kExplicit);
+    launch_explicit(sc, h->st, s);
+    launched(h, kLaunchesExplicit);
+    stage_mark(h, kDensity2);
+    launch_density(sc, h->st, s);
+    launched(h, kLaunchesDensity);
+    if (flags & MPS_FLAG_DS) {
+        launch_save_x(sc, h->st, s);
+        launched(h, kLaunchesSaveX);
+    }
+    stage_mark(h, kPpe);
+    launch_set_ppe(sc, h->st, h->prm.solver != MPS_SOLVER_CG64, s);
+    launched(h, kLaunchesSetPpe);
+    after_launch("stages");
+    stage_mark(h, kSolve);
+    do_solve(h);
+    stage_mark(h, kPressure);
+    launch_assign_pressure(sc, h->st, s);
+    launched(h, kLaunchesAssign);
+    stage_mark(h, kGradient);
+    launch_pressure_gradient(sc, h->st, s);
+    launched(h, kLaunchesGradient);
+    stage_mark(h, kDs);
+    if (flags & MPS_FLAG_DS) {
+        launch_dynamic_stabilize(sc, h->st, s);
+        launched(h, kLaunchesDs);
+    }
+    stage_mark(h, kNumStages);
+    after_launch("step");
+    read_status(h, true);
+    h->stats.steps += 1;
+    if (h->stage_timing) {
+        float total = 0.f;
+        for (int k = 0; k < kNumStages; k++) {
+            float ms = 0.f;
+            check(cudaEventElapsedTime(&ms, h->stage_events[k], h->stage_events[k + 1]), "elapsed");
+            h->stats.stage_ms[k] = ms;
+            total += ms;
+        }
+        h->stats.stage_ms[10] = 0.0;
+        h->stats.stage_ms[11] = total;
+    }
+}
+
+void upload(mps_handle* h, void* dst, const void* src, size_t bytes, bool device_src) {
+    if (!src) return;
+    check(cudaMemcpyAsync(dst, src, bytes, device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          h->stream),
+          "upload");
+}
+
+void download(mps_handle* h, void* dst, const void* src, size_t bytes, bool device_dst) {
+    if (!dst) return;
+    check(cudaMemcpyAsync(dst, src, bytes, device_dst ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          h->stream),
+          "download");
+}
+
+// Device buffers owned by one call (freed on every exit path).
+struct ScopedBuffers {
+    std::vector<void*> ptrs;
+    ~ScopedBuffers() {
+        for (void* q : ptrs) cudaFree(q);
+    }
+    template <class T>
+    T* get(size_t cnt) {
+        void* q = nullptr;
+        check(cudaMalloc(&q, std::max<size_t>(cnt, 1) * sizeof(T)), "cudaMalloc");
+        ptrs.push_back(q);
+        return static_cast<T*>(q);
+    }
+};
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+void mps_default_params(mps_params* prm) {
+    if (!prm) return;
+    std::memset(prm, 0, sizeof(*prm));
+    // Benchmark/Sample/Sample.xml constants with the stock method flags
+    prm->max_dt = 0.005 / 10;
+    prm->courant = 0.1;
+    prm->g = 9.8;
+    prm->rho = 998.2;
+    prm->nu = 1.004e-6;
+    prm->surface_ratio = 0.97;
+    prm->re_by_l0 = 2.4;
+    prm->re_lap_by_l0 = 0.0;
+    prm->l0 = 0.008;
+    prm->min_x = -0.032;
+    prm->min_z = -0.032;
+    prm->max_x = 0.584;
+    prm->max_z = 0.584;
+    prm->eps = 1e-10;
+    prm->flags = MPS_PRESET_REFERENCE;
+    prm->solver = MPS_SOLVER_CG64;
+    prm->criterion = MPS_CRIT_INITIAL_RESIDUAL;
+    prm->max_cg_iters = 0;
+    prm->inner_tol = 1e-3;
+    prm->max_refinements = 60;
+}
+
+size_t mps_params_size(void) { return sizeof(mps_params); }
+size_t mps_stats_size(void) { return sizeof(mps_stats); }
+size_t mps_environment_size(void) { return sizeof(mps_environment); }
+const char* mps_version(void) { return kVersion; }
+
+const char* mps_status_string(int status) {
+    switch (status) {
+        case MPS_OK: return "ok";
+        case MPS_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case MPS_ERR_CUDA: return "CUDA error";
+        case MPS_ERR_OUT_OF_MEMORY: return "out of memory";
+        case MPS_ERR_CELL_OVERFLOW: return "too many particles in a cell";
+        case MPS_ERR_CG_NOT_CONVERGED: return "CG did not converge";
+        case MPS_ERR_NOT_SUPPORTED: return "not supported";
+        case MPS_ERR_STATE: return "invalid state";
+        case MPS_ERR_NONFINITE: return "non-finite value";
+        case MPS_ERR_TIMEOUT: return "device wait timed out";
+        case MPS_ERR_DEVICE_CHECK: return "device bounds check";
+        default: return "unknown status";
+    }
+}
+
+const char* mps_last_error(const mps_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int mps_create(const mps_params* prm, int device, mps_handle** out) {
+    if (!prm || !out) return MPS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    mps_handle* h = nullptr;
+    try {
+        h = new mps_handle;
+    } catch (const std::bad_alloc&) {
+        return MPS_ERR_OUT_OF_MEMORY;
+    }
+    int dev = device;
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) {
+        delete h;
+        return MPS_ERR_CUDA;
+    }
+    h->device = dev;
+    h->prm = *prm;
+    const int rc = guarded(h, [&] {
+        validate(h->prm);
+        setup_constants(h);
+        check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+        for (auto& e : h->user_events) check(cudaEventCreate(&e), "event");
+        for (auto& e : h->stage_events) check(cudaEventCreate(&e), "event");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->h_status), sizeof(DevStatus)), "pinned");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->h_S), sizeof(CgScalars)), "pinned");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->h_step), sizeof(StepScalars)), "pinned");
+    });
+    if (rc != MPS_OK) {
+        mps_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return MPS_OK;
+}
+
+int mps_destroy(mps_handle* h) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->cg.reset();
+    dfree_all(h);
+    if (h->flush_buf) cudaFree(h->flush_buf);
+    for (auto& e : h->user_events)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : h->stage_events)
+        if (e) cudaEventDestroy(e);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->h_S) cudaFreeHost(h->h_S);
+    if (h->h_step) cudaFreeHost(h->h_step);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MPS_OK;
+}
+
+int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const double* x,
+                      const double* z, const double* u, const double* w, const double* p,
+                      const double* nd) {
+    if (!h || n < 0 || (n > 0 && (!type || !x || !z))) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (n == 0) return;
+        for (int64_t i = 0; i < n; i++)
+            if (type[i] < MPS_TYPE_FLUID || type[i] > MPS_TYPE_DISABLED)
+                throw StatusError{MPS_ERR_INVALID_ARGUMENT, "particle type out of range"};
+        const int64_t old = h->n;
+        const int64_t total = old + n;
+        if (total > (int64_t{1} << 31) / std::max(1, h->sc.ppe_stride))
+            throw StatusError{MPS_ERR_INVALID_ARGUMENT, "too many particles for 32-bit ELL indexing"};
+        allocate(h, total, old);
+        h->n = total;
+        h->sc.n = static_cast<int32_t>(total);
+        DeviceState& st = h->st;
+        const size_t b8 = sizeof(double) * n;
+        upload(h, st.type + old, type, sizeof(int32_t) * n, false);
+        upload(h, st.x + old, x, b8, false);
+        upload(h, st.z + old, z, b8, false);
+        upload(h, st.wall_x + old, x, b8, false);  // static walls: initial positions (Main.cpp:303-318)
+        upload(h, st.wall_z + old, z, b8, false);
+        upload(h, st.u + old, u, b8, false);
+        upload(h, st.w + old, w, b8, false);
+        upload(h, st.p + old, p, b8, false);
+        upload(h, st.nd + old, nd, b8, false);
+        check(cudaStreamSynchronize(h->stream), "add particles");
+    });
+}
+
+int64_t mps_particle_count(const mps_handle* h) { return h ? h->n : -1; }
+
+static int get_particles_impl(mps_handle* h, int32_t* type, double* x, double* z, double* u,
+                              double* w, double* p, double* nd, bool device) {
+    return guarded(h, [&] {
+        const int64_t n = h->n;
+        const DeviceState& st = h->st;
+        download(h, type, st.type, sizeof(int32_t) * n, device);
+        download(h, x, st.x, sizeof(double) * n, device);
+        download(h, z, st.z, sizeof(double) * n, device);
+        download(h, u, st.u, sizeof(double) * n, device);
+        download(h, w, st.w, sizeof(double) * n, device);
+        download(h, p, st.p, sizeof(double) * n, device);
+        download(h, nd, st.nd, sizeof(double) * n, device);
+        if (!device) check(cudaStreamSynchronize(h->stream), "get particles");
+    });
+}
+
+static int set_particles_impl(mps_handle* h, const int32_t* type, const double* x, const double* z,
+                              const double* u, const double* w, const double* p, const double* nd,
+                              bool device) {
+    return guarded(h, [&] {
+        const int64_t n = h->n;
+        DeviceState& st = h->st;
+        upload(h, st.type, type, sizeof(int32_t) * n, device);
+        upload(h, st.x, x, sizeof(double) * n, device);
+        upload(h, st.z, z, sizeof(double) * n, device);
+        upload(h, st.u, u, sizeof(double) * n, device);
+        upload(h, st.w, w, sizeof(double) * n, device);
+        upload(h, st.p, p, sizeof(double) * n, device);
+        upload(h, st.nd, nd, sizeof(double) * n, device);
+        if (!device) check(cudaStreamSynchronize(h->stream), "set particles");
+    });
+}
+
+int mps_get_particles(mps_handle* h, int32_t* type, double* x, double* z, double* u, double* w,
+                      double* p, double* nd) {
+    return get_particles_impl(h, type, x, z, u, w, p, nd, false);
+}
+
+int mps_set_particles(mps_handle* h, const int32_t* type, const double* x, const double* z,
+                      const double* u, const double* w, const double* p, const double* nd) {
+    return set_particles_impl(h, type, x, z, u, w, p, nd, false);
+}
+
+int mps_get_particles_device(mps_handle* h, int32_t* type, double* x, double* z, double* u,
+                             double* w, double* p, double* nd) {
+    return get_particles_impl(h, type, x, z, u, w, p, nd, true);
+}
+
+int mps_set_particles_device(mps_handle* h, const int32_t* type, const double* x,
+                             const double* z, const double* u, const double* w,
+                             const double* p, const double* nd) {
+    return set_particles_impl(h, type, x, z, u, w, p, nd, true);
+}
+
+int mps_set_wall_positions(mps_handle* h, const double* wx, const double* wz) {
+    return guarded(h, [&] {
+        upload(h, h->st.wall_x, wx, sizeof(double) * h->n, false);
+        upload(h, h->st.wall_z, wz, sizeof(double) * h->n, false);
+        check(cudaStreamSynchronize(h->stream), "wall positions");
+    });
+}
+
+int mps_forward_time(mps_handle* h, double dt) {
+    return guarded(h, [&] { forward(h, dt); });
+}
+
+int mps_forward_steps(mps_handle* h, double dt, int32_t nsteps) {
+    if (nsteps < 0) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        for (int32_t k = 0; k < nsteps; k++) forward(h, dt);
+    });
+}
+
+int mps_get_environment(const mps_handle* h, mps_environment* env) {
+    if (!h || !env) return MPS_ERR_INVALID_ARGUMENT;
+    const SceneConst& sc = h->sc;
+    std::memset(env, 0, sizeof(*env));
+    env->t = h->t;
+    env->dt = h->dt;
+    env->n0 = sc.n0;
+    env->lambda = sc.lambda;
+    env->n0_lap = sc.n0_lap;
+    env->lambda_lap = sc.lambda_lap;
+    env->max_dt = sc.max_dt;
+    env->max_dx = sc.max_dx;
+    env->l0 = sc.l0;
+    env->re = sc.re;
+    env->re_lap = sc.re_lap;
+    env->neighbor_length = sc.nl;
+    env->rho = sc.rho;
+    env->nu = sc.nu;
+    env->g = sc.g;
+    env->min_x = h->prm.min_x;
+    env->min_z = h->prm.min_z;
+    env->max_x = h->prm.max_x;
+    env->max_z = h->prm.max_z;
+    env->grid_nx = sc.gnx;
+    env->grid_nz = sc.gnz;
+    env->grid_max_per_cell = sc.max_per_cell;
+    return MPS_OK;
+}
+
+int mps_get_stats(const mps_handle* h, mps_stats* st) {
+    if (!h || !st) return MPS_ERR_INVALID_ARGUMENT;
+    *st = h->stats;
+    return MPS_OK;
+}
+
+int mps_set_solver(mps_handle* h, int32_t solver, int32_t criterion, double eps) {
+    return guarded(h, [&] {
+        mps_params p = h->prm;
+        p.solver = solver;
+        p.criterion = criterion;
+        p.eps = eps;
+        validate(p);
+        h->prm = p;
+    });
+}
+
+int mps_set_stage_timing(mps_handle* h, int32_t enable) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    h->stage_timing = enable != 0;
+    return MPS_OK;
+}
+
+int mps_synchronize(mps_handle* h) {
+    return guarded(h, [&] { check(cudaStreamSynchronize(h->stream), "synchronize"); });
+}
+
+int mps_event_record(mps_handle* h, int32_t slot) {
+    if (!h || slot < 0 || slot >= 16) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] { check(cudaEventRecord(h->user_events[slot], h->stream), "event"); });
+}
+
+int mps_event_elapsed(mps_handle* h, int32_t begin, int32_t end, float* ms) {
+    if (!h || !ms || begin < 0 || begin >= 16 || end < 0 || end >= 16) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        check(cudaEventSynchronize(h->user_events[end]), "event sync");
+        check(cudaEventElapsedTime(ms, h->user_events[begin], h->user_events[end]), "elapsed");
+    });
+}
+
+int mps_flush_l2(mps_handle* h, int64_t bytes) {
+    if (!h || bytes <= 0) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (h->flush_bytes < static_cast<size_t>(bytes)) {
+            if (h->flush_buf) cudaFree(h->flush_buf);
+            h->flush_buf = nullptr;
+            h->flush_bytes = 0;
+            check(cudaMalloc(&h->flush_buf, static_cast<size_t>(bytes)), "flush buffer");
+            h->flush_bytes = static_cast<size_t>(bytes);
+        }
+        check(cudaMemsetAsync(h->flush_buf, h->stats.steps & 0xff, static_cast<size_t>(bytes),
+                              h->stream),
+              "flush");
+    });
+}
+
+// ---------------------------------------------------------------- stages
+#define MPS_STAGE(name, body)                              \
+    int name(mps_handle* h) {                              \
+        return guarded(h, [&] {                            \
+            require_particles(h);                          \
+            body;                                          \
+            after_launch(#name);                           \
+            check(cudaStreamSynchronize(h->stream), #name); \
+        });                                                \
+    }
+
+MPS_STAGE(mps_stage_search_neighbor, do_search(h); read_status(h, false))
+MPS_STAGE(mps_stage_density, launch_density(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_error_correction, launch_error_correction(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_explicit, launch_explicit(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_save_x, launch_save_x(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_set_ppe, launch_set_ppe(h->sc, h->st, h->prm.solver != MPS_SOLVER_CG64, h->stream))
+MPS_STAGE(mps_stage_solve_ppe, do_solve(h); read_status(h, true))
+MPS_STAGE(mps_stage_assign_pressure, launch_assign_pressure(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_pressure_gradient, launch_pressure_gradient(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_dynamic_stabilize, launch_dynamic_stabilize(h->sc, h->st, h->stream))
+
+#undef MPS_STAGE
+
+int mps_stage_begin_step(mps_handle* h, double dt) {
+    return guarded(h, [&] {
+        require_particles(h);
+        if (dt > 0)
+            launch_set_dt(h->sc, h->st, dt, h->stream);
+        else
+            launch_cfl_dt(h->sc, h->st, h->stream);
+        after_launch("begin step");
+        check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), h->stream), "memset");
+        read_status(h, false);
+    });
+}
+
+int mps_stage_density_variation(mps_handle* h, double* speed_host) {
+    if (!speed_host) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        require_particles(h);
+        double* out = h->r;  // scratch vector of n doubles
+        launch_density_variation(h->sc, h->st, out, h->stream);
+        after_launch("density variation");
+        download(h, speed_host, out, sizeof(double) * h->n, false);
+        check(cudaStreamSynchronize(h->stream), "density variation");
+    });
+}
+
+int mps_debug_get_neighbors(mps_handle* h, int32_t* counts, int32_t* list, int64_t capacity,
+                            int64_t* total) {
+    return guarded(h, [&] {
+        const int64_t n = h->n;
+        std::vector<int32_t> cnt(static_cast<size_t>(n));
+        download(h, cnt.data(), h->st.nb_count, sizeof(int32_t) * n, false);
+        check(cudaStreamSynchronize(h->stream), "neighbors");
+        int64_t sum = 0;
+        for (int32_t c : cnt) sum += c;
+        if (counts) std::memcpy(counts, cnt.data(), sizeof(int32_t) * n);
+        if (total) *total = sum;
+        if (!list) return;
+        if (sum > capacity) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "neighbor list capacity too small"};
+        const int stride = h->sc.nb_stride;
+        int32_t maxc = 0;
+        for (int32_t c : cnt) maxc = std::max(maxc, c);
+        std::vector<int32_t> ellbuf(static_cast<size_t>(n) * std::max(maxc, 1));
+        if (maxc > 0) download(h, ellbuf.data(), h->st.nb, sizeof(int32_t) * n * maxc, false);
+        check(cudaStreamSynchronize(h->stream), "neighbors");
+        (void)stride;
+        int64_t off = 0;
+        for (int64_t i = 0; i < n; i++)
+            for (int32_t k = 0; k < cnt[static_cast<size_t>(i)]; k++)
+                list[off++] = ellbuf[static_cast<size_t>(k) * n + i];
+    });
+}
+
+int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val, double* b,
+                      double* x, int64_t capacity, int64_t* nnz) {
+    return guarded(h, [&] {
+        const int64_t n = h->n;
+        std::vector<int32_t> len(static_cast<size_t>(n));
+        download(h, len.data(), h->st.ppe_len, sizeof(int32_t) * n, false);
+        download(h, b, h->st.ppe_b, sizeof(double) * n, false);
+        download(h, x, h->st.ppe_x, sizeof(double) * n, false);
+        check(cudaStreamSynchronize(h->stream), "ppe");
+        int64_t sum = 0;
+        int32_t maxl = 0;
+        for (int32_t l : len) {
+            sum += l;
+            maxl = std::max(maxl, l);
+        }
+        if (nnz) *nnz = sum;
+        if (row_ptr) {
+            row_ptr[0] = 0;
+            for (int64_t i = 0; i < n; i++) row_ptr[i + 1] = row_ptr[i] + len[static_cast<size_t>(i)];
+        }
+        if (!col && !val) return;
+        if (sum > capacity) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "PPE capacity too small"};
+        std::vector<int32_t> cbuf(static_cast<size_t>(n) * std::max(maxl, 1));
+        std::vector<double> vbuf(static_cast<size_t>(n) * std::max(maxl, 1));
+        if (maxl > 0) {
+            download(h, cbuf.data(), h->st.ppe_col, sizeof(int32_t) * n * maxl, false);
+            download(h, vbuf.data(), h->st.ppe_val, sizeof(double) * n * maxl, false);
+        }
+        check(cudaStreamSynchronize(h->stream), "ppe");
+        int64_t off = 0;
+        for (int64_t i = 0; i < n; i++) {
+            for (int32_t k = 0; k < len[static_cast<size_t>(i)]; k++) {
+                const size_t e = static_cast<size_t>(k) * n + i;
+                if (col) col[off] = cbuf[e];
+                if (val) val[off] = vbuf[e];
+                off++;
+            }
+        }
+    });
+}
+
+int mps_debug_get_aux(mps_handle* h, double* n_without_spp, double* ecs, double* ox, double* oz) {
+    return guarded(h, [&] {
+        const size_t b = sizeof(double) * h->n;
+        download(h, n_without_spp, h->st.n_wo_spp, b, false);
+        download(h, ecs, h->st.ecs, b, false);
+        download(h, ox, h->st.ox, b, false);
+        download(h, oz, h->st.oz, b, false);
+        check(cudaStreamSynchronize(h->stream), "aux");
+    });
+}
+
+int mps_debug_set_aux(mps_handle* h, const double* n_without_spp, const double* ecs,
+                      const double* ox, const double* oz) {
+    return guarded(h, [&] {
+        const size_t b = sizeof(double) * h->n;
+        upload(h, h->st.n_wo_spp, n_without_spp, b, false);
+        upload(h, h->st.ecs, ecs, b, false);
+        upload(h, h->st.ox, ox, b, false);
+        upload(h, h->st.oz, oz, b, false);
+        check(cudaStreamSynchronize(h->stream), "aux");
+    });
+}
+
+int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int32_t* col,
+                     const double* val, const double* b, double* x, double eps, int32_t criterion,
+                     int32_t max_iters, int32_t solver, int32_t* iterations, double* true_relres) {
+    if (!h || n <= 0 || !row_ptr || !b || !x) return MPS_ERR_INVALID_ARGUMENT;
+    if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED) return MPS_ERR_NOT_SUPPORTED;
+    return guarded(h, [&] {
+        // CSR -> transposed ELL (host), into buffers owned by this call
+        int32_t maxl = 0;
+        for (int64_t i = 0; i < n; i++)
+            maxl = std::max<int32_t>(maxl, static_cast<int32_t>(row_ptr[i + 1] - row_ptr[i]));
+        maxl = std::max(maxl, 1);
+        std::vector<int32_t> len(static_cast<size_t>(n)), ecol(static_cast<size_t>(n) * maxl, 0);
+        std::vector<double> eval(static_cast<size_t>(n) * maxl, 0.0);
+        std::vector<float> eval32(static_cast<size_t>(n) * maxl, 0.0f);
+        for (int64_t i = 0; i < n; i++) {
+            len[static_cast<size_t>(i)] = static_cast<int32_t>(row_ptr[i + 1] - row_ptr[i]);
+            for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+                const int32_t c = col[k];
+                if (c < 0 || c >= n) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "column out of range"};
+                const size_t e = static_cast<size_t>(k - row_ptr[i]) * n + i;
+                ecol[e] = c;
+                eval[e] = val[k];
+                eval32[e] = static_cast<float>(val[k]);
+            }
+        }
+        ScopedBuffers loc;
+        const size_t nn = static_cast<size_t>(n);
+        CgOperands o{};
+        o.n = static_cast<int32_t>(n);
+        int32_t* dlen = loc.get<int32_t>(nn);
+        int32_t* dcol = loc.get<int32_t>(nn * maxl);
+        double* dval = loc.get<double>(nn * maxl);
+        float* dval32 = loc.get<float>(nn * maxl);
+        double* db = loc.get<double>(nn);
+        double* dx = loc.get<double>(nn);
+        o.len = dlen;
+        o.col = dcol;
+        o.val = dval;
+        o.val32 = dval32;
+        o.b = db;
+        o.x = dx;
+        o.r = loc.get<double>(nn);
+        o.p = loc.get<double>(nn);
+        o.Ap = loc.get<double>(nn);
+        o.r32 = loc.get<float>(nn);
+        o.p32 = loc.get<float>(nn);
+        o.q32 = loc.get<float>(nn);
+        o.d32 = loc.get<float>(nn);
+        o.partials = loc.get<double>(2 * static_cast<size_t>(grid_for(n)) + 64);
+        o.S = loc.get<CgScalars>(1);
+        cudaStream_t s = h->stream;
+        check(cudaMemcpyAsync(dlen, len.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemcpyAsync(dcol, ecol.data(), sizeof(int32_t) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemcpyAsync(dval, eval.data(), sizeof(double) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemcpyAsync(dval32, eval32.data(), sizeof(float) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemcpyAsync(db, b, sizeof(double) * nn, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemcpyAsync(dx, x, sizeof(double) * nn, cudaMemcpyHostToDevice, s), "up");
+        check(cudaMemsetAsync(o.S, 0, sizeof(CgScalars), s), "memset");
+        check(cudaMemsetAsync(o.d32, 0, sizeof(float) * nn, s), "memset");
+        launch_cg_configure(o.S, eps, criterion, max_iters > 0 ? max_iters : static_cast<int>(n), 0.01, s);
+        CgGraph g;
+        check(g.build(solver, o, s), "CG graph build");
+        check(g.launch(s), "CG graph launch");
+        CgScalars S{};
+        check(cudaMemcpyAsync(x, dx, sizeof(double) * nn, cudaMemcpyDeviceToHost, s), "down");
+        check(cudaMemcpyAsync(&S, o.S, sizeof(S), cudaMemcpyDeviceToHost, s), "down");
+        check(cudaStreamSynchronize(s), "cg solve");
+        if (iterations) *iterations = S.iter;
+        if (true_relres) *true_relres = (S.bb > 0) ? std::sqrt(S.true_rr / S.bb) : std::sqrt(S.true_rr);
+        h->stats.kernel_launches += 3 + S.iter * g.kernels_per_iteration();
+        if (!S.converged)
+            throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
+                              "Conjugate Gradient method couldn't solve Pressure Poison Equation"};
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,510 @@
+// stages.cu - the per-particle stages of Computer::ForwardTime (Computer.hpp:1700-1742):
+// number density, error-compensating source, explicit forces, PPE right-hand side and
+// matrix assembly, pressure assignment, midpoint pressure gradient, dynamic
+// stabilisation and the CFL time step.
+//
+// One thread per particle walks its neighbour row in reference order and accumulates
+// exactly like AccumulateNeighbor (Computer.hpp:618-695): the filter r^2 < r_e^2 on
+// current positions, the terms in list order, the SPP virtual particle last.  Every
+// formula keeps the reference's expression order and this file is compiled with
+// -fmad=false, so each result is bit-identical to the FP64 CPU path.
+#include "common.cuh"
+
+namespace mpsgb {
+
+namespace {
+
+__device__ __forceinline__ bool is_surface(const SceneConst& sc, double nd) {
+    return __ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
+}
+
+// The SPP virtual particle of AccumulateNeighbor (Computer.hpp:664-692).  (gx, gz)
+// holds sum W(r) dx over the neighbours within `radius`.
+__device__ __forceinline__ bool spp_particle(const SceneConst& sc, const DeviceState& st, int i,
+                                             double radius, double gx, double gz, double& xs,
+                                             double& zs) {
+    const double thisN = st.n_wo_spp[i];
+    gx = __ddiv_rn(gx, sc.n0);
+    gz = __ddiv_rn(gz, sc.n0);
+    if (thisN < sc.n0) {
+        const double r_g = __dsqrt_rn(dot2(gx, gz, gx, gz));
+        if (r_g > 2.220446049250313080847e-16) {  // std::numeric_limits<double>::epsilon()
+            const double w_spp = __dadd_rn(sc.n0, -thisN);
+            const double r_spp = __ddiv_rn(radius, __dadd_rn(w_spp, 1.0));
+            const double s = __ddiv_rn(r_spp, r_g);
+            xs = __dadd_rn(st.x[i], -__dmul_rn(s, gx));
+            zs = __dadd_rn(st.z[i], -__dmul_rn(s, gz));
+            return true;
+        }
+    }
+    return false;
+}
+
+// NeighborDensityVariationSpeed (Computer.hpp:838-872)
+__device__ double density_variation(const SceneConst& sc, const DeviceState& st, int i,
+                                    double dt) {
+    if (has_flag(sc.flags, MPS_FLAG_HS)) {
+        if (has_flag(sc.flags, MPS_FLAG_SPP) && st.n_wo_spp[i] < sc.n0) return 0.0;
+        const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
+        const int cnt = st.nb_count[i];
+        double sum = 0.0;
+        for (int k = 0; k < cnt; k++) {
+            const int j = st.nb[ell(k, sc.n, i)];
+            const double dx = st.x[j] - xi;
+            const double dz = st.z[j] - zi;
+            const double r2 = dot2(dx, dz, dx, dz);
+            if (r2 < sc.re2) {
+                const double du = st.u[j] - ui;
+                const double dw = st.w[j] - wi;
+                const double r = __dsqrt_rn(r2);
+                sum += dot2(dx, dz, du, dw) / (r * r * r);
+            }
+        }
+        return -sc.re * sum;
+    }
+    return (st.nd[i] - sc.n0) / dt;
+}
+
+// viscosity coefficient (Computer.hpp:963-970) at the Laplacian radius
+__device__ __forceinline__ double viscosity_coefficient(const SceneConst& sc, double r) {
+    if (has_flag(sc.flags, MPS_FLAG_HL)) return sc.nu * 3.0 * sc.re_lap / sc.n0_lap / (r * r * r);
+    const double wgt = weight(r, sc.re_lap);
+    return sc.nu * 2 * 2.0 / sc.lambda_lap / sc.n0_lap * wgt;
+}
+
+// PPE off-diagonal coefficient (Computer.hpp:1290-1297)
+__device__ __forceinline__ double ppe_coefficient(const SceneConst& sc, double r) {
+    if (has_flag(sc.flags, MPS_FLAG_HL)) return 3.0 * sc.re_lap / sc.n0_lap / (r * r * r);
+    const double wgt = weight(r, sc.re_lap);
+    return (4.0 / sc.lambda_lap / sc.n0_lap) * wgt;
+}
+
+__device__ __forceinline__ bool ppe_alive(const SceneConst& sc, const DeviceState& st, int i) {
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return false;
+    if (!has_flag(sc.flags, MPS_FLAG_SPP) && is_surface(sc, st.nd[i])) return false;
+    return true;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_set_dt(DeviceState st, double dt) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st.step->dt = dt;  // Computer.hpp:1703-1706
+        st.step->t = st.step->t + dt;
+    }
+}
+
+// DetermineDt (Computer.hpp:759-777), part 1: max |u|^2 over all particles.
+__global__ void k_max_speed(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < sc.n) v = dot2(st.u[i], st.w[i], st.u[i], st.w[i]);
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0.0)
+        atomicMax(&st.step->max_u2_bits, static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+// part 2: dt = maxU == 0 ? MaxDt : min(MaxDx / maxU, MaxDt); then t += dt.
+__global__ void k_cfl_dt(SceneConst sc, DeviceState st) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double u2 = __longlong_as_double(static_cast<long long>(st.step->max_u2_bits));
+        const double maxU = __dsqrt_rn(u2);
+        double dt;
+        if (maxU == 0) {
+            dt = sc.max_dt;
+        } else {
+            const double a = sc.max_dx / maxU;
+            dt = (sc.max_dt < a) ? sc.max_dt : a;
+        }
+        st.step->dt = dt;
+        st.step->t = st.step->t + dt;
+        st.step->max_u2_bits = 0ull;
+    }
+}
+
+// ComputeNeighborDensities (Computer.hpp:780-833)
+__global__ void k_density(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    if (spp) st.n_wo_spp[i] = sc.n0;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
+    const double xi = st.x[i], zi = st.z[i];
+    const int cnt = st.nb_count[i];
+    double thisN = 0.0;
+    for (int k = 0; k < cnt; k++) {
+        const int j = st.nb[ell(k, sc.n, i)];
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        if (r2 < sc.re2) thisN += weight(__dsqrt_rn(r2), sc.re);
+    }
+    if (spp) {
+        st.n_wo_spp[i] = thisN;
+        st.nd[i] = (thisN < sc.n0) ? sc.n0 : thisN;  // std::max(thisN, n0)
+    } else {
+        st.nd[i] = thisN;
+    }
+}
+
+// ComputeErrorCorrection (Computer.hpp:877-910)
+__global__ void k_error_correction(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
+    const double speed = density_variation(sc, st, i, st.step->dt);
+    const double error = (st.nd[i] - sc.n0) / sc.n0;
+    st.ecs[i] = fabs(error) * speed + fabs(speed) * error;
+}
+
+__global__ void k_density_variation(SceneConst sc, DeviceState st, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    const int t = st.type[i];
+    out[i] = (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED)
+                 ? 0.0
+                 : density_variation(sc, st, i, st.step->dt);
+}
+
+// ComputeExplicitForces, first loop (Computer.hpp:935-990): a = viscosity + g.
+__global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    if (st.type[i] != MPS_TYPE_FLUID) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
+    const int cnt = st.nb_count[i];
+    double vx = 0.0, vz = 0.0, gx = 0.0, gz = 0.0;
+    for (int k = 0; k < cnt; k++) {
+        const int j = st.nb[ell(k, sc.n, i)];
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        if (r2 < sc.rl2) {
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double c = viscosity_coefficient(sc, __dsqrt_rn(r2));
+                vx += c * (st.u[j] - ui);
+                vz += c * (st.w[j] - wi);
+            } else {
+                vx = __dadd_rn(vx, 0.0);
+                vz = __dadd_rn(vz, 0.0);
+            }
+            if (spp) {
+                const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    }
+    double xs, zs;
+    if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
+        const double ddx = xi - xs, ddz = zi - zs;
+        const double c = viscosity_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        vx += c * (ui - ui);
+        vz += c * (wi - wi);
+    }
+    st.dux[i] = __dadd_rn(vx, 0.0);  // a += G, G = (0, -g) (Environment.hpp:149)
+    st.duz[i] = vz + (-sc.g);
+}
+
+// ComputeExplicitForces, second loop (Computer.hpp:995-1020).
+__global__ void k_explicit_update(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const double dt = st.step->dt;
+    if (st.type[i] == MPS_TYPE_FLUID) {
+        const double u = st.u[i] + st.dux[i] * dt;
+        const double w = st.w[i] + st.duz[i] * dt;
+        st.u[i] = u;
+        st.w[i] = w;
+        st.x[i] = st.x[i] + u * dt;
+        st.z[i] = st.z[i] + w * dt;
+    } else {
+        const double nx = st.wall_x[i], nz = st.wall_z[i];
+        st.u[i] = (nx - st.x[i]) / dt;
+        st.w[i] = (nz - st.z[i]) / dt;
+        st.x[i] = nx;
+        st.z[i] = nz;
+    }
+}
+
+// SaveX (Computer.hpp:1025-1039)
+__global__ void k_save_x(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
+    st.ox[i] = st.x[i];
+    st.oz[i] = st.z[i];
+}
+
+// SetPressurePoissonEquation (Computer.hpp:1145-1328): right-hand side, initial guess
+// and one matrix row per particle in neighbour order (diagonal last) into the
+// scratch ELL arrays.
+__global__ void k_ppe_build(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const int n = sc.n;
+    if (!ppe_alive(sc, st, i)) {
+        st.ppe_b[i] = 0;
+        st.ppe_x[i] = 0;
+        st.ppe_col_tmp[ell(0, n, i)] = i;
+        st.ppe_val_tmp[ell(0, n, i)] = 1.0;
+        st.ppe_len[i] = 1;
+        return;
+    }
+    const double dt = st.step->dt;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    const double speed = density_variation(sc, st, i, dt);
+    if (has_flag(sc.flags, MPS_FLAG_ECS)) {
+        const double e = st.ecs[i];
+        st.ppe_b[i] = -sc.rho / (sc.n0 * dt) * (speed + e);
+    } else {
+        st.ppe_b[i] = -sc.rho / (sc.n0 * dt) * speed;
+    }
+    st.ppe_x[i] = st.p[i];
+
+    const double xi = st.x[i], zi = st.z[i];
+    const int cnt = st.nb_count[i];
+    double a_ii = 0.0, gx = 0.0, gz = 0.0;
+    int m = 0;
+    for (int k = 0; k < cnt; k++) {
+        const int j = st.nb[ell(k, n, i)];
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        if (r2 < sc.rl2) {
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double a_ij = ppe_coefficient(sc, __dsqrt_rn(r2));
+                if (spp || !is_surface(sc, st.nd[j])) {
+                    st.ppe_col_tmp[ell(m, n, i)] = j;
+                    st.ppe_val_tmp[ell(m, n, i)] = a_ij;
+                    m++;
+                }
+                a_ii += -a_ij;
+            } else {
+                a_ii = __dadd_rn(a_ii, 0.0);
+            }
+            if (spp) {
+                const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    }
+    double xs, zs;
+    if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
+        const double ddx = xi - xs, ddz = zi - zs;
+        a_ii += -ppe_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+    }
+    st.ppe_col_tmp[ell(m, n, i)] = i;
+    st.ppe_val_tmp[ell(m, n, i)] = a_ii;
+    st.ppe_len[i] = m + 1;
+}
+
+// Row entries to ascending column order (uBLAS compressed_matrix, Computer.hpp:1330-1350):
+// each entry goes to its rank among the row's columns (columns are distinct).
+__global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const int n = sc.n;
+    const int len = st.ppe_len[i];
+    for (int e = 0; e < len; e++) {
+        const int ce = st.ppe_col_tmp[ell(e, n, i)];
+        int rank = 0;
+        for (int f = 0; f < len; f++) rank += (st.ppe_col_tmp[ell(f, n, i)] < ce) ? 1 : 0;
+        const double v = st.ppe_val_tmp[ell(e, n, i)];
+        st.ppe_col[ell(rank, n, i)] = ce;
+        st.ppe_val[ell(rank, n, i)] = v;
+        if (want_fp32) st.ppe_val32[ell(rank, n, i)] = __double2float_rn(v);
+    }
+}
+
+// ComputeImplicitForces pressure assignment (Computer.hpp:1076-1097)
+__global__ void k_assign_pressure(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (solve_failed(sc, st)) return;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
+    const double v = st.ppe_x[i];
+    const bool surface = !has_flag(sc.flags, MPS_FLAG_SPP) && is_surface(sc, st.nd[i]);
+    st.p[i] = ((v < 0) || surface) ? 0.0 : v;
+}
+
+// ModifyByPressureGradient, midpoint branch (Computer.hpp:1501-1521): du only.
+__global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (solve_failed(sc, st)) return;
+    if (st.type[i] != MPS_TYPE_FLUID) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    const double dt = st.step->dt;
+    const double factor = -dt / sc.rho * 2.0 / sc.n0;
+    const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
+    const int cnt = st.nb_count[i];
+    double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
+    for (int k = 0; k < cnt; k++) {
+        const int j = st.nb[ell(k, sc.n, i)];
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        if (r2 < sc.re2) {
+            const double wg = weight(__dsqrt_rn(r2), sc.re);
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double c = (st.p[j] + pi) / r2 * wg;
+                sx += c * dx;
+                sz += c * dz;
+            } else {
+                sx = __dadd_rn(sx, 0.0);
+                sz = __dadd_rn(sz, 0.0);
+            }
+            if (spp) {
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    }
+    double xs, zs;
+    if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
+        const double dx = xs - xi;
+        const double dz = zs - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        const double c = (0.0 + pi) / r2 * weight(__dsqrt_rn(r2), sc.re);
+        sx += c * dx;
+        sz += c * dz;
+    }
+    st.dux[i] = factor * sx;
+    st.duz[i] = factor * sz;
+}
+
+// DynamicStabilize (Computer.hpp:1568-1635): du only.
+__global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (solve_failed(sc, st)) return;
+    if (st.type[i] != MPS_TYPE_FLUID) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    const double dt = st.step->dt;
+    const double d = sc.l0 - sc.max_dx;
+    const double d2 = d * d;
+    const double factor = -1.0 / (2 * dt * sc.n0);
+    const double xi = st.x[i], zi = st.z[i], oxi = st.ox[i], ozi = st.oz[i];
+    const int cnt = st.nb_count[i];
+    double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
+    for (int k = 0; k < cnt; k++) {
+        const int j = st.nb[ell(k, sc.n, i)];
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        if (r2 < sc.re2) {
+            if (st.type[j] != MPS_TYPE_DUMMY && r2 < d2) {
+                const double dx0 = st.ox[j] - oxi;
+                const double dz0 = st.oz[j] - ozi;
+                const double nrm = __dsqrt_rn(dot2(dx0, dz0, dx0, dz0));
+                const double ex = dx0 / nrm;
+                const double ez = dz0 / nrm;
+                const double r_par = dot2(dx, dz, ex, ez);
+                const double px = dx - r_par * ex;
+                const double pz = dz - r_par * ez;
+                const double r_perp2 = dot2(px, pz, px, pz);
+                const double mag = __dsqrt_rn(d2 - r_perp2) - r_par;
+                sx += mag * ex;
+                sz += mag * ez;
+            } else {
+                sx = __dadd_rn(sx, 0.0);
+                sz = __dadd_rn(sz, 0.0);
+            }
+            if (spp) {
+                const double wg = weight(__dsqrt_rn(r2), sc.re);
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    }
+    double xs, zs;
+    if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
+        sx = __dadd_rn(sx, 0.0);  // the virtual particle is excluded (Computer.hpp:1597-1598)
+        sz = __dadd_rn(sz, 0.0);
+    }
+    st.dux[i] = factor * sx;
+    st.duz[i] = factor * sz;
+}
+
+// u += du; x += du dt for fluid particles (Computer.hpp:1543-1563, :1637-1655)
+__global__ void k_apply_du(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (solve_failed(sc, st)) return;
+    if (st.type[i] != MPS_TYPE_FLUID) return;
+    const double dt = st.step->dt;
+    const double dx = st.dux[i], dz = st.duz[i];
+    st.u[i] = st.u[i] + dx;
+    st.w[i] = st.w[i] + dz;
+    st.x[i] = st.x[i] + dx * dt;
+    st.z[i] = st.z[i] + dz * dt;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_set_dt(const SceneConst&, const DeviceState& st, double dt, cudaStream_t s) {
+    k_set_dt<<<1, 32, 0, s>>>(st, dt);
+}
+
+void launch_cfl_dt(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_max_speed<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_cfl_dt<<<1, 32, 0, s>>>(sc, st);
+}
+
+void launch_density(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_density<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_error_correction(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_error_correction<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_density_variation(const SceneConst& sc, const DeviceState& st, double* out,
+                              cudaStream_t s) {
+    k_density_variation<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, out);
+}
+
+void launch_explicit(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_explicit_accel<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_explicit_update<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_save_x<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
+    k_ppe_build<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_ppe_sort<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, want_fp32 ? 1 : 0);
+}
+
+void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_assign_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_pressure_gradient<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_dynamic_stabilize<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+}  // namespace mpsgb

@@ -1,0 +1,76 @@
+/*
+ * mps_oracle.h - C API of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+ *
+ * The oracle is a plain C++ restatement of OpenMps's time step
+ * (src/OpenMps/Computer.hpp, Grid.hpp, Environment.hpp, Particle.hpp) used to
+ * check the CUDA path.  Only the tests, the smoke check and the CPU-baseline
+ * legs of bench.py load it; the product library never links or calls it.
+ *
+ * Entry points mirror include/mps.h with an `oracle_` prefix.
+ */
+#ifndef OPENMPS_GB300_ORACLE_H
+#define OPENMPS_GB300_ORACLE_H
+
+#include "../include/mps.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_handle oracle_handle;
+
+int oracle_create(const mps_params* prm, oracle_handle** out);
+void oracle_destroy(oracle_handle* h);
+const char* oracle_last_error(const oracle_handle* h);
+int oracle_num_threads(void);
+
+int oracle_add_particles(oracle_handle* h, int64_t n, const int32_t* type, const double* x,
+                         const double* z, const double* u, const double* w, const double* p,
+                         const double* nd);
+int64_t oracle_particle_count(const oracle_handle* h);
+int oracle_get_particles(const oracle_handle* h, int32_t* type, double* x, double* z, double* u,
+                         double* w, double* p, double* nd);
+int oracle_set_particles(oracle_handle* h, const int32_t* type, const double* x, const double* z,
+                         const double* u, const double* w, const double* p, const double* nd);
+int oracle_set_wall_positions(oracle_handle* h, const double* wx, const double* wz);
+int oracle_set_solver(oracle_handle* h, int32_t criterion, double eps, int32_t max_iters);
+
+int oracle_forward_time(oracle_handle* h, double dt);
+int oracle_get_environment(const oracle_handle* h, mps_environment* env);
+int oracle_get_stats(const oracle_handle* h, int32_t* cg_iterations, double* rr0, double* rr,
+                     int64_t* ppe_nnz, int64_t* neighbor_total);
+
+int oracle_stage_begin_step(oracle_handle* h, double dt);
+int oracle_stage_search_neighbor(oracle_handle* h);
+int oracle_stage_density(oracle_handle* h);
+int oracle_stage_error_correction(oracle_handle* h);
+int oracle_stage_explicit(oracle_handle* h);
+int oracle_stage_save_x(oracle_handle* h);
+int oracle_stage_set_ppe(oracle_handle* h);
+int oracle_stage_solve_ppe(oracle_handle* h);
+int oracle_stage_assign_pressure(oracle_handle* h);
+int oracle_stage_pressure_gradient(oracle_handle* h);
+int oracle_stage_dynamic_stabilize(oracle_handle* h);
+int oracle_stage_density_variation(oracle_handle* h, double* speed);
+double oracle_determine_dt(oracle_handle* h);
+
+int oracle_get_neighbors(const oracle_handle* h, int32_t* counts, int32_t* list, int64_t capacity,
+                         int64_t* total);
+int oracle_get_ppe(const oracle_handle* h, int64_t* row_ptr, int32_t* col, double* val, double* b,
+                   double* x, int64_t capacity, int64_t* nnz);
+int oracle_set_ppe_x(oracle_handle* h, const double* x);
+int oracle_get_aux(const oracle_handle* h, double* n_without_spp, double* ecs, double* ox,
+                   double* oz);
+int oracle_set_aux(oracle_handle* h, const double* n_without_spp, const double* ecs,
+                   const double* ox, const double* oz);
+
+/* Reference CG (Computer.hpp:1359-1429) on a caller CSR system; x: guess in, solution out. */
+int oracle_cg_solve_csr(int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val,
+                        const double* b, double* x, double eps, int32_t criterion,
+                        int32_t max_iters, int32_t* iterations, double* rr0, double* rr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,97 @@
+"""Shared helpers of the parity tests: paired GPU / oracle scenes and comparisons."""
+from __future__ import annotations
+
+import numpy as np
+
+from openmps_gb300 import _abi as abi
+from openmps_gb300 import scenes
+
+FIELDS = ("x", "z", "u", "w", "p", "n")
+
+
+def make_pair(scene, params, openmp=False):
+    """The same particles in a GPU Computer and in the CPU oracle."""
+    from openmps_gb300.computer import Computer
+    from oracle.oracle import Oracle
+
+    gpu = Computer(params)
+    gpu.add_scene(scene)
+    cpu = Oracle(params, openmp=openmp)
+    cpu.add_scene(scene)
+    return gpu, cpu
+
+
+def copy_state(src_cpu, dst_gpu):
+    """Copies particles and auxiliary arrays from the oracle into the GPU handle."""
+    P = src_cpu.particles()
+    dst_gpu.set_particles(P["type"], *[P[k] for k in FIELDS])
+    A = src_cpu.aux()
+    dst_gpu.set_aux(A["n_without_spp"], A["ecs"], A["ox"], A["oz"])
+
+
+def assert_same_particles(gpu, cpu, fields=FIELDS, what=""):
+    G = gpu.particles()
+    C = cpu.particles()
+    np.testing.assert_array_equal(G["type"], C["type"], err_msg="type " + what)
+    for k in fields:
+        np.testing.assert_array_equal(G[k], C[k], err_msg="%s %s" % (k, what))
+
+
+def assert_same_neighbors(gpu, cpu, what=""):
+    gc, gl = gpu.neighbors()
+    cc, cl = cpu.neighbors()
+    alive = cpu.particles()["type"] != abi.TYPE_DISABLED
+    np.testing.assert_array_equal(gc[alive], cc[alive], err_msg="neighbour counts " + what)
+    assert gl.size == cl.size, what
+    np.testing.assert_array_equal(gl, cl, err_msg="neighbour lists " + what)
+
+
+def assert_same_ppe(gpu, cpu, what=""):
+    grp, gcol, gval, gb, gx = gpu.ppe()
+    crp, ccol, cval, cb, cx = cpu.ppe()
+    np.testing.assert_array_equal(grp, crp, err_msg="row_ptr " + what)
+    np.testing.assert_array_equal(gcol, ccol, err_msg="columns " + what)
+    np.testing.assert_array_equal(gval, cval, err_msg="values " + what)
+    np.testing.assert_array_equal(gb, cb, err_msg="rhs " + what)
+    np.testing.assert_array_equal(gx, cx, err_msg="initial guess " + what)
+
+
+def rel_err(a, b, scale=None):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    s = np.max(np.abs(b)) if scale is None else scale
+    if s == 0:
+        return float(np.max(np.abs(a - b)))
+    return float(np.max(np.abs(a - b)) / s)
+
+
+# --------------------------------------------------------- small test scenes
+def reference_tank(l0=0.008):
+    """Stock-preset tank in the Sample.xml spirit (r_e = 2.4 l0, 1 wall + 3 dummy layers)."""
+    s = scenes.dam_break(l0, water_w=19 * l0, water_h=37 * l0, tank_w=73 * l0, tank_h=45 * l0,
+                         wall_layers=1, dummy_layers=3)
+    s.meta["params"] = dict(re_by_l0=2.4, flags=abi.PRESET_REFERENCE, eps=1e-10, max_dt=5e-4,
+                            rho=998.2, nu=1.004e-6, surface_ratio=0.97)
+    s.meta["dt"] = 5e-4
+    return s
+
+
+def plain_tank(l0=0.01, ds=False):
+    s = scenes.config_c0() if l0 == 0.01 else scenes.dam_break(l0)
+    s.meta.setdefault("params", dict(scenes.PLAIN_PHYSICS, eps=1e-10, max_dt=5e-4))
+    if ds:
+        s.meta["params"]["flags"] = abi.FLAG_DS
+    s.meta["dt"] = 5e-4
+    return s
+
+
+def jittered_tank(l0=0.01, jitter=0.05, seed=7, preset=abi.PRESET_PLAIN):
+    """Hydrostatic-style tank with seeded lattice jitter (breaks lattice ties)."""
+    s = scenes.tank(l0, 30, 20, 30, 30, jitter=jitter, seed=seed)
+    params = dict(scenes.PLAIN_PHYSICS, eps=1e-10, max_dt=5e-4)
+    params["flags"] = preset
+    if preset == abi.PRESET_REFERENCE:
+        params.update(re_by_l0=2.4, re_lap_by_l0=0.0)
+    s.meta["params"] = params
+    s.meta["dt"] = 5e-4
+    return s
