@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of the 320k-fluid-particle 2D dam break on GB300.
+
+Workload (one "step" = one ``ForwardTime(dt)`` of the whole scene): a 0.2 m x
+0.4 m water column at l0 = 5e-4 m (320,000 fluid particles) in a 0.8 m x 0.6 m
+tank with 3 wall + 2 dummy layers (340,050 particles in all), plain MPS with
+r_e = 2.1 l0 for density/gradient and 4.0 l0 for the Laplacian (PPE with ~45
+nonzeros per row), dt = 2.5e-5 s, PPE solved to |b - A x| <= 1e-8 |b|.  The data
+are synthetic (seeded lattice scene); the state and the CSR/ELL matrix exceed L2,
+and L2 is also flushed (512 MiB write) between timed steps.
+
+Output: one JSON line.  ``value`` is whole-job particle-steps/s with the state
+resident in HBM (CUDA events on the library's stream around each step); ``e2e``
+is the same metric through the public C ABI with host buffers (host-to-device
+copy of the full particle state, the step, device-to-host copy of the result);
+``roofline`` reports the PPE solver's SpMV kernel (the dominant kernel) against
+the measured HBM bandwidth; ``cpu_baseline`` times the CPU restatement of the
+reference step (OpenMP, all host cores) on a bounded sample of the same scene.
+
+``--impl reference`` times that CPU path alone (rank 0 only) on the same
+workload and metric.  With ``--gpus N`` (one process per GPU under torchrun)
+every rank advances its own independent replica of the scene (replicas only: the
+step has no data-parallel exchange), and ``value`` sums all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, 320k dam break"
+UNIT = "particle-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+FLUSH_BYTES = 512 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--solver", choices=("cg64", "mixed"), default="mixed")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0,
+                    help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+# --------------------------------------------------------------- clock sampler
+class ClockSampler:
+    """Samples SM clock and throttle reasons with nvidia-smi during a timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power = [], [], []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(scene, params, dt, budget_s: float, max_steps: int | None = None) -> dict:
+    """The CPU restatement of the reference step (OpenMP, all host threads)."""
+    from oracle import build_oracle
+    from oracle import oracle as orc
+
+    build_oracle.build()
+    o = orc.Oracle(params, openmp=True)
+    o.add_scene(scene)
+    threads = orc.num_threads(True)
+    times = []
+    n_active = scene.count
+    t_all = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        o.forward_time(dt)
+        times.append(time.perf_counter() - t0)
+        if max_steps is not None and len(times) >= max_steps:
+            break
+        if time.perf_counter() - t_all + times[-1] > budget_s or len(times) >= 50:
+            break
+    n_active = int((o.particles()["type"] != 3).sum())
+    sec = sum(times)
+    return {"value": n_active * len(times) / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d step(s) of the same scene from its initial state (%.1f s of CPU time), "
+                      "CG iterations of the last step %d" % (len(times), sec,
+                                                            o.stats()["cg_iterations"]),
+            "seconds_per_step": sec / len(times)}
+
+
+def load_peak() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_traffic(key: str):
+    """DRAM bytes per launch of the SpMV kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        return data.get(key)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world, local_rank):
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import build as gpu_build
+    from openmps_gb300 import scenes
+    from openmps_gb300.computer import Computer
+
+    gpu_build.build()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist  # noqa: F811
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    solver = abi.SOLVER_MIXED if args.solver == "mixed" else abi.SOLVER_CG64
+    scene = scenes.config_c2()
+    dt = scene.meta["dt"]
+    params = scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8)
+    comp = Computer(params, device=local_rank)
+    comp.add_scene(scene)
+
+    for _ in range(max(args.warmup, 0)):
+        comp.forward_time(dt)
+    n_active = comp.count - comp.stats()["disabled"]
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident timed region
+    sampler = ClockSampler(local_rank)
+    launches0 = comp.stats()["kernel_launches"]
+    iters = []
+    barrier()
+    comp.synchronize()
+    sampler.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        comp.flush_l2(FLUSH_BYTES)
+        comp.event_record(0)
+        comp.forward_time(dt)
+        comp.event_record(1)
+        total_ms += comp.event_elapsed(0, 1)
+        iters.append(comp.stats()["cg_iterations"])
+    comp.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    launches = comp.stats()["kernel_launches"] - launches0
+    n_active = comp.count - comp.stats()["disabled"]
+    relres = comp.stats()["cg_true_relres"]
+
+    # ---- end to end through the C ABI with pinned host buffers
+    try:
+        import torch
+
+        pin = lambda n, dt_: torch.empty(n, dtype=dt_, pin_memory=True).numpy()
+        import numpy as np
+
+        host = {"type": pin(comp.count, torch.int32)}
+        for k in ("x", "z", "u", "w", "p", "n"):
+            host[k] = pin(comp.count, torch.float64)
+        pinned = True
+    except Exception:  # torch missing or no pinned memory: pageable host arrays
+        import numpy as np
+
+        host = {"type": np.empty(comp.count, dtype=np.int32)}
+        for k in ("x", "z", "u", "w", "p", "n"):
+            host[k] = np.empty(comp.count)
+        pinned = False
+    order = ("type", "x", "z", "u", "w", "p", "n")
+    comp.get_particles_into(*[host[k] for k in order])
+    h2d = d2h = sum(host[k].nbytes for k in order)
+    barrier()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        comp.flush_l2(FLUSH_BYTES)
+        comp.event_record(2)
+        comp.set_particles(*[host[k] for k in order])
+        comp.forward_time(dt)
+        comp.get_particles_into(*[host[k] for k in order])
+        comp.event_record(3)
+        e2e_ms += comp.event_elapsed(2, 3)
+    barrier()
+
+    # ---- stage breakdown (one extra step with per-stage events)
+    comp.set_stage_timing(True)
+    comp.forward_time(dt)
+    stage_ms = {k: round(v, 3) for k, v in comp.stats()["stage_ms"].items()}
+    comp.set_stage_timing(False)
+
+    # ---- roofline of the dominant kernel (the solver's SpMV), timed alone
+    st = comp.stats()
+    nnz = st["ppe_nnz"]
+    n = comp.count
+    spmv_ms = comp.bench_spmv(solver, reps=20, flush_bytes=FLUSH_BYTES)
+    if solver == abi.SOLVER_CG64:
+        alg_bytes = 12 * nnz + 4 * (n + 1) + 16 * n
+        key = "cg64"
+    else:
+        alg_bytes = 8 * nnz + 4 * (n + 1) + 8 * n
+        key = "mixed"
+    spmv64_ms = comp.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
+    peak, peak_kind = load_peak()
+    achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
+    traffic = load_traffic(key)
+
+    # ---- reduce over ranks (max time)
+    t_steps = total_ms
+    t_e2e = e2e_ms
+    if dist is not None:
+        import torch
+
+        buf = torch.tensor([t_steps, t_e2e], dtype=torch.float64, device="cuda")
+        dist.all_reduce(buf, op=dist.ReduceOp.MAX)
+        t_steps, t_e2e = buf.tolist()
+    value = n_active * args.steps * world / (t_steps * 1e-3)
+    e2e_value = n_active * args.steps * world / (t_e2e * 1e-3)
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_steps / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if solver == abi.SOLVER_CG64 else "f64 (PPE iterations f32, f64 residual/refinement)",
+        "data": "synthetic (seeded lattice dam break)",
+        "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
+                               "plain MPS, re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
+                   "particles": n, "active_particles": n_active, "ppe_nnz": nnz,
+                   "solver": args.solver, "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
+                   "l2": "flushed between timed steps (512 MiB write); working set > L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "impl": "ours",
+        "cg_iterations_per_step": statistics.mean(iters) if iters else None,
+        "ppe_true_relres": relres,
+        "stage_ms": stage_ms,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "pinned_host_buffers": pinned},
+        "roofline": {"bound": "hbm", "kernel": "k_%s_spmv_dot" % ("cg" if key == "cg64" else "mx"),
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": spmv_ms,
+                     "spmv64_ms_per_launch": spmv64_ms,
+                     "spmv64_achieved_gbs": (12 * nnz + 4 * (n + 1) + 16 * n) / (spmv64_ms * 1e-3) / 1e9},
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(scene, scene.params(criterion=abi.CRIT_RHS, eps=1e-8), dt,
+                                            args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    """The CPU restatement of the reference step (OpenMP, all host threads)."""
+    if rank != 0:
+        return
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import scenes
+
+    scene = scenes.config_c2()
+    dt = scene.meta["dt"]
+    params = scene.params(criterion=abi.CRIT_RHS, eps=1e-8)
+    steps = max(1, min(args.steps, 5))
+    cb = cpu_baseline(scene, params, dt, budget_s=1e9, max_steps=steps)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": 0, "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lattice dam break)",
+        "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
+                               "plain MPS, re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
+                   "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
+                   "note": "the reference (header-only C++ with Boost/ViennaCL) cannot be built here; "
+                           "this arm runs its C++ restatement with OpenMP"},
+        "impl": "reference",
+        "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                         "sample": cb["sample"]},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -67,6 +67,12 @@ extern "C" {
 #define MPS_SOLVER_MIXED 1  /* FP32 inner CG + FP64 true residual / iterative refinement */
 #define MPS_SOLVER_LEARNED 2 /* MIXED with the learned initial guess + preconditioner scale */
 
+/* How the CG loop is launched: one CUDA graph with a device-driven while loop, or
+ * host-launched kernel batches (the same kernels; for profilers that cannot see
+ * kernels inside conditional graphs). */
+#define MPS_CG_LAUNCH_GRAPH 0
+#define MPS_CG_LAUNCH_HOST 1
+
 /* CG stopping rule */
 #define MPS_CRIT_INITIAL_RESIDUAL 0 /* reference: r_k.r_k < eps^2 r_0.r_0 (Computer.hpp:1386, :1408) */
 #define MPS_CRIT_RHS 1              /* |b - A x| <= eps |b| */
@@ -95,7 +101,7 @@ typedef struct mps_params {
     int32_t max_cg_iters; /* <= 0: number of unknowns, as the reference (Computer.hpp:1392) */
     double inner_tol;     /* MIXED: relative residual reduction of one FP32 inner solve */
     int32_t max_refinements; /* MIXED: maximum FP64 refinement passes */
-    int32_t reserved0;
+    int32_t cg_launch;       /* MPS_CG_LAUNCH_GRAPH (default) or MPS_CG_LAUNCH_HOST */
     double reserved[6];
 } mps_params;
 
@@ -195,6 +201,12 @@ int mps_event_record(mps_handle* h, int32_t slot);
 int mps_event_elapsed(mps_handle* h, int32_t begin, int32_t end, float* ms);
 /* Writes `bytes` of scratch on the handle's stream (evicts L2 between timed runs). */
 int mps_flush_l2(mps_handle* h, int64_t bytes);
+/* Times the PPE solver's SpMV kernel alone on the last assembled matrix: `reps`
+ * back-to-back launches (FP64 values for MPS_SOLVER_CG64, FP32 for MPS_SOLVER_MIXED);
+ * *ms_per_launch receives the mean CUDA-event time of one launch.  When flush_bytes
+ * > 0, L2 is flushed before every launch and only the launch is timed. */
+int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_bytes,
+                   float* ms_per_launch);
 
 /* ------------------------------------------------------------------------
  * Stage hooks.  They mirror the reference's friend-class test access to the

@@ -39,6 +39,9 @@ SOLVER_CG64 = 0
 SOLVER_MIXED = 1
 SOLVER_LEARNED = 2
 
+CG_LAUNCH_GRAPH = 0
+CG_LAUNCH_HOST = 1
+
 CRIT_INITIAL_RESIDUAL = 0
 CRIT_RHS = 1
 
@@ -65,7 +68,7 @@ class MpsParams(C.Structure):
         ("max_cg_iters", C.c_int32),
         ("inner_tol", C.c_double),
         ("max_refinements", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("cg_launch", C.c_int32),
         ("reserved", C.c_double * 6),
     ]
 

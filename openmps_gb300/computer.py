@@ -57,6 +57,7 @@ PROTOTYPES = {
     "mps_event_record": (C.c_int, [_P, C.c_int32]),
     "mps_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "mps_flush_l2": (C.c_int, [_P, C.c_int64]),
+    "mps_bench_spmv": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_float)]),
     "mps_stage_search_neighbor": (C.c_int, [_P]),
     "mps_stage_density": (C.c_int, [_P]),
     "mps_stage_error_correction": (C.c_int, [_P]),
@@ -235,6 +236,12 @@ class Computer:
 
     def flush_l2(self, nbytes: int = 512 << 20):
         self._check(self.lib.mps_flush_l2(self.h, nbytes))
+
+    def bench_spmv(self, solver: int, reps: int = 20, flush_bytes: int = 0) -> float:
+        """Mean milliseconds of one launch of the solver's SpMV kernel."""
+        ms = C.c_float()
+        self._check(self.lib.mps_bench_spmv(self.h, solver, reps, flush_bytes, C.byref(ms)))
+        return float(ms.value)
 
     # --------------------------------------------------------------- stages
     def stage(self, name: str):

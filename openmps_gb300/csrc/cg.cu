@@ -1,20 +1,32 @@
 // cg.cu - pressure Poisson solvers (Computer::SolvePressurePoissonEquation,
-// Computer.hpp:1359-1429) on the transposed ELL matrix, each run as one CUDA graph:
-// an init kernel, then a conditional WHILE node whose body is a few kernels; the last
-// block of each reduction decides the next step and sets the graph condition, so a
-// solve of thousands of iterations needs no host round trip.
+// Computer.hpp:1359-1429) on the SELL-4x8 matrix, each run as one CUDA graph: an init
+// kernel, then a conditional WHILE node whose body is a few kernels; the last block of
+// each reduction decides the next step and sets the graph condition, so a solve of
+// thousands of iterations needs no host round trip.
 //
-// Reductions: each block sums its rows with warp shuffles, writes one partial, and
-// the last block to finish (atomic ticket, no waiting) sums the partials in a fixed
-// order.  Results are deterministic run to run.
+// Work layout: vector kernels run one thread per row, SpMV kernels one warp per chunk of
+// 32 rows (one lane per row, as many warps as chunks, so the block scheduler balances
+// uneven chunks);
+// each warp load reads 32 consecutive matrix entries and a row is summed by its own lane
+// in ascending column order (no cross-lane reduction: in FP64 every instruction counts,
+// the FP64 pipe bounds this kernel on GB300).  Loads are unrolled 8 deep so that each
+// lane keeps that many matrix loads and gathers in flight.
 //
-// MPS_SOLVER_CG64: the reference CG in FP64.
-// MPS_SOLVER_MIXED: CG whose iterations run in FP32 (FP32 matrix, FP32 SpMV and
-// axpy with FP32 accumulation, dot products accumulated in FP64) with reliable
-// updates (Sleijpen & van der Vorst 1996): when the recursive residual has dropped by
-// `delta` since the last update, the FP32 correction is folded into the FP64
-// solution and the true residual b - A x is recomputed in FP64 (FP64 matrix), which
-// also decides convergence.
+// Reductions: each block sums its part with warp shuffles, writes one partial, and the
+// last block to finish (atomic ticket, no waiting) sums the partials in a fixed order.
+// Results are deterministic run to run.
+//
+// MPS_SOLVER_CG64: the reference CG in FP64 (3 kernels per iteration).
+// MPS_SOLVER_MIXED: CG whose iterations run in FP32 (FP32 matrix, FP32 SpMV and axpy with
+// FP32 accumulation, dot products accumulated in FP64) with reliable updates (Sleijpen &
+// van der Vorst 1996): when the recursive residual has dropped by `delta` since the last
+// update, the FP32 correction is folded into the FP64 solution and the true residual
+// b - A x is recomputed with the FP64 matrix, which also decides convergence.  The
+// direction update p = r + beta p is folded into the next SpMV (each lane forms
+// beta p_j + r_j while gathering), so an iteration is two kernels; the reliable update
+// runs under a conditional IF node only when due.
+#include <vector>
+
 #include "cg.cuh"
 
 namespace mpsgb {
@@ -28,17 +40,20 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Sum over the block; valid in thread 0.
+// Sum over the block, valid in thread 0.  FP64 issue is scarce on GB300 (a warp-wide
+// DADD occupies the FP64 pipe ~22 cycles), so the lanes park their values in shared
+// memory and a single warp adds them: 8 serial adds plus a 5-level shuffle tree per
+// block instead of a 5-level tree in every warp.  `ws` holds kBlock doubles.
 __device__ double block_sum(double v, double* ws) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) ws[wid] = v;
+    ws[threadIdx.x] = v;
     __syncthreads();
-    const int nw = blockDim.x >> 5;
-    v = (static_cast<int>(threadIdx.x) < nw) ? ws[threadIdx.x] : 0.0;
-    if (wid == 0) v = warp_sum(v);
+    double s = 0.0;
+    if (threadIdx.x < 32) {
+        for (int k = threadIdx.x; k < static_cast<int>(blockDim.x); k += 32) s += ws[k];
+        s = warp_sum(s);
+    }
     __syncthreads();
-    return v;
+    return s;
 }
 
 // Writes this block's partials; true in the last block to finish.
@@ -62,63 +77,69 @@ __device__ double gather_sum(const double* partials, int nparts, double* ws) {
     return block_sum(v, ws);
 }
 
-// Row i of the FP64 matrix times v (ascending columns, FMA).  The matrix is read
-// with streaming hints: in FP64 it is larger than L2 on big scenes, and evicting it
-// first keeps the solver's vectors resident.
-__device__ __forceinline__ double row64(const CgOperands& o, int i, const double* v) {
-    const int L = o.len[i];
-    const int n = o.n;
-    double s = 0.0;
-    int k = 0;
-    for (; k + 4 <= L; k += 4) {
-        const int c0 = __ldcs(o.col + ell(k, n, i)), c1 = __ldcs(o.col + ell(k + 1, n, i));
-        const int c2 = __ldcs(o.col + ell(k + 2, n, i)), c3 = __ldcs(o.col + ell(k + 3, n, i));
-        const double a0 = __ldcs(o.val + ell(k, n, i)), a1 = __ldcs(o.val + ell(k + 1, n, i));
-        const double a2 = __ldcs(o.val + ell(k + 2, n, i)), a3 = __ldcs(o.val + ell(k + 3, n, i));
-        const double v0 = v[c0], v1 = v[c1], v2 = v[c2], v3 = v[c3];
-        s = fma(a0, v0, s);
-        s = fma(a1, v1, s);
-        s = fma(a2, v2, s);
-        s = fma(a3, v3, s);
-    }
-    for (; k < L; k++) s = fma(__ldcs(o.val + ell(k, n, i)), v[__ldcs(o.col + ell(k, n, i))], s);
-    return s;
+__device__ __forceinline__ bool cg_done(const CgScalars* S) {
+    return S->converged || S->aborted || S->iter >= S->max_iter;
 }
 
-// Row i of the FP64 matrix times (x + d) with d the FP32 correction (MIXED true residual).
-__device__ __forceinline__ double row64_xd(const CgOperands& o, int i) {
-    const int L = o.len[i];
-    const int n = o.n;
-    double s = 0.0;
-    for (int k = 0; k < L; k++) {
-        const int c = __ldcs(o.col + ell(k, n, i));
-        const double xc = o.x[c] + static_cast<double>(o.d32[c]);
-        s = fma(__ldcs(o.val + ell(k, n, i)), xc, s);
+// Row i (lane of a chunk at `at`) times v in FP64, ascending columns.  The FP64 matrix
+// streams with evict-first hints: on big scenes it exceeds L2 and the solver's vectors
+// should stay resident instead.
+template <class V>
+__device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, V v) {
+    double acc = 0.0;
+    int k = 0;
+    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
+        int c[8];
+        double a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            c[u] = __ldcs(o.col + at + u * kSellRows);
+            a[u] = __ldcs(o.val + at + u * kSellRows);
+        }
+        double xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) xv[u] = v(c[u]);
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc = fma(a[u], xv[u], acc);
     }
-    return s;
+    for (; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
+    return acc;
 }
 
-// Row i of the FP32 matrix times v, FP32 accumulation.  Kept cacheable: the FP32
-// matrix is meant to stay in L2 across iterations.
-__device__ __forceinline__ float row32(const CgOperands& o, int i, const float* v) {
-    const int L = o.len[i];
-    const int n = o.n;
-    float s = 0.0f;
+// Row i of the FP32 matrix times (beta * pold + r), FP32 accumulation, ascending columns.
+// The {column, value} pairs keep default caching: the FP32 matrix is meant to stay in L2.
+__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
+                                       const float* __restrict__ pold,
+                                       const float* __restrict__ rv, float beta) {
+    float acc = 0.0f;
     int k = 0;
-    for (; k + 4 <= L; k += 4) {
-        const int c0 = __ldg(o.col + ell(k, n, i)), c1 = __ldg(o.col + ell(k + 1, n, i));
-        const int c2 = __ldg(o.col + ell(k + 2, n, i)), c3 = __ldg(o.col + ell(k + 3, n, i));
-        const float a0 = __ldg(o.val32 + ell(k, n, i)), a1 = __ldg(o.val32 + ell(k + 1, n, i));
-        const float a2 = __ldg(o.val32 + ell(k + 2, n, i)), a3 = __ldg(o.val32 + ell(k + 3, n, i));
-        const float v0 = v[c0], v1 = v[c1], v2 = v[c2], v3 = v[c3];
-        s = fmaf(a0, v0, s);
-        s = fmaf(a1, v1, s);
-        s = fmaf(a2, v2, s);
-        s = fmaf(a3, v3, s);
+    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
+        uint2 e[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = fmaf(beta, pold[e[u].x], rv[e[u].x]);
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc = fmaf(__uint_as_float(e[u].y), v[u], acc);
     }
-    for (; k < L; k++) s = fmaf(__ldg(o.val32 + ell(k, n, i)), v[__ldg(o.col + ell(k, n, i))], s);
-    return s;
+    for (; k < L; k++, at += kSellRows) {
+        const uint2 e = __ldg(o.cv32 + at);
+        acc = fmaf(__uint_as_float(e.y), fmaf(beta, pold[e.x], rv[e.x]), acc);
+    }
+    return acc;
 }
+
+// One warp per chunk of kSellRows rows (lane = row within the chunk).  The SpMV kernels
+// launch as many warps as chunks so the block scheduler balances uneven chunks.
+struct ChunkLoop {
+    int lane, warp, nwarps;
+    __device__ ChunkLoop() {
+        lane = threadIdx.x & 31;
+        warp = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+        nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    }
+};
 
 // Threshold and first convergence test (Computer.hpp:1382-1389).
 __device__ void init_scalars(CgScalars* S, double rr, double bb, cudaGraphConditionalHandle h,
@@ -130,6 +151,7 @@ __device__ void init_scalars(CgScalars* S, double rr, double bb, cudaGraphCondit
     S->rr_upd = rr;
     S->true_rr = rr;
     S->bb = bb;
+    S->beta = 0.0;
     double thr = rr * S->eps * S->eps;
     if (S->criterion == MPS_CRIT_RHS && bb > 0) thr = bb * S->eps * S->eps;
     S->thr = thr;
@@ -142,10 +164,8 @@ __device__ void init_scalars(CgScalars* S, double rr, double bb, cudaGraphCondit
     if (use_cond) cudaGraphSetConditional(h, (!conv && S->max_iter > 0) ? 1u : 0u);
 }
 
-// ------------------------------------------------------------- CG64 kernels
-// Ap = A x; r = b - Ap; p = r; rr = r.r (Computer.hpp:1382-1385)
-__global__ void k_cg_init(CgOperands o, cudaGraphConditionalHandle h, int use_cond) {
-    __shared__ double ws[32];
+__device__ __forceinline__ bool aborted_before_solve(const CgOperands& o,
+                                                     cudaGraphConditionalHandle h, int use_cond) {
     if (o.status && (o.status->flags & (kStatusCellOverflow | kStatusDeviceCheck))) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             o.S->aborted = 1;
@@ -153,17 +173,32 @@ __global__ void k_cg_init(CgOperands o, cudaGraphConditionalHandle h, int use_co
             o.S->iter = 0;
             if (use_cond) cudaGraphSetConditional(h, 0u);
         }
-        return;
+        return true;
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    return false;
+}
+
+// ------------------------------------------------------------- CG64 kernels
+// Ap = A x; r = b - Ap; p = r; rr = r.r (Computer.hpp:1382-1385)
+__global__ void __launch_bounds__(kBlock) k_cg_init(CgOperands o, cudaGraphConditionalHandle h,
+                                                   int use_cond) {
+    __shared__ double ws[kBlock];
+    if (aborted_before_solve(o, h, use_cond)) return;
+    const ChunkLoop cl;
+    const double* x = o.x;
     double vrr = 0.0, vbb = 0.0;
-    if (i < o.n) {
-        const double bi = o.b[i];
-        const double ri = bi - row64(o, i, o.x);
-        o.r[i] = ri;
-        o.p[i] = ri;
-        vrr = ri * ri;
-        vbb = bi * bi;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const double ax = row64(o, sell_index(o.off[c], cl.lane, 0), L, [&](int j) { return x[j]; });
+        if (i < o.n) {
+            const double bi = o.b[i];
+            const double ri = bi - ax;
+            o.r[i] = ri;
+            o.p[i] = ri;
+            vrr += ri * ri;
+            vbb += bi * bi;
+        }
     }
     const double s0 = block_sum(vrr, ws);
     const double s1 = block_sum(vbb, ws);
@@ -175,15 +210,20 @@ __global__ void k_cg_init(CgOperands o, cudaGraphConditionalHandle h, int use_co
 }
 
 // Ap = A p; alpha = rr / (p.Ap)
-__global__ void k_cg_spmv_dot(CgOperands o) {
-    __shared__ double ws[32];
-    if (o.S->converged) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) k_cg_spmv_dot(CgOperands o) {
+    __shared__ double ws[kBlock];
+    if (cg_done(o.S)) return;
+    const ChunkLoop cl;
+    const double* p = o.p;
     double v = 0.0;
-    if (i < o.n) {
-        const double s = row64(o, i, o.p);
-        o.Ap[i] = s;
-        v = o.p[i] * s;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const double s = row64(o, sell_index(o.off[c], cl.lane, 0), L, [&](int j) { return p[j]; });
+        if (i < o.n) {
+            o.Ap[i] = s;
+            v += p[i] * s;
+        }
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -197,17 +237,17 @@ __global__ void k_cg_spmv_dot(CgOperands o) {
 }
 
 // x += alpha p; r -= alpha Ap; rrNew = r.r; convergence; beta (Computer.hpp:1402-1420)
-__global__ void k_cg_update(CgOperands o, cudaGraphConditionalHandle h, int use_cond) {
-    __shared__ double ws[32];
-    if (o.S->converged) return;
+__global__ void __launch_bounds__(kBlock) k_cg_update(CgOperands o, cudaGraphConditionalHandle h,
+                                                     int use_cond) {
+    __shared__ double ws[kBlock];
+    if (cg_done(o.S)) return;
     const double alpha = o.S->alpha;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v = 0.0;
-    if (i < o.n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
         o.x[i] = fma(alpha, o.p[i], o.x[i]);
         const double ri = fma(-alpha, o.Ap[i], o.r[i]);
         o.r[i] = ri;
-        v = ri * ri;
+        v += ri * ri;
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -229,21 +269,28 @@ __global__ void k_cg_update(CgOperands o, cudaGraphConditionalHandle h, int use_
 }
 
 // p = r + beta p
-__global__ void k_cg_pupdate(CgOperands o) {
-    if (o.S->converged) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < o.n) o.p[i] = fma(o.S->beta, o.p[i], o.r[i]);
+__global__ void __launch_bounds__(kBlock) k_cg_pupdate(CgOperands o) {
+    if (cg_done(o.S)) return;
+    const double beta = o.S->beta;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x)
+        o.p[i] = fma(beta, o.p[i], o.r[i]);
 }
 
 // |b - A x|^2 in FP64 into S->true_rr (reported as the true relative residual)
-__global__ void k_true_residual(CgOperands o) {
-    __shared__ double ws[32];
+__global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
+    __shared__ double ws[kBlock];
     if (o.S->aborted) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const ChunkLoop cl;
+    const double* x = o.x;
     double v = 0.0;
-    if (i < o.n) {
-        const double ri = o.b[i] - row64(o, i, o.x);
-        v = ri * ri;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const double ax = row64(o, sell_index(o.off[c], cl.lane, 0), L, [&](int j) { return x[j]; });
+        if (i < o.n) {
+            const double ri = o.b[i] - ax;
+            v += ri * ri;
+        }
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -256,52 +303,59 @@ __global__ void k_true_residual(CgOperands o) {
 }
 
 // ------------------------------------------------------------ MIXED kernels
-// r = b - A x (FP64); r32 = r; p32 = r32; d32 = 0
-__global__ void k_mx_init(CgOperands o, cudaGraphConditionalHandle h, int use_cond) {
-    __shared__ double ws[32];
-    if (o.status && (o.status->flags & (kStatusCellOverflow | kStatusDeviceCheck))) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            o.S->aborted = 1;
-            o.S->converged = 0;
-            o.S->iter = 0;
-            if (use_cond) cudaGraphSetConditional(h, 0u);
-        }
-        return;
-    }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// r = b - A x (FP64); r32 = r; d = 0; the first direction is r (beta = 0, pold = 0)
+__global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphConditionalHandle h,
+                                                   int use_cond) {
+    __shared__ double ws[kBlock];
+    if (aborted_before_solve(o, h, use_cond)) return;
+    const ChunkLoop cl;
+    const double* x = o.x;
     double vrr = 0.0, vbb = 0.0;
-    if (i < o.n) {
-        const double bi = o.b[i];
-        const double ri = bi - row64(o, i, o.x);
-        const float r32 = __double2float_rn(ri);
-        o.r32[i] = r32;
-        o.p32[i] = r32;
-        o.d32[i] = 0.0f;
-        vrr = ri * ri;
-        vbb = bi * bi;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const double ax = row64(o, sell_index(o.off[c], cl.lane, 0), L, [&](int j) { return x[j]; });
+        if (i < o.n) {
+            const double bi = o.b[i];
+            const double ri = bi - ax;
+            o.r32[i] = __double2float_rn(ri);
+            o.p32a[i] = 0.0f;
+            o.d32[i] = 0.0f;
+            vrr += ri * ri;
+            vbb += bi * bi;
+        }
     }
     const double s0 = block_sum(vrr, ws);
     const double s1 = block_sum(vbb, ws);
     if (publish(s0, s1, o.partials, &o.S->counter)) {
         const double rr = gather_sum(o.partials, gridDim.x, ws);
         const double bb = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
-        if (threadIdx.x == 0) {
-            init_scalars(o.S, rr, bb, h, use_cond);
-            // the recursion runs on the FP32 copy of r
-        }
+        if (threadIdx.x == 0) init_scalars(o.S, rr, bb, h, use_cond);
     }
 }
 
-// q = A32 p32 (FP32); alpha = rr / (p.q) with the dot in FP64
-__global__ void k_mx_spmv_dot(CgOperands o) {
-    __shared__ double ws[32];
-    if (o.S->converged) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// p = r + beta pold (formed on the fly while gathering); q = A32 p; alpha = rr / (p.q)
+__global__ void __launch_bounds__(kBlock) k_mx_spmv_dot(CgOperands o) {
+    __shared__ double ws[kBlock];
+    if (cg_done(o.S)) return;
+    const ChunkLoop cl;
+    const int parity = o.S->iter & 1;
+    const float* __restrict__ pold = parity ? o.p32b : o.p32a;
+    float* __restrict__ pnew = parity ? o.p32a : o.p32b;
+    const float beta = __double2float_rn(o.S->beta);
+    const bool clear_d = o.S->do_update != 0;  // d was folded into x by the last reliable update
     double v = 0.0;
-    if (i < o.n) {
-        const float q = row32(o, i, o.p32);
-        o.q32[i] = q;
-        v = static_cast<double>(o.p32[i]) * static_cast<double>(q);
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const float q = row32(o, sell_index(o.off[c], cl.lane, 0), L, pold, o.r32, beta);
+        if (i < o.n) {
+            const float pn = fmaf(beta, pold[i], o.r32[i]);
+            pnew[i] = pn;
+            o.q32[i] = q;
+            if (clear_d) o.d32[i] = 0.0f;
+            v += static_cast<double>(pn) * static_cast<double>(q);
+        }
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -315,17 +369,19 @@ __global__ void k_mx_spmv_dot(CgOperands o) {
 }
 
 // d += alpha p; r -= alpha q (FP32); rr_new in FP64; decides a reliable update
-__global__ void k_mx_update(CgOperands o, cudaGraphConditionalHandle h, int use_cond) {
-    __shared__ double ws[32];
-    if (o.S->converged) return;
+__global__ void __launch_bounds__(kBlock) k_mx_update(CgOperands o, cudaGraphConditionalHandle h,
+                                                     cudaGraphConditionalHandle h_true,
+                                                     int use_cond) {
+    __shared__ double ws[kBlock];
+    if (cg_done(o.S)) return;
     const float a = __double2float_rn(o.S->alpha);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float* __restrict__ pnew = (o.S->iter & 1) ? o.p32a : o.p32b;
     double v = 0.0;
-    if (i < o.n) {
-        o.d32[i] = fmaf(a, o.p32[i], o.d32[i]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
+        o.d32[i] = fmaf(a, pnew[i], o.d32[i]);
         const float ri = fmaf(-a, o.q32[i], o.r32[i]);
         o.r32[i] = ri;
-        v = static_cast<double>(ri) * static_cast<double>(ri);
+        v += static_cast<double>(ri) * static_cast<double>(ri);
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -336,6 +392,7 @@ __global__ void k_mx_update(CgOperands o, cudaGraphConditionalHandle h, int use_
             S->rr_new = rr_new;
             const int reliable = (rr_new < S->delta2 * S->rr_upd) || (rr_new < S->thr);
             S->do_update = reliable;
+            if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
             if (!reliable) {
                 S->beta = rr_new / S->rr;
                 S->rr = rr_new;
@@ -346,16 +403,29 @@ __global__ void k_mx_update(CgOperands o, cudaGraphConditionalHandle h, int use_
     }
 }
 
-// reliable update: r = b - A (x + d) in FP64; r32 = r; convergence on the true residual
-__global__ void k_mx_true(CgOperands o, cudaGraphConditionalHandle h, int use_cond) {
-    __shared__ double ws[32];
-    if (o.S->converged || !o.S->do_update) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Reliable update: x' = x + d and r = b - A x' in FP64 (FP64 matrix); r32 = r;
+// convergence on this true residual.  d is cleared by the next SpMV kernel.
+__global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphConditionalHandle h,
+                                                   int use_cond) {
+    __shared__ double ws[kBlock];
+    if (o.S->converged || o.S->aborted || !o.S->do_update) return;
+    const ChunkLoop cl;
+    const bool odd = (o.S->updates & 1) != 0;
+    const double* __restrict__ xc = odd ? o.x2 : o.x;
+    double* __restrict__ xn = odd ? o.x : o.x2;
+    const float* __restrict__ d = o.d32;
     double v = 0.0;
-    if (i < o.n) {
-        const double ri = o.b[i] - row64_xd(o, i);
-        o.r32[i] = __double2float_rn(ri);
-        v = ri * ri;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const double ax = row64(o, sell_index(o.off[c], cl.lane, 0), L,
+                                [&](int j) { return xc[j] + static_cast<double>(d[j]); });
+        if (i < o.n) {
+            const double ri = o.b[i] - ax;
+            xn[i] = xc[i] + static_cast<double>(d[i]);
+            o.r32[i] = __double2float_rn(ri);
+            v += ri * ri;
+        }
     }
     const double s0 = block_sum(v, ws);
     if (publish(s0, 0.0, o.partials, &o.S->counter)) {
@@ -379,25 +449,15 @@ __global__ void k_mx_true(CgOperands o, cudaGraphConditionalHandle h, int use_co
     }
 }
 
-// fold d into x after a reliable update; p32 = r32 + beta p32
-__global__ void k_mx_pupdate(CgOperands o) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= o.n) return;
-    if (o.S->do_update) {
-        o.x[i] = o.x[i] + static_cast<double>(o.d32[i]);
-        o.d32[i] = 0.0f;
-    }
-    if (o.S->converged) return;
-    o.p32[i] = fmaf(__double2float_rn(o.S->beta), o.p32[i], o.r32[i]);
-}
-
-// after the loop: fold any remaining correction (iteration limit reached)
-__global__ void k_mx_finish(CgOperands o) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= o.n || o.S->aborted) return;
-    const float d = o.d32[i];
-    if (d != 0.0f) {
-        o.x[i] = o.x[i] + static_cast<double>(d);
+// After the loop: the solution into x (fold a pending correction, leave the x2 buffer).
+__global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
+    if (o.S->aborted) return;
+    const bool odd = (o.S->updates & 1) != 0;
+    const bool folded = o.S->do_update != 0;
+    const double* xc = odd ? o.x2 : o.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
+        const float di = o.d32[i];
+        o.x[i] = folded ? xc[i] : xc[i] + static_cast<double>(di);
         o.d32[i] = 0.0f;
     }
 }
@@ -413,18 +473,43 @@ __global__ void k_cg_configure(CgScalars* S, double eps, int criterion, int max_
         S->converged = 0;
         S->iter = 0;
         S->aborted = 0;
+        S->do_update = 0;
+        S->updates = 0;
+    }
+}
+
+void body_kernels(int solver, const CgOperands& ops, cudaGraphConditionalHandle h,
+                  cudaGraphConditionalHandle h_true, int use_cond, bool with_true, cudaStream_t s) {
+    const int gv = ops.grid_vec, gs = ops.grid_spmv;
+    if (solver == MPS_SOLVER_CG64) {
+        k_cg_spmv_dot<<<gs, kBlock, 0, s>>>(ops);
+        k_cg_update<<<gv, kBlock, 0, s>>>(ops, h, use_cond);
+        k_cg_pupdate<<<gv, kBlock, 0, s>>>(ops);
+    } else {
+        k_mx_spmv_dot<<<gs, kBlock, 0, s>>>(ops);
+        k_mx_update<<<gv, kBlock, 0, s>>>(ops, h, h_true, use_cond);
+        if (with_true) k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
     }
 }
 
 }  // namespace
+
+int cg_grid_vec(int64_t n) { return grid_for(n); }
+int cg_grid_spmv(int64_t n) { return grid_for(sell_chunks(n) * 32); }
+int64_t cg_partials(int64_t n) {
+    return 2 * static_cast<int64_t>(cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n)) + 64;
+}
 
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,
                          cudaStream_t s) {
     k_cg_configure<<<1, 32, 0, s>>>(S, eps, criterion, max_iter, delta2);
 }
 
-void launch_true_residual(const CgOperands& ops, double*, cudaStream_t s) {
-    k_true_residual<<<grid_for(ops.n), kBlock, 0, s>>>(ops);
+void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
+    if (solver == MPS_SOLVER_CG64)
+        k_cg_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
+    else
+        k_mx_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
 }
 
 CgGraph::~CgGraph() { reset(); }
@@ -435,34 +520,71 @@ void CgGraph::reset() {
     exec_ = nullptr;
     graph_ = nullptr;
     solver_ = -1;
+    nested_ = false;
 }
 
-cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s) {
+cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win) {
+    if (solver != MPS_SOLVER_CG64) {
+        // preferred: the reliable update under an IF node nested in the WHILE body
+        if (build_impl(solver, ops, s, true, win) == cudaSuccess) return cudaSuccess;
+        cudaGetLastError();
+    }
+    return build_impl(solver, ops, s, false, win);
+}
+
+namespace {
+// Sets the L2 access policy window on every kernel node of `g`.
+cudaError_t apply_window(cudaGraph_t g, const L2Window& win) {
+    if (win.num_bytes == 0) return cudaSuccess;
+    size_t nn = 0;
+    cudaError_t e = cudaGraphGetNodes(g, nullptr, &nn);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> nodes(nn);
+    e = cudaGraphGetNodes(g, nodes.data(), &nn);
+    if (e != cudaSuccess) return e;
+    cudaKernelNodeAttrValue v = {};
+    v.accessPolicyWindow.base_ptr = win.base;
+    v.accessPolicyWindow.num_bytes = win.num_bytes;
+    v.accessPolicyWindow.hitRatio = win.hit_ratio;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    for (cudaGraphNode_t node : nodes) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(node, &t);
+        if (e != cudaSuccess) return e;
+        if (t != cudaGraphNodeTypeKernel) continue;
+        e = cudaGraphKernelNodeSetAttribute(node, cudaKernelNodeAttributeAccessPolicyWindow, &v);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
+                                const L2Window& win) {
     reset();
     ops_ = ops;
     solver_ = solver;
-    const int grid = grid_for(ops.n);
+    nested_ = nested;
+    const int gv = ops.grid_vec, gs = ops.grid_spmv;
     cudaError_t e = cudaGraphCreate(&graph_, 0);
     if (e != cudaSuccess) return e;
     cudaGraphConditionalHandle h;
     e = cudaGraphConditionalHandleCreate(&h, graph_, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return e;
+    cudaGraph_t captured = nullptr;
 
     // init kernel
     e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     if (solver == MPS_SOLVER_CG64)
-        k_cg_init<<<grid, kBlock, 0, s>>>(ops, h, 1);
+        k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
     else
-        k_mx_init<<<grid, kBlock, 0, s>>>(ops, h, 1);
-    cudaGraph_t captured = nullptr;
+        k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
-
-    size_t nn = 0;
-    e = cudaGraphGetNodes(graph_, nullptr, &nn);
-    if (e != cudaSuccess || nn != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
+    size_t nn = 1;
     cudaGraphNode_t init_node;
     e = cudaGraphGetNodes(graph_, &init_node, &nn);
     if (e != cudaSuccess) return e;
@@ -477,37 +599,98 @@ cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s) {
     e = cudaGraphAddNode(&while_node, graph_, &init_node, nullptr, 1, &cp);
     if (e != cudaSuccess) return e;
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    if (solver == MPS_SOLVER_CG64) {
-        k_cg_spmv_dot<<<grid, kBlock, 0, s>>>(ops);
-        k_cg_update<<<grid, kBlock, 0, s>>>(ops, h, 1);
-        k_cg_pupdate<<<grid, kBlock, 0, s>>>(ops);
-    } else {
-        k_mx_spmv_dot<<<grid, kBlock, 0, s>>>(ops);
-        k_mx_update<<<grid, kBlock, 0, s>>>(ops, h, 1);
-        k_mx_true<<<grid, kBlock, 0, s>>>(ops, h, 1);
-        k_mx_pupdate<<<grid, kBlock, 0, s>>>(ops);
+
+    cudaGraphConditionalHandle h_true = 0;
+    if (nested) {
+        e = cudaGraphConditionalHandleCreate(&h_true, body, 0, 0);
+        if (e != cudaSuccess) return e;
     }
+    e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    body_kernels(solver, ops, h, h_true, 1, !nested, s);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
+    e = apply_window(body, win);
+    if (e != cudaSuccess) return e;
 
-    // tail: fold the last correction (MIXED) and measure the true residual
+    if (nested) {
+        // if (reliable update due) { k_mx_true } after the update kernel
+        size_t ne = 0;
+        e = cudaGraphGetEdges(body, nullptr, nullptr, nullptr, &ne);
+        if (e != cudaSuccess || ne != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
+        cudaGraphNode_t from, to;
+        e = cudaGraphGetEdges(body, &from, &to, nullptr, &ne);
+        if (e != cudaSuccess) return e;
+        cudaGraphNodeParams ip = {};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h_true;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t if_node;
+        e = cudaGraphAddNode(&if_node, body, &to, nullptr, 1, &ip);
+        if (e != cudaSuccess) return e;
+        cudaGraph_t if_body = ip.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(s, if_body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, 1);
+        e = cudaStreamEndCapture(s, &captured);
+        if (e != cudaSuccess) return e;
+    }
+
+    // tail: the solution into x (MIXED) and the true residual
     e = cudaStreamBeginCaptureToGraph(s, graph_, &while_node, nullptr, 1,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    if (solver != MPS_SOLVER_CG64) k_mx_finish<<<grid, kBlock, 0, s>>>(ops);
-    k_true_residual<<<grid, kBlock, 0, s>>>(ops);
+    if (solver != MPS_SOLVER_CG64) k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
+    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
 
-    return cudaGraphInstantiate(&exec_, graph_, 0);
+    e = cudaGraphInstantiate(&exec_, graph_, 0);
+    if (e != cudaSuccess) {
+        exec_ = nullptr;
+        return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t CgGraph::launch(cudaStream_t s) {
     if (!exec_) return cudaErrorInvalidValue;
     return cudaGraphLaunch(exec_, s);
+}
+
+cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
+                          cudaStream_t s, int64_t* launches) {
+    const int gv = ops.grid_vec, gs = ops.grid_spmv;
+    const cudaGraphConditionalHandle none = 0;
+    int64_t k = 0;
+    if (solver == MPS_SOLVER_CG64)
+        k_cg_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
+    else
+        k_mx_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
+    k++;
+    cudaError_t e = cudaGetLastError();
+    for (;;) {
+        if (e != cudaSuccess) return e;
+        e = cudaMemcpyAsync(host_S, ops.S, sizeof(CgScalars), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (host_S->converged || host_S->aborted || host_S->iter >= host_S->max_iter) break;
+        for (int c = 0; c < chunk; c++) {
+            body_kernels(solver, ops, none, none, 0, true, s);
+            k += 3;
+        }
+        e = cudaGetLastError();
+    }
+    if (solver != MPS_SOLVER_CG64) {
+        k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
+        k++;
+    }
+    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    k++;
+    if (launches) *launches = k;
+    return cudaGetLastError();
 }
 
 }  // namespace mpsgb

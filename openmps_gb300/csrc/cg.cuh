@@ -1,4 +1,4 @@
-// cg.cuh - pressure Poisson solvers on the transposed ELL matrix.
+// cg.cuh - pressure Poisson solvers on the SELL-32 matrix.
 #pragma once
 
 #include "common.cuh"
@@ -18,57 +18,84 @@ struct CgScalars {
     double eps;
     double rr_upd;    // MIXED: true r.r at the last reliable update
     double delta2;    // MIXED: reliable-update trigger (rr_new < delta2 * rr_upd)
-    double true_rr;   // MIXED: last true residual r.r
+    double true_rr;   // last true residual r.r (FP64)
     int32_t iter;
     int32_t max_iter;
     int32_t converged;
-    int32_t do_update;
+    int32_t do_update;  // MIXED: a reliable update is due / was just made
     int32_t criterion;
-    int32_t updates;
-    uint32_t counter;  // last-block ticket
-    int32_t aborted;   // the step failed before the solve: nothing runs
+    int32_t updates;    // MIXED: reliable updates made (parity selects the x buffer)
+    uint32_t counter;   // last-block ticket
+    int32_t aborted;    // the step failed before the solve: nothing runs
 };
 
 struct CgOperands {
-    int32_t n;
-    const int32_t* len;
-    const int32_t* col;
-    const double* val;
-    const float* val32;
+    int32_t n;          // rows
+    int32_t nchunks;    // chunks of kSellRows rows
+    int32_t grid_vec;   // blocks of the vector kernels (one thread per row)
+    int32_t grid_spmv;  // blocks of the SpMV kernels (one warp per chunk)
+    const int32_t* len; // row lengths, kSellRows * nchunks (rows >= n have length 0)
+    const int32_t* off; // chunk offsets, nchunks + 1
+    const int32_t* col; // SELL-32 columns
+    const double* val;  // SELL-32 FP64 values
+    const uint2* cv32;  // SELL-32 {column, FP32 value}
     const double* b;
-    double* x;
-    // FP64 CG
+    double* x;          // initial guess in, solution out
+    // CG64
     double *r, *p, *Ap;
     // MIXED
-    float *r32, *p32, *q32, *d32;
-    double* partials;  // 2 * grid doubles
+    double* x2;         // second FP64 solution buffer (reliable updates alternate)
+    float *r32, *q32, *d32, *p32a, *p32b;
+    double* partials;   // 2 * max(grid_vec, grid_spmv) doubles
     CgScalars* S;
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
+};
+
+// L2 persisting window applied to the kernels of the CG loop (num_bytes 0: none).
+struct L2Window {
+    void* base = nullptr;
+    size_t num_bytes = 0;
+    float hit_ratio = 0.f;
 };
 
 // A CUDA graph running one whole solve: init kernel + device-driven while loop.
 class CgGraph {
 public:
     ~CgGraph();
-    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s);
+    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {});
     cudaError_t launch(cudaStream_t s);
     void reset();
     bool valid() const { return exec_ != nullptr; }
     int solver() const { return solver_; }
     const CgOperands& operands() const { return ops_; }
-    int kernels_per_iteration() const { return solver_ == MPS_SOLVER_CG64 ? 3 : 4; }
+    // kernels per iteration (the MIXED reliable-update kernel runs only when due)
+    int kernels_per_iteration() const { return solver_ == MPS_SOLVER_CG64 ? 3 : (nested_ ? 2 : 3); }
+    bool nested() const { return nested_; }
 
 private:
+    cudaError_t build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
+                           const L2Window& win);
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int solver_ = -1;
+    bool nested_ = false;
     CgOperands ops_{};
 };
+
+// The same solve with host-launched kernels: `chunk` iterations per launch batch, the
+// device status read back between batches (kernels past convergence return at once).
+// Used when kernels must be visible one by one (profilers) and as a fallback.
+cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
+                          cudaStream_t s, int64_t* launches);
 
 // Sets eps / criterion / max_iter / delta for the next solve (stream-ordered).
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,
                          cudaStream_t s);
-// r.r of b - A x in FP64 (true residual) into *out (device), stream-ordered.
-void launch_true_residual(const CgOperands& ops, double* out2, cudaStream_t s);
+// One launch of the solver's SpMV kernel (the CG iteration's dominant kernel) alone.
+void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s);
+// Launch shapes of the solver kernels for n rows, and the partials they need.
+int cg_grid_vec(int64_t n);
+int cg_grid_spmv(int64_t n);
+int64_t cg_partials(int64_t n);
 
 }  // namespace mpsgb

@@ -6,10 +6,16 @@
 //   cells   dense buckets cell_count[nx*nz], cell_slot[nx*nz*maxPerCell] like the
 //           reference Grid (src/OpenMps/Grid.hpp:76, :140-150); each bucket is sorted
 //           to ascending particle index after the parallel fill.
-//   lists   neighbour lists and the PPE matrix in transposed padded ELL form:
-//           entry k of row i lives at [k * N + i], so consecutive threads (rows) touch
-//           consecutive addresses.  Row capacity is the reference's own bound
-//           9 * maxPerCell (Computer.hpp:1763-1765), +1 for the PPE diagonal.
+//   lists   neighbour lists in transposed padded ELL form: entry k of row i lives at
+//           [k * N + i], so consecutive threads (rows) touch consecutive addresses.
+//           Row capacity is the reference's own bound 9 * maxPerCell
+//           (Computer.hpp:1763-1765).
+//   PPE     the matrix in compact sliced ELL "SELL-32": rows grouped in chunks of 32
+//           (one warp, one lane per row), each chunk column-major, so a warp reads 32
+//           consecutive entries per load; chunk c starts at off[c] (prefix sum of the
+//           chunk sizes), so the whole matrix is a dense stream of about nnz entries.
+//           Columns are ascending within a row next to FP64 values, and the FP32
+//           solver reads {column, FP32 value} pairs from one 8-byte array.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,6 +41,8 @@ struct SceneConst {
     int32_t nb_stride;   // neighbour row capacity (9 * max_per_cell)
     int32_t ppe_stride;  // PPE row capacity (nb_stride + 1)
     int32_t guard;       // 1 inside a full step: stages skip themselves after a failure
+    int32_t nchunks;     // PPE chunks of kSellRows rows
+    int32_t pad1;
     double l0, re, re2, re_lap, rl2;
     double nl, nl2_lo, nl2_hi;  // neighbour length and a guard band around nl^2
     double n0, lambda, n0_lap, lambda_lap;
@@ -56,7 +64,15 @@ struct DevStatus {
     int disabled;
     int check_index;
     int pad;
+    unsigned long long nb_total;  // neighbour-list entries of the last search
+    unsigned long long ppe_nnz;   // nonzeros of the last PPE assembly
 };
+
+// Adds v over the warp and lets lane 0 add it to *dst (few atomics per kernel).
+__device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
 
 struct DeviceState {
     int32_t* type;
@@ -65,9 +81,12 @@ struct DeviceState {
     double *n_wo_spp, *ecs, *ox, *oz, *dux, *duz;
     int32_t *cell_count, *cell_slot;
     int32_t *nb_count, *nb;
-    int32_t *ppe_len, *ppe_col, *ppe_col_tmp;
-    double *ppe_val, *ppe_val_tmp, *ppe_b, *ppe_x;
-    float* ppe_val32;
+    int32_t *ppe_len, *ppe_col_tmp;
+    double *ppe_val_tmp, *ppe_b, *ppe_x;
+    int32_t *ppe_chunk, *ppe_off, *scan_scratch;  // chunk sizes, chunk offsets
+    int32_t* ppe_col;                              // SELL-32 columns
+    double* ppe_val;                               // SELL-32 FP64 values
+    uint2* ppe_cv32;                               // SELL-32 {column, FP32 value}
     StepScalars* step;
     DevStatus* status;
     const int32_t* solve_ok;  // converged flag of the last PPE solve
@@ -101,6 +120,23 @@ __device__ __forceinline__ int64_t ell(int k, int n, int i) {
     return static_cast<int64_t>(k) * n + i;
 }
 
+// SELL-32: rows in chunks of 32 (one warp, one lane per row); entry k of the chunk's row
+// r sits at chunk_off + 32 k + r, so a warp's load at step k reads 32 consecutive
+// entries.  A chunk reserves 32 x (its longest row) entries.
+constexpr int kSellRows = 32;
+
+__host__ __device__ __forceinline__ int64_t sell_index(int64_t chunk_off, int r, int k) {
+    return chunk_off + static_cast<int64_t>(k) * kSellRows + r;
+}
+
+__host__ __device__ __forceinline__ int64_t sell_chunk_size(int maxlen) {
+    return static_cast<int64_t>(maxlen) * kSellRows;
+}
+
+__host__ __device__ __forceinline__ int64_t sell_chunks(int64_t n) {
+    return (n + kSellRows - 1) / kSellRows;
+}
+
 inline int grid_for(int64_t n, int block = kBlock) {
     return static_cast<int>((n + block - 1) / block);
 }
@@ -123,9 +159,12 @@ void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32,
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// scan.cu
+int scan_scratch_ints(int m);
+void launch_exclusive_scan(const int* in, int* out, int m, int* scratch, cudaStream_t s);
 // number of kernels each launcher issues (for the launch counter)
 constexpr int kLaunchesSearch = 3, kLaunchesDensity = 1, kLaunchesEcs = 1, kLaunchesExplicit = 2,
-              kLaunchesSaveX = 1, kLaunchesSetPpe = 2, kLaunchesAssign = 1, kLaunchesGradient = 2,
+              kLaunchesSaveX = 1, kLaunchesSetPpe = 6, kLaunchesAssign = 1, kLaunchesGradient = 2,
               kLaunchesDs = 2, kLaunchesDt = 1, kLaunchesCfl = 2;
 
 }  // namespace mpsgb

@@ -78,13 +78,7 @@ __global__ void k_cell_sort(SceneConst sc, DeviceState st) {
 
 // Neighbour rows: the nine cells in Grid::Iterator order (Grid.hpp:393-401), each in
 // slot order, keeping j != i with R(x_i, x_j) < NeighborLength (Computer.hpp:740-749).
-__global__ void k_neighbors(SceneConst sc, DeviceState st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.n) return;
-    if (st.type[i] == MPS_TYPE_DISABLED) {
-        st.nb_count[i] = 0;
-        return;
-    }
+__device__ __forceinline__ int neighbor_row(const SceneConst& sc, const DeviceState& st, int i) {
     const double xi = st.x[i], zi = st.z[i];
     const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
     const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
@@ -124,7 +118,15 @@ __global__ void k_neighbors(SceneConst sc, DeviceState st) {
             }
         }
     }
-    st.nb_count[i] = min(cnt, sc.nb_stride);
+    return min(cnt, sc.nb_stride);
+}
+
+__global__ void k_neighbors(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int cnt = 0;
+    if (i < sc.n && st.type[i] != MPS_TYPE_DISABLED) cnt = neighbor_row(sc, st, i);
+    if (i < sc.n) st.nb_count[i] = cnt;
+    warp_add_u64(&st.status->nb_total, static_cast<unsigned long long>(cnt));
 }
 
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {

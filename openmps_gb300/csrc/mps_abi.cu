@@ -52,9 +52,14 @@ struct mps_handle {
     // CG buffers
     CgScalars* S = nullptr;
     double* partials = nullptr;
-    double *r = nullptr, *p = nullptr, *Ap = nullptr;
-    float *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *d32 = nullptr;
+    double *r = nullptr, *p = nullptr, *Ap = nullptr, *x2 = nullptr;
+    float *r32 = nullptr, *q32 = nullptr, *d32 = nullptr, *p32a = nullptr, *p32b = nullptr;
+    int sm_count = 1;
     CgGraph cg;
+    int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
+    L2Window l2win;                // persisting window over the FP32 matrix (MIXED)
+    bool l2_limit_changed = false;
+    size_t l2_limit_before = 0;
 
     // pinned host mirrors of the status block
     DevStatus* h_status = nullptr;
@@ -145,7 +150,7 @@ void validate(const mps_params& p) {
     auto bad = [](const char* m) { throw StatusError{MPS_ERR_INVALID_ARGUMENT, m}; };
     if (!(p.l0 > 0)) bad("l0 must be positive");
     if (!(p.re_by_l0 > 0)) bad("re_by_l0 must be positive");
-    if (!(p.g > 0)) bad("g must be positive (MaxDt uses sqrt(2 courant l0 / g))");
+    if (!(p.g >= 0)) bad("g must be non-negative");
     if (!(p.rho > 0)) bad("rho must be positive");
     if (!(p.courant > 0)) bad("courant must be positive");
     if (!(p.max_x > p.min_x) || !(p.max_z > p.min_z)) bad("empty domain");
@@ -155,6 +160,7 @@ void validate(const mps_params& p) {
     if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
         bad("unknown criterion");
     if (p.flags & ~static_cast<uint32_t>(MPS_PRESET_REFERENCE)) bad("unknown method flag");
+    if (p.cg_launch != MPS_CG_LAUNCH_GRAPH && p.cg_launch != MPS_CG_LAUNCH_HOST) bad("unknown cg_launch");
 }
 
 void setup_constants(mps_handle* h) {
@@ -214,26 +220,33 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.cell_slot = dalloc<int32_t>(h, cells * sc.max_per_cell);
     st.nb_count = dalloc<int32_t>(h, n);
     st.nb = dalloc<int32_t>(h, n * sc.nb_stride);
-    st.ppe_len = dalloc<int32_t>(h, n);
-    st.ppe_col = dalloc<int32_t>(h, n * sc.ppe_stride);
+    const int64_t nchunks = sell_chunks(n);
+    const int64_t sell_cap = nchunks * sell_chunk_size(sc.ppe_stride);
+    st.ppe_len = dalloc<int32_t>(h, nchunks * kSellRows);
     st.ppe_col_tmp = dalloc<int32_t>(h, n * sc.ppe_stride);
-    st.ppe_val = dalloc<double>(h, n * sc.ppe_stride);
     st.ppe_val_tmp = dalloc<double>(h, n * sc.ppe_stride);
-    st.ppe_val32 = dalloc<float>(h, n * sc.ppe_stride);
+    st.ppe_chunk = dalloc<int32_t>(h, nchunks);
+    st.ppe_off = dalloc<int32_t>(h, nchunks + 1);
+    st.scan_scratch = dalloc<int32_t>(h, scan_scratch_ints(static_cast<int>(nchunks)));
+    st.ppe_col = dalloc<int32_t>(h, sell_cap);
+    st.ppe_val = dalloc<double>(h, sell_cap);
+    st.ppe_cv32 = dalloc<uint2>(h, sell_cap);
     st.ppe_b = dalloc<double>(h, n);
     st.ppe_x = dalloc<double>(h, n);
     st.step = dalloc<StepScalars>(h, 1);
     st.status = dalloc<DevStatus>(h, 1);
     h->S = dalloc<CgScalars>(h, 1);
     st.solve_ok = &h->S->converged;
-    h->partials = dalloc<double>(h, 2 * static_cast<int64_t>(grid_for(n)) + 64);
+    h->partials = dalloc<double>(h, cg_partials(n));
     h->r = dalloc<double>(h, n);
     h->p = dalloc<double>(h, n);
     h->Ap = dalloc<double>(h, n);
+    h->x2 = dalloc<double>(h, n);
     h->r32 = dalloc<float>(h, n);
-    h->p32 = dalloc<float>(h, n);
     h->q32 = dalloc<float>(h, n);
     h->d32 = dalloc<float>(h, n);
+    h->p32a = dalloc<float>(h, n);
+    h->p32b = dalloc<float>(h, n);
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -243,7 +256,9 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(h->S, 0, sizeof(CgScalars), s), "memset");
     check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(st.nb_count, 0, sizeof(int32_t) * n, s), "memset");
-    check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * n, s), "memset");
+    check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * kSellRows * sell_chunks(n), s), "memset");
+    check(cudaMemsetAsync(h->p32a, 0, sizeof(float) * n, s), "memset");
+    check(cudaMemsetAsync(h->p32b, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(st.cell_count, 0, sizeof(int32_t) * cells, s), "memset");
     if (keep > 0) {
         check(cudaMemcpyAsync(st.type, old.type, sizeof(int32_t) * keep, cudaMemcpyDeviceToDevice, s),
@@ -262,24 +277,31 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     for (void* ptr : old_allocs) cudaFree(ptr);
     h->cap = n;
     h->cg.reset();
+    h->l2win = L2Window{};
 }
 
 CgOperands cg_operands(mps_handle* h) {
     CgOperands o{};
     o.n = static_cast<int32_t>(h->n);
+    o.nchunks = static_cast<int32_t>(sell_chunks(h->n));
+    o.grid_vec = cg_grid_vec(h->n);
+    o.grid_spmv = cg_grid_spmv(h->n);
     o.len = h->st.ppe_len;
+    o.off = h->st.ppe_off;
     o.col = h->st.ppe_col;
     o.val = h->st.ppe_val;
-    o.val32 = h->st.ppe_val32;
+    o.cv32 = h->st.ppe_cv32;
     o.b = h->st.ppe_b;
     o.x = h->st.ppe_x;
     o.r = h->r;
     o.p = h->p;
     o.Ap = h->Ap;
+    o.x2 = h->x2;
     o.r32 = h->r32;
-    o.p32 = h->p32;
     o.q32 = h->q32;
     o.d32 = h->d32;
+    o.p32a = h->p32a;
+    o.p32b = h->p32b;
     o.partials = h->partials;
     o.S = h->S;
     o.status = h->st.status;
@@ -291,6 +313,15 @@ void require_particles(mps_handle* h) {
 }
 
 void launched(mps_handle* h, int k) { h->stats.kernel_launches += k; }
+
+// Iteration limit: the reference stops after as many iterations as unknowns
+// (Computer.hpp:1392).  The mixed solver restarts its FP32 recursion at every reliable
+// update, so it gets twice that plus a margin.
+int default_max_iter(int32_t requested, int64_t n, int32_t solver) {
+    if (requested > 0) return requested;
+    const int64_t lim = (solver == MPS_SOLVER_CG64) ? n : 2 * n + 200;
+    return static_cast<int>(std::min<int64_t>(lim, 0x7fffffff));
+}
 
 void after_launch(const char* what) { check(cudaGetLastError(), what); }
 
@@ -307,6 +338,8 @@ void read_status(mps_handle* h, bool solve_done) {
     h->t = h->h_step->t;
     h->dt = h->h_step->dt;
     h->stats.disabled = h->h_status->disabled;
+    h->stats.neighbor_total = static_cast<int64_t>(h->h_status->nb_total);
+    h->stats.ppe_nnz = static_cast<int64_t>(h->h_status->ppe_nnz);
     if (solve_done) {
         const CgScalars& S = *h->h_S;
         h->stats.cg_iterations = S.iter;
@@ -314,8 +347,13 @@ void read_status(mps_handle* h, bool solve_done) {
         h->stats.cg_rr0 = S.rr0;
         h->stats.cg_rr = S.rr_new;
         h->stats.cg_true_relres = (S.bb > 0) ? std::sqrt(S.true_rr / S.bb) : std::sqrt(S.true_rr);
-        launched(h, 2 + (h->prm.solver == MPS_SOLVER_CG64 ? 0 : 1) +
-                        S.iter * h->cg.kernels_per_iteration());
+        if (h->direct_launches >= 0)
+            launched(h, static_cast<int>(h->direct_launches));
+        else
+            launched(h, 2 + (h->prm.solver == MPS_SOLVER_CG64 ? 0 : 1) +
+                            (h->prm.solver == MPS_SOLVER_CG64
+                                 ? 3 * S.iter
+                                 : (h->cg.nested() ? 2 * S.iter + S.updates : 3 * S.iter)));
     }
     const int f = h->h_status->flags;
     if (f & kStatusCellOverflow) throw StatusError{MPS_ERR_CELL_OVERFLOW, "Too many particle in a block"};
@@ -347,15 +385,66 @@ void do_search(mps_handle* h) {
     launched(h, kLaunchesSearch);
 }
 
+// Keeps as much of the FP32 matrix ({column, value} pairs, read every iteration) in L2
+// as the persisting set-aside allows: the matrix of the 320k-particle scene is about the
+// size of L2.  The set-aside is a limit of this process's context; the handle restores
+// the previous value when it is destroyed.
+void setup_l2_window(mps_handle* h) {
+    if (h->l2win.num_bytes != 0) return;
+    int maxp = 0, maxw = 0;
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, h->device) != cudaSuccess ||
+        maxp <= 0 || maxw <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    const size_t used = static_cast<size_t>(sell_chunks(h->n) * sell_chunk_size(h->sc.ppe_stride)) * sizeof(uint2);
+    const size_t win = std::min(used, static_cast<size_t>(maxw));
+    size_t cur = 0;
+    check(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "L2 limit");
+    const size_t want = std::min(static_cast<size_t>(maxp), win);
+    if (cur < want) {
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess) {
+            if (!h->l2_limit_changed) {
+                h->l2_limit_changed = true;
+                h->l2_limit_before = cur;
+            }
+        } else {
+            cudaGetLastError();
+        }
+        check(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "L2 limit");
+    }
+    if (cur == 0) return;
+    h->l2win.base = h->st.ppe_cv32;
+    h->l2win.num_bytes = win;
+    h->l2win.hit_ratio = std::min(1.0f, static_cast<float>(cur) / static_cast<float>(win));
+    cudaStreamAttrValue av = {};
+    av.accessPolicyWindow.base_ptr = h->l2win.base;
+    av.accessPolicyWindow.num_bytes = h->l2win.num_bytes;
+    av.accessPolicyWindow.hitRatio = h->l2win.hit_ratio;
+    av.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    av.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    check(cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &av), "L2 window");
+}
+
 void do_solve(mps_handle* h) {
     cudaStream_t s = h->stream;
-    const int max_iter = h->prm.max_cg_iters > 0 ? h->prm.max_cg_iters : static_cast<int>(h->n);
+    const int max_iter = default_max_iter(h->prm.max_cg_iters, h->n, h->prm.solver);
     launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter, 0.01, s);
     after_launch("cg configure");
     launched(h, 1);
     const int solver = h->prm.solver == MPS_SOLVER_CG64 ? MPS_SOLVER_CG64 : MPS_SOLVER_MIXED;
+    if (solver == MPS_SOLVER_MIXED) setup_l2_window(h);
+    if (h->prm.cg_launch == MPS_CG_LAUNCH_HOST) {
+        int64_t k = 0;
+        check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k), "CG host loop");
+        h->direct_launches = k;
+        return;
+    }
+    h->direct_launches = -1;
     if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
-        check(h->cg.build(solver, cg_operands(h), s), "CG graph build");
+        check(h->cg.build(solver, cg_operands(h), s, solver == MPS_SOLVER_MIXED ? h->l2win : L2Window{}),
+              "CG graph build");
     }
     check(h->cg.launch(s), "CG graph launch");
 }
@@ -530,6 +619,7 @@ int mps_create(const mps_params* prm, int device, mps_handle** out) {
     const int rc = guarded(h, [&] {
         validate(h->prm);
         setup_constants(h);
+        check(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device), "SM count");
         check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
         for (auto& e : h->user_events) check(cudaEventCreate(&e), "event");
         for (auto& e : h->stage_events) check(cudaEventCreate(&e), "event");
@@ -550,6 +640,11 @@ int mps_destroy(mps_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->cg.reset();
+    if (h->l2win.num_bytes != 0 || h->l2_limit_changed) {
+        cudaCtxResetPersistingL2Cache();
+        if (h->l2_limit_changed) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_limit_before);
+        cudaGetLastError();
+    }
     dfree_all(h);
     if (h->flush_buf) cudaFree(h->flush_buf);
     for (auto& e : h->user_events)
@@ -575,11 +670,13 @@ int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const doubl
                 throw StatusError{MPS_ERR_INVALID_ARGUMENT, "particle type out of range"};
         const int64_t old = h->n;
         const int64_t total = old + n;
-        if (total > (int64_t{1} << 31) / std::max(1, h->sc.ppe_stride))
-            throw StatusError{MPS_ERR_INVALID_ARGUMENT, "too many particles for 32-bit ELL indexing"};
+        if (total > (int64_t{1} << 31) / std::max(1, h->sc.ppe_stride) ||
+            sell_chunks(total) * sell_chunk_size(h->sc.ppe_stride) >= (int64_t{1} << 31))
+            throw StatusError{MPS_ERR_INVALID_ARGUMENT, "too many particles for 32-bit matrix offsets"};
         allocate(h, total, old);
         h->n = total;
         h->sc.n = static_cast<int32_t>(total);
+        h->sc.nchunks = static_cast<int32_t>(sell_chunks(total));
         DeviceState& st = h->st;
         const size_t b8 = sizeof(double) * n;
         upload(h, st.type + old, type, sizeof(int32_t) * n, false);
@@ -755,6 +852,40 @@ int mps_flush_l2(mps_handle* h, int64_t bytes) {
     });
 }
 
+int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_bytes,
+                   float* ms_per_launch) {
+    if (!h || !ms_per_launch || reps <= 0) return MPS_ERR_INVALID_ARGUMENT;
+    if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED) return MPS_ERR_NOT_SUPPORTED;
+    return guarded(h, [&] {
+        require_particles(h);
+        cudaStream_t s = h->stream;
+        CgOperands o = cg_operands(h);
+        launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1, 0.01, s);
+        if (flush_bytes > 0 && h->flush_bytes < static_cast<size_t>(flush_bytes)) {
+            if (h->flush_buf) cudaFree(h->flush_buf);
+            h->flush_buf = nullptr;
+            h->flush_bytes = 0;
+            check(cudaMalloc(&h->flush_buf, static_cast<size_t>(flush_bytes)), "flush buffer");
+            h->flush_bytes = static_cast<size_t>(flush_bytes);
+        }
+        float total = 0.f;
+        for (int32_t k = 0; k < reps; k++) {
+            if (flush_bytes > 0)
+                check(cudaMemsetAsync(h->flush_buf, k & 0xff, static_cast<size_t>(flush_bytes), s), "flush");
+            check(cudaEventRecord(h->user_events[14], s), "event");
+            launch_spmv_only(solver, o, s);
+            check(cudaEventRecord(h->user_events[15], s), "event");
+            check(cudaEventSynchronize(h->user_events[15]), "event sync");
+            float ms = 0.f;
+            check(cudaEventElapsedTime(&ms, h->user_events[14], h->user_events[15]), "elapsed");
+            total += ms;
+        }
+        after_launch("spmv bench");
+        h->stats.kernel_launches += reps + 1;
+        *ms_per_launch = total / static_cast<float>(reps);
+    });
+}
+
 // ---------------------------------------------------------------- stages
 #define MPS_STAGE(name, body)                              \
     int name(mps_handle* h) {                              \
@@ -835,17 +966,15 @@ int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val
                       double* x, int64_t capacity, int64_t* nnz) {
     return guarded(h, [&] {
         const int64_t n = h->n;
-        std::vector<int32_t> len(static_cast<size_t>(n));
-        download(h, len.data(), h->st.ppe_len, sizeof(int32_t) * n, false);
+        const int64_t nchunks = sell_chunks(n);
+        std::vector<int32_t> len(static_cast<size_t>(nchunks * kSellRows)), off(static_cast<size_t>(nchunks + 1));
+        download(h, len.data(), h->st.ppe_len, sizeof(int32_t) * nchunks * kSellRows, false);
+        download(h, off.data(), h->st.ppe_off, sizeof(int32_t) * (nchunks + 1), false);
         download(h, b, h->st.ppe_b, sizeof(double) * n, false);
         download(h, x, h->st.ppe_x, sizeof(double) * n, false);
         check(cudaStreamSynchronize(h->stream), "ppe");
         int64_t sum = 0;
-        int32_t maxl = 0;
-        for (int32_t l : len) {
-            sum += l;
-            maxl = std::max(maxl, l);
-        }
+        for (int64_t i = 0; i < n; i++) sum += len[static_cast<size_t>(i)];
         if (nnz) *nnz = sum;
         if (row_ptr) {
             row_ptr[0] = 0;
@@ -853,20 +982,22 @@ int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val
         }
         if (!col && !val) return;
         if (sum > capacity) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "PPE capacity too small"};
-        std::vector<int32_t> cbuf(static_cast<size_t>(n) * std::max(maxl, 1));
-        std::vector<double> vbuf(static_cast<size_t>(n) * std::max(maxl, 1));
-        if (maxl > 0) {
-            download(h, cbuf.data(), h->st.ppe_col, sizeof(int32_t) * n * maxl, false);
-            download(h, vbuf.data(), h->st.ppe_val, sizeof(double) * n * maxl, false);
+        const int64_t total = off[static_cast<size_t>(nchunks)];
+        std::vector<int32_t> cbuf(static_cast<size_t>(std::max<int64_t>(total, 1)));
+        std::vector<double> vbuf(static_cast<size_t>(std::max<int64_t>(total, 1)));
+        if (total > 0) {
+            download(h, cbuf.data(), h->st.ppe_col, sizeof(int32_t) * total, false);
+            download(h, vbuf.data(), h->st.ppe_val, sizeof(double) * total, false);
         }
         check(cudaStreamSynchronize(h->stream), "ppe");
-        int64_t off = 0;
+        int64_t o = 0;
         for (int64_t i = 0; i < n; i++) {
+            const int64_t base = off[static_cast<size_t>(i / kSellRows)];
             for (int32_t k = 0; k < len[static_cast<size_t>(i)]; k++) {
-                const size_t e = static_cast<size_t>(k) * n + i;
-                if (col) col[off] = cbuf[e];
-                if (val) val[off] = vbuf[e];
-                off++;
+                const size_t e = static_cast<size_t>(sell_index(base, static_cast<int>(i % kSellRows), k));
+                if (col) col[o] = cbuf[e];
+                if (val) val[o] = vbuf[e];
+                o++;
             }
         }
     });
@@ -901,60 +1032,88 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
     if (!h || n <= 0 || !row_ptr || !b || !x) return MPS_ERR_INVALID_ARGUMENT;
     if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED) return MPS_ERR_NOT_SUPPORTED;
     return guarded(h, [&] {
-        // CSR -> transposed ELL (host), into buffers owned by this call
-        int32_t maxl = 0;
-        for (int64_t i = 0; i < n; i++)
-            maxl = std::max<int32_t>(maxl, static_cast<int32_t>(row_ptr[i + 1] - row_ptr[i]));
-        maxl = std::max(maxl, 1);
-        std::vector<int32_t> len(static_cast<size_t>(n)), ecol(static_cast<size_t>(n) * maxl, 0);
-        std::vector<double> eval(static_cast<size_t>(n) * maxl, 0.0);
-        std::vector<float> eval32(static_cast<size_t>(n) * maxl, 0.0f);
+        // CSR -> SELL-32 on the host, into buffers owned by this call
+        const int64_t nchunks = sell_chunks(n);
+        std::vector<int32_t> len(static_cast<size_t>(nchunks * kSellRows), 0), off(static_cast<size_t>(nchunks + 1), 0);
         for (int64_t i = 0; i < n; i++) {
-            len[static_cast<size_t>(i)] = static_cast<int32_t>(row_ptr[i + 1] - row_ptr[i]);
+            const int64_t l = row_ptr[i + 1] - row_ptr[i];
+            if (l < 0 || l > (1 << 24)) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "bad row_ptr"};
+            len[static_cast<size_t>(i)] = static_cast<int32_t>(l);
+        }
+        for (int64_t c = 0; c < nchunks; c++) {
+            int32_t m = 0;
+            for (int r = 0; r < kSellRows; r++) m = std::max(m, len[static_cast<size_t>(kSellRows * c + r)]);
+            const int64_t next = off[static_cast<size_t>(c)] + sell_chunk_size(m);
+            if (next >= (int64_t{1} << 31)) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "matrix too large"};
+            off[static_cast<size_t>(c + 1)] = static_cast<int32_t>(next);
+        }
+        const size_t total = static_cast<size_t>(std::max<int32_t>(off[static_cast<size_t>(nchunks)], 1));
+        std::vector<int32_t> ecol(total, 0);
+        std::vector<double> eval(total, 0.0);
+        std::vector<uint2> ecv(total, make_uint2(0u, 0u));
+        for (int64_t i = 0; i < n; i++) {
+            const int64_t base = off[static_cast<size_t>(i / kSellRows)];
             for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
                 const int32_t c = col[k];
                 if (c < 0 || c >= n) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "column out of range"};
-                const size_t e = static_cast<size_t>(k - row_ptr[i]) * n + i;
+                const size_t e = static_cast<size_t>(sell_index(base, static_cast<int>(i % kSellRows),
+                                                                static_cast<int>(k - row_ptr[i])));
                 ecol[e] = c;
                 eval[e] = val[k];
-                eval32[e] = static_cast<float>(val[k]);
+                const float f = static_cast<float>(val[k]);
+                uint32_t bits;
+                std::memcpy(&bits, &f, sizeof(bits));
+                ecv[e] = make_uint2(static_cast<uint32_t>(c), bits);
             }
         }
         ScopedBuffers loc;
         const size_t nn = static_cast<size_t>(n);
         CgOperands o{};
         o.n = static_cast<int32_t>(n);
-        int32_t* dlen = loc.get<int32_t>(nn);
-        int32_t* dcol = loc.get<int32_t>(nn * maxl);
-        double* dval = loc.get<double>(nn * maxl);
-        float* dval32 = loc.get<float>(nn * maxl);
+        o.nchunks = static_cast<int32_t>(nchunks);
+        o.grid_vec = cg_grid_vec(n);
+        o.grid_spmv = cg_grid_spmv(n);
+        int32_t* dlen = loc.get<int32_t>(len.size());
+        int32_t* doff = loc.get<int32_t>(off.size());
+        int32_t* dcol = loc.get<int32_t>(total);
+        double* dval = loc.get<double>(total);
+        uint2* dcv = loc.get<uint2>(total);
         double* db = loc.get<double>(nn);
         double* dx = loc.get<double>(nn);
         o.len = dlen;
+        o.off = doff;
         o.col = dcol;
         o.val = dval;
-        o.val32 = dval32;
+        o.cv32 = dcv;
         o.b = db;
         o.x = dx;
         o.r = loc.get<double>(nn);
         o.p = loc.get<double>(nn);
         o.Ap = loc.get<double>(nn);
+        o.x2 = loc.get<double>(nn);
         o.r32 = loc.get<float>(nn);
-        o.p32 = loc.get<float>(nn);
         o.q32 = loc.get<float>(nn);
         o.d32 = loc.get<float>(nn);
-        o.partials = loc.get<double>(2 * static_cast<size_t>(grid_for(n)) + 64);
+        o.p32a = loc.get<float>(nn);
+        o.p32b = loc.get<float>(nn);
+        o.partials = loc.get<double>(static_cast<size_t>(cg_partials(n)));
         o.S = loc.get<CgScalars>(1);
         cudaStream_t s = h->stream;
-        check(cudaMemcpyAsync(dlen, len.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice, s), "up");
-        check(cudaMemcpyAsync(dcol, ecol.data(), sizeof(int32_t) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
-        check(cudaMemcpyAsync(dval, eval.data(), sizeof(double) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
-        check(cudaMemcpyAsync(dval32, eval32.data(), sizeof(float) * nn * maxl, cudaMemcpyHostToDevice, s), "up");
-        check(cudaMemcpyAsync(db, b, sizeof(double) * nn, cudaMemcpyHostToDevice, s), "up");
-        check(cudaMemcpyAsync(dx, x, sizeof(double) * nn, cudaMemcpyHostToDevice, s), "up");
+        auto up = [&](void* d, const void* src, size_t bytes) {
+            check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s), "upload");
+        };
+        up(dlen, len.data(), sizeof(int32_t) * len.size());
+        up(doff, off.data(), sizeof(int32_t) * off.size());
+        up(dcol, ecol.data(), sizeof(int32_t) * total);
+        up(dval, eval.data(), sizeof(double) * total);
+        up(dcv, ecv.data(), sizeof(uint2) * total);
+        up(db, b, sizeof(double) * nn);
+        up(dx, x, sizeof(double) * nn);
         check(cudaMemsetAsync(o.S, 0, sizeof(CgScalars), s), "memset");
         check(cudaMemsetAsync(o.d32, 0, sizeof(float) * nn, s), "memset");
-        launch_cg_configure(o.S, eps, criterion, max_iters > 0 ? max_iters : static_cast<int>(n), 0.01, s);
+        check(cudaMemsetAsync(o.p32a, 0, sizeof(float) * nn, s), "memset");
+        check(cudaMemsetAsync(o.p32b, 0, sizeof(float) * nn, s), "memset");
+        launch_cg_configure(o.S, eps, criterion, default_max_iter(max_iters, n, solver), 0.01, s);
         CgGraph g;
         check(g.build(solver, o, s), "CG graph build");
         check(g.launch(s), "CG graph launch");

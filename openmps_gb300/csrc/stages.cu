@@ -310,22 +310,39 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     st.ppe_len[i] = m + 1;
 }
 
+// Chunk sizes of the SELL-32 layout: one warp per chunk of 32 rows.
+__global__ void k_ppe_chunks(SceneConst sc, DeviceState st) {
+    const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (c >= sc.nchunks) return;
+    if (step_failed(sc, st)) return;
+    const int lane = threadIdx.x & 31;
+    const int len = st.ppe_len[c * kSellRows + lane];
+    const int m = __reduce_max_sync(0xffffffffu, len);
+    if (lane == 0) st.ppe_chunk[c] = static_cast<int>(sell_chunk_size(m));
+}
+
 // Row entries to ascending column order (uBLAS compressed_matrix, Computer.hpp:1330-1350):
-// each entry goes to its rank among the row's columns (columns are distinct).
+// each entry goes to its rank among the row's columns (columns are distinct), at its
+// SELL-32 position.
 __global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
     const int n = sc.n;
-    const int len = st.ppe_len[i];
+    const int len = (i < n) ? st.ppe_len[i] : 0;
+    warp_add_u64(&st.status->ppe_nnz, static_cast<unsigned long long>(len));
+    if (i >= n) return;
+    const int64_t base = st.ppe_off[i / kSellRows];
+    const int r = i % kSellRows;
     for (int e = 0; e < len; e++) {
         const int ce = st.ppe_col_tmp[ell(e, n, i)];
         int rank = 0;
         for (int f = 0; f < len; f++) rank += (st.ppe_col_tmp[ell(f, n, i)] < ce) ? 1 : 0;
         const double v = st.ppe_val_tmp[ell(e, n, i)];
-        st.ppe_col[ell(rank, n, i)] = ce;
-        st.ppe_val[ell(rank, n, i)] = v;
-        if (want_fp32) st.ppe_val32[ell(rank, n, i)] = __double2float_rn(v);
+        const int64_t at = sell_index(base, r, rank);
+        st.ppe_col[at] = ce;
+        st.ppe_val[at] = v;
+        if (want_fp32) st.ppe_cv32[at] = make_uint2(static_cast<unsigned>(ce),
+                                                     __float_as_uint(__double2float_rn(v)));
     }
 }
 
@@ -490,6 +507,8 @@ void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s) 
 
 void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
     k_ppe_build<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_ppe_chunks<<<grid_for(static_cast<int64_t>(sc.nchunks) * 32), kBlock, 0, s>>>(sc, st);
+    launch_exclusive_scan(st.ppe_chunk, st.ppe_off, sc.nchunks, st.scan_scratch, s);
     k_ppe_sort<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, want_fp32 ? 1 : 0);
 }
 

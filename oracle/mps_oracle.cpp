@@ -776,7 +776,7 @@ extern "C" {
 
 int oracle_create(const mps_params* prm, oracle_handle** out) {
     if (!prm || !out) return MPS_ERR_INVALID_ARGUMENT;
-    if (!(prm->l0 > 0) || !(prm->re_by_l0 > 0) || !(prm->g > 0) || !(prm->max_x > prm->min_x) ||
+    if (!(prm->l0 > 0) || !(prm->re_by_l0 > 0) || !(prm->g >= 0) || !(prm->max_x > prm->min_x) ||
         !(prm->max_z > prm->min_z))
         return MPS_ERR_INVALID_ARGUMENT;
     auto* h = new oracle_handle;

@@ -77,12 +77,17 @@ def reference_tank(l0=0.008):
 
 
 def plain_tank(l0=0.01, ds=False):
-    s = scenes.config_c0() if l0 == 0.01 else scenes.dam_break(l0)
+    s = scenes.config_c0_plain() if l0 == 0.01 else scenes.dam_break(l0)
     s.meta.setdefault("params", dict(scenes.PLAIN_PHYSICS, eps=1e-10, max_dt=5e-4))
     if ds:
         s.meta["params"]["flags"] = abi.FLAG_DS
     s.meta["dt"] = 5e-4
     return s
+
+
+def stock_tank():
+    """The l0 = 0.01 dam break with the stock method set and two radii (the workload physics)."""
+    return scenes.config_c0()
 
 
 def jittered_tank(l0=0.01, jitter=0.05, seed=7, preset=abi.PRESET_PLAIN):

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from helpers import (assert_same_neighbors, assert_same_particles, assert_same_ppe, copy_state,
-                     jittered_tank, make_pair, plain_tank, reference_tank)
+                     jittered_tank, make_pair, plain_tank, reference_tank, stock_tank)
 from openmps_gb300 import _abi as abi
 
 pytestmark = pytest.mark.gpu
@@ -22,6 +22,7 @@ CASES = {
     "plain_two_radii_ds": lambda: plain_tank(ds=True),
     "jittered_reference": lambda: jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
     "jittered_plain": lambda: jittered_tank(jitter=0.1),
+    "stock_two_radii": stock_tank,
 }
 
 

@@ -9,7 +9,8 @@ both sit at the discrete solution.
 import numpy as np
 import pytest
 
-from helpers import copy_state, jittered_tank, make_pair, plain_tank, reference_tank, rel_err
+from helpers import (copy_state, jittered_tank, make_pair, plain_tank, reference_tank, rel_err,
+                     stock_tank)
 from openmps_gb300 import _abi as abi
 from openmps_gb300 import scenes
 
@@ -23,6 +24,7 @@ CASES = {
     "plain_two_radii": plain_tank,
     "plain_two_radii_ds": lambda: plain_tank(ds=True),
     "jittered_reference": lambda: jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
+    "stock_two_radii": stock_tank,
 }
 
 
@@ -84,20 +86,24 @@ def test_cfl_step(gpu_lib, oracle_lib):
 
 
 def test_hydrostatic_pressure(gpu_lib):
-    # physics check: a tank at rest settles to p ~ rho g (h - z) away from the surface
+    # physics check: a tank at rest develops a pressure that grows linearly with depth,
+    # dp/dz ~ -rho g (fitted over the bulk, time-averaged over the last half of 0.6 s)
     s = scenes.tank(0.01, 40, 30, 40, 40)
-    prm = s.params(**dict(scenes.PLAIN_PHYSICS, eps=1e-8, max_dt=1e-3, flags=abi.FLAG_DS))
+    prm = s.params(**dict(scenes.STOCK_PHYSICS, eps=1e-8, max_dt=1e-3))
     from openmps_gb300.computer import Computer
 
     c = Computer(prm)
     c.add_scene(s)
-    c.forward_steps(1e-3, 300)
+    acc = None
+    for k in range(600):
+        c.forward_time(1e-3)
+        if k >= 300:
+            p = c.particles()["p"]
+            acc = p.copy() if acc is None else acc + p
     P = c.particles()
     fluid = P["type"] == abi.TYPE_FLUID
-    depth = 29 * 0.01
     z = P["z"][fluid]
-    p = P["p"][fluid]
-    sel = (z > 0.05) & (z < depth - 0.08)
-    expect = prm.rho * prm.g * (depth - z[sel])
-    err = np.abs(np.mean(p[sel]) - np.mean(expect)) / np.mean(expect)
-    assert err < 0.15, err
+    p = acc[fluid] / 300.0
+    sel = (z > 0.03) & (z < 0.24)
+    slope = np.polyfit(z[sel], p[sel], 1)[0]
+    assert abs(-slope / (prm.rho * prm.g) - 1.0) < 0.15, slope
