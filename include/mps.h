@@ -42,6 +42,8 @@ extern "C" {
 #define MPS_ERR_TIMEOUT 9
 /* a device-side bounds check fired (index recorded, access skipped) */
 #define MPS_ERR_DEVICE_CHECK 10
+/* the system is larger than the allocation-free solve's fixed scratch (MPS_NOALLOC_MAX_ROWS) */
+#define MPS_ERR_NOALLOC_TOO_LARGE 11
 
 /* ------------------------------------------------- particle types (Particle.hpp:16-29) */
 #define MPS_TYPE_FLUID 0    /* Particle::Type::IncompressibleNewton */
@@ -249,6 +251,30 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
                      const double* val, const double* b, double* x, double eps,
                      int32_t criterion, int32_t max_iters, int32_t solver, int32_t* iterations,
                      double* true_relres);
+
+/* ------------------------------------------------------------------------
+ * Allocation-free PPE solve.  No counterpart in the reference: the reference owns all
+ * its memory.  For callers that cannot allocate device memory -- an application whose
+ * device memory is already reserved by its own caching allocator or arena, or code on
+ * a latency-critical path where cudaMalloc/cudaFree would synchronize the device --
+ * this solves A x = b with the FP64 CG of the reference (Computer.hpp:1359-1429) on a
+ * CSR system that already lives in the caller's device memory, and allocates nothing:
+ * its scratch vectors sit in one static device array sized for MPS_NOALLOC_MAX_ROWS
+ * rows (about 6 MiB, held by every GPU that loads the library until the process
+ * exits).  Larger systems return MPS_ERR_NOALLOC_TOO_LARGE.
+ *
+ * All pointers are device pointers on the current device; `stream` is a
+ * cudaStream_t (NULL: the default stream); x holds the initial guess on entry and the
+ * solution on return.  The first call on a device resolves the scratch array's
+ * address (cudaGetSymbolAddress) and should come before any stream capture.  Every
+ * call shares the one array: calls that overlap on the GPU (other streams or host
+ * threads at the same time) race.  The call returns when the solve is complete.
+ * ---------------------------------------------------------------------- */
+#define MPS_NOALLOC_MAX_ROWS 262144
+int mps_cg_solve_csr_device_noalloc(int64_t n, const int64_t* row_ptr, const int32_t* col,
+                                    const double* val, const double* b, double* x, double eps,
+                                    int32_t criterion, int32_t max_iters, void* stream,
+                                    int32_t* iterations, double* true_relres);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,8 @@ MPS_ERR_STATE = 7
 MPS_ERR_NONFINITE = 8
 MPS_ERR_TIMEOUT = 9
 MPS_ERR_DEVICE_CHECK = 10
+MPS_ERR_NOALLOC_TOO_LARGE = 11
+NOALLOC_MAX_ROWS = 262144
 
 # particle types (src/OpenMps/Particle.hpp:16-29)
 TYPE_FLUID = 0

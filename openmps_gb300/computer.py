@@ -76,6 +76,8 @@ PROTOTYPES = {
     "mps_debug_set_aux": (C.c_int, [_P, _D, _D, _D, _D]),
     "mps_cg_solve_csr": (C.c_int, [_P, C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int32,
                                    C.c_int32, C.c_int32, _I32, _D]),
+    "mps_cg_solve_csr_device_noalloc": (C.c_int, [C.c_int64, _P, _P, _P, _P, _P, C.c_double,
+                                                  C.c_int32, C.c_int32, _P, _I32, _D]),
 }
 
 

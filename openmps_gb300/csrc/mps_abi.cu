@@ -594,6 +594,7 @@ const char* mps_status_string(int status) {
         case MPS_ERR_NONFINITE: return "non-finite value";
         case MPS_ERR_TIMEOUT: return "device wait timed out";
         case MPS_ERR_DEVICE_CHECK: return "device bounds check";
+        case MPS_ERR_NOALLOC_TOO_LARGE: return "system larger than the allocation-free scratch";
         default: return "unknown status";
     }
 }
