@@ -106,30 +106,6 @@ __device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, 
     return acc;
 }
 
-// Row i of the FP32 matrix times (beta * pold + r), FP32 accumulation, ascending columns.
-// The {column, value} pairs keep default caching: the FP32 matrix is meant to stay in L2.
-__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
-                                       const float* __restrict__ pold,
-                                       const float* __restrict__ rv, float beta) {
-    float acc = 0.0f;
-    int k = 0;
-    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
-        uint2 e[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
-        float v[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) v[u] = fmaf(beta, pold[e[u].x], rv[e[u].x]);
-#pragma unroll
-        for (int u = 0; u < 8; u++) acc = fmaf(__uint_as_float(e[u].y), v[u], acc);
-    }
-    for (; k < L; k++, at += kSellRows) {
-        const uint2 e = __ldg(o.cv32 + at);
-        acc = fmaf(__uint_as_float(e.y), fmaf(beta, pold[e.x], rv[e.x]), acc);
-    }
-    return acc;
-}
-
 // One warp per chunk of kSellRows rows (lane = row within the chunk).  The SpMV kernels
 // launch as many warps as chunks so the block scheduler balances uneven chunks.
 struct ChunkLoop {
@@ -303,7 +279,35 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
 }
 
 // ------------------------------------------------------------ MIXED kernels
-// r = b - A x (FP64); r32 = r; d = 0; the first direction is r (beta = 0, pold = 0)
+// Chronopoulos-Gear CG (Chronopoulos & Gear 1989): with s = A p and w = A r kept as
+// vectors, both dot products of an iteration (gamma = r.r, delta = w.r) come out of one
+// reduction.  An iteration is an elementwise kernel (s, p, d, r updates, no reduction)
+// followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
+
+// Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
+// The {column, value} pairs keep default caching: the FP32 matrix is meant to stay in L2.
+__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
+                                       const float* __restrict__ v) {
+    float acc = 0.0f;
+    int k = 0;
+    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
+        uint2 e[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
+        float xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) xv[u] = v[e[u].x];
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
+    }
+    for (; k < L; k++, at += kSellRows) {
+        const uint2 e = __ldg(o.cv32 + at);
+        acc = fmaf(__uint_as_float(e.y), v[e.x], acc);
+    }
+    return acc;
+}
+
+// init: r_0 = b - A x (FP64); r32 = r_0; d = 0; p = 0; s = 0; rr, bb
 __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
     __shared__ double ws[kBlock];
@@ -319,7 +323,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphCondi
             const double bi = o.b[i];
             const double ri = bi - ax;
             o.r32[i] = __double2float_rn(ri);
-            o.p32a[i] = 0.0f;
+            o.s32[i] = 0.0f;
+            o.p32[i] = 0.0f;
             o.d32[i] = 0.0f;
             vrr += ri * ri;
             vbb += bi * bi;
@@ -334,77 +339,86 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphCondi
     }
 }
 
-// p = r + beta pold (formed on the fly while gathering); q = A32 p; alpha = rr / (p.q)
-__global__ void __launch_bounds__(kBlock) k_mx_spmv_dot(CgOperands o) {
-    __shared__ double ws[kBlock];
+// s = w + beta s; p = r + beta p; d += alpha p; r -= alpha s (FP32, no reduction)
+__global__ void __launch_bounds__(kBlock) k_mx_axpy(CgOperands o) {
     if (cg_done(o.S)) return;
-    const ChunkLoop cl;
-    const int parity = o.S->iter & 1;
-    const float* __restrict__ pold = parity ? o.p32b : o.p32a;
-    float* __restrict__ pnew = parity ? o.p32a : o.p32b;
+    const float alpha = __double2float_rn(o.S->alpha);
     const float beta = __double2float_rn(o.S->beta);
-    const bool clear_d = o.S->do_update != 0;  // d was folded into x by the last reliable update
-    double v = 0.0;
-    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
-        const int i = kSellRows * c + cl.lane;
-        const int L = o.len[i];
-        const float q = row32(o, sell_index(o.off[c], cl.lane, 0), L, pold, o.r32, beta);
-        if (i < o.n) {
-            const float pn = fmaf(beta, pold[i], o.r32[i]);
-            pnew[i] = pn;
-            o.q32[i] = q;
-            if (clear_d) o.d32[i] = 0.0f;
-            v += static_cast<double>(pn) * static_cast<double>(q);
-        }
-    }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double pq = gather_sum(o.partials, gridDim.x, ws);
-        if (threadIdx.x == 0) {
-            o.S->counter = 0;
-            o.S->pAp = pq;
-            o.S->alpha = o.S->rr / pq;
-        }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
+        const float ri = o.r32[i];
+        const float si = fmaf(beta, o.s32[i], o.w32[i]);
+        const float pi = fmaf(beta, o.p32[i], ri);
+        o.s32[i] = si;
+        o.p32[i] = pi;
+        o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+        o.r32[i] = fmaf(-alpha, si, ri);
     }
 }
 
-// d += alpha p; r -= alpha q (FP32); rr_new in FP64; decides a reliable update
-__global__ void __launch_bounds__(kBlock) k_mx_update(CgOperands o, cudaGraphConditionalHandle h,
-                                                     cudaGraphConditionalHandle h_true,
-                                                     int use_cond) {
+// w = A r (FP32); gamma = r.r and delta = w.r in FP64; the next Chronopoulos-Gear step
+// sizes; decides a reliable update.  mode 0: after init (beta = 0); mode 1: an
+// iteration; mode 2: after a reliable update (also clears d, folded into x).
+__global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
+                                                   cudaGraphConditionalHandle h,
+                                                   cudaGraphConditionalHandle h_true, int use_cond) {
     __shared__ double ws[kBlock];
-    if (cg_done(o.S)) return;
-    const float a = __double2float_rn(o.S->alpha);
-    const float* __restrict__ pnew = (o.S->iter & 1) ? o.p32a : o.p32b;
-    double v = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
-        o.d32[i] = fmaf(a, pnew[i], o.d32[i]);
-        const float ri = fmaf(-a, o.q32[i], o.r32[i]);
-        o.r32[i] = ri;
-        v += static_cast<double>(ri) * static_cast<double>(ri);
+    CgScalars* S = o.S;
+    if (mode == 2) {
+        if (S->converged || S->aborted || !S->do_update) return;
+    } else if (mode == 1) {
+        if (cg_done(S)) return;
+    } else if (S->converged || S->aborted) {
+        return;
     }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double rr_new = gather_sum(o.partials, gridDim.x, ws);
+    const ChunkLoop cl;
+    const float* __restrict__ r = o.r32;
+    double vg = 0.0, vd = 0.0;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const float wi = row32(o, sell_index(o.off[c], cl.lane, 0), L, r);
+        if (i < o.n) {
+            const double ri = static_cast<double>(r[i]);
+            o.w32[i] = wi;
+            if (mode == 2) o.d32[i] = 0.0f;
+            vg += ri * ri;
+            vd += static_cast<double>(wi) * ri;
+        }
+    }
+    const double s0 = block_sum(vg, ws);
+    const double s1 = block_sum(vd, ws);
+    if (publish(s0, s1, o.partials, &o.S->counter)) {
+        const double gam = gather_sum(o.partials, gridDim.x, ws);
+        const double del = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
         if (threadIdx.x == 0) {
-            CgScalars* S = o.S;
             S->counter = 0;
-            S->rr_new = rr_new;
-            const int reliable = (rr_new < S->delta2 * S->rr_upd) || (rr_new < S->thr);
-            S->do_update = reliable;
-            if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
+            S->rr_new = gam;
+            int reliable = 0;
+            if (mode == 1) {
+                reliable = (gam < S->delta2 * S->rr_upd) || (gam < S->thr);
+                S->do_update = reliable;
+                if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
+            }
             if (!reliable) {
-                S->beta = rr_new / S->rr;
-                S->rr = rr_new;
-                S->iter += 1;
-                if (use_cond) cudaGraphSetConditional(h, (S->iter < S->max_iter) ? 1u : 0u);
+                if (mode == 0) {
+                    S->beta = 0.0;
+                    S->alpha = gam / del;
+                } else {
+                    const double beta = gam / S->rr;
+                    S->beta = beta;
+                    S->alpha = gam / (del - beta * gam / S->alpha);
+                    S->iter += 1;
+                    if (use_cond) cudaGraphSetConditional(h, (S->iter < S->max_iter) ? 1u : 0u);
+                }
+                S->rr = gam;
+                S->pAp = del;
             }
         }
     }
 }
 
-// Reliable update: x' = x + d and r = b - A x' in FP64 (FP64 matrix); r32 = r;
-// convergence on this true residual.  d is cleared by the next SpMV kernel.
+// Reliable update, part 1: x' = x + d and r = b - A x' in FP64 (FP64 matrix), written
+// over the r the iteration produced; convergence on this true residual.
 __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
     __shared__ double ws[kBlock];
@@ -414,6 +428,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
     const double* __restrict__ xc = odd ? o.x2 : o.x;
     double* __restrict__ xn = odd ? o.x : o.x2;
     const float* __restrict__ d = o.d32;
+    float* __restrict__ rslot = o.r32;
     double v = 0.0;
     for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
@@ -423,7 +438,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
         if (i < o.n) {
             const double ri = o.b[i] - ax;
             xn[i] = xc[i] + static_cast<double>(d[i]);
-            o.r32[i] = __double2float_rn(ri);
+            rslot[i] = __double2float_rn(ri);
             v += ri * ri;
         }
     }
@@ -439,12 +454,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
             S->updates += 1;
             const int conv = rr < S->thr;
             S->converged = conv;
-            if (!conv) {
-                S->beta = rr / S->rr;
-                S->rr = rr;
+            if (conv) {
+                S->iter += 1;
+                if (use_cond) cudaGraphSetConditional(h, 0u);
             }
-            S->iter += 1;
-            if (use_cond) cudaGraphSetConditional(h, (!conv && S->iter < S->max_iter) ? 1u : 0u);
         }
     }
 }
@@ -486,9 +499,12 @@ void body_kernels(int solver, const CgOperands& ops, cudaGraphConditionalHandle 
         k_cg_update<<<gv, kBlock, 0, s>>>(ops, h, use_cond);
         k_cg_pupdate<<<gv, kBlock, 0, s>>>(ops);
     } else {
-        k_mx_spmv_dot<<<gs, kBlock, 0, s>>>(ops);
-        k_mx_update<<<gv, kBlock, 0, s>>>(ops, h, h_true, use_cond);
-        if (with_true) k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
+        k_mx_axpy<<<gv, kBlock, 0, s>>>(ops);
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
+        if (with_true) {
+            k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
+            k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
+        }
     }
 }
 
@@ -509,7 +525,7 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
     if (solver == MPS_SOLVER_CG64)
         k_cg_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
     else
-        k_mx_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
+        k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
 }
 
 CgGraph::~CgGraph() { reset(); }
@@ -578,16 +594,34 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    if (solver == MPS_SOLVER_CG64)
+    if (solver == MPS_SOLVER_CG64) {
         k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
-    else
+    } else {
         k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, 1);
+    }
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
-    size_t nn = 1;
+    // the last node of the init chain
     cudaGraphNode_t init_node;
-    e = cudaGraphGetNodes(graph_, &init_node, &nn);
-    if (e != cudaSuccess) return e;
+    {
+        size_t nn = 0;
+        e = cudaGraphGetNodes(graph_, nullptr, &nn);
+        if (e != cudaSuccess) return e;
+        std::vector<cudaGraphNode_t> nodes(nn);
+        e = cudaGraphGetNodes(graph_, nodes.data(), &nn);
+        if (e != cudaSuccess) return e;
+        init_node = nodes[0];
+        if (nn > 1) {
+            size_t ne = 0;
+            e = cudaGraphGetEdges(graph_, nullptr, nullptr, nullptr, &ne);
+            if (e != cudaSuccess || ne != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
+            cudaGraphNode_t from, to;
+            e = cudaGraphGetEdges(graph_, &from, &to, nullptr, &ne);
+            if (e != cudaSuccess) return e;
+            init_node = to;
+        }
+    }
 
     // while (cond) { body }
     cudaGraphNodeParams cp = {};
@@ -614,7 +648,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     if (e != cudaSuccess) return e;
 
     if (nested) {
-        // if (reliable update due) { k_mx_true } after the update kernel
+        // if (reliable update due) { true residual; w = A r } after the SpMV kernel
         size_t ne = 0;
         e = cudaGraphGetEdges(body, nullptr, nullptr, nullptr, &ne);
         if (e != cudaSuccess || ne != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
@@ -634,7 +668,10 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
                                           cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
         k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, 1);
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 2, h, 0, 1);
         e = cudaStreamEndCapture(s, &captured);
+        if (e != cudaSuccess) return e;
+        e = apply_window(if_body, win);
         if (e != cudaSuccess) return e;
     }
 
@@ -665,11 +702,14 @@ cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, 
     const int gv = ops.grid_vec, gs = ops.grid_spmv;
     const cudaGraphConditionalHandle none = 0;
     int64_t k = 0;
-    if (solver == MPS_SOLVER_CG64)
+    if (solver == MPS_SOLVER_CG64) {
         k_cg_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
-    else
+        k++;
+    } else {
         k_mx_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
-    k++;
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, none, none, 0);
+        k += 2;
+    }
     cudaError_t e = cudaGetLastError();
     for (;;) {
         if (e != cudaSuccess) return e;
@@ -679,7 +719,7 @@ cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, 
         if (host_S->converged || host_S->aborted || host_S->iter >= host_S->max_iter) break;
         for (int c = 0; c < chunk; c++) {
             body_kernels(solver, ops, none, none, 0, true, s);
-            k += 3;
+            k += solver == MPS_SOLVER_CG64 ? 3 : 4;  // MIXED: axpy, SpMV + 2 reliable-update kernels
         }
         e = cudaGetLastError();
     }

@@ -43,9 +43,9 @@ struct CgOperands {
     double* x;          // initial guess in, solution out
     // CG64
     double *r, *p, *Ap;
-    // MIXED
+    // MIXED (Chronopoulos-Gear CG in FP32): r, w = A r, s = A p, p, correction d
     double* x2;         // second FP64 solution buffer (reliable updates alternate)
-    float *r32, *q32, *d32, *p32a, *p32b;
+    float *r32, *w32, *s32, *p32, *d32;
     double* partials;   // 2 * max(grid_vec, grid_spmv) doubles
     CgScalars* S;
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
@@ -69,7 +69,7 @@ public:
     int solver() const { return solver_; }
     const CgOperands& operands() const { return ops_; }
     // kernels per iteration (the MIXED reliable-update kernel runs only when due)
-    int kernels_per_iteration() const { return solver_ == MPS_SOLVER_CG64 ? 3 : (nested_ ? 2 : 3); }
+    int kernels_per_iteration() const { return solver_ == MPS_SOLVER_CG64 ? 3 : (nested_ ? 2 : 4); }
     bool nested() const { return nested_; }
 
 private:

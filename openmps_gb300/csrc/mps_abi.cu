@@ -53,7 +53,7 @@ struct mps_handle {
     CgScalars* S = nullptr;
     double* partials = nullptr;
     double *r = nullptr, *p = nullptr, *Ap = nullptr, *x2 = nullptr;
-    float *r32 = nullptr, *q32 = nullptr, *d32 = nullptr, *p32a = nullptr, *p32b = nullptr;
+    float *r32 = nullptr, *w32 = nullptr, *s32 = nullptr, *p32 = nullptr, *d32 = nullptr;
     int sm_count = 1;
     CgGraph cg;
     int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
@@ -243,10 +243,10 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     h->Ap = dalloc<double>(h, n);
     h->x2 = dalloc<double>(h, n);
     h->r32 = dalloc<float>(h, n);
-    h->q32 = dalloc<float>(h, n);
+    h->w32 = dalloc<float>(h, n);
+    h->s32 = dalloc<float>(h, n);
+    h->p32 = dalloc<float>(h, n);
     h->d32 = dalloc<float>(h, n);
-    h->p32a = dalloc<float>(h, n);
-    h->p32b = dalloc<float>(h, n);
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -257,8 +257,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(st.nb_count, 0, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * kSellRows * sell_chunks(n), s), "memset");
-    check(cudaMemsetAsync(h->p32a, 0, sizeof(float) * n, s), "memset");
-    check(cudaMemsetAsync(h->p32b, 0, sizeof(float) * n, s), "memset");
+    check(cudaMemsetAsync(h->p32, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(st.cell_count, 0, sizeof(int32_t) * cells, s), "memset");
     if (keep > 0) {
         check(cudaMemcpyAsync(st.type, old.type, sizeof(int32_t) * keep, cudaMemcpyDeviceToDevice, s),
@@ -298,10 +297,10 @@ CgOperands cg_operands(mps_handle* h) {
     o.Ap = h->Ap;
     o.x2 = h->x2;
     o.r32 = h->r32;
-    o.q32 = h->q32;
+    o.w32 = h->w32;
+    o.s32 = h->s32;
+    o.p32 = h->p32;
     o.d32 = h->d32;
-    o.p32a = h->p32a;
-    o.p32b = h->p32b;
     o.partials = h->partials;
     o.S = h->S;
     o.status = h->st.status;
@@ -350,10 +349,9 @@ void read_status(mps_handle* h, bool solve_done) {
         if (h->direct_launches >= 0)
             launched(h, static_cast<int>(h->direct_launches));
         else
-            launched(h, 2 + (h->prm.solver == MPS_SOLVER_CG64 ? 0 : 1) +
-                            (h->prm.solver == MPS_SOLVER_CG64
-                                 ? 3 * S.iter
-                                 : (h->cg.nested() ? 2 * S.iter + S.updates : 3 * S.iter)));
+            launched(h, h->prm.solver == MPS_SOLVER_CG64
+                            ? 2 + 3 * S.iter
+                            : 4 + (h->cg.nested() ? 2 * S.iter + 2 * S.updates : 4 * S.iter));
     }
     const int f = h->h_status->flags;
     if (f & kStatusCellOverflow) throw StatusError{MPS_ERR_CELL_OVERFLOW, "Too many particle in a block"};
@@ -871,6 +869,7 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
         }
         float total = 0.f;
         for (int32_t k = 0; k < reps; k++) {
+            launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1 << 30, 0.01, s);
             if (flush_bytes > 0)
                 check(cudaMemsetAsync(h->flush_buf, k & 0xff, static_cast<size_t>(flush_bytes), s), "flush");
             check(cudaEventRecord(h->user_events[14], s), "event");
@@ -1093,10 +1092,10 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         o.Ap = loc.get<double>(nn);
         o.x2 = loc.get<double>(nn);
         o.r32 = loc.get<float>(nn);
-        o.q32 = loc.get<float>(nn);
+        o.w32 = loc.get<float>(nn);
+        o.s32 = loc.get<float>(nn);
+        o.p32 = loc.get<float>(nn);
         o.d32 = loc.get<float>(nn);
-        o.p32a = loc.get<float>(nn);
-        o.p32b = loc.get<float>(nn);
         o.partials = loc.get<double>(static_cast<size_t>(cg_partials(n)));
         o.S = loc.get<CgScalars>(1);
         cudaStream_t s = h->stream;
@@ -1112,8 +1111,7 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         up(dx, x, sizeof(double) * nn);
         check(cudaMemsetAsync(o.S, 0, sizeof(CgScalars), s), "memset");
         check(cudaMemsetAsync(o.d32, 0, sizeof(float) * nn, s), "memset");
-        check(cudaMemsetAsync(o.p32a, 0, sizeof(float) * nn, s), "memset");
-        check(cudaMemsetAsync(o.p32b, 0, sizeof(float) * nn, s), "memset");
+        check(cudaMemsetAsync(o.p32, 0, sizeof(float) * nn, s), "memset");
         launch_cg_configure(o.S, eps, criterion, default_max_iter(max_iters, n, solver), 0.01, s);
         CgGraph g;
         check(g.build(solver, o, s), "CG graph build");
@@ -1124,7 +1122,7 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         check(cudaStreamSynchronize(s), "cg solve");
         if (iterations) *iterations = S.iter;
         if (true_relres) *true_relres = (S.bb > 0) ? std::sqrt(S.true_rr / S.bb) : std::sqrt(S.true_rr);
-        h->stats.kernel_launches += 3 + S.iter * g.kernels_per_iteration();
+        h->stats.kernel_launches += 4 + S.iter * g.kernels_per_iteration() + 2 * S.updates;
         if (!S.converged)
             throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
                               "Conjugate Gradient method couldn't solve Pressure Poison Equation"};
