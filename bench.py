@@ -3,9 +3,11 @@
 
 Workload (one "step" = one ``ForwardTime(dt)`` of the whole scene): a 0.2 m x
 0.4 m water column at l0 = 5e-4 m (320,000 fluid particles) in a 0.8 m x 0.6 m
-tank with 3 wall + 2 dummy layers (340,050 particles in all), plain MPS with
-r_e = 2.1 l0 for density/gradient and 4.0 l0 for the Laplacian (PPE with ~45
-nonzeros per row), dt = 2.5e-5 s, PPE solved to |b - A x| <= 1e-8 |b|.  The data
+tank with 3 wall + 2 dummy layers (340,050 particles in all), the reference's
+stock scheme (higher-order source and Laplacian, error-compensating source,
+dynamic stabilisation, space potential particles) with r_e = 2.1 l0 for
+density/gradient and 4.0 l0 for the Laplacian (PPE with ~45 nonzeros per row),
+dt = 2.5e-5 s, PPE solved to |b - A x| <= 1e-8 |b|.  The data
 are synthetic (seeded lattice scene); the state and the CSR/ELL matrix exceed L2,
 and L2 is also flushed (512 MiB write) between timed steps.
 
@@ -40,6 +42,7 @@ METRIC = "particle-steps/s, 320k dam break"
 UNIT = "particle-steps/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 512 << 20
+SOLVERS = {"cg64": 0, "mixed": 1, "mg": 3}
 
 
 def parse_args():
@@ -48,10 +51,15 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--solver", choices=("cg64", "mixed"), default="mixed")
+    ap.add_argument("--solver", choices=("cg64", "mixed", "mg"), default="mg")
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cg-launch", choices=("graph", "host"), default="graph",
+                    help="host: CG kernels launched one by one (profilers cannot see kernels "
+                         "inside conditional CUDA graphs)")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only run --warmup + this many steps and exit (for ncu)")
     return ap.parse_args()
 
 
@@ -189,15 +197,23 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
-    solver = abi.SOLVER_MIXED if args.solver == "mixed" else abi.SOLVER_CG64
+    solver = SOLVERS[args.solver]
     scene = scenes.config_c2()
     dt = scene.meta["dt"]
-    params = scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8)
+    launch = abi.CG_LAUNCH_HOST if args.cg_launch == "host" else abi.CG_LAUNCH_GRAPH
+    params = scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8, cg_launch=launch)
     comp = Computer(params, device=local_rank)
     comp.add_scene(scene)
 
     for _ in range(max(args.warmup, 0)):
         comp.forward_time(dt)
+    if args.profile_steps > 0:
+        for _ in range(args.profile_steps):
+            comp.forward_time(dt)
+        st = comp.stats()
+        print(json.dumps({"profile_steps": args.profile_steps, "cg_iterations": st["cg_iterations"],
+                          "ppe_nnz": st["ppe_nnz"], "kernel_launches": st["kernel_launches"]}))
+        return
     n_active = comp.count - comp.stats()["disabled"]
 
     def barrier():
@@ -272,10 +288,13 @@ def run_ours(args, rank, world, local_rank):
     spmv_ms = comp.bench_spmv(solver, reps=20, flush_bytes=FLUSH_BYTES)
     if solver == abi.SOLVER_CG64:
         alg_bytes = 12 * nnz + 4 * (n + 1) + 16 * n
-        key = "cg64"
-    else:
+        key, kernel = "cg64", "k_cg_spmv_dot"
+    elif solver == abi.SOLVER_MIXED:
         alg_bytes = 8 * nnz + 4 * (n + 1) + 8 * n
-        key = "mixed"
+        key, kernel = "mixed", "k_mx_spmv"
+    else:  # preconditioned: also reads u (own row) next to r
+        alg_bytes = 8 * nnz + 4 * (n + 1) + 12 * n
+        key, kernel = "mg", "k_pmx_spmv"
     spmv64_ms = comp.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
     peak, peak_kind = load_peak()
     achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
@@ -311,9 +330,11 @@ def run_ours(args, rank, world, local_rank):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if solver == abi.SOLVER_CG64 else "f64 (PPE iterations f32, f64 residual/refinement)",
+        "ppe_solver": {0: "FP64 CG (reference algorithm)", 1: "FP32 CG + FP64 reliable updates",
+                       3: "FP32 CG preconditioned by the cell multigrid + FP64 reliable updates"}[solver],
         "data": "synthetic (seeded lattice dam break)",
         "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
-                               "plain MPS, re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
+                               "reference MPS scheme (HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
                    "particles": n, "active_particles": n_active, "ppe_nnz": nnz,
                    "solver": args.solver, "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
                    "l2": "flushed between timed steps (512 MiB write); working set > L2",
@@ -326,7 +347,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "pinned_host_buffers": pinned},
-        "roofline": {"bound": "hbm", "kernel": "k_%s_spmv_dot" % ("cg" if key == "cg64" else "mx"),
+        "roofline": {"bound": "hbm", "kernel": kernel,
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": spmv_ms,
@@ -361,7 +382,7 @@ def run_reference(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded lattice dam break)",
         "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
-                               "plain MPS, re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
+                               "reference MPS scheme (HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
                    "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
                    "note": "the reference (header-only C++ with Boost/ViennaCL) cannot be built here; "
                            "this arm runs its C++ restatement with OpenMP"},

@@ -67,7 +67,11 @@ extern "C" {
 /* ----------------------------------------------------------- PPE solver */
 #define MPS_SOLVER_CG64 0   /* FP64 CG, the reference algorithm (Computer.hpp:1359-1429) */
 #define MPS_SOLVER_MIXED 1  /* FP32 inner CG + FP64 true residual / iterative refinement */
-#define MPS_SOLVER_LEARNED 2 /* MIXED with the learned initial guess + preconditioner scale */
+#define MPS_SOLVER_LEARNED 2 /* MIXED_MG with the learned initial guess + diagonal scale */
+/* MIXED preconditioned by a cell-aggregation multigrid (Jacobi on the particles plus a
+ * V-cycle on the neighbour-search cells), FP64 CG fallback when it stalls.  Not in the
+ * reference, whose CG is unpreconditioned. */
+#define MPS_SOLVER_MIXED_MG 3
 
 /* How the CG loop is launched: one CUDA graph with a device-driven while loop, or
  * host-launched kernel batches (the same kernels; for profilers that cannot see

@@ -40,6 +40,7 @@ PRESET_PLAIN = 0
 SOLVER_CG64 = 0
 SOLVER_MIXED = 1
 SOLVER_LEARNED = 2
+SOLVER_MIXED_MG = 3
 
 CG_LAUNCH_GRAPH = 0
 CG_LAUNCH_HOST = 1

@@ -29,6 +29,7 @@ UNITS = {
     "grid.cu": ["-fmad=false"],
     "stages.cu": ["-fmad=false"],
     "cg.cu": [],
+    "mg.cu": [],
     "scan.cu": [],
     "noalloc.cu": [],
     "mps_abi.cu": [],

@@ -1,5 +1,5 @@
 // cg.cu - pressure Poisson solvers (Computer::SolvePressurePoissonEquation,
-// Computer.hpp:1359-1429) on the SELL-4x8 matrix, each run as one CUDA graph: an init
+// Computer.hpp:1359-1429) on the SELL-32 matrix, each run as one CUDA graph: an init
 // kernel, then a conditional WHILE node whose body is a few kernels; the last block of
 // each reduction decides the next step and sets the graph condition, so a solve of
 // thousands of iterations needs no host round trip.
@@ -25,9 +25,14 @@
 // direction update p = r + beta p is folded into the next SpMV (each lane forms
 // beta p_j + r_j while gathering), so an iteration is two kernels; the reliable update
 // runs under a conditional IF node only when due.
+// MPS_SOLVER_MIXED_MG / LEARNED: the same FP32 iteration preconditioned by the cell
+// multigrid (mg.cu), three dot products per reduction; if it stalls or runs out of
+// iterations the plain FP64 CG continues from the solution it reached, inside the same
+// graph (a second WHILE node that runs zero times after a converged solve).
+#include <cmath>
 #include <vector>
 
-#include "cg.cuh"
+#include "mg.cuh"
 
 namespace mpsgb {
 
@@ -57,11 +62,13 @@ __device__ double block_sum(double v, double* ws) {
 }
 
 // Writes this block's partials; true in the last block to finish.
-__device__ bool publish(double s0, double s1, double* partials, uint32_t* counter) {
+__device__ bool publish(double s0, double s1, double* partials, uint32_t* counter,
+                        double s2 = 0.0) {
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = s0;
         partials[gridDim.x + blockIdx.x] = s1;
+        partials[2 * gridDim.x + blockIdx.x] = s2;
         __threadfence();
         const uint32_t t = atomicAdd(counter, 1u);
         last = (t == gridDim.x - 1);
@@ -137,6 +144,8 @@ __device__ void init_scalars(CgScalars* S, double rr, double bb, cudaGraphCondit
     S->do_update = 0;
     S->updates = 0;
     S->aborted = 0;
+    S->stalled = 0;
+    S->prev_true_rr = rr;
     if (use_cond) cudaGraphSetConditional(h, (!conv && S->max_iter > 0) ? 1u : 0u);
 }
 
@@ -155,10 +164,20 @@ __device__ __forceinline__ bool aborted_before_solve(const CgOperands& o,
 }
 
 // ------------------------------------------------------------- CG64 kernels
-// Ap = A x; r = b - Ap; p = r; rr = r.r (Computer.hpp:1382-1385)
+// Ap = A x; r = b - Ap; p = r; rr = r.r (Computer.hpp:1382-1385).  With `gate` (the
+// fallback after a preconditioned solve) nothing runs unless that solve failed.
 __global__ void __launch_bounds__(kBlock) k_cg_init(CgOperands o, cudaGraphConditionalHandle h,
-                                                   int use_cond) {
+                                                   int use_cond, const CgScalars* gate) {
     __shared__ double ws[kBlock];
+    if (gate && (gate->converged || gate->aborted)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            o.S->converged = gate->converged;
+            o.S->aborted = gate->aborted;
+            o.S->iter = 0;
+            if (use_cond) cudaGraphSetConditional(h, 0u);
+        }
+        return;
+    }
     if (aborted_before_solve(o, h, use_cond)) return;
     const ChunkLoop cl;
     const double* x = o.x;
@@ -413,6 +432,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                 S->rr = gam;
                 S->pAp = del;
             }
+            if (mode == 2) S->do_update = 0;
         }
     }
 }
@@ -422,7 +442,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
 __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
     __shared__ double ws[kBlock];
-    if (o.S->converged || o.S->aborted || !o.S->do_update) return;
+    if (o.S->converged || o.S->aborted || o.S->stalled || !o.S->do_update) return;
     const ChunkLoop cl;
     const bool odd = (o.S->updates & 1) != 0;
     const double* __restrict__ xc = odd ? o.x2 : o.x;
@@ -475,6 +495,105 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
     }
 }
 
+// -------------------------------------------------- preconditioned MIXED kernels
+// Preconditioned Chronopoulos-Gear CG with u = M r, w = A u and s = A p kept as vectors:
+// gamma = r.u, delta = w.u and rho = r.r (convergence and reliable updates) come out of
+// one reduction.  A and M are both negative definite on the rows the solve acts on, so
+// this is CG on the SPD pair (-A, -M).
+
+// s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s (FP32, no reduction)
+__global__ void __launch_bounds__(kBlock) k_pmx_axpy(CgOperands o) {
+    if (pcg_skip(o.S, 1)) return;
+    const float alpha = __double2float_rn(o.S->alpha);
+    const float beta = __double2float_rn(o.S->beta);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
+        const float si = fmaf(beta, o.s32[i], o.w32[i]);
+        const float pi = fmaf(beta, o.p32[i], o.u32[i]);
+        o.s32[i] = si;
+        o.p32[i] = pi;
+        o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+        o.r32[i] = fmaf(-alpha, si, o.r32[i]);
+    }
+}
+
+// w = A u (FP32); gamma, delta, rho in FP64; next step sizes; reliable-update decision
+// (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
+__global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
+                                                    cudaGraphConditionalHandle h,
+                                                    cudaGraphConditionalHandle h_true, int use_cond) {
+    __shared__ double ws[kBlock];
+    CgScalars* S = o.S;
+    if (pcg_skip(S, mode)) return;
+    const ChunkLoop cl;
+    const float* __restrict__ u = o.u32;
+    double vg = 0.0, vd = 0.0, vr = 0.0;
+    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const int L = o.len[i];
+        const float wi = row32(o, sell_index(o.off[c], cl.lane, 0), L, u);
+        if (i < o.n) {
+            const double ri = static_cast<double>(o.r32[i]);
+            const double ui = static_cast<double>(u[i]);
+            o.w32[i] = wi;
+            if (mode == 2) o.d32[i] = 0.0f;
+            vg += ri * ui;
+            vd += static_cast<double>(wi) * ui;
+            vr += ri * ri;
+        }
+    }
+    const double s0 = block_sum(vg, ws);
+    const double s1 = block_sum(vd, ws);
+    const double s2 = block_sum(vr, ws);
+    if (publish(s0, s1, o.partials, &o.S->counter, s2)) {
+        const double gam = gather_sum(o.partials, gridDim.x, ws);
+        const double del = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
+        const double rho = gather_sum(o.partials + 2 * gridDim.x, gridDim.x, ws);
+        if (threadIdx.x == 0) {
+            S->counter = 0;
+            S->rr_new = rho;
+            int reliable = 0;
+            int stalled = 0;
+            if (mode == 1) {
+                reliable = (rho < S->delta2 * S->rr_upd) || (rho < S->thr);
+                S->do_update = reliable;
+                if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
+            } else if (mode == 2) {
+                stalled = S->true_rr > 0.25 * S->prev_true_rr;
+                S->prev_true_rr = S->true_rr;
+            }
+            if (!reliable && !stalled) {
+                double alpha, beta = 0.0;
+                if (mode == 0) {
+                    alpha = gam / del;
+                } else {
+                    beta = gam / S->rr;
+                    alpha = gam / (del - beta * gam / S->alpha);
+                    S->iter += 1;
+                }
+                stalled = !(std::isfinite(alpha) && std::isfinite(beta) && alpha != 0.0);
+                S->alpha = alpha;
+                S->beta = beta;
+                S->rr = gam;
+                S->pAp = del;
+            }
+            if (mode == 2) S->do_update = 0;
+            S->stalled = stalled;
+            if (use_cond && (mode != 1 || !reliable))
+                cudaGraphSetConditional(h, (!stalled && S->iter < S->max_iter) ? 1u : 0u);
+        }
+    }
+}
+
+// After the fallback: report it in the primary scalars.
+__global__ void k_fb_merge(CgScalars* S, const CgScalars* F) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (S->converged || S->aborted) return;
+    S->fallback = 1;
+    S->fb_iter = F->iter;
+    S->converged = F->converged;
+    S->iter += F->iter;
+}
+
 __global__ void k_cg_configure(CgScalars* S, double eps, int criterion, int max_iter,
                                double delta2) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -488,23 +607,64 @@ __global__ void k_cg_configure(CgScalars* S, double eps, int criterion, int max_
         S->aborted = 0;
         S->do_update = 0;
         S->updates = 0;
+        S->stalled = 0;
+        S->fallback = 0;
+        S->fb_iter = 0;
     }
 }
 
-void body_kernels(int solver, const CgOperands& ops, cudaGraphConditionalHandle h,
-                  cudaGraphConditionalHandle h_true, int use_cond, bool with_true, cudaStream_t s) {
+bool is_pcg(int solver) { return solver == MPS_SOLVER_MIXED_MG || solver == MPS_SOLVER_LEARNED; }
+
+void cg64_body(const CgOperands& ops, cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+    k_cg_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
+    k_cg_update<<<ops.grid_vec, kBlock, 0, s>>>(ops, h, use_cond);
+    k_cg_pupdate<<<ops.grid_vec, kBlock, 0, s>>>(ops);
+}
+
+void reliable_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
+                      cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+    k_mx_true<<<ops.grid_spmv, kBlock, 0, s>>>(ops, h, use_cond);
+    if (is_pcg(solver)) {
+        mg_apply(*mg, ops.S, 2, ops.r32, ops.u32, s);
+        k_pmx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
+    } else {
+        k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
+    }
+}
+
+void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
+                  cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_true, int use_cond,
+                  bool with_true, cudaStream_t s) {
     const int gv = ops.grid_vec, gs = ops.grid_spmv;
     if (solver == MPS_SOLVER_CG64) {
-        k_cg_spmv_dot<<<gs, kBlock, 0, s>>>(ops);
-        k_cg_update<<<gv, kBlock, 0, s>>>(ops, h, use_cond);
-        k_cg_pupdate<<<gv, kBlock, 0, s>>>(ops);
+        cg64_body(ops, h, use_cond, s);
+        return;
+    }
+    if (is_pcg(solver)) {
+        k_pmx_axpy<<<gv, kBlock, 0, s>>>(ops);
+        mg_apply(*mg, ops.S, 1, ops.r32, ops.u32, s);
+        k_pmx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
     } else {
         k_mx_axpy<<<gv, kBlock, 0, s>>>(ops);
         k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
-        if (with_true) {
-            k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
-            k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
-        }
+    }
+    if (with_true) reliable_kernels(solver, ops, mg, h, use_cond, s);
+}
+
+void init_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
+                  cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+    const int gs = ops.grid_spmv;
+    if (solver == MPS_SOLVER_CG64) {
+        k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond, nullptr);
+        return;
+    }
+    if (is_pcg(solver)) mg_setup(*mg, ops, s);
+    k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
+    if (is_pcg(solver)) {
+        mg_apply(*mg, ops.S, 0, ops.r32, ops.u32, s);
+        k_pmx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, use_cond);
+    } else {
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, use_cond);
     }
 }
 
@@ -513,7 +673,7 @@ void body_kernels(int solver, const CgOperands& ops, cudaGraphConditionalHandle 
 int cg_grid_vec(int64_t n) { return grid_for(n); }
 int cg_grid_spmv(int64_t n) { return grid_for(sell_chunks(n) * 32); }
 int64_t cg_partials(int64_t n) {
-    return 2 * static_cast<int64_t>(cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n)) + 64;
+    return 3 * static_cast<int64_t>(cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n)) + 64;
 }
 
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,
@@ -524,8 +684,15 @@ void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, 
 void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
     if (solver == MPS_SOLVER_CG64)
         k_cg_spmv_dot<<<ops.grid_spmv, kBlock, 0, s>>>(ops);
+    else if (is_pcg(solver))
+        k_pmx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
     else
         k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
+}
+
+int cg_kernels_per_iteration(int solver, const MgHierarchy* mg) {
+    if (solver == MPS_SOLVER_CG64) return 3;
+    return 2 + (is_pcg(solver) && mg ? mg_apply_launches(*mg) : 0);
 }
 
 CgGraph::~CgGraph() { reset(); }
@@ -539,13 +706,15 @@ void CgGraph::reset() {
     nested_ = false;
 }
 
-cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win) {
+cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win,
+                           const MgHierarchy* mg, const CgOperands* fb) {
+    if (is_pcg(solver) && (!mg || !fb)) return cudaErrorInvalidValue;
     if (solver != MPS_SOLVER_CG64) {
         // preferred: the reliable update under an IF node nested in the WHILE body
-        if (build_impl(solver, ops, s, true, win) == cudaSuccess) return cudaSuccess;
+        if (build_impl(solver, ops, s, true, win, mg, fb) == cudaSuccess) return cudaSuccess;
         cudaGetLastError();
     }
-    return build_impl(solver, ops, s, false, win);
+    return build_impl(solver, ops, s, false, win, mg, fb);
 }
 
 namespace {
@@ -574,66 +743,85 @@ cudaError_t apply_window(cudaGraph_t g, const L2Window& win) {
     }
     return cudaSuccess;
 }
-}  // namespace
 
-cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                                const L2Window& win) {
-    reset();
-    ops_ = ops;
-    solver_ = solver;
-    nested_ = nested;
-    const int gv = ops.grid_vec, gs = ops.grid_spmv;
-    cudaError_t e = cudaGraphCreate(&graph_, 0);
+// The one node of a linear chain that has no successor.
+cudaError_t sink_node(cudaGraph_t g, cudaGraphNode_t* out) {
+    size_t nn = 0, ne = 0;
+    cudaError_t e = cudaGraphGetNodes(g, nullptr, &nn);
     if (e != cudaSuccess) return e;
-    cudaGraphConditionalHandle h;
-    e = cudaGraphConditionalHandleCreate(&h, graph_, 0, cudaGraphCondAssignDefault);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    e = cudaGraphGetNodes(g, nodes.data(), &nn);
     if (e != cudaSuccess) return e;
-    cudaGraph_t captured = nullptr;
-
-    // init kernel
-    e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal);
+    e = cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &ne);
     if (e != cudaSuccess) return e;
-    if (solver == MPS_SOLVER_CG64) {
-        k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
-    } else {
-        k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, 1);
-        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, 1);
+    std::vector<cudaGraphNode_t> from(ne), to(ne);
+    if (ne > 0) {
+        e = cudaGraphGetEdges(g, from.data(), to.data(), nullptr, &ne);
+        if (e != cudaSuccess) return e;
     }
-    e = cudaStreamEndCapture(s, &captured);
-    if (e != cudaSuccess) return e;
-    // the last node of the init chain
-    cudaGraphNode_t init_node;
-    {
-        size_t nn = 0;
-        e = cudaGraphGetNodes(graph_, nullptr, &nn);
-        if (e != cudaSuccess) return e;
-        std::vector<cudaGraphNode_t> nodes(nn);
-        e = cudaGraphGetNodes(graph_, nodes.data(), &nn);
-        if (e != cudaSuccess) return e;
-        init_node = nodes[0];
-        if (nn > 1) {
-            size_t ne = 0;
-            e = cudaGraphGetEdges(graph_, nullptr, nullptr, nullptr, &ne);
-            if (e != cudaSuccess || ne != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
-            cudaGraphNode_t from, to;
-            e = cudaGraphGetEdges(graph_, &from, &to, nullptr, &ne);
-            if (e != cudaSuccess) return e;
-            init_node = to;
+    int found = 0;
+    for (cudaGraphNode_t node : nodes) {
+        bool has_succ = false;
+        for (size_t k = 0; k < ne; k++) has_succ = has_succ || from[k] == node;
+        if (!has_succ) {
+            *out = node;
+            found++;
         }
     }
+    return found == 1 ? cudaSuccess : cudaErrorInvalidValue;
+}
 
-    // while (cond) { body }
+// Adds a WHILE node after `dep` (or as a root) and returns its body graph.
+cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
+                      cudaGraphNode_t* node, cudaGraph_t* body) {
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
-    cudaGraphNode_t while_node;
-    e = cudaGraphAddNode(&while_node, graph_, &init_node, nullptr, 1, &cp);
+    cudaError_t e = cudaGraphAddNode(node, g, dep, nullptr, dep ? 1 : 0, &cp);
     if (e != cudaSuccess) return e;
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    *body = cp.conditional.phGraph_out[0];
+    return cudaSuccess;
+}
+}  // namespace
 
+cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
+                                const L2Window& win, const MgHierarchy* mg, const CgOperands* fb) {
+    reset();
+    ops_ = ops;
+    solver_ = solver;
+    nested_ = nested;
+    kpi_ = cg_kernels_per_iteration(solver, mg);
+    kri_ = (solver == MPS_SOLVER_CG64) ? 0 : kpi_;  // reliable update: true + apply + SpMV
+    const int gv = ops.grid_vec, gs = ops.grid_spmv;
+    cudaError_t e = cudaGraphCreate(&graph_, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h, h_fb = 0;
+    e = cudaGraphConditionalHandleCreate(&h, graph_, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    if (is_pcg(solver)) {
+        e = cudaGraphConditionalHandleCreate(&h_fb, graph_, 0, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) return e;
+    }
+    cudaGraph_t captured = nullptr;
+
+    // init chain
+    e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    init_kernels(solver, ops, mg, h, 1, s);
+    e = cudaStreamEndCapture(s, &captured);
+    if (e != cudaSuccess) return e;
+    cudaGraphNode_t init_node;
+    e = sink_node(graph_, &init_node);
+    if (e != cudaSuccess) return e;
+
+    // while (cond) { body }
+    cudaGraphNode_t while_node;
+    cudaGraph_t body;
+    e = add_while(graph_, &init_node, h, &while_node, &body);
+    if (e != cudaSuccess) return e;
     cudaGraphConditionalHandle h_true = 0;
     if (nested) {
         e = cudaGraphConditionalHandleCreate(&h_true, body, 0, 0);
@@ -641,19 +829,16 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     }
     e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    body_kernels(solver, ops, h, h_true, 1, !nested, s);
+    body_kernels(solver, ops, mg, h, h_true, 1, !nested, s);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
     e = apply_window(body, win);
     if (e != cudaSuccess) return e;
 
     if (nested) {
-        // if (reliable update due) { true residual; w = A r } after the SpMV kernel
-        size_t ne = 0;
-        e = cudaGraphGetEdges(body, nullptr, nullptr, nullptr, &ne);
-        if (e != cudaSuccess || ne != 1) return e != cudaSuccess ? e : cudaErrorInvalidValue;
-        cudaGraphNode_t from, to;
-        e = cudaGraphGetEdges(body, &from, &to, nullptr, &ne);
+        // if (reliable update due) { true residual; [u = M r]; w = A u } after the SpMV
+        cudaGraphNode_t last;
+        e = sink_node(body, &last);
         if (e != cudaSuccess) return e;
         cudaGraphNodeParams ip = {};
         ip.type = cudaGraphNodeTypeConditional;
@@ -661,28 +846,53 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
         ip.conditional.type = cudaGraphCondTypeIf;
         ip.conditional.size = 1;
         cudaGraphNode_t if_node;
-        e = cudaGraphAddNode(&if_node, body, &to, nullptr, 1, &ip);
+        e = cudaGraphAddNode(&if_node, body, &last, nullptr, 1, &ip);
         if (e != cudaSuccess) return e;
         cudaGraph_t if_body = ip.conditional.phGraph_out[0];
         e = cudaStreamBeginCaptureToGraph(s, if_body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        k_mx_true<<<gs, kBlock, 0, s>>>(ops, h, 1);
-        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 2, h, 0, 1);
+        reliable_kernels(solver, ops, mg, h, 1, s);
         e = cudaStreamEndCapture(s, &captured);
         if (e != cudaSuccess) return e;
         e = apply_window(if_body, win);
         if (e != cudaSuccess) return e;
     }
 
-    // tail: the solution into x (MIXED) and the true residual
+    // tail: the solution into x, [plain FP64 CG fallback], the true residual
     e = cudaStreamBeginCaptureToGraph(s, graph_, &while_node, nullptr, 1,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     if (solver != MPS_SOLVER_CG64) k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
-    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    if (is_pcg(solver)) {
+        k_cg_init<<<gs, kBlock, 0, s>>>(*fb, h_fb, 1, ops.S);
+    } else {
+        k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    }
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
+    if (is_pcg(solver)) {
+        cudaGraphNode_t fb_init;
+        e = sink_node(graph_, &fb_init);
+        if (e != cudaSuccess) return e;
+        cudaGraphNode_t fb_while;
+        cudaGraph_t fb_body;
+        e = add_while(graph_, &fb_init, h_fb, &fb_while, &fb_body);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamBeginCaptureToGraph(s, fb_body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cg64_body(*fb, h_fb, 1, s);
+        e = cudaStreamEndCapture(s, &captured);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamBeginCaptureToGraph(s, graph_, &fb_while, nullptr, 1,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
+        k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+        e = cudaStreamEndCapture(s, &captured);
+        if (e != cudaSuccess) return e;
+    }
 
     e = cudaGraphInstantiate(&exec_, graph_, 0);
     if (e != cudaSuccess) {
@@ -697,34 +907,51 @@ cudaError_t CgGraph::launch(cudaStream_t s) {
     return cudaGraphLaunch(exec_, s);
 }
 
-cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
-                          cudaStream_t s, int64_t* launches) {
-    const int gv = ops.grid_vec, gs = ops.grid_spmv;
+namespace {
+// Host loop: `chunk` iterations per batch, the scalars read back between batches.
+cudaError_t host_loop(int solver, const CgOperands& ops, const MgHierarchy* mg, CgScalars* host_S,
+                      int chunk, cudaStream_t s, int64_t* k) {
     const cudaGraphConditionalHandle none = 0;
-    int64_t k = 0;
-    if (solver == MPS_SOLVER_CG64) {
-        k_cg_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
-        k++;
-    } else {
-        k_mx_init<<<gs, kBlock, 0, s>>>(ops, none, 0);
-        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, none, none, 0);
-        k += 2;
-    }
     cudaError_t e = cudaGetLastError();
     for (;;) {
         if (e != cudaSuccess) return e;
         e = cudaMemcpyAsync(host_S, ops.S, sizeof(CgScalars), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
-        if (host_S->converged || host_S->aborted || host_S->iter >= host_S->max_iter) break;
+        if (host_S->converged || host_S->aborted || host_S->stalled || host_S->iter >= host_S->max_iter)
+            return cudaSuccess;
         for (int c = 0; c < chunk; c++) {
-            body_kernels(solver, ops, none, none, 0, true, s);
-            k += solver == MPS_SOLVER_CG64 ? 3 : 4;  // MIXED: axpy, SpMV + 2 reliable-update kernels
+            body_kernels(solver, ops, mg, none, none, 0, true, s);
+            // CG64: 3; MIXED: axpy, SpMV + 2 reliable-update kernels; PCG: also 2 cycles
+            *k += solver == MPS_SOLVER_CG64 ? 3 : 2 * cg_kernels_per_iteration(solver, mg);
         }
         e = cudaGetLastError();
     }
+}
+}  // namespace
+
+cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
+                          cudaStream_t s, int64_t* launches, const MgHierarchy* mg,
+                          const CgOperands* fb) {
+    if (is_pcg(solver) && (!mg || !fb)) return cudaErrorInvalidValue;
+    const int gv = ops.grid_vec, gs = ops.grid_spmv;
+    const cudaGraphConditionalHandle none = 0;
+    int64_t k = 0;
+    init_kernels(solver, ops, mg, none, 0, s);
+    k += solver == MPS_SOLVER_CG64 ? 1 : 2;
+    if (is_pcg(solver)) k += mg_setup_launches(*mg) + mg_apply_launches(*mg);
+    cudaError_t e = host_loop(solver, ops, mg, host_S, chunk, s, &k);
+    if (e != cudaSuccess) return e;
     if (solver != MPS_SOLVER_CG64) {
         k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
+        k++;
+    }
+    if (is_pcg(solver)) {
+        k_cg_init<<<gs, kBlock, 0, s>>>(*fb, none, 0, ops.S);
+        k++;
+        e = host_loop(MPS_SOLVER_CG64, *fb, nullptr, host_S, chunk, s, &k);
+        if (e != cudaSuccess) return e;
+        k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
         k++;
     }
     k_true_residual<<<gs, kBlock, 0, s>>>(ops);

@@ -27,6 +27,12 @@ struct CgScalars {
     int32_t updates;    // MIXED: reliable updates made (parity selects the x buffer)
     uint32_t counter;   // last-block ticket
     int32_t aborted;    // the step failed before the solve: nothing runs
+    // preconditioned solve (MIXED_MG, LEARNED)
+    int32_t stalled;      // breakdown or a reliable update that did not halve |r|
+    int32_t fallback;     // the plain FP64 CG ran after the preconditioned solve
+    int32_t fb_iter;      // iterations of that fallback
+    int32_t pad0;
+    double prev_true_rr;  // true r.r at the previous reliable update
 };
 
 struct CgOperands {
@@ -46,7 +52,8 @@ struct CgOperands {
     // MIXED (Chronopoulos-Gear CG in FP32): r, w = A r, s = A p, p, correction d
     double* x2;         // second FP64 solution buffer (reliable updates alternate)
     float *r32, *w32, *s32, *p32, *d32;
-    double* partials;   // 2 * max(grid_vec, grid_spmv) doubles
+    float* u32;         // preconditioned residual u = M r (MIXED_MG, LEARNED)
+    double* partials;   // 3 * max(grid_vec, grid_spmv) doubles
     CgScalars* S;
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
 };
@@ -58,27 +65,35 @@ struct L2Window {
     float hit_ratio = 0.f;
 };
 
-// A CUDA graph running one whole solve: init kernel + device-driven while loop.
+struct MgHierarchy;
+
+// A CUDA graph running one whole solve: init kernels + device-driven while loop (+ for
+// the preconditioned solvers the FP64 CG fallback loop, which runs only after a failure).
 class CgGraph {
 public:
     ~CgGraph();
-    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {});
+    // `mg` and `fb` (operands of the FP64 fallback, own scalars) are required for
+    // MPS_SOLVER_MIXED_MG and MPS_SOLVER_LEARNED and ignored otherwise.
+    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {},
+                      const MgHierarchy* mg = nullptr, const CgOperands* fb = nullptr);
     cudaError_t launch(cudaStream_t s);
     void reset();
     bool valid() const { return exec_ != nullptr; }
     int solver() const { return solver_; }
     const CgOperands& operands() const { return ops_; }
-    // kernels per iteration (the MIXED reliable-update kernel runs only when due)
-    int kernels_per_iteration() const { return solver_ == MPS_SOLVER_CG64 ? 3 : (nested_ ? 2 : 4); }
+    // kernels per iteration, and per reliable update when it runs under its IF node
+    int kernels_per_iteration() const { return nested_ ? kpi_ : kpi_ + kri_; }
+    int kernels_per_update() const { return nested_ ? kri_ : 0; }
     bool nested() const { return nested_; }
 
 private:
     cudaError_t build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                           const L2Window& win);
+                           const L2Window& win, const MgHierarchy* mg, const CgOperands* fb);
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int solver_ = -1;
     bool nested_ = false;
+    int kpi_ = 0, kri_ = 0;
     CgOperands ops_{};
 };
 
@@ -86,7 +101,10 @@ private:
 // device status read back between batches (kernels past convergence return at once).
 // Used when kernels must be visible one by one (profilers) and as a fallback.
 cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
-                          cudaStream_t s, int64_t* launches);
+                          cudaStream_t s, int64_t* launches, const MgHierarchy* mg = nullptr,
+                          const CgOperands* fb = nullptr);
+// Kernels of one iteration of the solver (without the reliable update).
+int cg_kernels_per_iteration(int solver, const MgHierarchy* mg);
 
 // Sets eps / criterion / max_iter / delta for the next solve (stream-ordered).
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,

@@ -80,6 +80,7 @@ struct DeviceState {
     double *wall_x, *wall_z;
     double *n_wo_spp, *ecs, *ox, *oz, *dux, *duz;
     int32_t *cell_count, *cell_slot;
+    int32_t* cell_xz;  // (cx << 16) | cz of each particle's cell at the last search, -1: none
     int32_t *nb_count, *nb;
     int32_t *ppe_len, *ppe_col_tmp;
     double *ppe_val_tmp, *ppe_b, *ppe_x;

@@ -21,6 +21,7 @@ namespace mpsgb {
 __global__ void k_bucket(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
+    st.cell_xz[i] = -1;
     if (st.type[i] == MPS_TYPE_DISABLED) {
         atomicAdd(&st.status->disabled, 1);
         return;
@@ -34,6 +35,7 @@ __global__ void k_bucket(SceneConst sc, DeviceState st) {
         return;
     }
     const int cell = static_cast<int>(fx) * sc.gnz + static_cast<int>(fz);
+    st.cell_xz[i] = (static_cast<int>(fx) << 16) | static_cast<int>(fz);
     const int slot = atomicAdd(&st.cell_count[cell], 1);
     if (slot < sc.max_per_cell) {
         st.cell_slot[static_cast<int64_t>(cell) * sc.max_per_cell + slot] = i;

@@ -1,0 +1,406 @@
+// mg.cu - cell-aggregation multigrid preconditioner (setup and cycle kernels).
+//
+// Setup, once per solve (the matrix changes every step):
+//   k_mg_bins    one pass over the FP64 SELL-32 matrix: for every active row the sums of
+//                its entries per neighbouring cell (9 bins, FP64, in shared memory) and
+//                the Jacobi factor omega_0 / a_ii;
+//   k_mg_cells   level-1 operator: per cell, the bins of its particles in slot order
+//                (deterministic, no atomics);
+//   k_mg_coarsen Galerkin product of a 2 x 2 aggregation, FP64;
+//   k_mg_dense   dense inverse of the coarsest level (Gauss-Jordan in FP32 in shared
+//                memory, symmetrised).
+// Cycle, once per iteration (FP32, reads L2-resident planes):
+//   k_mg_restrict0, k_mg_down (levels above the bottom), k_mg_bottom (every level of at
+//   most kMgBottomCells cells in one block, __syncthreads between levels), k_mg_up,
+//   k_mg_prolong0.
+// Every kernel reads only what the previous kernel wrote, so the sequence captures into
+// the solver's CUDA graph unchanged.
+#include <algorithm>
+
+#include "mg.cuh"
+
+namespace mpsgb {
+
+namespace {
+
+__device__ __forceinline__ bool setup_failed(const DevStatus* st) {
+    return st && (st->flags & (kStatusCellOverflow | kStatusDeviceCheck)) != 0;
+}
+
+// --------------------------------------------------------------------- setup
+// Row i of the FP64 matrix binned by the cell offset of each column.  One warp per SELL
+// chunk, one lane per row (coalesced matrix reads); the nine FP64 accumulators of a
+// lane live in shared memory (one FP64 add per matrix entry).
+__global__ void __launch_bounds__(kBlock) k_mg_bins(CgOperands o, const int32_t* cell_xz,
+                                                    double* bins, float* dinv0, float omega,
+                                                    DevStatus* status) {
+    if (setup_failed(status)) return;
+    __shared__ double acc[9 * kBlock];
+    const int t = threadIdx.x;
+    const int lane = t & 31;
+    const int warp = static_cast<int>((blockIdx.x * blockDim.x + t) >> 5);
+    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int c = warp; c < o.nchunks; c += nwarps) {
+        const int i = kSellRows * c + lane;
+        if (i >= o.n) continue;
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q * kBlock + t] = 0.0;
+        const int ci = cell_xz[i];
+        double aii = 0.0;
+        bool bad = false;
+        if (ci >= 0) {
+            const int L = o.len[i];
+            int64_t at = sell_index(o.off[c], lane, 0);
+            for (int k = 0; k < L; k++, at += kSellRows) {
+                const int j = o.col[at];
+                const double a = o.val[at];
+                if (j == i) aii = a;
+                const int cj = cell_xz[j];
+                const int dx = (cj >> 16) - (ci >> 16);
+                const int dz = (cj & 0xffff) - (ci & 0xffff);
+                if (cj < 0 || dx < -1 || dx > 1 || dz < -1 || dz > 1) {
+                    bad = true;
+                    continue;
+                }
+                acc[((dx + 1) * 3 + dz + 1) * kBlock + t] += a;
+            }
+        }
+        if (bad) {
+            atomicOr(&status->flags, kStatusDeviceCheck);
+            status->check_index = i;
+        }
+        const bool active = ci >= 0 && aii < 0.0;
+#pragma unroll
+        for (int q = 0; q < 9; q++) bins[static_cast<int64_t>(q) * o.n + i] = active ? acc[q * kBlock + t] : 0.0;
+        dinv0[i] = active ? omega / static_cast<float>(aii) : 0.0f;
+    }
+}
+
+__device__ __forceinline__ void store_level(const MgLevel& L, int c, const double* k, float omega) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        L.k64[q * L.cells + c] = k[q];
+        L.k32[q * L.cells + c] = static_cast<float>(k[q]);
+    }
+    L.dinv[c] = k[4] < 0.0 ? omega / static_cast<float>(k[4]) : 0.0f;
+}
+
+// Level-1 operator: per search cell, the bins of its particles in slot order.
+__global__ void k_mg_cells(MgLevel L1, const int32_t* cell_count, const int32_t* cell_slot,
+                           int max_per_cell, const double* bins, int n, float omega,
+                           const DevStatus* status) {
+    if (setup_failed(status)) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= L1.cells) return;
+    const int cnt = min(cell_count[c], max_per_cell);
+    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+    double k[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) k[q] = 0.0;
+    for (int s = 0; s < cnt; s++) {
+        const int i = slots[s];
+#pragma unroll
+        for (int q = 0; q < 9; q++) k[q] += bins[static_cast<int64_t>(q) * n + i];
+    }
+    store_level(L1, c, k, omega);
+}
+
+// Galerkin product of the 2 x 2 aggregation of level f into level c (FP64).
+__global__ void k_mg_coarsen(MgLevel f, MgLevel c, float omega, const DevStatus* status) {
+    if (setup_failed(status)) return;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= c.cells) return;
+    const int X = I / c.nz, Z = I - (I / c.nz) * c.nz;
+    double k[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) k[q] = 0.0;
+    for (int a = 0; a < 2; a++) {
+        const int cx = 2 * X + a;
+        if (cx >= f.nx) continue;
+        for (int b = 0; b < 2; b++) {
+            const int cz = 2 * Z + b;
+            if (cz >= f.nz) continue;
+            const int child = cx * f.nz + cz;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int nx = cx + dx;
+                if (nx < 0 || nx >= f.nx) continue;
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int nz = cz + dz;
+                    if (nz < 0 || nz >= f.nz) continue;
+                    const double v = f.k64[((dx + 1) * 3 + dz + 1) * f.cells + child];
+                    const int DX = (nx >> 1) - X, DZ = (nz >> 1) - Z;
+                    k[(DX + 1) * 3 + DZ + 1] += v;
+                }
+            }
+        }
+    }
+    store_level(c, I, k, omega);
+}
+
+// Dense inverse of the coarsest level: Gauss-Jordan without pivoting (the operator is
+// negative definite on its non-empty cells; empty cells get a unit diagonal and a zero
+// row and column in the inverse), FP32 in shared memory, symmetrised on output.
+__global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float* dense,
+                                                               const DevStatus* status) {
+    if (setup_failed(status)) return;
+    extern __shared__ float A[];  // m * m, then m (column) + 1 (pivot)
+    const int m = L.cells;
+    float* colp = A + m * m;
+    float* piv = colp + m;
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) A[idx] = 0.0f;
+    __syncthreads();
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        const int X = c / L.nz, Z = c - (c / L.nz) * L.nz;
+        if (L.k64[4 * m + c] == 0.0) {
+            A[c * m + c] = 1.0f;
+            continue;
+        }
+        for (int dx = -1; dx <= 1; dx++) {
+            const int nx = X + dx;
+            if (nx < 0 || nx >= L.nx) continue;
+            for (int dz = -1; dz <= 1; dz++) {
+                const int nz = Z + dz;
+                if (nz < 0 || nz >= L.nz) continue;
+                A[c * m + nx * L.nz + nz] = static_cast<float>(L.k64[((dx + 1) * 3 + dz + 1) * m + c]);
+            }
+        }
+    }
+    for (int p = 0; p < m; p++) {
+        __syncthreads();
+        if (threadIdx.x == 0) piv[0] = 1.0f / A[p * m + p];
+        for (int i = threadIdx.x; i < m; i += blockDim.x) colp[i] = A[i * m + p];
+        __syncthreads();
+        const float ip = piv[0];
+        for (int j = threadIdx.x; j < m; j += blockDim.x) A[p * m + j] = (j == p ? 1.0f : A[p * m + j]) * ip;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+            const int i = idx / m, j = idx - (idx / m) * m;
+            if (i == p) continue;
+            A[idx] = (j == p ? 0.0f : A[idx]) - colp[i] * A[p * m + j];
+        }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+        const int i = idx / m, j = idx - (idx / m) * m;
+        const bool live = L.k64[4 * m + i] != 0.0 && L.k64[4 * m + j] != 0.0;
+        dense[idx] = live ? 0.5f * (A[i * m + j] + A[j * m + i]) : 0.0f;
+    }
+}
+
+// --------------------------------------------------------------------- cycle
+// Residual of level f after the pre-smoothing x = dinv * r, summed over the children of
+// coarse cell I (the restriction of the piecewise-constant aggregation).
+__device__ __forceinline__ float child_residuals(const MgLevel& f, const float* fr, int X, int Z) {
+    float sum = 0.0f;
+    for (int a = 0; a < 2; a++) {
+        const int cx = 2 * X + a;
+        if (cx >= f.nx) continue;
+        for (int b = 0; b < 2; b++) {
+            const int cz = 2 * Z + b;
+            if (cz >= f.nz) continue;
+            const int ch = cx * f.nz + cz;
+            float res = fr[ch];
+            if (f.dinv[ch] != 0.0f) {
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int nx = cx + dx;
+                    if (nx < 0 || nx >= f.nx) continue;
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int nz = cz + dz;
+                        if (nz < 0 || nz >= f.nz) continue;
+                        const int nb = nx * f.nz + nz;
+                        res -= f.k32[((dx + 1) * 3 + dz + 1) * f.cells + ch] * (f.dinv[nb] * fr[nb]);
+                    }
+                }
+            }
+            sum += res;
+        }
+    }
+    return sum;
+}
+
+// Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
+__device__ __forceinline__ float smoothed_correction(const MgLevel& f, const float* fr,
+                                                     const MgLevel& c, const float* ce, int ch) {
+    const int cx = ch / f.nz, cz = ch - (ch / f.nz) * f.nz;
+    const float xc = f.dinv[ch] * fr[ch] + ce[(cx >> 1) * c.nz + (cz >> 1)];
+    if (f.dinv[ch] == 0.0f) return xc;
+    float res = fr[ch];
+    for (int dx = -1; dx <= 1; dx++) {
+        const int nx = cx + dx;
+        if (nx < 0 || nx >= f.nx) continue;
+        for (int dz = -1; dz <= 1; dz++) {
+            const int nz = cz + dz;
+            if (nz < 0 || nz >= f.nz) continue;
+            const int nb = nx * f.nz + nz;
+            const float xn = f.dinv[nb] * fr[nb] + ce[(nx >> 1) * c.nz + (nz >> 1)];
+            res -= f.k32[((dx + 1) * 3 + dz + 1) * f.cells + ch] * xn;
+        }
+    }
+    return xc + f.dinv[ch] * res;
+}
+
+// Level-1 residual: per search cell, the sum of its particles' residuals in slot order.
+__global__ void k_mg_restrict0(MgLevel L1, const int32_t* cell_count, const int32_t* cell_slot,
+                               int max_per_cell, const float* r, const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= L1.cells) return;
+    const int cnt = min(cell_count[c], max_per_cell);
+    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+    float sum = 0.0f;
+    for (int s = 0; s < cnt; s++) sum += r[slots[s]];
+    L1.r[c] = sum;
+}
+
+__global__ void k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= c.cells) return;
+    c.r[I] = child_residuals(f, f.r, I / c.nz, I - (I / c.nz) * c.nz);
+}
+
+__global__ void k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= f.cells) return;
+    f.e[ch] = smoothed_correction(f, f.r, c, c.e, ch);
+}
+
+struct MgBottom {
+    int32_t first, last;
+    MgLevel lv[kMgMaxLevels + 1];
+    const float* dense;
+};
+
+// Levels first..last in one block: residuals and corrections in shared memory.
+__global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, const CgScalars* S,
+                                                                int mode) {
+    if (pcg_skip(S, mode)) return;
+    extern __shared__ float sm[];
+    float* rs[kMgMaxLevels + 1];
+    float* es[kMgMaxLevels + 1];
+    {
+        float* at = sm;
+        for (int l = B.first; l <= B.last; l++) {
+            rs[l] = at;
+            es[l] = at + B.lv[l].cells;
+            at += 2 * B.lv[l].cells;
+        }
+    }
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int c = tid; c < B.lv[B.first].cells; c += nt) rs[B.first][c] = B.lv[B.first].r[c];
+    __syncthreads();
+    for (int l = B.first; l < B.last; l++) {
+        const MgLevel& c = B.lv[l + 1];
+        for (int I = tid; I < c.cells; I += nt)
+            rs[l + 1][I] = child_residuals(B.lv[l], rs[l], I / c.nz, I - (I / c.nz) * c.nz);
+        __syncthreads();
+    }
+    {
+        const int m = B.lv[B.last].cells;
+        for (int i = tid; i < m; i += nt) {
+            float v = 0.0f;
+            for (int k = 0; k < m; k++) v += B.dense[k * m + i] * rs[B.last][k];
+            es[B.last][i] = v;
+        }
+        __syncthreads();
+    }
+    for (int l = B.last - 1; l >= B.first; l--) {
+        const MgLevel& f = B.lv[l];
+        for (int ch = tid; ch < f.cells; ch += nt)
+            es[l][ch] = smoothed_correction(f, rs[l], B.lv[l + 1], es[l + 1], ch);
+        __syncthreads();
+    }
+    for (int c = tid; c < B.lv[B.first].cells; c += nt) B.lv[B.first].e[c] = es[B.first][c];
+}
+
+// u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows.
+__global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* cell_xz, int gnz,
+                                                        const float* dinv0, const float* scale,
+                                                        const float* r, const float* e1, float* u,
+                                                        const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float d = dinv0[i];
+        float v = 0.0f;
+        if (d != 0.0f) {
+            const int c = cell_xz[i];
+            const float sc = scale ? scale[i] : 1.0f;
+            v = sc * d * r[i] + (c >= 0 ? e1[(c >> 16) * gnz + (c & 0xffff)] : 0.0f);
+        }
+        u[i] = v;
+    }
+}
+
+size_t bottom_smem(const MgHierarchy& mg) {
+    size_t cells = 0;
+    for (int l = mg.bottom; l <= mg.levels; l++) cells += static_cast<size_t>(mg.lv[l].cells);
+    return 2 * cells * sizeof(float);
+}
+
+size_t dense_smem(const MgHierarchy& mg) {
+    const size_t m = static_cast<size_t>(mg.lv[mg.levels].cells);
+    return (m * m + m + 1) * sizeof(float);
+}
+
+}  // namespace
+
+int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom) {
+    if (gnx <= 0 || gnz <= 0 || gnx >= 32768 || gnz >= 32768) return 0;
+    int l = 1;
+    lv[1] = MgLevel{gnx, gnz, gnx * gnz, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
+    while (lv[l].cells > kMgDenseCells) {
+        if (l == kMgMaxLevels) return 0;
+        const int nx = (lv[l].nx + 1) / 2, nz = (lv[l].nz + 1) / 2;
+        lv[l + 1] = MgLevel{nx, nz, nx * nz, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
+        l++;
+    }
+    int b = l;
+    while (b > 1 && lv[b - 1].cells <= kMgBottomCells) b--;
+    *bottom = b;
+    return l;
+}
+
+cudaError_t mg_prepare_device() {
+    const int dense_max = (kMgDenseCells * kMgDenseCells + kMgDenseCells + 1) * static_cast<int>(sizeof(float));
+    cudaError_t e = cudaFuncSetAttribute(k_mg_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, dense_max);
+    if (e != cudaSuccess) return e;
+    const int bottom_max = 2 * 2 * (kMgBottomCells + 64) * static_cast<int>(sizeof(float));
+    return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize, bottom_max);
+}
+
+void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
+    k_mg_bins<<<o.grid_spmv, kBlock, 0, s>>>(o, mg.cell_xz, mg.bins, mg.dinv0, kMgOmegaFine, mg.status);
+    k_mg_cells<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1], mg.cell_count, mg.cell_slot,
+                                                          mg.max_per_cell, mg.bins, mg.n,
+                                                          kMgOmegaCoarse, mg.status);
+    for (int l = 1; l < mg.levels; l++)
+        k_mg_coarsen<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1],
+                                                                    kMgOmegaCoarse, mg.status);
+    k_mg_dense<<<1, kMgBottomThreads, dense_smem(mg), s>>>(mg.lv[mg.levels], mg.dense, mg.status);
+}
+
+int mg_setup_launches(const MgHierarchy& mg) { return 2 + (mg.levels - 1) + 1; }
+
+void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
+              cudaStream_t s) {
+    const MgLevel& L1 = mg.lv[1];
+    k_mg_restrict0<<<grid_for(L1.cells), kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot,
+                                                        mg.max_per_cell, r, S, mode);
+    for (int l = 1; l < mg.bottom; l++)
+        k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+    MgBottom B{};
+    B.first = mg.bottom;
+    B.last = mg.levels;
+    for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
+    B.dense = mg.dense;
+    k_mg_bottom<<<1, kMgBottomThreads, bottom_smem(mg), s>>>(B, S, mode);
+    for (int l = mg.bottom - 1; l >= 1; l--)
+        k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+    k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, mg.lv[1].nz, mg.dinv0,
+                                                   mg.scale, r, L1.e, u, S, mode);
+}
+
+int mg_apply_launches(const MgHierarchy& mg) { return 3 + 2 * (mg.bottom - 1); }
+
+}  // namespace mpsgb

@@ -1,0 +1,80 @@
+// mg.cuh - cell-aggregation multigrid preconditioner of the PPE solve.
+//
+// The unknowns are aggregated by the cells of the neighbour search (side NeighborLength
+// >= the Laplacian radius), so two particles coupled by the PPE always sit in the same or
+// in adjacent cells: the Galerkin operator P^T A P of the piecewise-constant aggregation
+// is a 9-point stencil on the cell grid.  Coarser levels merge 2 x 2 cells and stay
+// 9-point, so every level below the particles is a small structured grid held as nine
+// coefficient planes (L2-resident).
+//
+// Preconditioner (symmetric, negative definite like A on the rows it acts on):
+//   u = s_i * omega_0 * r_i / a_ii  +  P_1 V_1(P_1^T r)
+// i.e. a (learned-)scaled Jacobi term on the particles plus a V(1,1) cycle with damped
+// Jacobi on the cell levels; the levels of at most kMgBottomCells cells run inside one
+// thread block and the coarsest level (at most kMgDenseCells cells) is solved with its
+// dense inverse.  Identity rows of the PPE (dummy, disabled, free-surface rows) get u = 0.
+#pragma once
+
+#include "cg.cuh"
+
+namespace mpsgb {
+
+constexpr int kMgMaxLevels = 14;
+constexpr int kMgBottomCells = 2048;   // levels this small run in the single-block kernel
+constexpr int kMgDenseCells = 128;     // the coarsest level, solved with its dense inverse
+constexpr int kMgBottomThreads = 1024;
+constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
+constexpr float kMgOmegaCoarse = 0.7f; // Jacobi weight of the cell levels
+
+// One cell level: nine coefficient planes K[d * cells + c], d = 3 (dx + 1) + (dz + 1).
+struct MgLevel {
+    int32_t nx, nz, cells, pad;
+    double* k64;  // FP64 Galerkin coefficients (setup)
+    float* k32;   // the same in FP32 (cycle)
+    float* dinv;  // omega / K_centre, 0 for cells without unknowns
+    float* r;     // restricted residual
+    float* e;     // correction
+};
+
+struct MgHierarchy {
+    int32_t levels = 0;  // cell levels; level 1 = neighbour-search cells
+    int32_t bottom = 0;  // first level of the single-block kernel
+    MgLevel lv[kMgMaxLevels + 1] = {};  // lv[1..levels]
+    float* dense = nullptr;             // inverse of the coarsest operator, cells^2
+    // particle level
+    int32_t n = 0;
+    int32_t max_per_cell = 0;
+    const int32_t* cell_xz = nullptr;   // (cx << 16) | cz of each particle's cell, -1: none
+    const int32_t* cell_count = nullptr;
+    const int32_t* cell_slot = nullptr;
+    float* dinv0 = nullptr;             // omega_0 / a_ii on active rows, 0 on identity rows
+    const float* scale = nullptr;       // per-row scale of the Jacobi term (null: 1)
+    double* bins = nullptr;             // 9 * n FP64 scratch of the level-1 product
+    DevStatus* status = nullptr;
+};
+
+// Level sizes for a gnx x gnz search grid (returns the level count, 0 if the grid is
+// too large for the 16-bit cell coordinates).
+int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom);
+// Setup of one solve: level-1 operator from the FP64 matrix, the coarser Galerkin
+// operators and the dense inverse.  Skips itself when the step already failed.
+void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s);
+int mg_setup_launches(const MgHierarchy& mg);
+// u = M r.  `mode` gates the kernels on the solve state like the PCG kernels: 0 init,
+// 1 iteration, 2 after a reliable update (see pcg_skip).
+void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
+              cudaStream_t s);
+int mg_apply_launches(const MgHierarchy& mg);
+// Shared-memory bytes the single-block kernels need (opt-in set once per device).
+cudaError_t mg_prepare_device();
+
+// Gate of a preconditioned-solve kernel: mode 0 after init, 1 an iteration, 2 after a
+// reliable update.
+__device__ __forceinline__ bool pcg_skip(const CgScalars* S, int mode) {
+    if (S->converged || S->aborted) return true;
+    if (mode == 1) return S->iter >= S->max_iter || S->stalled;
+    if (mode == 2) return !S->do_update;
+    return false;
+}
+
+}  // namespace mpsgb

@@ -15,7 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "cg.cuh"
+#include "mg.cuh"
 #include "common.cuh"
 
 using namespace mpsgb;
@@ -54,6 +54,10 @@ struct mps_handle {
     double* partials = nullptr;
     double *r = nullptr, *p = nullptr, *Ap = nullptr, *x2 = nullptr;
     float *r32 = nullptr, *w32 = nullptr, *s32 = nullptr, *p32 = nullptr, *d32 = nullptr;
+    float* u32 = nullptr;
+    CgScalars* S_fb = nullptr;  // scalars of the FP64 fallback after a preconditioned solve
+    MgHierarchy mg;             // cell multigrid (MIXED_MG, LEARNED)
+    bool mg_device_ready = false;
     int sm_count = 1;
     CgGraph cg;
     int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
@@ -154,7 +158,7 @@ void validate(const mps_params& p) {
     if (!(p.rho > 0)) bad("rho must be positive");
     if (!(p.courant > 0)) bad("courant must be positive");
     if (!(p.max_x > p.min_x) || !(p.max_z > p.min_z)) bad("empty domain");
-    if (p.solver < MPS_SOLVER_CG64 || p.solver > MPS_SOLVER_LEARNED) bad("unknown solver");
+    if (p.solver < MPS_SOLVER_CG64 || p.solver > MPS_SOLVER_MIXED_MG) bad("unknown solver");
     if (p.solver == MPS_SOLVER_LEARNED)
         throw StatusError{MPS_ERR_NOT_SUPPORTED, "learned solver needs mps_learned_* setup"};
     if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
@@ -247,6 +251,35 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     h->s32 = dalloc<float>(h, n);
     h->p32 = dalloc<float>(h, n);
     h->d32 = dalloc<float>(h, n);
+    h->u32 = dalloc<float>(h, n);
+    h->S_fb = dalloc<CgScalars>(h, 1);
+    st.cell_xz = dalloc<int32_t>(h, n);
+    // multigrid hierarchy over the search cells (level sizes fixed by the domain)
+    MgHierarchy& mg = h->mg;
+    mg = MgHierarchy{};
+    int bottom = 0;
+    mg.levels = mg_plan(sc.gnx, sc.gnz, mg.lv, &bottom);
+    mg.bottom = bottom;
+    if (mg.levels > 0) {
+        for (int l = 1; l <= mg.levels; l++) {
+            MgLevel& L = mg.lv[l];
+            L.k64 = dalloc<double>(h, 9 * static_cast<int64_t>(L.cells));
+            L.k32 = dalloc<float>(h, 9 * static_cast<int64_t>(L.cells));
+            L.dinv = dalloc<float>(h, L.cells);
+            L.r = dalloc<float>(h, L.cells);
+            L.e = dalloc<float>(h, L.cells);
+        }
+        const int64_t m = mg.lv[mg.levels].cells;
+        mg.dense = dalloc<float>(h, m * m);
+        mg.bins = dalloc<double>(h, 9 * n);
+        mg.dinv0 = dalloc<float>(h, n);
+        mg.n = static_cast<int32_t>(n);
+        mg.max_per_cell = sc.max_per_cell;
+        mg.cell_xz = st.cell_xz;
+        mg.cell_count = st.cell_count;
+        mg.cell_slot = st.cell_slot;
+        mg.status = st.status;
+    }
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -255,6 +288,8 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(st.status, 0, sizeof(DevStatus), s), "memset");
     check(cudaMemsetAsync(h->S, 0, sizeof(CgScalars), s), "memset");
     check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
+    check(cudaMemsetAsync(h->S_fb, 0, sizeof(CgScalars), s), "memset");
+    check(cudaMemsetAsync(st.cell_xz, 0xff, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.nb_count, 0, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * kSellRows * sell_chunks(n), s), "memset");
     check(cudaMemsetAsync(h->p32, 0, sizeof(float) * n, s), "memset");
@@ -301,6 +336,7 @@ CgOperands cg_operands(mps_handle* h) {
     o.s32 = h->s32;
     o.p32 = h->p32;
     o.d32 = h->d32;
+    o.u32 = h->u32;
     o.partials = h->partials;
     o.S = h->S;
     o.status = h->st.status;
@@ -313,11 +349,20 @@ void require_particles(mps_handle* h) {
 
 void launched(mps_handle* h, int k) { h->stats.kernel_launches += k; }
 
+bool is_preconditioned(int32_t solver) {
+    return solver == MPS_SOLVER_MIXED_MG || solver == MPS_SOLVER_LEARNED;
+}
+
+// A preconditioned solve that has not converged after this many iterations has stalled
+// (it needs tens); the FP64 CG fallback then runs with the reference's own limit.
+constexpr int kPcgMaxIter = 400;
+
 // Iteration limit: the reference stops after as many iterations as unknowns
 // (Computer.hpp:1392).  The mixed solver restarts its FP32 recursion at every reliable
 // update, so it gets twice that plus a margin.
 int default_max_iter(int32_t requested, int64_t n, int32_t solver) {
     if (requested > 0) return requested;
+    if (is_preconditioned(solver)) return kPcgMaxIter;
     const int64_t lim = (solver == MPS_SOLVER_CG64) ? n : 2 * n + 200;
     return static_cast<int>(std::min<int64_t>(lim, 0x7fffffff));
 }
@@ -342,16 +387,25 @@ void read_status(mps_handle* h, bool solve_done) {
     if (solve_done) {
         const CgScalars& S = *h->h_S;
         h->stats.cg_iterations = S.iter;
+        h->stats.fallback = is_preconditioned(h->prm.solver) ? S.fallback : 0;
         h->stats.cg_refinements = (h->prm.solver == MPS_SOLVER_CG64) ? 1 : S.updates + 1;
         h->stats.cg_rr0 = S.rr0;
         h->stats.cg_rr = S.rr_new;
         h->stats.cg_true_relres = (S.bb > 0) ? std::sqrt(S.true_rr / S.bb) : std::sqrt(S.true_rr);
-        if (h->direct_launches >= 0)
+        if (h->direct_launches >= 0) {
             launched(h, static_cast<int>(h->direct_launches));
-        else
-            launched(h, h->prm.solver == MPS_SOLVER_CG64
-                            ? 2 + 3 * S.iter
-                            : 4 + (h->cg.nested() ? 2 * S.iter + 2 * S.updates : 4 * S.iter));
+        } else if (h->prm.solver == MPS_SOLVER_CG64) {
+            launched(h, 2 + 3 * S.iter);
+        } else {
+            const int kpi = h->cg.kernels_per_iteration(), kpu = h->cg.kernels_per_update();
+            if (is_preconditioned(h->prm.solver)) {
+                const int own = S.iter - S.fb_iter;
+                launched(h, mg_setup_launches(h->mg) + 2 + mg_apply_launches(h->mg) + own * kpi +
+                                S.updates * kpu + 4 + 3 * S.fb_iter);
+            } else {
+                launched(h, 4 + S.iter * kpi + S.updates * kpu);
+            }
+        }
     }
     const int f = h->h_status->flags;
     if (f & kStatusCellOverflow) throw StatusError{MPS_ERR_CELL_OVERFLOW, "Too many particle in a block"};
@@ -427,21 +481,40 @@ void setup_l2_window(mps_handle* h) {
 
 void do_solve(mps_handle* h) {
     cudaStream_t s = h->stream;
-    const int max_iter = default_max_iter(h->prm.max_cg_iters, h->n, h->prm.solver);
+    const int solver = h->prm.solver;
+    const bool pcg = is_preconditioned(solver);
+    const int max_iter = default_max_iter(h->prm.max_cg_iters, h->n, solver);
     launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter, 0.01, s);
     after_launch("cg configure");
     launched(h, 1);
-    const int solver = h->prm.solver == MPS_SOLVER_CG64 ? MPS_SOLVER_CG64 : MPS_SOLVER_MIXED;
-    if (solver == MPS_SOLVER_MIXED) setup_l2_window(h);
+    CgOperands fb{};
+    if (pcg) {
+        if (h->mg.levels == 0)
+            throw StatusError{MPS_ERR_NOT_SUPPORTED, "search grid too large for the multigrid preconditioner"};
+        if (!h->mg_device_ready) {
+            check(mg_prepare_device(), "multigrid kernel attributes");
+            h->mg_device_ready = true;
+        }
+        launch_cg_configure(h->S_fb, h->prm.eps, h->prm.criterion,
+                            default_max_iter(0, h->n, MPS_SOLVER_CG64), 0.01, s);
+        after_launch("cg configure");
+        launched(h, 1);
+        fb = cg_operands(h);
+        fb.S = h->S_fb;
+    }
+    if (solver != MPS_SOLVER_CG64) setup_l2_window(h);
     if (h->prm.cg_launch == MPS_CG_LAUNCH_HOST) {
         int64_t k = 0;
-        check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k), "CG host loop");
+        check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k, pcg ? &h->mg : nullptr,
+                            pcg ? &fb : nullptr),
+              "CG host loop");
         h->direct_launches = k;
         return;
     }
     h->direct_launches = -1;
     if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
-        check(h->cg.build(solver, cg_operands(h), s, solver == MPS_SOLVER_MIXED ? h->l2win : L2Window{}),
+        check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
+                          pcg ? &h->mg : nullptr, pcg ? &fb : nullptr),
               "CG graph build");
     }
     check(h->cg.launch(s), "CG graph launch");
@@ -854,7 +927,8 @@ int mps_flush_l2(mps_handle* h, int64_t bytes) {
 int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_bytes,
                    float* ms_per_launch) {
     if (!h || !ms_per_launch || reps <= 0) return MPS_ERR_INVALID_ARGUMENT;
-    if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED) return MPS_ERR_NOT_SUPPORTED;
+    if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED && solver != MPS_SOLVER_MIXED_MG)
+        return MPS_ERR_NOT_SUPPORTED;
     return guarded(h, [&] {
         require_particles(h);
         cudaStream_t s = h->stream;
