@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphCondi
             o.s32[i] = 0.0f;
             o.p32[i] = 0.0f;
             o.d32[i] = 0.0f;
+            if (o.u32) o.u32[i] = 0.0f;  // rows outside every cell keep u = 0
             vrr += ri * ri;
             vbb += bi * bi;
         }
@@ -501,21 +502,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 // one reduction.  A and M are both negative definite on the rows the solve acts on, so
 // this is CG on the SPD pair (-A, -M).
 
-// s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s (FP32, no reduction)
-__global__ void __launch_bounds__(kBlock) k_pmx_axpy(CgOperands o) {
-    if (pcg_skip(o.S, 1)) return;
-    const float alpha = __double2float_rn(o.S->alpha);
-    const float beta = __double2float_rn(o.S->beta);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
-        const float si = fmaf(beta, o.s32[i], o.w32[i]);
-        const float pi = fmaf(beta, o.p32[i], o.u32[i]);
-        o.s32[i] = si;
-        o.p32[i] = pi;
-        o.d32[i] = fmaf(alpha, pi, o.d32[i]);
-        o.r32[i] = fmaf(-alpha, si, o.r32[i]);
-    }
-}
-
 // w = A u (FP32); gamma, delta, rho in FP64; next step sizes; reliable-update decision
 // (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
 __global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
@@ -641,8 +627,7 @@ void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
         return;
     }
     if (is_pcg(solver)) {
-        k_pmx_axpy<<<gv, kBlock, 0, s>>>(ops);
-        mg_apply(*mg, ops.S, 1, ops.r32, ops.u32, s);
+        mg_apply(*mg, ops.S, 1, ops.r32, ops.u32, s, &ops);  // vector updates + u = M r
         k_pmx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
     } else {
         k_mx_axpy<<<gv, kBlock, 0, s>>>(ops);
@@ -692,7 +677,12 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
 
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg) {
     if (solver == MPS_SOLVER_CG64) return 3;
-    return 2 + (is_pcg(solver) && mg ? mg_apply_launches(*mg) : 0);
+    return is_pcg(solver) && mg ? 1 + mg_apply_launches(*mg) : 2;
+}
+
+int cg_kernels_per_update(int solver, const MgHierarchy* mg) {
+    if (solver == MPS_SOLVER_CG64) return 0;
+    return is_pcg(solver) && mg ? 2 + mg_apply_launches(*mg) : 2;
 }
 
 CgGraph::~CgGraph() { reset(); }
@@ -793,7 +783,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     solver_ = solver;
     nested_ = nested;
     kpi_ = cg_kernels_per_iteration(solver, mg);
-    kri_ = (solver == MPS_SOLVER_CG64) ? 0 : kpi_;  // reliable update: true + apply + SpMV
+    kri_ = cg_kernels_per_update(solver, mg);
     const int gv = ops.grid_vec, gs = ops.grid_spmv;
     cudaError_t e = cudaGraphCreate(&graph_, 0);
     if (e != cudaSuccess) return e;
@@ -922,8 +912,8 @@ cudaError_t host_loop(int solver, const CgOperands& ops, const MgHierarchy* mg, 
             return cudaSuccess;
         for (int c = 0; c < chunk; c++) {
             body_kernels(solver, ops, mg, none, none, 0, true, s);
-            // CG64: 3; MIXED: axpy, SpMV + 2 reliable-update kernels; PCG: also 2 cycles
-            *k += solver == MPS_SOLVER_CG64 ? 3 : 2 * cg_kernels_per_iteration(solver, mg);
+            // every kernel of the iteration and of the reliable update is launched
+            *k += cg_kernels_per_iteration(solver, mg) + cg_kernels_per_update(solver, mg);
         }
         e = cudaGetLastError();
     }

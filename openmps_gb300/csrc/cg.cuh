@@ -103,8 +103,9 @@ private:
 cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
                           cudaStream_t s, int64_t* launches, const MgHierarchy* mg = nullptr,
                           const CgOperands* fb = nullptr);
-// Kernels of one iteration of the solver (without the reliable update).
+// Kernels of one iteration of the solver, and of one reliable update.
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg);
+int cg_kernels_per_update(int solver, const MgHierarchy* mg);
 
 // Sets eps / criterion / max_iter / delta for the next solve (stream-ordered).
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,

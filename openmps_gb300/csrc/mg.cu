@@ -10,9 +10,11 @@
 //   k_mg_dense   dense inverse of the coarsest level (Gauss-Jordan in FP32 in shared
 //                memory, symmetrised).
 // Cycle, once per iteration (FP32, reads L2-resident planes):
-//   k_mg_restrict0, k_mg_down (levels above the bottom), k_mg_bottom (every level of at
-//   most kMgBottomCells cells in one block, __syncthreads between levels), k_mg_up,
-//   k_mg_prolong0.
+//   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
+//   and after a reliable update k_mg_restrict0), k_mg_down (levels above the bottom),
+//   k_mg_bottom (the coarsest levels in one block, all in shared memory, __syncthreads
+//   between levels), k_mg_up, k_mg_up_prolong (level-1 post-smoothing + prolongation to
+//   the particles).
 // Every kernel reads only what the previous kernel wrote, so the sequence captures into
 // the solver's CUDA graph unchanged.
 #include <algorithm>
@@ -188,82 +190,142 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
 }
 
 // --------------------------------------------------------------------- cycle
+// The 9-point gathers are branchless: a neighbour outside the grid is clamped to a valid
+// cell, and its coefficient is zero (no particle can sit outside the grid), so all the
+// loads of a cell issue at once.
+__device__ __forceinline__ int clampi(int v, int hi) { return min(max(v, 0), hi); }
+
 // Residual of level f after the pre-smoothing x = dinv * r, summed over the children of
-// coarse cell I (the restriction of the piecewise-constant aggregation).
-__device__ __forceinline__ float child_residuals(const MgLevel& f, const float* fr, int X, int Z) {
+// coarse cell (X, Z) (the restriction of the piecewise-constant aggregation).
+__device__ __forceinline__ float child_residuals(int nx, int nz, int cells, const float* k,
+                                                 const float* dinv, const float* r, int X, int Z) {
     float sum = 0.0f;
+#pragma unroll
     for (int a = 0; a < 2; a++) {
-        const int cx = 2 * X + a;
-        if (cx >= f.nx) continue;
+#pragma unroll
         for (int b = 0; b < 2; b++) {
-            const int cz = 2 * Z + b;
-            if (cz >= f.nz) continue;
-            const int ch = cx * f.nz + cz;
-            float res = fr[ch];
-            if (f.dinv[ch] != 0.0f) {
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int nx = cx + dx;
-                    if (nx < 0 || nx >= f.nx) continue;
-                    for (int dz = -1; dz <= 1; dz++) {
-                        const int nz = cz + dz;
-                        if (nz < 0 || nz >= f.nz) continue;
-                        const int nb = nx * f.nz + nz;
-                        res -= f.k32[((dx + 1) * 3 + dz + 1) * f.cells + ch] * (f.dinv[nb] * fr[nb]);
-                    }
+            const int cx = 2 * X + a, cz = 2 * Z + b;
+            const bool valid = cx < nx && cz < nz;
+            const int ccx = min(cx, nx - 1), ccz = min(cz, nz - 1);
+            const int ch = ccx * nz + ccz;
+            float res = r[ch];
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int nb = clampi(ccx + dx, nx - 1) * nz + clampi(ccz + dz, nz - 1);
+                    res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * (dinv[nb] * r[nb]);
                 }
             }
-            sum += res;
+            sum += valid ? res : 0.0f;
         }
     }
     return sum;
 }
 
 // Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
-__device__ __forceinline__ float smoothed_correction(const MgLevel& f, const float* fr,
-                                                     const MgLevel& c, const float* ce, int ch) {
-    const int cx = ch / f.nz, cz = ch - (ch / f.nz) * f.nz;
-    const float xc = f.dinv[ch] * fr[ch] + ce[(cx >> 1) * c.nz + (cz >> 1)];
-    if (f.dinv[ch] == 0.0f) return xc;
-    float res = fr[ch];
+__device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
+                                                     const float* dinv, const float* r, int cnz,
+                                                     const float* ce, int ch) {
+    const int cx = ch / nz, cz = ch - (ch / nz) * nz;
+    const float xc = dinv[ch] * r[ch] + ce[(cx >> 1) * cnz + (cz >> 1)];
+    float res = r[ch];
+#pragma unroll
     for (int dx = -1; dx <= 1; dx++) {
-        const int nx = cx + dx;
-        if (nx < 0 || nx >= f.nx) continue;
+#pragma unroll
         for (int dz = -1; dz <= 1; dz++) {
-            const int nz = cz + dz;
-            if (nz < 0 || nz >= f.nz) continue;
-            const int nb = nx * f.nz + nz;
-            const float xn = f.dinv[nb] * fr[nb] + ce[(nx >> 1) * c.nz + (nz >> 1)];
-            res -= f.k32[((dx + 1) * 3 + dz + 1) * f.cells + ch] * xn;
+            const int nx_ = clampi(cx + dx, nx - 1), nz_ = clampi(cz + dz, nz - 1);
+            const int nb = nx_ * nz + nz_;
+            const float xn = dinv[nb] * r[nb] + ce[(nx_ >> 1) * cnz + (nz_ >> 1)];
+            res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * xn;
         }
     }
-    return xc + f.dinv[ch] * res;
+    return xc + dinv[ch] * res;
 }
 
-// Level-1 residual: per search cell, the sum of its particles' residuals in slot order.
-__global__ void k_mg_restrict0(MgLevel L1, const int32_t* cell_count, const int32_t* cell_slot,
-                               int max_per_cell, const float* r, const CgScalars* S, int mode) {
+// Level-1 residual: per search cell, the sum of its particles' residuals (one warp per
+// cell, lanes over the slots, fixed-order shuffle sum).
+__global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_count,
+                                                         const int32_t* cell_slot, int max_per_cell,
+                                                         const float* r, const CgScalars* S, int mode) {
     if (pcg_skip(S, mode)) return;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (c >= L1.cells) return;
     const int cnt = min(cell_count[c], max_per_cell);
     const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
     float sum = 0.0f;
-    for (int s = 0; s < cnt; s++) sum += r[slots[s]];
-    L1.r[c] = sum;
+    for (int s = lane; s < cnt; s += 32) sum += r[slots[s]];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0) L1.r[c] = sum;
 }
 
-__global__ void k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+// An iteration's vector updates fused with the level-1 restriction of the new residual:
+// s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s for the particles of each
+// cell (particles outside every cell are identity rows whose vectors stay zero).
+__global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1,
+                                                             const int32_t* cell_count,
+                                                             const int32_t* cell_slot,
+                                                             int max_per_cell) {
+    if (pcg_skip(o.S, 1)) return;
+    const int lane = threadIdx.x & 31;
+    const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (c >= L1.cells) return;
+    const float alpha = __double2float_rn(o.S->alpha);
+    const float beta = __double2float_rn(o.S->beta);
+    const int cnt = min(cell_count[c], max_per_cell);
+    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+    float sum = 0.0f;
+    for (int s = lane; s < cnt; s += 32) {
+        const int i = slots[s];
+        const float si = fmaf(beta, o.s32[i], o.w32[i]);
+        const float pi = fmaf(beta, o.p32[i], o.u32[i]);
+        const float ri = fmaf(-alpha, si, o.r32[i]);
+        o.s32[i] = si;
+        o.p32[i] = pi;
+        o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+        o.r32[i] = ri;
+        sum += ri;
+    }
+    for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, k);
+    if (lane == 0) L1.r[c] = sum;
+}
+
+__global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
     if (pcg_skip(S, mode)) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= c.cells) return;
-    c.r[I] = child_residuals(f, f.r, I / c.nz, I - (I / c.nz) * c.nz);
+    c.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz, I - (I / c.nz) * c.nz);
 }
 
-__global__ void k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+__global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
     if (pcg_skip(S, mode)) return;
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     if (ch >= f.cells) return;
-    f.e[ch] = smoothed_correction(f, f.r, c, c.e, ch);
+    f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
+}
+
+// Level-1 post-smoothing fused with the prolongation to the particles of the cell:
+// u = s_i dinv0_i r_i + e_1 on active rows, 0 on identity rows (one warp per cell).
+__global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_count,
+                                                          const int32_t* cell_slot, int max_per_cell,
+                                                          const float* dinv0, const float* scale,
+                                                          const float* r, float* u,
+                                                          const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    const int lane = threadIdx.x & 31;
+    const int ch = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (ch >= f.cells) return;
+    const int cnt = min(cell_count[ch], max_per_cell);
+    if (cnt == 0) return;
+    const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
+    const int32_t* slots = cell_slot + static_cast<int64_t>(ch) * max_per_cell;
+    for (int s = lane; s < cnt; s += 32) {
+        const int i = slots[s];
+        const float d = dinv0[i];
+        const float sc = scale ? scale[i] : 1.0f;
+        u[i] = d != 0.0f ? sc * d * r[i] + e : 0.0f;
+    }
 }
 
 struct MgBottom {
@@ -272,49 +334,64 @@ struct MgBottom {
     const float* dense;
 };
 
-// Levels first..last in one block: residuals and corrections in shared memory.
+// Levels first..last in one block, everything in shared memory: per level the nine
+// coefficient planes, dinv, r and e, then the dense inverse of the last level.
 __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, const CgScalars* S,
                                                                 int mode) {
     if (pcg_skip(S, mode)) return;
     extern __shared__ float sm[];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    float* ks[kMgMaxLevels + 1];
+    float* ds[kMgMaxLevels + 1];
     float* rs[kMgMaxLevels + 1];
     float* es[kMgMaxLevels + 1];
-    {
-        float* at = sm;
-        for (int l = B.first; l <= B.last; l++) {
-            rs[l] = at;
-            es[l] = at + B.lv[l].cells;
-            at += 2 * B.lv[l].cells;
-        }
+    float* at = sm;
+    for (int l = B.first; l <= B.last; l++) {
+        const int cells = B.lv[l].cells;
+        ks[l] = at;
+        ds[l] = at + 9 * cells;
+        rs[l] = ds[l] + cells;
+        es[l] = rs[l] + cells;
+        at = es[l] + cells;
+        for (int idx = tid; idx < 9 * cells; idx += nt) ks[l][idx] = B.lv[l].k32[idx];
+        for (int idx = tid; idx < cells; idx += nt) ds[l][idx] = B.lv[l].dinv[idx];
     }
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int m = B.lv[B.last].cells;
+    float* dn = at;
+    for (int idx = tid; idx < m * m; idx += nt) dn[idx] = B.dense[idx];
     for (int c = tid; c < B.lv[B.first].cells; c += nt) rs[B.first][c] = B.lv[B.first].r[c];
     __syncthreads();
     for (int l = B.first; l < B.last; l++) {
+        const MgLevel& f = B.lv[l];
         const MgLevel& c = B.lv[l + 1];
         for (int I = tid; I < c.cells; I += nt)
-            rs[l + 1][I] = child_residuals(B.lv[l], rs[l], I / c.nz, I - (I / c.nz) * c.nz);
+            rs[l + 1][I] = child_residuals(f.nx, f.nz, f.cells, ks[l], ds[l], rs[l], I / c.nz,
+                                           I - (I / c.nz) * c.nz);
         __syncthreads();
     }
     {
-        const int m = B.lv[B.last].cells;
-        for (int i = tid; i < m; i += nt) {
+        const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+        const float* rl = rs[B.last];
+        for (int row = warp; row < m; row += nwarps) {
             float v = 0.0f;
-            for (int k = 0; k < m; k++) v += B.dense[k * m + i] * rs[B.last][k];
-            es[B.last][i] = v;
+            for (int k = lane; k < m; k += 32) v += dn[row * m + k] * rl[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) es[B.last][row] = v;
         }
         __syncthreads();
     }
     for (int l = B.last - 1; l >= B.first; l--) {
         const MgLevel& f = B.lv[l];
+        const int cnz = B.lv[l + 1].nz;
         for (int ch = tid; ch < f.cells; ch += nt)
-            es[l][ch] = smoothed_correction(f, rs[l], B.lv[l + 1], es[l + 1], ch);
+            es[l][ch] = smoothed_correction(f.nx, f.nz, f.cells, ks[l], ds[l], rs[l], cnz, es[l + 1], ch);
         __syncthreads();
     }
     for (int c = tid; c < B.lv[B.first].cells; c += nt) B.lv[B.first].e[c] = es[B.first][c];
 }
 
-// u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows.
+// u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows (used when the
+// bottom kernel covers level 1).
 __global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* cell_xz, int gnz,
                                                         const float* dinv0, const float* scale,
                                                         const float* r, const float* e1, float* u,
@@ -332,16 +409,19 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* ce
     }
 }
 
-size_t bottom_smem(const MgHierarchy& mg) {
-    size_t cells = 0;
-    for (int l = mg.bottom; l <= mg.levels; l++) cells += static_cast<size_t>(mg.lv[l].cells);
-    return 2 * cells * sizeof(float);
+size_t bottom_bytes(const MgLevel* lv, int first, int last) {
+    size_t floats = 0;
+    for (int l = first; l <= last; l++) floats += 12 * static_cast<size_t>(lv[l].cells);
+    const size_t m = static_cast<size_t>(lv[last].cells);
+    return (floats + m * m) * sizeof(float);
 }
 
 size_t dense_smem(const MgHierarchy& mg) {
     const size_t m = static_cast<size_t>(mg.lv[mg.levels].cells);
     return (m * m + m + 1) * sizeof(float);
 }
+
+int warp_grid(int cells) { return grid_for(static_cast<int64_t>(cells) * 32); }
 
 }  // namespace
 
@@ -356,7 +436,8 @@ int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom) {
         l++;
     }
     int b = l;
-    while (b > 1 && lv[b - 1].cells <= kMgBottomCells) b--;
+    while (b > 1 && bottom_bytes(lv, b - 1, l) <= kMgBottomBytes) b--;
+    if (bottom_bytes(lv, b, l) > kMgBottomBytes) return 0;
     *bottom = b;
     return l;
 }
@@ -365,8 +446,8 @@ cudaError_t mg_prepare_device() {
     const int dense_max = (kMgDenseCells * kMgDenseCells + kMgDenseCells + 1) * static_cast<int>(sizeof(float));
     cudaError_t e = cudaFuncSetAttribute(k_mg_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, dense_max);
     if (e != cudaSuccess) return e;
-    const int bottom_max = 2 * 2 * (kMgBottomCells + 64) * static_cast<int>(sizeof(float));
-    return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize, bottom_max);
+    return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kMgBottomBytes));
 }
 
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
@@ -383,10 +464,14 @@ void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
 int mg_setup_launches(const MgHierarchy& mg) { return 2 + (mg.levels - 1) + 1; }
 
 void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
-              cudaStream_t s) {
+              cudaStream_t s, const CgOperands* fuse_axpy) {
     const MgLevel& L1 = mg.lv[1];
-    k_mg_restrict0<<<grid_for(L1.cells), kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot,
-                                                        mg.max_per_cell, r, S, mode);
+    if (fuse_axpy)
+        k_mg_axpy_restrict<<<warp_grid(L1.cells), kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_count,
+                                                                 mg.cell_slot, mg.max_per_cell);
+    else
+        k_mg_restrict0<<<warp_grid(L1.cells), kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot,
+                                                             mg.max_per_cell, r, S, mode);
     for (int l = 1; l < mg.bottom; l++)
         k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
     MgBottom B{};
@@ -394,13 +479,18 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
     B.dense = mg.dense;
-    k_mg_bottom<<<1, kMgBottomThreads, bottom_smem(mg), s>>>(B, S, mode);
-    for (int l = mg.bottom - 1; l >= 1; l--)
+    k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, mg.bottom, mg.levels), s>>>(B, S, mode);
+    for (int l = mg.bottom - 1; l >= 2; l--)
         k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
-    k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, mg.lv[1].nz, mg.dinv0,
-                                                   mg.scale, r, L1.e, u, S, mode);
+    if (mg.bottom > 1)
+        k_mg_up_prolong<<<warp_grid(L1.cells), kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_count, mg.cell_slot,
+                                                              mg.max_per_cell, mg.dinv0, mg.scale,
+                                                              r, u, S, mode);
+    else
+        k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
+                                                       r, L1.e, u, S, mode);
 }
 
-int mg_apply_launches(const MgHierarchy& mg) { return 3 + 2 * (mg.bottom - 1); }
+int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * mg.bottom : 3; }
 
 }  // namespace mpsgb

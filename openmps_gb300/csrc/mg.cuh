@@ -10,9 +10,10 @@
 // Preconditioner (symmetric, negative definite like A on the rows it acts on):
 //   u = s_i * omega_0 * r_i / a_ii  +  P_1 V_1(P_1^T r)
 // i.e. a (learned-)scaled Jacobi term on the particles plus a V(1,1) cycle with damped
-// Jacobi on the cell levels; the levels of at most kMgBottomCells cells run inside one
-// thread block and the coarsest level (at most kMgDenseCells cells) is solved with its
-// dense inverse.  Identity rows of the PPE (dummy, disabled, free-surface rows) get u = 0.
+// Jacobi on the cell levels.  The coarsest levels run inside one thread block from
+// shared memory, and the coarsest of all (at most kMgDenseCells cells) is solved with
+// its dense inverse.  Identity rows of the PPE (dummy, disabled and free-surface rows)
+// get u = 0.
 #pragma once
 
 #include "cg.cuh"
@@ -20,8 +21,10 @@
 namespace mpsgb {
 
 constexpr int kMgMaxLevels = 14;
-constexpr int kMgBottomCells = 2048;   // levels this small run in the single-block kernel
 constexpr int kMgDenseCells = 128;     // the coarsest level, solved with its dense inverse
+// The single-block kernel takes the coarsest levels whose planes, vectors and the dense
+// inverse fit this much shared memory.
+constexpr size_t kMgBottomBytes = 200 * 1024;
 constexpr int kMgBottomThreads = 1024;
 constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
 constexpr float kMgOmegaCoarse = 0.7f; // Jacobi weight of the cell levels
@@ -54,16 +57,17 @@ struct MgHierarchy {
 };
 
 // Level sizes for a gnx x gnz search grid (returns the level count, 0 if the grid is
-// too large for the 16-bit cell coordinates).
+// too large for the 16-bit cell coordinates or the level count).
 int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom);
 // Setup of one solve: level-1 operator from the FP64 matrix, the coarser Galerkin
 // operators and the dense inverse.  Skips itself when the step already failed.
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s);
 int mg_setup_launches(const MgHierarchy& mg);
 // u = M r.  `mode` gates the kernels on the solve state like the PCG kernels: 0 init,
-// 1 iteration, 2 after a reliable update (see pcg_skip).
+// 1 iteration, 2 after a reliable update (see pcg_skip).  With `fuse_axpy` (mode 1) the
+// iteration's vector updates run in the restriction kernel, which then produces r.
 void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
-              cudaStream_t s);
+              cudaStream_t s, const CgOperands* fuse_axpy = nullptr);
 int mg_apply_launches(const MgHierarchy& mg);
 // Shared-memory bytes the single-block kernels need (opt-in set once per device).
 cudaError_t mg_prepare_device();
