@@ -280,6 +280,43 @@ int mps_cg_solve_csr_device_noalloc(int64_t n, const int64_t* row_ptr, const int
                                     int32_t criterion, int32_t max_iters, void* stream,
                                     int32_t* iterations, double* true_relres);
 
+/* ------------------------------------------------------------ learned solve
+ * No counterpart in the reference (its CG is unpreconditioned and starts from the
+ * previous pressure).  MPS_SOLVER_LEARNED is MPS_SOLVER_MIXED_MG started from a
+ * network-predicted initial guess and with a network-predicted scale of each particle's
+ * Jacobi term; the FP64 CG fallback and the FP64 true residual judge its result.
+ *
+ * Weight blob (FP32, MPS_MLP_BLOB_FLOATS): feature mean[16], feature std[16],
+ * W1[64][16], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[2][64], b4[2]
+ * (W[out][in], GELU after the three hidden layers).
+ * Outputs: out0 = correction of the initial guess (units of the RMS Jacobi-scaled
+ * residual), s = 1 + 0.25 tanh(out1) = scale of the particle's Jacobi term.
+ * Sample (FP32, MPS_MLP_SAMPLE_FLOATS): features[16], target y, Jacobi term g. */
+#define MPS_MLP_BLOB_FLOATS 9570
+#define MPS_MLP_SAMPLE_FLOATS 18
+
+/* Loads the network used by MPS_SOLVER_LEARNED (converted to the tensor-core image). */
+int mps_learned_set_weights(mps_handle* h, const float* blob, int64_t count);
+/* When enabled, every solve also records one training sample per particle: the
+ * features of the step and the targets from the solution (any solver). */
+int mps_learned_collect(mps_handle* h, int32_t enable);
+/* The last step's samples (n x MPS_MLP_SAMPLE_FLOATS) and active-row flags (n);
+ * with both pointers null only *count (= n) is returned. */
+int mps_learned_samples(mps_handle* h, float* samples, int32_t* active, int64_t capacity,
+                        int64_t* count);
+/* Network inference on the tensor cores (BF16 operands, FP32 accumulation) for n
+ * feature rows (n x 16, residual features already in units of sigma): out n x 2. */
+int mps_mlp_infer(int32_t device, const float* blob, const float* features, int64_t n, float* out);
+/* Mean loss over n samples and its gradient (FP32 training kernels); grad has
+ * MPS_MLP_BLOB_FLOATS entries, the first 32 (feature mean/std) are zero. */
+int mps_mlp_loss_grad(int32_t device, const float* blob, const float* samples, int64_t n,
+                      float* grad, double* loss);
+/* Adam training on the GPU: `epochs` passes over the samples in seeded shuffled order,
+ * minibatches of `batch`; blob holds the initial weights in and the trained ones out;
+ * epoch_loss (optional, `epochs` entries) the mean loss of each pass. */
+int mps_mlp_train(int32_t device, float* blob, const float* samples, int64_t n, int32_t epochs,
+                  int32_t batch, float lr, uint64_t seed, double* epoch_loss);
+
 #ifdef __cplusplus
 }
 #endif

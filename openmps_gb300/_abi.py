@@ -42,6 +42,9 @@ SOLVER_MIXED = 1
 SOLVER_LEARNED = 2
 SOLVER_MIXED_MG = 3
 
+MLP_BLOB_FLOATS = 9570
+MLP_SAMPLE_FLOATS = 18
+
 CG_LAUNCH_GRAPH = 0
 CG_LAUNCH_HOST = 1
 

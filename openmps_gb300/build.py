@@ -30,6 +30,7 @@ UNITS = {
     "stages.cu": ["-fmad=false"],
     "cg.cu": [],
     "mg.cu": [],
+    "learned.cu": [],
     "scan.cu": [],
     "noalloc.cu": [],
     "mps_abi.cu": [],

@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "libopenmps_gb300.so")
 _LIB = None
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I32 = C.POINTER(C.c_int32)
 _I64 = C.POINTER(C.c_int64)
 _P = C.c_void_p
@@ -78,6 +79,13 @@ PROTOTYPES = {
                                    C.c_int32, C.c_int32, _I32, _D]),
     "mps_cg_solve_csr_device_noalloc": (C.c_int, [C.c_int64, _P, _P, _P, _P, _P, C.c_double,
                                                   C.c_int32, C.c_int32, _P, _I32, _D]),
+    "mps_learned_set_weights": (C.c_int, [_P, _F, C.c_int64]),
+    "mps_learned_collect": (C.c_int, [_P, C.c_int32]),
+    "mps_learned_samples": (C.c_int, [_P, _F, _I32, C.c_int64, _I64]),
+    "mps_mlp_infer": (C.c_int, [C.c_int32, _F, _F, C.c_int64, _F]),
+    "mps_mlp_loss_grad": (C.c_int, [C.c_int32, _F, _F, C.c_int64, _F, _D]),
+    "mps_mlp_train": (C.c_int, [C.c_int32, _F, _F, C.c_int64, C.c_int32, C.c_int32, C.c_float,
+                                C.c_uint64, _D]),
 }
 
 
@@ -293,6 +301,24 @@ class Computer:
         self._check(self.lib.mps_debug_set_aux(self.h, *[_ptr(_f64(a)) for a in
                                                          (n_without_spp, ecs, ox, oz)]))
 
+    # ---------------------------------------------------------- learned solve
+    def learned_set_weights(self, blob):
+        w = _f32(blob)
+        self._check(self.lib.mps_learned_set_weights(self.h, _ptr(w, C.c_float), w.size))
+
+    def learned_collect(self, enable: bool):
+        self._check(self.lib.mps_learned_collect(self.h, 1 if enable else 0))
+
+    def learned_samples(self):
+        """The last step's (n, 18) samples and (n,) active-row flags."""
+        n = self.count
+        out = np.zeros((n, abi.MLP_SAMPLE_FLOATS), dtype=np.float32)
+        act = np.zeros(n, dtype=np.int32)
+        cnt = C.c_int64()
+        self._check(self.lib.mps_learned_samples(self.h, _ptr(out, C.c_float), _ptr(act, C.c_int32), n,
+                                                 C.byref(cnt)))
+        return out, act
+
     def cg_solve_csr(self, row_ptr, col, val, b, x0, eps, criterion=abi.CRIT_INITIAL_RESIDUAL,
                      max_iters=0, solver=abi.SOLVER_CG64):
         """SolvePressurePoissonEquation on a caller CSR system; returns (x, iterations, relres)."""
@@ -307,6 +333,51 @@ class Computer:
                                               _ptr(va), _ptr(bb), _ptr(x), eps, criterion, max_iters,
                                               solver, C.byref(it), C.byref(rel)))
         return x, it.value, rel.value
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _status(rc: int, what: str):
+    if rc != abi.MPS_OK:
+        raise ComputerError(rc, what)
+
+
+def mlp_infer(blob, features, device: int = 0) -> np.ndarray:
+    """Tensor-core inference of the learned-solve network: (n, 16) features -> (n, 2)."""
+    lib = load_library()
+    w = _f32(blob)
+    f = _f32(features)
+    n = f.shape[0]
+    out = np.zeros((n, 2), dtype=np.float32)
+    _status(lib.mps_mlp_infer(device, _ptr(w, C.c_float), _ptr(f, C.c_float), n, _ptr(out, C.c_float)),
+            "mps_mlp_infer")
+    return out
+
+
+def mlp_loss_grad(blob, samples, device: int = 0):
+    """(mean loss, gradient) of the learned-solve network on (n, 18) samples (GPU kernels)."""
+    lib = load_library()
+    w = _f32(blob)
+    s = _f32(samples)
+    grad = np.zeros(abi.MLP_BLOB_FLOATS, dtype=np.float32)
+    loss = C.c_double()
+    _status(lib.mps_mlp_loss_grad(device, _ptr(w, C.c_float), _ptr(s, C.c_float), s.shape[0],
+                                  _ptr(grad, C.c_float), C.byref(loss)), "mps_mlp_loss_grad")
+    return loss.value, grad
+
+
+def mlp_train(blob, samples, epochs: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0,
+              device: int = 0):
+    """Adam training on the GPU; returns (trained blob, mean loss per epoch)."""
+    lib = load_library()
+    w = np.array(blob, dtype=np.float32, copy=True)
+    s = _f32(samples)
+    losses = np.zeros(epochs)
+    _status(lib.mps_mlp_train(device, _ptr(w, C.c_float), _ptr(s, C.c_float), s.shape[0], epochs,
+                              batch, lr, seed, _ptr(losses)), "mps_mlp_train")
+    return w, losses
 
 
 def create_computer(eps: float, params: abi.MpsParams, device: int = 0) -> Computer:

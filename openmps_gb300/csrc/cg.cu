@@ -32,7 +32,7 @@
 #include <cmath>
 #include <vector>
 
-#include "mg.cuh"
+#include "learned.cuh"
 
 namespace mpsgb {
 
@@ -637,13 +637,18 @@ void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
 }
 
 void init_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
-                  cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+                  cudaGraphConditionalHandle h, int use_cond, cudaStream_t s,
+                  const LearnedRun* lrn) {
     const int gs = ops.grid_spmv;
     if (solver == MPS_SOLVER_CG64) {
         k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond, nullptr);
         return;
     }
     if (is_pcg(solver)) mg_setup(*mg, ops, s);
+    if (solver == MPS_SOLVER_LEARNED && lrn) {
+        k_cg_configure<<<1, 32, 0, s>>>(lrn->S, 0.0, MPS_CRIT_RHS, 1, 0.0);
+        learned_prep(*lrn->L, ops, *mg, lrn->S, true, s);
+    }
     k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
     if (is_pcg(solver)) {
         mg_apply(*mg, ops.S, 0, ops.r32, ops.u32, s);
@@ -675,6 +680,26 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
         k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
 }
 
+void learned_prep(const LearnedOps& L, const CgOperands& o, const MgHierarchy& mg, CgScalars* S,
+                  bool infer, cudaStream_t s) {
+    CgOperands p = o;
+    p.S = S;
+    k_mx_init<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0);  // r0 = b - A x0 in FP64, into r32
+    MgHierarchy plain = mg;
+    plain.scale = nullptr;
+    mg_apply(plain, S, 0, o.r32, o.u32, s);
+    k_pmx_spmv<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0, 0, 0);  // alpha0 = r0.u0 / (A u0).u0
+    launch_learned_features(L, p, S, s);
+    if (infer) {
+        launch_mlp_infer(L.packed, L.feat, L.n, L.sigma, L.out, L.error, s);
+        launch_learned_apply(L, p, S, s);
+    }
+}
+
+int learned_prep_launches(const MgHierarchy& mg, bool infer) {
+    return 1 + mg_apply_launches(mg) + 1 + 2 + (infer ? 2 : 0);
+}
+
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg) {
     if (solver == MPS_SOLVER_CG64) return 3;
     return is_pcg(solver) && mg ? 1 + mg_apply_launches(*mg) : 2;
@@ -697,14 +722,15 @@ void CgGraph::reset() {
 }
 
 cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win,
-                           const MgHierarchy* mg, const CgOperands* fb) {
+                           const MgHierarchy* mg, const CgOperands* fb, const LearnedRun* lrn) {
     if (is_pcg(solver) && (!mg || !fb)) return cudaErrorInvalidValue;
+    if (solver == MPS_SOLVER_LEARNED && !lrn) return cudaErrorInvalidValue;
     if (solver != MPS_SOLVER_CG64) {
         // preferred: the reliable update under an IF node nested in the WHILE body
-        if (build_impl(solver, ops, s, true, win, mg, fb) == cudaSuccess) return cudaSuccess;
+        if (build_impl(solver, ops, s, true, win, mg, fb, lrn) == cudaSuccess) return cudaSuccess;
         cudaGetLastError();
     }
-    return build_impl(solver, ops, s, false, win, mg, fb);
+    return build_impl(solver, ops, s, false, win, mg, fb, lrn);
 }
 
 namespace {
@@ -777,7 +803,8 @@ cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* dep, cudaGraphConditionalH
 }  // namespace
 
 cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                                const L2Window& win, const MgHierarchy* mg, const CgOperands* fb) {
+                                const L2Window& win, const MgHierarchy* mg, const CgOperands* fb,
+                                const LearnedRun* lrn) {
     reset();
     ops_ = ops;
     solver_ = solver;
@@ -800,7 +827,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    init_kernels(solver, ops, mg, h, 1, s);
+    init_kernels(solver, ops, mg, h, 1, s, lrn);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
     cudaGraphNode_t init_node;
@@ -922,14 +949,16 @@ cudaError_t host_loop(int solver, const CgOperands& ops, const MgHierarchy* mg, 
 
 cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
                           cudaStream_t s, int64_t* launches, const MgHierarchy* mg,
-                          const CgOperands* fb) {
+                          const CgOperands* fb, const LearnedRun* lrn) {
     if (is_pcg(solver) && (!mg || !fb)) return cudaErrorInvalidValue;
+    if (solver == MPS_SOLVER_LEARNED && !lrn) return cudaErrorInvalidValue;
     const int gv = ops.grid_vec, gs = ops.grid_spmv;
     const cudaGraphConditionalHandle none = 0;
     int64_t k = 0;
-    init_kernels(solver, ops, mg, none, 0, s);
+    init_kernels(solver, ops, mg, none, 0, s, lrn);
     k += solver == MPS_SOLVER_CG64 ? 1 : 2;
     if (is_pcg(solver)) k += mg_setup_launches(*mg) + mg_apply_launches(*mg);
+    if (solver == MPS_SOLVER_LEARNED) k += 1 + learned_prep_launches(*mg, true);
     cudaError_t e = host_loop(solver, ops, mg, host_S, chunk, s, &k);
     if (e != cudaSuccess) return e;
     if (solver != MPS_SOLVER_CG64) {

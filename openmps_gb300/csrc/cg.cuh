@@ -66,6 +66,13 @@ struct L2Window {
 };
 
 struct MgHierarchy;
+struct LearnedOps;
+
+// The learned start of a solve: its device state and the scalars its kernels gate on.
+struct LearnedRun {
+    const LearnedOps* L;
+    CgScalars* S;
+};
 
 // A CUDA graph running one whole solve: init kernels + device-driven while loop (+ for
 // the preconditioned solvers the FP64 CG fallback loop, which runs only after a failure).
@@ -75,7 +82,8 @@ public:
     // `mg` and `fb` (operands of the FP64 fallback, own scalars) are required for
     // MPS_SOLVER_MIXED_MG and MPS_SOLVER_LEARNED and ignored otherwise.
     cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {},
-                      const MgHierarchy* mg = nullptr, const CgOperands* fb = nullptr);
+                      const MgHierarchy* mg = nullptr, const CgOperands* fb = nullptr,
+                      const LearnedRun* lrn = nullptr);
     cudaError_t launch(cudaStream_t s);
     void reset();
     bool valid() const { return exec_ != nullptr; }
@@ -88,7 +96,8 @@ public:
 
 private:
     cudaError_t build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                           const L2Window& win, const MgHierarchy* mg, const CgOperands* fb);
+                           const L2Window& win, const MgHierarchy* mg, const CgOperands* fb,
+                           const LearnedRun* lrn);
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int solver_ = -1;
@@ -102,7 +111,7 @@ private:
 // Used when kernels must be visible one by one (profilers) and as a fallback.
 cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
                           cudaStream_t s, int64_t* launches, const MgHierarchy* mg = nullptr,
-                          const CgOperands* fb = nullptr);
+                          const CgOperands* fb = nullptr, const LearnedRun* lrn = nullptr);
 // Kernels of one iteration of the solver, and of one reliable update.
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg);
 int cg_kernels_per_update(int solver, const MgHierarchy* mg);

@@ -15,7 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "mg.cuh"
+#include "learned.cuh"
 #include "common.cuh"
 
 using namespace mpsgb;
@@ -58,6 +58,13 @@ struct mps_handle {
     CgScalars* S_fb = nullptr;  // scalars of the FP64 fallback after a preconditioned solve
     MgHierarchy mg;             // cell multigrid (MIXED_MG, LEARNED)
     bool mg_device_ready = false;
+    // learned warm start / preconditioner scale
+    LearnedOps lrn;
+    CgScalars* S_lrn = nullptr;
+    void* lrn_packed = nullptr;  // tensor-core weight image (separate allocation)
+    bool lrn_loaded = false;
+    bool lrn_collect = false;
+    bool ppe_fp32 = false;       // the last assembly also wrote the FP32 matrix
     int sm_count = 1;
     CgGraph cg;
     int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
@@ -159,8 +166,6 @@ void validate(const mps_params& p) {
     if (!(p.courant > 0)) bad("courant must be positive");
     if (!(p.max_x > p.min_x) || !(p.max_z > p.min_z)) bad("empty domain");
     if (p.solver < MPS_SOLVER_CG64 || p.solver > MPS_SOLVER_MIXED_MG) bad("unknown solver");
-    if (p.solver == MPS_SOLVER_LEARNED)
-        throw StatusError{MPS_ERR_NOT_SUPPORTED, "learned solver needs mps_learned_* setup"};
     if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
         bad("unknown criterion");
     if (p.flags & ~static_cast<uint32_t>(MPS_PRESET_REFERENCE)) bad("unknown method flag");
@@ -202,6 +207,36 @@ void setup_constants(mps_handle* h) {
     sc.max_per_cell = (c + 1) * (c + 1);
     sc.nb_stride = sc.max_per_cell * 9;
     sc.ppe_stride = sc.nb_stride + 1;
+}
+
+// Interior PPE diagonal and row length on the undisturbed lattice (feature scales of the
+// learned solve): a_ii = -sum_j a_ij over the lattice points within the Laplacian radius.
+double lattice_diagonal(const mps_handle* h) {
+    const SceneConst& sc = h->sc;
+    const double l0 = sc.l0;
+    const int range = static_cast<int>(std::ceil(sc.re_lap / l0));
+    double sum = 0.0;
+    for (int i = -range; i <= range; i++)
+        for (int j = -range; j <= range; j++) {
+            if (i == 0 && j == 0) continue;
+            const double r = std::sqrt(static_cast<double>(i * i + j * j)) * l0;
+            if (r >= sc.re_lap) continue;
+            if (sc.flags & MPS_FLAG_HL)
+                sum += (5.0 - 2.0) * sc.re_lap / sc.n0_lap / (r * r * r);
+            else
+                sum += 2.0 * 2.0 / (sc.lambda_lap * sc.n0_lap) * (sc.re_lap / r - 1.0);
+        }
+    return -sum;
+}
+
+int lattice_row_length(const mps_handle* h) {
+    const SceneConst& sc = h->sc;
+    const int range = static_cast<int>(std::ceil(sc.re_lap / sc.l0));
+    int cnt = 1;
+    for (int i = -range; i <= range; i++)
+        for (int j = -range; j <= range; j++)
+            if (!(i == 0 && j == 0) && std::sqrt(static_cast<double>(i * i + j * j)) * sc.l0 < sc.re_lap) cnt++;
+    return cnt;
 }
 
 // (Re)allocates every per-particle buffer for n particles, preserving the first
@@ -280,6 +315,39 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         mg.cell_slot = st.cell_slot;
         mg.status = st.status;
     }
+    // learned-solve buffers
+    LearnedOps& L = h->lrn;
+    const void* packed = L.packed;
+    L = LearnedOps{};
+    L.packed = packed;
+    L.n = static_cast<int32_t>(n);
+    L.feat = dalloc<float>(h, 16 * n);
+    L.out = dalloc<float>(h, 2 * n);
+    L.scale = dalloc<float>(h, n);
+    L.coarse = dalloc<float>(h, n);
+    L.sample = dalloc<float>(h, static_cast<int64_t>(kMlpSampleFloats) * n);
+    L.active = dalloc<int32_t>(h, n);
+    L.sigma = dalloc<double>(h, 2);
+    L.partials = dalloc<double>(h, 2 * static_cast<int64_t>(cg_grid_spmv(n)) + 2);
+    L.counter = dalloc<uint32_t>(h, 1);
+    L.error = dalloc<int32_t>(h, 1);
+    L.q4 = dalloc<float4>(h, n);
+    L.q2 = dalloc<float2>(h, n);
+    L.x0d = dalloc<double>(h, n);
+    L.rho = h->prm.rho;
+    L.rho_l02 = h->prm.rho * h->prm.l0 * h->prm.l0;
+    L.n0 = sc.n0;
+    L.a_ref = lattice_diagonal(h);
+    L.len_ref = static_cast<float>(lattice_row_length(h));
+    L.nd = st.nd;
+    L.n_wo_spp = st.n_wo_spp;
+    L.ecs = st.ecs;
+    L.p = st.p;
+    L.type = st.type;
+    L.step = st.step;
+    L.dinv0 = mg.dinv0;
+    L.flags = sc.flags;
+    h->S_lrn = dalloc<CgScalars>(h, 1);
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -290,6 +358,12 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(h->S_fb, 0, sizeof(CgScalars), s), "memset");
     check(cudaMemsetAsync(st.cell_xz, 0xff, sizeof(int32_t) * n, s), "memset");
+    check(cudaMemsetAsync(st.ppe_cv32, 0, sizeof(uint2) * sell_cap, s), "memset");
+    h->ppe_fp32 = false;
+    check(cudaMemsetAsync(h->S_lrn, 0, sizeof(CgScalars), s), "memset");
+    check(cudaMemsetAsync(L.counter, 0, sizeof(uint32_t), s), "memset");
+    check(cudaMemsetAsync(L.error, 0, sizeof(int32_t), s), "memset");
+    check(cudaMemsetAsync(L.active, 0, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.nb_count, 0, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.ppe_len, 0, sizeof(int32_t) * kSellRows * sell_chunks(n), s), "memset");
     check(cudaMemsetAsync(h->p32, 0, sizeof(float) * n, s), "memset");
@@ -349,6 +423,12 @@ void require_particles(mps_handle* h) {
 
 void launched(mps_handle* h, int k) { h->stats.kernel_launches += k; }
 
+// The FP32 matrix is assembled next to the FP64 one when a solver or the learned-sample
+// collection reads it.
+bool wants_fp32(const mps_handle* h) {
+    return h->prm.solver != MPS_SOLVER_CG64 || h->lrn_collect;
+}
+
 bool is_preconditioned(int32_t solver) {
     return solver == MPS_SOLVER_MIXED_MG || solver == MPS_SOLVER_LEARNED;
 }
@@ -401,7 +481,8 @@ void read_status(mps_handle* h, bool solve_done) {
             if (is_preconditioned(h->prm.solver)) {
                 const int own = S.iter - S.fb_iter;
                 launched(h, mg_setup_launches(h->mg) + 2 + mg_apply_launches(h->mg) + own * kpi +
-                                S.updates * kpu + 4 + 3 * S.fb_iter);
+                                S.updates * kpu + 4 + 3 * S.fb_iter +
+                                (h->prm.solver == MPS_SOLVER_LEARNED ? 1 + learned_prep_launches(h->mg, true) : 0));
             } else {
                 launched(h, 4 + S.iter * kpi + S.updates * kpu);
             }
@@ -482,19 +563,38 @@ void setup_l2_window(mps_handle* h) {
 void do_solve(mps_handle* h) {
     cudaStream_t s = h->stream;
     const int solver = h->prm.solver;
+    if (wants_fp32(h) && !h->ppe_fp32)
+        throw StatusError{MPS_ERR_STATE, "the PPE was assembled for the FP64 solver: assemble it again"};
     const bool pcg = is_preconditioned(solver);
     const int max_iter = default_max_iter(h->prm.max_cg_iters, h->n, solver);
     launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter, 0.01, s);
     after_launch("cg configure");
     launched(h, 1);
     CgOperands fb{};
-    if (pcg) {
+    const bool learned = solver == MPS_SOLVER_LEARNED;
+    if (learned && !h->lrn_loaded)
+        throw StatusError{MPS_ERR_STATE, "learned solver: load weights with mps_learned_set_weights"};
+    if (pcg || h->lrn_collect) {
         if (h->mg.levels == 0)
             throw StatusError{MPS_ERR_NOT_SUPPORTED, "search grid too large for the multigrid preconditioner"};
         if (!h->mg_device_ready) {
             check(mg_prepare_device(), "multigrid kernel attributes");
+            check(mlp_prepare_device(), "network kernel attributes");
             h->mg_device_ready = true;
         }
+    }
+    MgHierarchy mg = h->mg;
+    if (learned) mg.scale = h->lrn.scale;
+    const LearnedRun run{&h->lrn, h->S_lrn};
+    if (h->lrn_collect) {
+        // features of the step before the solve (the samples are completed after it)
+        launch_cg_configure(h->S_lrn, 0.0, MPS_CRIT_RHS, 1, 0.0, s);
+        mg_setup(h->mg, cg_operands(h), s);
+        learned_prep(h->lrn, cg_operands(h), h->mg, h->S_lrn, false, s);
+        after_launch("learned features");
+        launched(h, 1 + mg_setup_launches(h->mg) + learned_prep_launches(h->mg, false));
+    }
+    if (pcg) {
         launch_cg_configure(h->S_fb, h->prm.eps, h->prm.criterion,
                             default_max_iter(0, h->n, MPS_SOLVER_CG64), 0.01, s);
         after_launch("cg configure");
@@ -505,19 +605,24 @@ void do_solve(mps_handle* h) {
     if (solver != MPS_SOLVER_CG64) setup_l2_window(h);
     if (h->prm.cg_launch == MPS_CG_LAUNCH_HOST) {
         int64_t k = 0;
-        check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k, pcg ? &h->mg : nullptr,
-                            pcg ? &fb : nullptr),
+        check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k, pcg ? &mg : nullptr,
+                            pcg ? &fb : nullptr, learned ? &run : nullptr),
               "CG host loop");
         h->direct_launches = k;
-        return;
+    } else {
+        h->direct_launches = -1;
+        if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
+            check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
+                              pcg ? &mg : nullptr, pcg ? &fb : nullptr, learned ? &run : nullptr),
+                  "CG graph build");
+        }
+        check(h->cg.launch(s), "CG graph launch");
     }
-    h->direct_launches = -1;
-    if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
-        check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
-                          pcg ? &h->mg : nullptr, pcg ? &fb : nullptr),
-              "CG graph build");
+    if (h->lrn_collect) {
+        launch_learned_targets(h->lrn, cg_operands(h), h->S_lrn, s);
+        after_launch("learned samples");
+        launched(h, 1);
     }
-    check(h->cg.launch(s), "CG graph launch");
 }
 
 void forward(mps_handle* h, double dt) {
@@ -554,7 +659,8 @@ void forward(mps_handle* h, double dt) {
         launched(h, kLaunchesSaveX);
     }
     stage_mark(h, kPpe);
-    launch_set_ppe(sc, h->st, h->prm.solver != MPS_SOLVER_CG64, s);
+    launch_set_ppe(sc, h->st, wants_fp32(h), s);
+    h->ppe_fp32 = wants_fp32(h);
     launched(h, kLaunchesSetPpe);
     after_launch("stages");
     stage_mark(h, kSolve);
@@ -615,6 +721,34 @@ struct ScopedBuffers {
         return static_cast<T*>(q);
     }
 };
+
+// Runs f with `device` current, converting errors into status codes (standalone calls
+// that have no handle).
+template <class F>
+int on_device(int32_t device, F f) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    int rc = MPS_OK;
+    try {
+        if (cudaSetDevice(device) != cudaSuccess) throw StatusError{MPS_ERR_CUDA, "cudaSetDevice failed"};
+        f();
+    } catch (const StatusError& e) {
+        rc = e.code;
+    } catch (const std::bad_alloc&) {
+        rc = MPS_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception&) {
+        rc = MPS_ERR_STATE;
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+void check_blob(const float* blob) {
+    for (int k = 0; k < kMlpBlobFloats; k++)
+        if (!std::isfinite(blob[k])) throw StatusError{MPS_ERR_NONFINITE, "non-finite network weight"};
+    for (int k = 0; k < kMlpIn; k++)
+        if (!(blob[kMlpOffSd + k] > 0.0f)) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "feature std must be positive"};
+}
 
 }  // namespace
 
@@ -718,6 +852,7 @@ int mps_destroy(mps_handle* h) {
         cudaGetLastError();
     }
     dfree_all(h);
+    if (h->lrn_packed) cudaFree(h->lrn_packed);
     if (h->flush_buf) cudaFree(h->flush_buf);
     for (auto& e : h->user_events)
         if (e) cudaEventDestroy(e);
@@ -976,7 +1111,8 @@ MPS_STAGE(mps_stage_density, launch_density(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_error_correction, launch_error_correction(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_explicit, launch_explicit(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_save_x, launch_save_x(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_set_ppe, launch_set_ppe(h->sc, h->st, h->prm.solver != MPS_SOLVER_CG64, h->stream))
+MPS_STAGE(mps_stage_set_ppe, launch_set_ppe(h->sc, h->st, wants_fp32(h), h->stream);
+          h->ppe_fp32 = wants_fp32(h))
 MPS_STAGE(mps_stage_solve_ppe, do_solve(h); read_status(h, true))
 MPS_STAGE(mps_stage_assign_pressure, launch_assign_pressure(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_pressure_gradient, launch_pressure_gradient(h->sc, h->st, h->stream))
@@ -1200,6 +1336,153 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         if (!S.converged)
             throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
                               "Conjugate Gradient method couldn't solve Pressure Poison Equation"};
+    });
+}
+
+// ------------------------------------------------------------- learned solve
+int mps_learned_set_weights(mps_handle* h, const float* blob, int64_t count) {
+    if (!h || !blob) return MPS_ERR_INVALID_ARGUMENT;
+    if (count != kMlpBlobFloats) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        check_blob(blob);
+        std::vector<unsigned char> image(mlp_packed_bytes());
+        mlp_pack_weights(blob, image.data());
+        if (!h->lrn_packed) check(cudaMalloc(&h->lrn_packed, image.size()), "cudaMalloc");
+        check(cudaMemcpyAsync(h->lrn_packed, image.data(), image.size(), cudaMemcpyHostToDevice, h->stream),
+              "weights");
+        check(cudaStreamSynchronize(h->stream), "weights");
+        h->lrn.packed = h->lrn_packed;
+        h->lrn_loaded = true;
+        h->cg.reset();  // the solve graph holds the weight image address
+    });
+}
+
+int mps_learned_collect(mps_handle* h, int32_t enable) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    h->lrn_collect = enable != 0;
+    return MPS_OK;
+}
+
+int mps_learned_samples(mps_handle* h, float* samples, int32_t* active, int64_t capacity, int64_t* count) {
+    if (!h || !count) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        require_particles(h);
+        *count = h->n;
+        if (!samples && !active) return;
+        if (capacity < h->n) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "capacity below the particle count"};
+        cudaStream_t s = h->stream;
+        if (samples)
+            check(cudaMemcpyAsync(samples, h->lrn.sample, sizeof(float) * kMlpSampleFloats * h->n,
+                                  cudaMemcpyDeviceToHost, s),
+                  "samples");
+        if (active)
+            check(cudaMemcpyAsync(active, h->lrn.active, sizeof(int32_t) * h->n, cudaMemcpyDeviceToHost, s),
+                  "samples");
+        check(cudaStreamSynchronize(s), "samples");
+    });
+}
+
+int mps_mlp_infer(int32_t device, const float* blob, const float* features, int64_t n, float* out) {
+    if (!blob || !features || !out || n <= 0 || n > 0x7fffffff) return MPS_ERR_INVALID_ARGUMENT;
+    return on_device(device, [&] {
+        check_blob(blob);
+        check(mlp_prepare_device(), "network kernel attributes");
+        std::vector<unsigned char> image(mlp_packed_bytes());
+        mlp_pack_weights(blob, image.data());
+        ScopedBuffers b;
+        unsigned char* dimg = b.get<unsigned char>(image.size());
+        float* dfeat = b.get<float>(static_cast<size_t>(n) * kMlpIn);
+        float* dout = b.get<float>(static_cast<size_t>(n) * 2);
+        int32_t* derr = b.get<int32_t>(1);
+        check(cudaMemcpy(dimg, image.data(), image.size(), cudaMemcpyHostToDevice), "copy");
+        check(cudaMemcpy(dfeat, features, sizeof(float) * kMlpIn * n, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemset(derr, 0, sizeof(int32_t)), "memset");
+        launch_mlp_infer(dimg, dfeat, static_cast<int>(n), nullptr, dout, derr, 0);
+        check(cudaGetLastError(), "network inference");
+        int32_t err = 0;
+        check(cudaMemcpy(&err, derr, sizeof(int32_t), cudaMemcpyDeviceToHost), "copy");
+        if (err) throw StatusError{MPS_ERR_TIMEOUT, "tensor-core wait timed out"};
+        check(cudaMemcpy(out, dout, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost), "copy");
+    });
+}
+
+int mps_mlp_loss_grad(int32_t device, const float* blob, const float* samples, int64_t n, float* grad,
+                      double* loss) {
+    if (!blob || !samples || !grad || !loss || n <= 0) return MPS_ERR_INVALID_ARGUMENT;
+    return on_device(device, [&] {
+        check_blob(blob);
+        check(mlp_train_prepare_device(), "training kernel attributes");
+        ScopedBuffers b;
+        MlpTrainer T;
+        T.w = b.get<float>(kMlpBlobFloats);
+        T.grad = b.get<float>(kMlpBlobFloats);
+        T.partials = b.get<float>(static_cast<size_t>(mlp_train_blocks(n)) * (kMlpParams + 1));
+        T.loss = b.get<double>(1);
+        float* ds = b.get<float>(static_cast<size_t>(n) * kMlpSampleFloats);
+        check(cudaMemcpy(T.w, blob, sizeof(float) * kMlpBlobFloats, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemset(T.grad, 0, sizeof(float) * kMlpBlobFloats), "memset");
+        check(cudaMemcpy(ds, samples, sizeof(float) * kMlpSampleFloats * n, cudaMemcpyHostToDevice), "copy");
+        launch_mlp_loss_grad(T, ds, n, 0);
+        check(cudaGetLastError(), "training kernels");
+        check(cudaMemcpy(grad, T.grad, sizeof(float) * kMlpBlobFloats, cudaMemcpyDeviceToHost), "copy");
+        double l = 0.0;
+        check(cudaMemcpy(&l, T.loss, sizeof(double), cudaMemcpyDeviceToHost), "copy");
+        *loss = l / static_cast<double>(n);
+    });
+}
+
+int mps_mlp_train(int32_t device, float* blob, const float* samples, int64_t n, int32_t epochs,
+                  int32_t batch, float lr, uint64_t seed, double* epoch_loss) {
+    if (!blob || !samples || n <= 0 || epochs <= 0 || batch <= 0 || !(lr > 0.0f)) return MPS_ERR_INVALID_ARGUMENT;
+    return on_device(device, [&] {
+        check_blob(blob);
+        check(mlp_train_prepare_device(), "training kernel attributes");
+        ScopedBuffers b;
+        MlpTrainer T;
+        const int64_t bsz = std::min<int64_t>(batch, n);
+        T.w = b.get<float>(kMlpBlobFloats);
+        T.m = b.get<float>(kMlpBlobFloats);
+        T.v = b.get<float>(kMlpBlobFloats);
+        T.grad = b.get<float>(kMlpBlobFloats);
+        T.partials = b.get<float>(static_cast<size_t>(mlp_train_blocks(bsz)) * (kMlpParams + 1));
+        T.loss = b.get<double>(1);
+        float* ds = b.get<float>(static_cast<size_t>(n) * kMlpSampleFloats);
+        check(cudaMemcpy(T.w, blob, sizeof(float) * kMlpBlobFloats, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemset(T.m, 0, sizeof(float) * kMlpBlobFloats), "memset");
+        check(cudaMemset(T.v, 0, sizeof(float) * kMlpBlobFloats), "memset");
+        check(cudaMemset(T.grad, 0, sizeof(float) * kMlpBlobFloats), "memset");
+        // per epoch: a seeded Fisher-Yates shuffle of the samples (SplitMix64), then
+        // minibatches in order
+        std::vector<float> shuffled(static_cast<size_t>(n) * kMlpSampleFloats);
+        std::vector<int64_t> perm(static_cast<size_t>(n));
+        uint64_t state = seed;
+        auto next = [&state]() {
+            uint64_t z = (state += 0x9e3779b97f4a7c15ull);
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+            return z ^ (z >> 31);
+        };
+        int step = 0;
+        for (int ep = 0; ep < epochs; ep++) {
+            for (int64_t i = 0; i < n; i++) perm[i] = i;
+            for (int64_t i = n - 1; i > 0; i--) std::swap(perm[i], perm[next() % static_cast<uint64_t>(i + 1)]);
+            for (int64_t i = 0; i < n; i++)
+                std::memcpy(&shuffled[i * kMlpSampleFloats], samples + perm[i] * kMlpSampleFloats,
+                            sizeof(float) * kMlpSampleFloats);
+            check(cudaMemcpy(ds, shuffled.data(), sizeof(float) * shuffled.size(), cudaMemcpyHostToDevice), "copy");
+            double total = 0.0;
+            for (int64_t at = 0; at < n; at += bsz) {
+                const int64_t cnt = std::min(bsz, n - at);
+                launch_mlp_loss_grad(T, ds + at * kMlpSampleFloats, cnt, 0);
+                launch_mlp_adam(T, lr, ++step, 0);
+                double l = 0.0;
+                check(cudaMemcpy(&l, T.loss, sizeof(double), cudaMemcpyDeviceToHost), "copy");
+                total += l;
+            }
+            check(cudaGetLastError(), "training kernels");
+            if (epoch_loss) epoch_loss[ep] = total / static_cast<double>(n);
+        }
+        check(cudaMemcpy(blob, T.w, sizeof(float) * kMlpBlobFloats, cudaMemcpyDeviceToHost), "copy");
     });
 }
 
