@@ -42,7 +42,10 @@ METRIC = "particle-steps/s, 320k dam break"
 UNIT = "particle-steps/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 512 << 20
-SOLVERS = {"cg64": 0, "mixed": 1, "mg": 3}
+SOLVERS = {"cg64": 0, "mixed": 1, "mg": 3, "learned": 2}
+SOLVER_DESC = {0: "FP64 CG (reference algorithm)", 1: "FP32 CG + FP64 reliable updates",
+               3: "FP32 CG preconditioned by the cell multigrid + FP64 reliable updates",
+               2: "multigrid FP32 CG + FP64 reliable updates, learned initial guess and Jacobi scale"}
 
 
 def parse_args():
@@ -51,7 +54,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--solver", choices=("cg64", "mixed", "mg"), default="mg")
+    ap.add_argument("--solver", choices=("cg64", "mixed", "mg", "learned"), default="learned")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the same-state comparison of the PPE solvers")
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -161,6 +166,21 @@ def cpu_baseline(scene, params, dt, budget_s: float, max_steps: int | None = Non
             "seconds_per_step": sec / len(times)}
 
 
+def reduce_max(values, dist):
+    """Max over ranks of per-rank timings: the slowest replica sets the job's time."""
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    buf = torch.tensor(list(values), dtype=torch.float64, device=dev)
+    dist.all_reduce(buf, op=dist.ReduceOp.MAX)
+    return buf.tolist()
+
+
+def job_value(particles_per_replica: int, steps: int, world: int, total_ms: float) -> float:
+    """Whole-job particle-steps/s: every rank advances its own replica of the scene."""
+    return particles_per_replica * steps * world / (total_ms * 1e-3)
+
+
 def load_peak() -> tuple[float, str]:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -203,6 +223,10 @@ def run_ours(args, rank, world, local_rank):
     launch = abi.CG_LAUNCH_HOST if args.cg_launch == "host" else abi.CG_LAUNCH_GRAPH
     params = scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8, cg_launch=launch)
     comp = Computer(params, device=local_rank)
+    if solver == abi.SOLVER_LEARNED:
+        from openmps_gb300 import learned
+
+        comp.learned_set_weights(learned.load())
     comp.add_scene(scene)
 
     for _ in range(max(args.warmup, 0)):
@@ -281,11 +305,17 @@ def run_ours(args, rank, world, local_rank):
     stage_ms = {k: round(v, 3) for k, v in comp.stats()["stage_ms"].items()}
     comp.set_stage_timing(False)
 
+    # ---- the PPE solvers on the same state (a few steps each from a snapshot)
+    compare = None
+    if not args.no_compare and rank == 0:
+        compare = compare_solvers(comp, scene, dt, local_rank)
+
     # ---- roofline of the dominant kernel (the solver's SpMV), timed alone
     st = comp.stats()
     nnz = st["ppe_nnz"]
     n = comp.count
-    spmv_ms = comp.bench_spmv(solver, reps=20, flush_bytes=FLUSH_BYTES)
+    spmv_solver = abi.SOLVER_MIXED_MG if solver == abi.SOLVER_LEARNED else solver
+    spmv_ms = comp.bench_spmv(spmv_solver, reps=20, flush_bytes=FLUSH_BYTES)
     if solver == abi.SOLVER_CG64:
         alg_bytes = 12 * nnz + 4 * (n + 1) + 16 * n
         key, kernel = "cg64", "k_cg_spmv_dot"
@@ -301,16 +331,11 @@ def run_ours(args, rank, world, local_rank):
     traffic = load_traffic(key)
 
     # ---- reduce over ranks (max time)
-    t_steps = total_ms
-    t_e2e = e2e_ms
+    t_steps, t_e2e = total_ms, e2e_ms
     if dist is not None:
-        import torch
-
-        buf = torch.tensor([t_steps, t_e2e], dtype=torch.float64, device="cuda")
-        dist.all_reduce(buf, op=dist.ReduceOp.MAX)
-        t_steps, t_e2e = buf.tolist()
-    value = n_active * args.steps * world / (t_steps * 1e-3)
-    e2e_value = n_active * args.steps * world / (t_e2e * 1e-3)
+        t_steps, t_e2e = reduce_max([t_steps, t_e2e], dist)
+    value = job_value(n_active, args.steps, world, t_steps)
+    e2e_value = job_value(n_active, args.steps, world, t_e2e)
 
     if rank != 0:
         if dist is not None:
@@ -330,8 +355,7 @@ def run_ours(args, rank, world, local_rank):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if solver == abi.SOLVER_CG64 else "f64 (PPE iterations f32, f64 residual/refinement)",
-        "ppe_solver": {0: "FP64 CG (reference algorithm)", 1: "FP32 CG + FP64 reliable updates",
-                       3: "FP32 CG preconditioned by the cell multigrid + FP64 reliable updates"}[solver],
+        "ppe_solver": SOLVER_DESC[solver],
         "data": "synthetic (seeded lattice dam break)",
         "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
                                "reference MPS scheme (HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
@@ -354,6 +378,8 @@ def run_ours(args, rank, world, local_rank):
                      "spmv64_ms_per_launch": spmv64_ms,
                      "spmv64_achieved_gbs": (12 * nnz + 4 * (n + 1) + 16 * n) / (spmv64_ms * 1e-3) / 1e9},
     }
+    if compare is not None:
+        line["ppe_solvers_same_state"] = compare
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, scene.params(criterion=abi.CRIT_RHS, eps=1e-8), dt,
                                             args.cpu_seconds)
@@ -361,6 +387,47 @@ def run_ours(args, rank, world, local_rank):
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def compare_solvers(comp, scene, dt, device, steps=3):
+    """Step and PPE-solve time of every solver from the same particle state (a snapshot
+    of the timed run), `steps` steps each, with per-stage CUDA events."""
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import learned
+    from openmps_gb300.computer import Computer
+
+    P = comp.particles()
+    A = comp.aux()
+    out = {}
+    for name in ("cg64", "mixed", "mg", "learned"):
+        sv = SOLVERS[name]
+        c = Computer(scene.params(solver=sv, criterion=abi.CRIT_RHS, eps=1e-8), device=device)
+        if sv == abi.SOLVER_LEARNED:
+            c.learned_set_weights(learned.load())
+        c.add_particles(P["type"], P["x"], P["z"], P["u"], P["w"], P["p"], P["n"])
+        c.set_aux(A["n_without_spp"], A["ecs"], A["ox"], A["oz"])
+        c.set_stage_timing(True)
+        step_ms, solve_ms, its = [], [], []
+        for _ in range(steps):
+            c.flush_l2(FLUSH_BYTES)
+            c.event_record(0)
+            c.forward_time(dt)
+            c.event_record(1)
+            step_ms.append(c.event_elapsed(0, 1))
+            st = c.stats()
+            solve_ms.append(st["stage_ms"]["solve"])
+            its.append(st["cg_iterations"])
+            assert st["cg_true_relres"] <= 1e-8
+        c.close()
+        out[name] = {"step_ms": statistics.mean(step_ms), "ppe_ms": statistics.mean(solve_ms),
+                     "iterations": statistics.mean(its), "solver": SOLVER_DESC[sv]}
+    base = out["cg64"]
+    for name, v in out.items():
+        v["step_speedup_vs_cg64"] = base["step_ms"] / v["step_ms"]
+        v["ppe_speedup_vs_cg64"] = base["ppe_ms"] / v["ppe_ms"]
+    out["note"] = ("same snapshot for every solver, %d steps each, L2 flushed before each step; "
+                   "step_ms includes the per-stage events" % steps)
+    return out
 
 
 # ------------------------------------------------------------ reference arm

@@ -21,6 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libopenmps_gb300.so")
+DRIVER_SRC = os.path.join(HERE, "driver", "main.cpp")
+DRIVER = os.path.join(HERE, "openmps_gb300_main")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -89,7 +91,26 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
         if res.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), res.stderr))
         os.replace(tmp, LIB)
+    build_driver(force)
     return LIB
+
+
+def build_driver(force: bool = False) -> str:
+    """The command-line driver (reference XML/CSV in, CSV out) linked to the library."""
+    deps = [DRIVER_SRC, LIB, os.path.join(INCLUDE, "mps.h"), os.path.join(INCLUDE, "openmps_gb300.hpp")]
+    if not force and not _stale(DRIVER, deps):
+        return DRIVER
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the driver")
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-ffp-contract=off", "-I", INCLUDE, DRIVER_SRC, "-o", tmp,
+           "-L", HERE, "-lopenmps_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (" ".join(cmd), res.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

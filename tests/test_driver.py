@@ -1,0 +1,105 @@
+"""The command-line driver: the reference's XML/CSV input and CSV output contract.
+
+The input is written in the reference driver's format (src/OpenMps/Main.cpp:63-274:
+<condition>/<environment> value attributes, <particles type="csv"> with a Type, x, z,
+u, w, p, n header); the parse check runs without a GPU, the run is compared with the
+same steps taken through the Python binding of the same library.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from openmps_gb300 import _abi as abi
+from openmps_gb300 import build, scenes
+
+DRIVER = build.DRIVER
+
+
+def write_case(path, scene, end=0.004, interval=0.002, eps=1e-10, steps_per_output=4, extra=""):
+    P = dict(scene.meta["params"])
+    rows = ["Type, x, z, u, w, p, n"]
+    for k in range(scene.count):
+        rows.append("%d, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g" % (
+            scene.type[k], scene.x[k], scene.z[k], scene.u[k], scene.w[k], scene.p[k], scene.n[k]))
+    env = "\n".join('    <%s value="%r" />' % (k, v) for k, v in (
+        ("l_0", scene.l0), ("minStepCountPerOutput", steps_per_output), ("courant", P["courant"]),
+        ("g", P["g"]), ("rho", P["rho"]), ("nu", P["nu"]), ("r_eByl_0", P["re_by_l0"]),
+        ("surfaceRatio", P["surface_ratio"]), ("minX", scene.min_x), ("minZ", scene.min_z),
+        ("maxX", scene.max_x), ("maxZ", scene.max_z), ("r_lapByl_0", P["re_lap_by_l0"]),
+        ("flags", P["flags"])))
+    xml = ('<?xml version="1.0" encoding="utf-8"?>\n<openmps>\n  <condition>\n'
+           '    <startTime value="0" />\n    <endTime value="%r" />\n    <outputInterval value="%r" />\n'
+           '    <eps value="%r" />\n  </condition>\n  <environment>\n%s\n%s  </environment>\n'
+           '  <particles type="csv">\n%s\n  </particles>\n</openmps>\n'
+           % (end, interval, eps, env, extra, "\n".join(rows)))
+    with open(path, "w") as f:
+        f.write(xml)
+
+
+@pytest.fixture(scope="module")
+def driver():
+    build.build()
+    return DRIVER
+
+
+def test_parse_only(driver, tmp_path):
+    s = scenes.config_c0()
+    xml = tmp_path / "case.xml"
+    write_case(xml, s, end=0.01, interval=0.005, steps_per_output=10)
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode == 0, out.stderr
+    assert "%d particles" % s.count in out.stdout
+    kv = dict(item.split("=", 1) for item in out.stdout.strip().splitlines()[-1].split()
+              if "=" in item and not item.startswith(("min=", "max=")))
+    assert float(kv["maxDt"]) == 0.005 / 10
+    assert float(kv["l_0"]) == s.l0
+    assert float(kv["r_eByl_0"]) == s.meta["params"]["re_by_l0"]
+    assert int(kv["flags"]) == abi.PRESET_REFERENCE
+    assert float(kv["eps"]) == 1e-10
+
+
+def test_rejects_bad_header(driver, tmp_path):
+    s = scenes.config_c0()
+    xml = tmp_path / "bad.xml"
+    write_case(xml, s)
+    text = xml.read_text().replace("Type, x, z, u, w, p, n", "Type, x, y, u, w, p, n")
+    xml.write_text(text)
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode != 0
+    assert "Illegal header item" in (out.stdout + out.stderr)
+
+
+def _read_csv(path):
+    with open(path) as f:
+        head = f.readline().strip()
+    assert head == "Type, x, z, u, w, p, n"
+    return np.loadtxt(path, delimiter=",", skiprows=1)
+
+
+@pytest.mark.gpu
+def test_run_matches_python_binding(driver, tmp_path):
+    from openmps_gb300.computer import Computer
+
+    s = scenes.config_c0()
+    xml = tmp_path / "case.xml"
+    write_case(xml, s, end=0.004, interval=0.002, steps_per_output=4)
+    out = subprocess.run([driver, str(xml)], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "finished" in out.stdout
+    files = sorted(os.listdir(tmp_path / "result"))
+    assert files == ["particles_00000.csv", "particles_00001.csv", "particles_00002.csv"]
+    # the same loop through the Python binding: ForwardTime() until t passes each output
+    c = Computer(s.params(eps=1e-10, max_dt=0.002 / 4))
+    c.add_scene(s)
+    nxt = 0.0
+    for k in (1, 2):
+        nxt += 0.002
+        while c.environment().t < nxt:
+            c.forward_time()
+        got = _read_csv(tmp_path / "result" / ("particles_%05d.csv" % k))
+        P = c.particles()
+        ref = np.stack([P["type"], P["x"], P["z"], P["u"], P["w"], P["p"], P["n"]], axis=1)
+        # the driver prints six significant digits (default ostream formatting)
+        np.testing.assert_allclose(got, ref, rtol=2e-6, atol=1e-9 * max(1.0, np.abs(ref).max()))
