@@ -317,6 +317,47 @@ int mps_mlp_loss_grad(int32_t device, const float* blob, const float* samples, i
 int mps_mlp_train(int32_t device, float* blob, const float* samples, int64_t n, int32_t epochs,
                   int32_t batch, float lr, uint64_t seed, double* epoch_loss);
 
+/* ------------------------------------------------------------ batched scenes
+ * No counterpart in the reference (one Computer per scene there).  A batch handle holds
+ * `nscenes` independent scenes that share one mps_params (tank, l0, physics); each
+ * scene behaves as a separate Computer (no interaction), all advance together with a
+ * fixed dt: the stages run over all scenes at once and the PPEs are solved by one
+ * persistent kernel, a thread block per scene (mixed-precision multigrid-preconditioned
+ * CG, FP64 CG fallback).  The first mps_batch_forward step runs an autotuner (threads
+ * per block and scene order of the solve, timed on the assembled step); later steps
+ * replay one captured CUDA graph per step.  Limits: dt > 0; the scene's cell hierarchy
+ * must fit one block's shared memory (MPS_ERR_NOT_SUPPORTED otherwise). */
+typedef struct mps_batch_scene_stats {
+    int32_t iterations;          /* PPE iterations of the last step (incl. fallback) */
+    int32_t reliable_updates;
+    int32_t fallback;            /* 1 if the FP64 CG finished the solve */
+    int32_t converged;
+    int32_t fallback_iterations;
+    int32_t pad;
+    double true_relres;          /* |b - A x| / |b| in FP64 after the solve */
+    double initial_relres;       /* |b - A x0| / |b| */
+} mps_batch_scene_stats;
+
+typedef struct mps_batch_tuning {
+    int32_t threads, blocks, order;  /* chosen launch; order 0 = scene index, 1 = largest first */
+    int32_t candidates;
+    float candidate_ms[16];
+    int32_t candidate_threads[16];
+    int32_t candidate_order[16];
+} mps_batch_tuning;
+
+int mps_batch_create(const mps_params* prm, int device, int32_t nscenes, const int64_t* counts,
+                     mps_handle** out);
+/* Particles of one scene (counts[scene] of each array, the scene's own order). */
+int mps_batch_set_scene(mps_handle* h, int32_t scene, const int32_t* type, const double* x,
+                        const double* z, const double* u, const double* w, const double* p,
+                        const double* nd);
+int mps_batch_get_scene(mps_handle* h, int32_t scene, int32_t* type, double* x, double* z,
+                        double* u, double* w, double* p, double* nd);
+int mps_batch_forward(mps_handle* h, double dt, int32_t nsteps);
+int mps_batch_get_scene_stats(mps_handle* h, int32_t scene, mps_batch_scene_stats* st);
+int mps_batch_tuning_info(const mps_handle* h, mps_batch_tuning* t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,6 +123,31 @@ class MpsStats(C.Structure):
     ]
 
 
+class MpsBatchSceneStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32),
+        ("reliable_updates", C.c_int32),
+        ("fallback", C.c_int32),
+        ("converged", C.c_int32),
+        ("fallback_iterations", C.c_int32),
+        ("pad", C.c_int32),
+        ("true_relres", C.c_double),
+        ("initial_relres", C.c_double),
+    ]
+
+
+class MpsBatchTuning(C.Structure):
+    _fields_ = [
+        ("threads", C.c_int32),
+        ("blocks", C.c_int32),
+        ("order", C.c_int32),
+        ("candidates", C.c_int32),
+        ("candidate_ms", C.c_float * 16),
+        ("candidate_threads", C.c_int32 * 16),
+        ("candidate_order", C.c_int32 * 16),
+    ]
+
+
 STAGE_NAMES = (
     "search", "density", "ecs", "explicit", "density2", "ppe", "solve", "pressure",
     "gradient", "ds", "other", "total",

@@ -33,6 +33,7 @@ UNITS = {
     "cg.cu": [],
     "mg.cu": [],
     "learned.cu": [],
+    "batch.cu": [],
     "scan.cu": [],
     "noalloc.cu": [],
     "mps_abi.cu": [],

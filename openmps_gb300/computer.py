@@ -86,6 +86,12 @@ PROTOTYPES = {
     "mps_mlp_loss_grad": (C.c_int, [C.c_int32, _F, _F, C.c_int64, _F, _D]),
     "mps_mlp_train": (C.c_int, [C.c_int32, _F, _F, C.c_int64, C.c_int32, C.c_int32, C.c_float,
                                 C.c_uint64, _D]),
+    "mps_batch_create": (C.c_int, [C.POINTER(abi.MpsParams), C.c_int, C.c_int32, _I64, C.POINTER(_P)]),
+    "mps_batch_set_scene": (C.c_int, [_P, C.c_int32, _I32, _D, _D, _D, _D, _D, _D]),
+    "mps_batch_get_scene": (C.c_int, [_P, C.c_int32, _I32, _D, _D, _D, _D, _D, _D]),
+    "mps_batch_forward": (C.c_int, [_P, C.c_double, C.c_int32]),
+    "mps_batch_get_scene_stats": (C.c_int, [_P, C.c_int32, C.POINTER(abi.MpsBatchSceneStats)]),
+    "mps_batch_tuning_info": (C.c_int, [_P, C.POINTER(abi.MpsBatchTuning)]),
 }
 
 
@@ -333,6 +339,56 @@ class Computer:
                                               _ptr(va), _ptr(bb), _ptr(x), eps, criterion, max_iters,
                                               solver, C.byref(it), C.byref(rel)))
         return x, it.value, rel.value
+
+
+class Batch(Computer):
+    """Independent scenes sharing one parameter set, advanced together (mps_batch_*).
+
+    Each scene behaves like its own ``Computer``; ``forward(dt, nsteps)`` advances all of
+    them with a fixed dt (the first step autotunes the batched PPE solve, later steps
+    replay one captured CUDA graph per step).
+    """
+
+    def __init__(self, params: abi.MpsParams, scenes, device: int = 0):
+        self.lib = load_library()
+        self.h = None
+        counts = np.array([s.count for s in scenes], dtype=np.int64)
+        h = C.c_void_p()
+        rc = self.lib.mps_batch_create(C.byref(params), device, len(scenes), _ptr(counts, C.c_int64),
+                                       C.byref(h))
+        if rc != abi.MPS_OK:
+            raise ComputerError(rc, "mps_batch_create")
+        self.h = h
+        self.params = params
+        self.counts = counts
+        for k, s in enumerate(scenes):
+            self._check(self.lib.mps_batch_set_scene(self.h, k, _ptr(np.ascontiguousarray(s.type, np.int32), C.c_int32),
+                                                     *[_ptr(_f64(a)) for a in (s.x, s.z, s.u, s.w, s.p, s.n)]))
+
+    def forward(self, dt: float, nsteps: int = 1):
+        self._check(self.lib.mps_batch_forward(self.h, dt, nsteps))
+
+    def scene(self, k: int) -> dict:
+        n = int(self.counts[k])
+        out = {"type": np.zeros(n, dtype=np.int32)}
+        for key in ("x", "z", "u", "w", "p", "n"):
+            out[key] = np.zeros(n)
+        self._check(self.lib.mps_batch_get_scene(self.h, k, _ptr(out["type"], C.c_int32),
+                                                 *[_ptr(out[key]) for key in ("x", "z", "u", "w", "p", "n")]))
+        return out
+
+    def scene_stats(self, k: int) -> dict:
+        st = abi.MpsBatchSceneStats()
+        self._check(self.lib.mps_batch_get_scene_stats(self.h, k, C.byref(st)))
+        return {name: getattr(st, name) for name, _ in abi.MpsBatchSceneStats._fields_ if name != "pad"}
+
+    def tuning(self) -> dict:
+        t = abi.MpsBatchTuning()
+        self._check(self.lib.mps_batch_tuning_info(self.h, C.byref(t)))
+        n = t.candidates
+        return {"threads": t.threads, "blocks": t.blocks, "order": t.order,
+                "candidates": [{"threads": t.candidate_threads[k], "order": t.candidate_order[k],
+                                "ms": t.candidate_ms[k]} for k in range(n)]}
 
 
 def _f32(a):

@@ -42,6 +42,8 @@ struct SceneConst {
     int32_t ppe_stride;  // PPE row capacity (nb_stride + 1)
     int32_t guard;       // 1 inside a full step: stages skip themselves after a failure
     int32_t nchunks;     // PPE chunks of kSellRows rows
+    int32_t cells_per_scene;  // gnx * gnz: cells of one scene
+    int32_t nscenes;          // scenes of a batch (1 for a single scene)
     int32_t pad1;
     double l0, re, re2, re_lap, rl2;
     double nl, nl2_lo, nl2_hi;  // neighbour length and a guard band around nl^2
@@ -81,6 +83,8 @@ struct DeviceState {
     double *n_wo_spp, *ecs, *ox, *oz, *dux, *duz;
     int32_t *cell_count, *cell_slot;
     int32_t* cell_xz;  // (cx << 16) | cz of each particle's cell at the last search, -1: none
+    const int32_t* scene_of;  // batch: scene of each particle (its cells start at
+                              // scene * cells_per_scene); null for a single scene
     int32_t *nb_count, *nb;
     int32_t *ppe_len, *ppe_col_tmp;
     double *ppe_val_tmp, *ppe_b, *ppe_x;
@@ -147,6 +151,7 @@ inline int grid_for(int64_t n, int block = kBlock) {
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_status_counters_reset(DevStatus* st, cudaStream_t s);
 // stages.cu
 void launch_set_dt(const SceneConst& sc, const DeviceState& st, double dt, cudaStream_t s);
 void launch_cfl_dt(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

@@ -34,7 +34,8 @@ __global__ void k_bucket(SceneConst sc, DeviceState st) {
         atomicAdd(&st.status->disabled, 1);
         return;
     }
-    const int cell = static_cast<int>(fx) * sc.gnz + static_cast<int>(fz);
+    const int base = st.scene_of ? st.scene_of[i] * sc.cells_per_scene : 0;
+    const int cell = base + static_cast<int>(fx) * sc.gnz + static_cast<int>(fz);
     st.cell_xz[i] = (static_cast<int>(fx) << 16) | static_cast<int>(fz);
     const int slot = atomicAdd(&st.cell_count[cell], 1);
     if (slot < sc.max_per_cell) {
@@ -47,7 +48,7 @@ __global__ void k_bucket(SceneConst sc, DeviceState st) {
 // Restores the serial insertion order of each cell (ascending particle index).
 __global__ void k_cell_sort(SceneConst sc, DeviceState st) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= sc.gnx * sc.gnz) return;
+    if (c >= sc.cells_per_scene * sc.nscenes) return;
     const int cnt = min(st.cell_count[c], sc.max_per_cell);
     if (cnt < 2) return;
     int32_t* s = st.cell_slot + static_cast<int64_t>(c) * sc.max_per_cell;
@@ -84,6 +85,7 @@ __device__ __forceinline__ int neighbor_row(const SceneConst& sc, const DeviceSt
     const double xi = st.x[i], zi = st.z[i];
     const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
     const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
+    const int base = st.scene_of ? st.scene_of[i] * sc.cells_per_scene : 0;
     int cnt = 0;
     for (int di = -1; di <= 1; di++) {
         const int cx = bx + di;
@@ -91,7 +93,7 @@ __device__ __forceinline__ int neighbor_row(const SceneConst& sc, const DeviceSt
         for (int dk = -1; dk <= 1; dk++) {
             const int cz = bz + dk;
             if (cz < 0 || cz >= sc.gnz) continue;
-            const int cell = cx * sc.gnz + cz;
+            const int cell = base + cx * sc.gnz + cz;
             const int m = min(st.cell_count[cell], sc.max_per_cell);
             const int32_t* slots = st.cell_slot + static_cast<int64_t>(cell) * sc.max_per_cell;
             for (int l = 0; l < m; l++) {
@@ -131,12 +133,23 @@ __global__ void k_neighbors(SceneConst sc, DeviceState st) {
     warp_add_u64(&st.status->nb_total, static_cast<unsigned long long>(cnt));
 }
 
+// Zeroes the per-step counters of the status block and keeps its failure flags.
+__global__ void k_status_counters_reset(DevStatus* st) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->disabled = 0;
+        st->nb_total = 0;
+        st->ppe_nnz = 0;
+    }
+}
+
+void launch_status_counters_reset(DevStatus* st, cudaStream_t s) { k_status_counters_reset<<<1, 32, 0, s>>>(st); }
+
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     k_bucket<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_cell_sort<<<grid_for(static_cast<int64_t>(sc.gnx) * sc.gnz), kBlock, 0, s>>>(sc, st);
+    k_cell_sort<<<grid_for(static_cast<int64_t>(sc.cells_per_scene) * sc.nscenes), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {

@@ -72,6 +72,60 @@ int mg_apply_launches(const MgHierarchy& mg);
 // Shared-memory bytes the single-block kernels need (opt-in set once per device).
 cudaError_t mg_prepare_device();
 
+// ------------------------------------------------------ 9-point cell stencils
+// The 9-point gathers are branchless: a neighbour outside the grid is clamped to a valid
+// cell, and its coefficient is zero (no particle can sit outside the grid), so all the
+// loads of a cell issue at once.
+__device__ __forceinline__ int clampi(int v, int hi) { return min(max(v, 0), hi); }
+
+// Residual of level f after the pre-smoothing x = dinv * r, summed over the children of
+// coarse cell (X, Z) (the restriction of the piecewise-constant aggregation).
+__device__ __forceinline__ float child_residuals(int nx, int nz, int cells, const float* k,
+                                                 const float* dinv, const float* r, int X, int Z) {
+    float sum = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            const int cx = 2 * X + a, cz = 2 * Z + b;
+            const bool valid = cx < nx && cz < nz;
+            const int ccx = min(cx, nx - 1), ccz = min(cz, nz - 1);
+            const int ch = ccx * nz + ccz;
+            float res = r[ch];
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int nb = clampi(ccx + dx, nx - 1) * nz + clampi(ccz + dz, nz - 1);
+                    res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * (dinv[nb] * r[nb]);
+                }
+            }
+            sum += valid ? res : 0.0f;
+        }
+    }
+    return sum;
+}
+
+// Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
+__device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
+                                                     const float* dinv, const float* r, int cnz,
+                                                     const float* ce, int ch) {
+    const int cx = ch / nz, cz = ch - (ch / nz) * nz;
+    const float xc = dinv[ch] * r[ch] + ce[(cx >> 1) * cnz + (cz >> 1)];
+    float res = r[ch];
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+        for (int dz = -1; dz <= 1; dz++) {
+            const int nx_ = clampi(cx + dx, nx - 1), nz_ = clampi(cz + dz, nz - 1);
+            const int nb = nx_ * nz + nz_;
+            const float xn = dinv[nb] * r[nb] + ce[(nx_ >> 1) * cnz + (nz_ >> 1)];
+            res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * xn;
+        }
+    }
+    return xc + dinv[ch] * res;
+}
+
 // Gate of a preconditioned-solve kernel: mode 0 after init, 1 an iteration, 2 after a
 // reliable update.
 __device__ __forceinline__ bool pcg_skip(const CgScalars* S, int mode) {

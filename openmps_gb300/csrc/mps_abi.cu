@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.cuh"
 #include "learned.cuh"
 #include "common.cuh"
 
@@ -65,6 +66,19 @@ struct mps_handle {
     bool lrn_loaded = false;
     bool lrn_collect = false;
     bool ppe_fp32 = false;       // the last assembly also wrote the FP32 matrix
+    // batch of scenes (nscenes > 0): layout, solve state, tuning, captured step
+    int32_t nscenes = 0;
+    std::vector<int64_t> scene_counts;
+    std::vector<BatchScene> scenes;
+    BatchScene* d_scenes = nullptr;
+    int32_t *d_order = nullptr, *d_queue = nullptr, *d_all_ok = nullptr, *d_scene_of = nullptr;
+    BatchSolveStats* d_bstats = nullptr;
+    int batch_threads = 0, batch_blocks = 0, batch_order = 0;  // tuned launch
+    std::vector<float> tune_ms;
+    std::vector<int32_t> tune_threads, tune_order;
+    cudaGraphExec_t batch_graph = nullptr;
+    double batch_graph_dt = 0.0;
+    int64_t batch_step_launches = 0;
     int sm_count = 1;
     CgGraph cg;
     int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
@@ -203,6 +217,8 @@ void setup_constants(mps_handle* h) {
         throw StatusError{MPS_ERR_INVALID_ARGUMENT, "domain has too many cells"};
     sc.gnx = static_cast<int32_t>(cx) + 2;
     sc.gnz = static_cast<int32_t>(cz) + 2;
+    sc.cells_per_scene = sc.gnx * sc.gnz;
+    sc.nscenes = 1;
     const int c = static_cast<int>(std::ceil(sc.nl / p.l0));
     sc.max_per_cell = (c + 1) * (c + 1);
     sc.nb_stride = sc.max_per_cell * 9;
@@ -247,7 +263,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     std::vector<void*> old_allocs;
     old_allocs.swap(h->allocations);
     DeviceState& st = h->st;
-    const int64_t cells = static_cast<int64_t>(sc.gnx) * sc.gnz;
+    const int64_t cells = static_cast<int64_t>(sc.cells_per_scene) * sc.nscenes;
     st.type = dalloc<int32_t>(h, n);
     double** dbl[] = {&st.x, &st.z, &st.u, &st.w, &st.p, &st.nd, &st.wall_x, &st.wall_z,
                       &st.n_wo_spp, &st.ecs, &st.ox, &st.oz, &st.dux, &st.duz};
@@ -508,9 +524,12 @@ void stage_mark(mps_handle* h, int k) {
 // ---- individual stages (stream-ordered, no sync)
 void do_search(mps_handle* h) {
     cudaStream_t s = h->stream;
-    const int64_t cells = static_cast<int64_t>(h->sc.gnx) * h->sc.gnz;
+    const int64_t cells = static_cast<int64_t>(h->sc.cells_per_scene) * h->sc.nscenes;
     check(cudaMemsetAsync(h->st.cell_count, 0, sizeof(int32_t) * cells, s), "memset");
-    check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
+    if (h->nscenes > 0)
+        launch_status_counters_reset(h->st.status, s);  // batch: failures stay flagged across steps
+    else
+        check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
     launch_bucket(h->sc, h->st, s);
     launch_cell_sort(h->sc, h->st, s);
     launch_neighbors(h->sc, h->st, s);
@@ -627,6 +646,7 @@ void do_solve(mps_handle* h) {
 
 void forward(mps_handle* h, double dt) {
     require_particles(h);
+    if (h->nscenes > 0) throw StatusError{MPS_ERR_STATE, "batch handle: use mps_batch_forward"};
     cudaStream_t s = h->stream;
     const uint32_t flags = h->prm.flags;
     SceneConst sc = h->sc;
@@ -743,6 +763,138 @@ int on_device(int32_t device, F f) {
     return rc;
 }
 
+// --------------------------------------------------------------- batches
+BatchOps batch_ops(mps_handle* h) {
+    BatchOps B{};
+    B.o = cg_operands(h);
+    B.scenes = h->d_scenes;
+    B.order = h->d_order;
+    B.queue = h->d_queue;
+    B.nscenes = h->nscenes;
+    B.cells_per_scene = h->sc.cells_per_scene;
+    B.cell_count = h->st.cell_count;
+    B.cell_slot = h->st.cell_slot;
+    B.max_per_cell = h->sc.max_per_cell;
+    B.levels = h->mg.levels;
+    for (int l = 1; l <= h->mg.levels; l++) B.lv[l] = h->mg.lv[l];
+    B.cell_xz = h->st.cell_xz;
+    B.bins = h->mg.bins;
+    B.dinv0 = h->mg.dinv0;
+    B.r64 = h->r;
+    B.p64 = h->p;
+    B.Ap64 = h->Ap;
+    B.stats = h->d_bstats;
+    B.all_ok = h->d_all_ok;
+    B.status = h->st.status;
+    B.eps = h->prm.eps;
+    B.delta2 = 0.01;
+    B.criterion = h->prm.criterion;
+    B.max_iter = h->prm.max_cg_iters > 0 ? h->prm.max_cg_iters : kPcgMaxIter;
+    return B;
+}
+
+// The stages of a batch step before the solve (fixed dt), stream-ordered and capturable.
+void batch_stages_pre(mps_handle* h, double dt) {
+    cudaStream_t s = h->stream;
+    SceneConst sc = h->sc;
+    sc.guard = 1;
+    launch_set_dt(sc, h->st, dt, s);
+    do_search(h);
+    launch_density(sc, h->st, s);
+    if (h->prm.flags & MPS_FLAG_ECS) launch_error_correction(sc, h->st, s);
+    launch_explicit(sc, h->st, s);
+    launch_density(sc, h->st, s);
+    if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
+    launch_set_ppe(sc, h->st, true, s);
+    h->ppe_fp32 = true;
+    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
+    after_launch("batch stages");
+    launched(h, kLaunchesDt + kLaunchesSearch + 2 * kLaunchesDensity + kLaunchesExplicit + kLaunchesSetPpe +
+                    ((h->prm.flags & MPS_FLAG_ECS) ? kLaunchesEcs : 0) +
+                    ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
+}
+
+void batch_stages_post(mps_handle* h) {
+    cudaStream_t s = h->stream;
+    SceneConst sc = h->sc;
+    sc.guard = 1;
+    launch_assign_pressure(sc, h->st, s);
+    launch_pressure_gradient(sc, h->st, s);
+    if (h->prm.flags & MPS_FLAG_DS) launch_dynamic_stabilize(sc, h->st, s);
+    after_launch("batch stages");
+    launched(h, kLaunchesAssign + kLaunchesGradient + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesDs : 0));
+}
+
+void batch_solve(mps_handle* h) {
+    check(launch_batch_solve(batch_ops(h), h->batch_blocks, h->batch_threads, h->stream), "batch solve");
+    launched(h, 1);
+}
+
+std::vector<int32_t> batch_order(const mps_handle* h, int kind) {
+    std::vector<int32_t> ord(h->nscenes);
+    for (int32_t k = 0; k < h->nscenes; k++) ord[k] = k;
+    if (kind == 1)  // largest scene first: the longest solves start first
+        std::stable_sort(ord.begin(), ord.end(),
+                         [h](int32_t a, int32_t b) { return h->scene_counts[a] > h->scene_counts[b]; });
+    return ord;
+}
+
+// Autotuner: times the batched solve of the assembled step for every launch shape
+// (threads per block) and scene order, each from the same initial guess, and keeps the
+// fastest.  Blocks = resident blocks per SM x SMs (at most one per scene).
+void batch_autotune(mps_handle* h) {
+    cudaStream_t s = h->stream;
+    const BatchOps B = batch_ops(h);
+    const size_t smem = batch_smem_bytes(B, 0);
+    check(cudaMemcpyAsync(h->x2, h->st.ppe_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, s), "copy");
+    h->tune_ms.clear();
+    h->tune_threads.clear();
+    h->tune_order.clear();
+    float best = 1e30f;
+    for (int kind = 0; kind < 2; kind++) {
+        const std::vector<int32_t> ord = batch_order(h, kind);
+        check(cudaMemcpyAsync(h->d_order, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, s),
+              "copy");
+        for (int threads : {128, 256, 512, 1024}) {
+            const int bpsm = batch_blocks_per_sm(threads, smem);
+            if (bpsm <= 0) continue;
+            const int blocks = std::min(h->nscenes, bpsm * h->sm_count);
+            check(cudaMemcpyAsync(h->st.ppe_x, h->x2, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, s), "copy");
+            check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
+            check(cudaEventRecord(h->user_events[12], s), "event");
+            check(launch_batch_solve(B, blocks, threads, s), "batch solve");
+            check(cudaEventRecord(h->user_events[13], s), "event");
+            check(cudaEventSynchronize(h->user_events[13]), "event");
+            float ms = 0.f;
+            check(cudaEventElapsedTime(&ms, h->user_events[12], h->user_events[13]), "elapsed");
+            launched(h, 1);
+            h->tune_ms.push_back(ms);
+            h->tune_threads.push_back(threads);
+            h->tune_order.push_back(kind);
+            if (ms < best) {
+                best = ms;
+                h->batch_threads = threads;
+                h->batch_blocks = blocks;
+                h->batch_order = kind;
+            }
+        }
+    }
+    if (h->batch_threads == 0) throw StatusError{MPS_ERR_NOT_SUPPORTED, "batched solve cannot launch"};
+    const std::vector<int32_t> ord = batch_order(h, h->batch_order);
+    check(cudaMemcpyAsync(h->d_order, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice, s), "copy");
+    check(cudaMemcpyAsync(h->st.ppe_x, h->x2, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, s), "copy");
+    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
+}
+
+void batch_read_status(mps_handle* h) {
+    read_status(h, false);
+    int32_t ok = 0;
+    check(cudaMemcpy(&ok, h->d_all_ok, sizeof(int32_t), cudaMemcpyDeviceToHost), "status");
+    if (ok == 0)
+        throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
+                          "Conjugate Gradient method couldn't solve Pressure Poison Equation (a scene of the batch)"};
+}
+
 void check_blob(const float* blob) {
     for (int k = 0; k < kMlpBlobFloats; k++)
         if (!std::isfinite(blob[k])) throw StatusError{MPS_ERR_NONFINITE, "non-finite network weight"};
@@ -851,6 +1003,7 @@ int mps_destroy(mps_handle* h) {
         if (h->l2_limit_changed) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_limit_before);
         cudaGetLastError();
     }
+    if (h->batch_graph) cudaGraphExecDestroy(h->batch_graph);
     dfree_all(h);
     if (h->lrn_packed) cudaFree(h->lrn_packed);
     if (h->flush_buf) cudaFree(h->flush_buf);
@@ -1484,6 +1637,210 @@ int mps_mlp_train(int32_t device, float* blob, const float* samples, int64_t n, 
         }
         check(cudaMemcpy(blob, T.w, sizeof(float) * kMlpBlobFloats, cudaMemcpyDeviceToHost), "copy");
     });
+}
+
+// ------------------------------------------------------------- batched scenes
+int mps_batch_create(const mps_params* prm, int device, int32_t nscenes, const int64_t* counts,
+                     mps_handle** out) {
+    if (!prm || !out || nscenes <= 0 || !counts) return MPS_ERR_INVALID_ARGUMENT;
+    for (int32_t k = 0; k < nscenes; k++)
+        if (counts[k] <= 0) return MPS_ERR_INVALID_ARGUMENT;
+    mps_handle* h = nullptr;
+    int rc = mps_create(prm, device, &h);
+    if (rc != MPS_OK) return rc;
+    rc = guarded(h, [&] {
+        if (h->mg.levels == 0 && mg_plan(h->sc.gnx, h->sc.gnz, h->mg.lv, &h->mg.bottom) == 0)
+            throw StatusError{MPS_ERR_NOT_SUPPORTED, "scene grid too large for a batch"};
+        h->nscenes = nscenes;
+        h->sc.nscenes = nscenes;
+        h->scene_counts.assign(counts, counts + nscenes);
+        h->scenes.resize(nscenes);
+        int64_t total = 0;
+        for (int32_t k = 0; k < nscenes; k++) {
+            const int64_t padded = (counts[k] + kSellRows - 1) / kSellRows * kSellRows;
+            h->scenes[k] = BatchScene{static_cast<int32_t>(total), static_cast<int32_t>(padded)};
+            total += padded;
+        }
+        if (total > (int64_t{1} << 31) / std::max(1, h->sc.ppe_stride) ||
+            sell_chunks(total) * sell_chunk_size(h->sc.ppe_stride) >= (int64_t{1} << 31) ||
+            static_cast<int64_t>(h->sc.cells_per_scene) * nscenes * h->sc.max_per_cell >= (int64_t{1} << 31))
+            throw StatusError{MPS_ERR_INVALID_ARGUMENT, "batch too large for 32-bit offsets"};
+        allocate(h, total, 0);
+        h->n = total;
+        h->sc.n = static_cast<int32_t>(total);
+        h->sc.nchunks = static_cast<int32_t>(sell_chunks(total));
+        const BatchOps B0 = batch_ops(h);
+        const size_t smem = batch_smem_bytes(B0, 0);
+        if (smem == 0) throw StatusError{MPS_ERR_NOT_SUPPORTED, "scene hierarchy exceeds one block's shared memory"};
+        check(batch_prepare_device(smem), "batch kernel attributes");
+        h->d_scenes = dalloc<BatchScene>(h, nscenes);
+        h->d_order = dalloc<int32_t>(h, nscenes);
+        h->d_queue = dalloc<int32_t>(h, 1);
+        h->d_all_ok = dalloc<int32_t>(h, 1);
+        h->d_bstats = dalloc<BatchSolveStats>(h, nscenes);
+        int32_t* scene_of = dalloc<int32_t>(h, total);
+        std::vector<int32_t> host_scene(total), host_type(total, MPS_TYPE_DISABLED);
+        for (int32_t k = 0; k < nscenes; k++)
+            for (int32_t r = 0; r < h->scenes[k].rows; r++) host_scene[h->scenes[k].row0 + r] = k;
+        cudaStream_t s = h->stream;
+        check(cudaMemcpyAsync(scene_of, host_scene.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, s), "copy");
+        check(cudaMemcpyAsync(h->st.type, host_type.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, s), "copy");
+        check(cudaMemcpyAsync(h->d_scenes, h->scenes.data(), sizeof(BatchScene) * nscenes, cudaMemcpyHostToDevice, s),
+              "copy");
+        const std::vector<int32_t> ord = batch_order(h, 0);
+        check(cudaMemcpyAsync(h->d_order, ord.data(), sizeof(int32_t) * nscenes, cudaMemcpyHostToDevice, s), "copy");
+        check(cudaMemsetAsync(h->d_bstats, 0, sizeof(BatchSolveStats) * nscenes, s), "memset");
+        check(cudaStreamSynchronize(s), "batch create");
+        h->st.scene_of = scene_of;
+        h->st.solve_ok = h->d_all_ok;
+    });
+    if (rc != MPS_OK) {
+        mps_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return MPS_OK;
+}
+
+namespace {
+void batch_rows(const mps_handle* h, int32_t scene, int64_t* row0, int64_t* n) {
+    if (h->nscenes <= 0) throw StatusError{MPS_ERR_STATE, "not a batch handle"};
+    if (scene < 0 || scene >= h->nscenes) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "scene index out of range"};
+    *row0 = h->scenes[scene].row0;
+    *n = h->scene_counts[scene];
+}
+}  // namespace
+
+int mps_batch_set_scene(mps_handle* h, int32_t scene, const int32_t* type, const double* x, const double* z,
+                        const double* u, const double* w, const double* p, const double* nd) {
+    if (!h || !type || !x || !z) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        int64_t r0, n;
+        batch_rows(h, scene, &r0, &n);
+        for (int64_t i = 0; i < n; i++)
+            if (type[i] < MPS_TYPE_FLUID || type[i] > MPS_TYPE_DISABLED)
+                throw StatusError{MPS_ERR_INVALID_ARGUMENT, "particle type out of range"};
+        DeviceState& st = h->st;
+        const size_t b8 = sizeof(double) * n;
+        upload(h, st.type + r0, type, sizeof(int32_t) * n, false);
+        upload(h, st.x + r0, x, b8, false);
+        upload(h, st.z + r0, z, b8, false);
+        upload(h, st.wall_x + r0, x, b8, false);
+        upload(h, st.wall_z + r0, z, b8, false);
+        upload(h, st.u + r0, u, b8, false);
+        upload(h, st.w + r0, w, b8, false);
+        upload(h, st.p + r0, p, b8, false);
+        upload(h, st.nd + r0, nd, b8, false);
+        check(cudaStreamSynchronize(h->stream), "batch scene");
+    });
+}
+
+int mps_batch_get_scene(mps_handle* h, int32_t scene, int32_t* type, double* x, double* z, double* u, double* w,
+                        double* p, double* nd) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        int64_t r0, n;
+        batch_rows(h, scene, &r0, &n);
+        cudaStream_t s = h->stream;
+        const DeviceState& st = h->st;
+        const size_t b8 = sizeof(double) * n;
+        auto get = [&](void* dst, const void* src, size_t bytes) {
+            if (dst) check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), "copy");
+        };
+        get(type, st.type + r0, sizeof(int32_t) * n);
+        get(x, st.x + r0, b8);
+        get(z, st.z + r0, b8);
+        get(u, st.u + r0, b8);
+        get(w, st.w + r0, b8);
+        get(p, st.p + r0, b8);
+        get(nd, st.nd + r0, b8);
+        check(cudaStreamSynchronize(s), "batch scene");
+    });
+}
+
+int mps_batch_forward(mps_handle* h, double dt, int32_t nsteps) {
+    if (!h || nsteps < 0) return MPS_ERR_INVALID_ARGUMENT;
+    if (!(dt > 0)) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (h->nscenes <= 0) throw StatusError{MPS_ERR_STATE, "not a batch handle"};
+        if (nsteps == 0) return;
+        cudaStream_t s = h->stream;
+        check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
+        int32_t left = nsteps;
+        if (h->batch_threads == 0) {
+            // first step: eager, with the autotuner between assembly and solve
+            batch_stages_pre(h, dt);
+            batch_autotune(h);
+            batch_solve(h);
+            batch_stages_post(h);
+            batch_read_status(h);
+            h->stats.steps += 1;
+            left--;
+        }
+        if (left == 0) return;
+        if (!h->batch_graph || h->batch_graph_dt != dt) {
+            // one step captured as a graph (stages + the persistent solve), replayed
+            if (h->batch_graph) cudaGraphExecDestroy(h->batch_graph);
+            h->batch_graph = nullptr;
+            const int64_t before = h->stats.kernel_launches;
+            cudaGraph_t g = nullptr;
+            check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+            try {
+                batch_stages_pre(h, dt);
+                batch_solve(h);
+                batch_stages_post(h);
+            } catch (...) {
+                cudaStreamEndCapture(s, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            check(cudaStreamEndCapture(s, &g), "capture");
+            const cudaError_t e = cudaGraphInstantiate(&h->batch_graph, g, 0);
+            cudaGraphDestroy(g);
+            check(e, "graph instantiate");
+            h->batch_graph_dt = dt;
+            h->batch_step_launches = h->stats.kernel_launches - before;
+            h->stats.kernel_launches = before;
+        }
+        for (int32_t k = 0; k < left; k++) check(cudaGraphLaunch(h->batch_graph, s), "graph launch");
+        h->stats.kernel_launches += h->batch_step_launches * left;
+        batch_read_status(h);
+        h->stats.steps += left;
+    });
+}
+
+int mps_batch_get_scene_stats(mps_handle* h, int32_t scene, mps_batch_scene_stats* out) {
+    if (!h || !out) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        int64_t r0, n;
+        batch_rows(h, scene, &r0, &n);
+        BatchSolveStats b;
+        check(cudaMemcpy(&b, h->d_bstats + scene, sizeof(b), cudaMemcpyDeviceToHost), "copy");
+        std::memset(out, 0, sizeof(*out));
+        out->iterations = b.iterations;
+        out->reliable_updates = b.updates;
+        out->fallback = b.fallback;
+        out->converged = b.converged;
+        out->fallback_iterations = b.fb_iterations;
+        out->true_relres = b.bb > 0 ? std::sqrt(b.true_rr / b.bb) : std::sqrt(b.true_rr);
+        out->initial_relres = b.bb > 0 ? std::sqrt(b.rr0 / b.bb) : std::sqrt(b.rr0);
+    });
+}
+
+int mps_batch_tuning_info(const mps_handle* h, mps_batch_tuning* out) {
+    if (!h || !out) return MPS_ERR_INVALID_ARGUMENT;
+    if (h->nscenes <= 0) return MPS_ERR_STATE;
+    std::memset(out, 0, sizeof(*out));
+    out->threads = h->batch_threads;
+    out->blocks = h->batch_blocks;
+    out->order = h->batch_order;
+    out->candidates = static_cast<int32_t>(std::min<size_t>(h->tune_ms.size(), 16));
+    for (int32_t k = 0; k < out->candidates; k++) {
+        out->candidate_ms[k] = h->tune_ms[k];
+        out->candidate_threads[k] = h->tune_threads[k];
+        out->candidate_order[k] = h->tune_order[k];
+    }
+    return MPS_OK;
 }
 
 }  // extern "C"
