@@ -57,6 +57,11 @@ def parse_args():
     ap.add_argument("--solver", choices=("cg64", "mixed", "mg", "learned"), default="learned")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the same-state comparison of the PPE solvers")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched 256-scene workload")
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched workload and print its JSON (for profilers)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -190,15 +195,19 @@ def load_peak() -> tuple[float, str]:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def load_traffic(key: str):
-    """DRAM bytes per launch of the SpMV kernel from the committed ncu summary."""
+def load_traffic(key: str, alg_bytes: float):
+    """DRAM bytes per launch of the SpMV kernel from the committed ncu capture, scaled from
+    the captured launch to this launch by algorithmic bytes (the matrix grows a little as
+    the dam breaks); None without a capture for this solver."""
     path = os.path.join(ROOT, "profiles", "spmv_traffic.json")
     try:
         with open(path) as f:
-            data = json.load(f)
-        return data.get(key)
+            rec = json.load(f).get(key)
     except (OSError, ValueError):
         return None
+    if not rec:
+        return None
+    return rec["dram_bytes"] * alg_bytes / rec["algorithmic_bytes"]
 
 
 # ------------------------------------------------------------------ our arm
@@ -310,6 +319,11 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_compare and rank == 0:
         compare = compare_solvers(comp, scene, dt, local_rank)
 
+    # ---- the batched workload: 256 uneven dam breaks in one handle
+    batched = None
+    if not args.no_batch and rank == 0:
+        batched = batched_workload(local_rank, args.batch_scenes, steps=max(2, min(args.steps, 10)))
+
     # ---- roofline of the dominant kernel (the solver's SpMV), timed alone
     st = comp.stats()
     nnz = st["ppe_nnz"]
@@ -328,7 +342,7 @@ def run_ours(args, rank, world, local_rank):
     spmv64_ms = comp.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
     peak, peak_kind = load_peak()
     achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
-    traffic = load_traffic(key)
+    traffic = load_traffic(key, alg_bytes)
 
     # ---- reduce over ranks (max time)
     t_steps, t_e2e = total_ms, e2e_ms
@@ -380,6 +394,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if compare is not None:
         line["ppe_solvers_same_state"] = compare
+    if batched is not None:
+        line["batched"] = batched
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, scene.params(criterion=abi.CRIT_RHS, eps=1e-8), dt,
                                             args.cpu_seconds)
@@ -430,6 +446,54 @@ def compare_solvers(comp, scene, dt, device, steps=3):
     return out
 
 
+def batched_workload(device, nscenes, steps):
+    """Particle-steps/s of `nscenes` independent dam breaks (width U[0.1, 0.3] m, height
+    U[0.2, 0.5] m, l0 = 5 mm, seeded) advanced together: the first step autotunes the
+    batched solve, the timed steps replay the captured per-step graph."""
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import scenes as sc_mod
+    from openmps_gb300.computer import Batch
+
+    l0 = 5e-3
+    dt = l0 / 20.0
+    scs = []
+    for k in range(nscenes):
+        s = sc_mod.batch_scene(k, seed=20261203, l0=l0)
+        s.meta["params"] = dict(sc_mod.STOCK_PHYSICS, eps=1e-8, max_dt=dt)
+        scs.append(s)
+    prm = scs[0].params(solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS, eps=1e-8)
+    b = Batch(prm, scs, device=device)
+    b.forward(dt, 1)  # autotune + first step
+    b.forward(dt, 2)  # capture + warm-up
+    b.synchronize()
+    b.flush_l2(FLUSH_BYTES)
+    b.event_record(0)
+    b.forward(dt, steps)
+    b.event_record(1)
+    ms = b.event_elapsed(0, 1)
+    particles = int(sum(s.count for s in scs))
+    fluid = int(sum(int((s.type == abi.TYPE_FLUID).sum()) for s in scs))
+    its = [b.scene_stats(k) for k in range(nscenes)]
+    out = {
+        "workload": "%d independent 2D dam breaks, l0=5e-3 m, columns U[0.1,0.3] x U[0.2,0.5] m in "
+                    "0.8 x 0.6 m tanks, reference MPS scheme, dt=%.2e s" % (nscenes, dt),
+        "scenes": nscenes, "particles": particles, "fluid_particles": fluid,
+        "fluid_per_scene_min": int(min((s.type == abi.TYPE_FLUID).sum() for s in scs)),
+        "fluid_per_scene_max": int(max((s.type == abi.TYPE_FLUID).sum() for s in scs)),
+        "steps": steps, "ms_per_step": ms / steps,
+        "value": particles * steps / (ms * 1e-3), "unit": UNIT,
+        "ppe_iterations_mean": statistics.mean(t["iterations"] for t in its),
+        "ppe_iterations_max": max(t["iterations"] for t in its),
+        "fallbacks": int(sum(t["fallback"] for t in its)),
+        "max_true_relres": max(t["true_relres"] for t in its),
+        "tuning": b.tuning(),
+        "launch": "per step one replay of a captured CUDA graph: stage kernels over all scenes + "
+                  "one persistent block-per-scene PPE solve",
+    }
+    b.close()
+    return out
+
+
 # ------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
     """The CPU restatement of the reference step (OpenMP, all host threads)."""
@@ -464,6 +528,12 @@ def run_reference(args, rank, world):
 def main():
     args = parse_args()
     rank, world, local_rank = dist_env()
+    if args.batch_only:
+        from openmps_gb300 import build as gpu_build
+
+        gpu_build.build()
+        print(json.dumps(batched_workload(local_rank, args.batch_scenes, steps=max(2, args.steps))), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:
