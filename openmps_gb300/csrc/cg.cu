@@ -45,43 +45,103 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Sum over the block, valid in thread 0.  FP64 issue is scarce on GB300 (a warp-wide
-// DADD occupies the FP64 pipe ~22 cycles), so the lanes park their values in shared
-// memory and a single warp adds them: 8 serial adds plus a 5-level shuffle tree per
-// block instead of a 5-level tree in every warp.  `ws` holds kBlock doubles.
-__device__ double block_sum(double v, double* ws) {
-    ws[threadIdx.x] = v;
+// Grid-wide sums of up to three values without block barriers: every lane parks its
+// values in shared memory; the last warp of the block to arrive (shared-memory ticket)
+// adds the block's values in a fixed order and publishes one partial per block; groups
+// of blocks and then the groups are summed the same way (global tickets).  Warps that
+// finish their rows early leave at once instead of waiting at __syncthreads for the
+// block's longest row.  The order of every addition is fixed, so the sums are the same
+// run to run.
+struct BlockTicket {
+    unsigned count;
+    double lanes[3][kBlock];
+};
+
+// Must run in every thread of the block before the first grid_sum (uniform code path).
+__device__ __forceinline__ void ticket_init(BlockTicket& t) {
+    if (threadIdx.x == 0) t.count = 0;
     __syncthreads();
-    double s = 0.0;
-    if (threadIdx.x < 32) {
-        for (int k = threadIdx.x; k < static_cast<int>(blockDim.x); k += 32) s += ws[k];
-        s = warp_sum(s);
-    }
-    __syncthreads();
-    return s;
 }
 
-// Writes this block's partials; true in the last block to finish.
-__device__ bool publish(double s0, double s1, double* partials, uint32_t* counter,
-                        double s2 = 0.0) {
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
+// True in exactly one thread of the grid, which then holds the totals in out[0..2].
+// Blocks publish partials in groups of 32: the last block of a group adds its group's
+// partials (one load per lane) and the last group adds the group sums, so the final sum
+// costs a few L2 round trips however many blocks the grid has.  `partials` holds
+// 3 * (blocks + groups) doubles, `tickets` one counter per group, `counter` the last one.
+__device__ bool grid_sum(double a, double b, double c, double* partials, uint32_t* tickets,
+                         uint32_t* counter, BlockTicket& T, double* out) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = static_cast<int>(blockDim.x >> 5);
+    // FP64 instructions are scarce on GB300: lanes park raw values in shared memory and
+    // only the block's last warp adds them (8 adds + one 5-level tree per value)
+    T.lanes[0][threadIdx.x] = a;
+    T.lanes[1][threadIdx.x] = b;
+    T.lanes[2][threadIdx.x] = c;
+    __threadfence_block();
+    unsigned last = 0;
+    if (lane == 0) last = atomicAdd(&T.count, 1u) == static_cast<unsigned>(nwarps - 1);
+    if (!__shfl_sync(kFull, last, 0)) return false;
+    __threadfence_block();
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < nwarps; w++) {
+        s0 += T.lanes[0][32 * w + lane];
+        s1 += T.lanes[1][32 * w + lane];
+        s2 += T.lanes[2][32 * w + lane];
+    }
+    s0 = warp_sum(s0);
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    const int G = static_cast<int>(gridDim.x);
+    const int NG = (G + 31) / 32;
+    const int group = static_cast<int>(blockIdx.x) / 32;
+    const int gsize = min(32, G - group * 32);
+    unsigned group_last = 0;
+    if (lane == 0) {
         partials[blockIdx.x] = s0;
-        partials[gridDim.x + blockIdx.x] = s1;
-        partials[2 * gridDim.x + blockIdx.x] = s2;
+        partials[G + blockIdx.x] = s1;
+        partials[2 * G + blockIdx.x] = s2;
         __threadfence();
-        const uint32_t t = atomicAdd(counter, 1u);
-        last = (t == gridDim.x - 1);
+        group_last = atomicAdd(tickets + group, 1u) == static_cast<unsigned>(gsize - 1);
     }
-    __syncthreads();
-    return last;
-}
-
-// In the last block: fixed-order sum of the partials (valid in thread 0).
-__device__ double gather_sum(const double* partials, int nparts, double* ws) {
-    double v = 0.0;
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) v += __ldcg(partials + k);
-    return block_sum(v, ws);
+    if (!__shfl_sync(kFull, group_last, 0)) return false;
+    __threadfence();
+    double x = 0.0, y = 0.0, z = 0.0;
+    if (lane < gsize) {
+        const int k = group * 32 + lane;
+        x = __ldcg(partials + k);
+        y = __ldcg(partials + G + k);
+        z = __ldcg(partials + 2 * G + k);
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    z = warp_sum(z);
+    double* gp = partials + 3 * G;
+    unsigned all_last = 0;
+    if (lane == 0) {
+        tickets[group] = 0;
+        gp[group] = x;
+        gp[NG + group] = y;
+        gp[2 * NG + group] = z;
+        __threadfence();
+        all_last = atomicAdd(counter, 1u) == static_cast<unsigned>(NG - 1);
+    }
+    if (!__shfl_sync(kFull, all_last, 0)) return false;
+    __threadfence();
+    x = y = z = 0.0;
+    for (int k = lane; k < NG; k += 32) {
+        x += __ldcg(gp + k);
+        y += __ldcg(gp + NG + k);
+        z += __ldcg(gp + 2 * NG + k);
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    z = warp_sum(z);
+    if (lane != 0) return false;
+    out[0] = x;
+    out[1] = y;
+    out[2] = z;
+    *counter = 0;
+    return true;
 }
 
 __device__ __forceinline__ bool cg_done(const CgScalars* S) {
@@ -90,26 +150,45 @@ __device__ __forceinline__ bool cg_done(const CgScalars* S) {
 
 // Row i (lane of a chunk at `at`) times v in FP64, ascending columns.  The FP64 matrix
 // streams with evict-first hints: on big scenes it exceeds L2 and the solver's vectors
-// should stay resident instead.
+// should stay resident instead.  Software-pipelined: the next eight entries are loaded
+// before this batch's gathers, so a lane keeps both kinds of loads in flight.
 template <class V>
 __device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, V v) {
     double acc = 0.0;
-    int k = 0;
-    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
-        int c[8];
-        double a[8];
+    const int nb = L >> 3;
+    int c[8];
+    double a[8];
+    if (nb > 0) {
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             c[u] = __ldcs(o.col + at + u * kSellRows);
             a[u] = __ldcs(o.val + at + u * kSellRows);
         }
+    }
+    for (int bt = 0; bt < nb; bt++) {
         double xv[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) xv[u] = v(c[u]);
+        int cn[8];
+        double an[8];
+        if (bt + 1 < nb) {
+            const int64_t nx = at + static_cast<int64_t>(bt + 1) * 8 * kSellRows;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                cn[u] = __ldcs(o.col + nx + u * kSellRows);
+                an[u] = __ldcs(o.val + nx + u * kSellRows);
+            }
+        }
 #pragma unroll
         for (int u = 0; u < 8; u++) acc = fma(a[u], xv[u], acc);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            c[u] = cn[u];
+            a[u] = an[u];
+        }
     }
-    for (; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
+    at += static_cast<int64_t>(nb) * 8 * kSellRows;
+    for (int k = nb * 8; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
     return acc;
 }
 
@@ -168,7 +247,7 @@ __device__ __forceinline__ bool aborted_before_solve(const CgOperands& o,
 // fallback after a preconditioned solve) nothing runs unless that solve failed.
 __global__ void __launch_bounds__(kBlock) k_cg_init(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond, const CgScalars* gate) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (gate && (gate->converged || gate->aborted)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             o.S->converged = gate->converged;
@@ -179,6 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(CgOperands o, cudaGraphCondi
         return;
     }
     if (aborted_before_solve(o, h, use_cond)) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const double* x = o.x;
     double vrr = 0.0, vbb = 0.0;
@@ -195,19 +275,15 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(CgOperands o, cudaGraphCondi
             vbb += bi * bi;
         }
     }
-    const double s0 = block_sum(vrr, ws);
-    const double s1 = block_sum(vbb, ws);
-    if (publish(s0, s1, o.partials, &o.S->counter)) {
-        const double rr = gather_sum(o.partials, gridDim.x, ws);
-        const double bb = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
-        if (threadIdx.x == 0) init_scalars(o.S, rr, bb, h, use_cond);
-    }
+    double tot[3];
+    if (grid_sum(vrr, vbb, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) init_scalars(o.S, tot[0], tot[1], h, use_cond);
 }
 
 // Ap = A p; alpha = rr / (p.Ap)
 __global__ void __launch_bounds__(kBlock) k_cg_spmv_dot(CgOperands o) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (cg_done(o.S)) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const double* p = o.p;
     double v = 0.0;
@@ -220,10 +296,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_dot(CgOperands o) {
             v += p[i] * s;
         }
     }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double pap = gather_sum(o.partials, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double pap = tot[0];
+        {
             o.S->counter = 0;
             o.S->pAp = pap;
             o.S->alpha = o.S->rr / pap;
@@ -234,8 +310,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv_dot(CgOperands o) {
 // x += alpha p; r -= alpha Ap; rrNew = r.r; convergence; beta (Computer.hpp:1402-1420)
 __global__ void __launch_bounds__(kBlock) k_cg_update(CgOperands o, cudaGraphConditionalHandle h,
                                                      int use_cond) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (cg_done(o.S)) return;
+    ticket_init(tk);
     const double alpha = o.S->alpha;
     double v = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x) {
@@ -244,10 +321,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(CgOperands o, cudaGraphCon
         o.r[i] = ri;
         v += ri * ri;
     }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double rr_new = gather_sum(o.partials, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double rr_new = tot[0];
+        {
             CgScalars* S = o.S;
             S->counter = 0;
             S->rr_new = rr_new;
@@ -273,8 +350,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_pupdate(CgOperands o) {
 
 // |b - A x|^2 in FP64 into S->true_rr (reported as the true relative residual)
 __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (o.S->aborted) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const double* x = o.x;
     double v = 0.0;
@@ -287,10 +365,10 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
             v += ri * ri;
         }
     }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double rr = gather_sum(o.partials, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double rr = tot[0];
+        {
             o.S->counter = 0;
             o.S->true_rr = rr;
         }
@@ -305,23 +383,35 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
 
 // Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
 // The {column, value} pairs keep default caching: the FP32 matrix is meant to stay in L2.
+// Software-pipelined like row64.
 __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
                                        const float* __restrict__ v) {
     float acc = 0.0f;
-    int k = 0;
-    for (; k + 8 <= L; k += 8, at += 8 * kSellRows) {
-        uint2 e[8];
+    const int nb = L >> 3;
+    uint2 e[8];
+    if (nb > 0) {
 #pragma unroll
         for (int u = 0; u < 8; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
+    }
+    for (int bt = 0; bt < nb; bt++) {
         float xv[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) xv[u] = v[e[u].x];
+        uint2 f[8];
+        if (bt + 1 < nb) {
+            const int64_t nx = at + static_cast<int64_t>(bt + 1) * 8 * kSellRows;
+#pragma unroll
+            for (int u = 0; u < 8; u++) f[u] = __ldg(o.cv32 + nx + u * kSellRows);
+        }
 #pragma unroll
         for (int u = 0; u < 8; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
+#pragma unroll
+        for (int u = 0; u < 8; u++) e[u] = f[u];
     }
-    for (; k < L; k++, at += kSellRows) {
-        const uint2 e = __ldg(o.cv32 + at);
-        acc = fmaf(__uint_as_float(e.y), v[e.x], acc);
+    at += static_cast<int64_t>(nb) * 8 * kSellRows;
+    for (int k = nb * 8; k < L; k++, at += kSellRows) {
+        const uint2 t = __ldg(o.cv32 + at);
+        acc = fmaf(__uint_as_float(t.y), v[t.x], acc);
     }
     return acc;
 }
@@ -329,8 +419,9 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
 // init: r_0 = b - A x (FP64); r32 = r_0; d = 0; p = 0; s = 0; rr, bb
 __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (aborted_before_solve(o, h, use_cond)) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const double* x = o.x;
     double vrr = 0.0, vbb = 0.0;
@@ -350,13 +441,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphCondi
             vbb += bi * bi;
         }
     }
-    const double s0 = block_sum(vrr, ws);
-    const double s1 = block_sum(vbb, ws);
-    if (publish(s0, s1, o.partials, &o.S->counter)) {
-        const double rr = gather_sum(o.partials, gridDim.x, ws);
-        const double bb = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
-        if (threadIdx.x == 0) init_scalars(o.S, rr, bb, h, use_cond);
-    }
+    double tot[3];
+    if (grid_sum(vrr, vbb, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) init_scalars(o.S, tot[0], tot[1], h, use_cond);
 }
 
 // s = w + beta s; p = r + beta p; d += alpha p; r -= alpha s (FP32, no reduction)
@@ -381,7 +467,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_axpy(CgOperands o) {
 __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                                                    cudaGraphConditionalHandle h,
                                                    cudaGraphConditionalHandle h_true, int use_cond) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     CgScalars* S = o.S;
     if (mode == 2) {
         if (S->converged || S->aborted || !S->do_update) return;
@@ -390,6 +476,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
     } else if (S->converged || S->aborted) {
         return;
     }
+    ticket_init(tk);
     const ChunkLoop cl;
     const float* __restrict__ r = o.r32;
     double vg = 0.0, vd = 0.0;
@@ -405,12 +492,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
             vd += static_cast<double>(wi) * ri;
         }
     }
-    const double s0 = block_sum(vg, ws);
-    const double s1 = block_sum(vd, ws);
-    if (publish(s0, s1, o.partials, &o.S->counter)) {
-        const double gam = gather_sum(o.partials, gridDim.x, ws);
-        const double del = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(vg, vd, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double gam = tot[0];
+        const double del = tot[1];
+        {
             S->counter = 0;
             S->rr_new = gam;
             int reliable = 0;
@@ -442,8 +528,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
 // over the r the iteration produced; convergence on this true residual.
 __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     if (o.S->converged || o.S->aborted || o.S->stalled || !o.S->do_update) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const bool odd = (o.S->updates & 1) != 0;
     const double* __restrict__ xc = odd ? o.x2 : o.x;
@@ -463,10 +550,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
             v += ri * ri;
         }
     }
-    const double s0 = block_sum(v, ws);
-    if (publish(s0, 0.0, o.partials, &o.S->counter)) {
-        const double rr = gather_sum(o.partials, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double rr = tot[0];
+        {
             CgScalars* S = o.S;
             S->counter = 0;
             S->true_rr = rr;
@@ -507,9 +594,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 __global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
-    __shared__ double ws[kBlock];
+    __shared__ BlockTicket tk;
     CgScalars* S = o.S;
     if (pcg_skip(S, mode)) return;
+    ticket_init(tk);
     const ChunkLoop cl;
     const float* __restrict__ u = o.u32;
     double vg = 0.0, vd = 0.0, vr = 0.0;
@@ -527,14 +615,12 @@ __global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
             vr += ri * ri;
         }
     }
-    const double s0 = block_sum(vg, ws);
-    const double s1 = block_sum(vd, ws);
-    const double s2 = block_sum(vr, ws);
-    if (publish(s0, s1, o.partials, &o.S->counter, s2)) {
-        const double gam = gather_sum(o.partials, gridDim.x, ws);
-        const double del = gather_sum(o.partials + gridDim.x, gridDim.x, ws);
-        const double rho = gather_sum(o.partials + 2 * gridDim.x, gridDim.x, ws);
-        if (threadIdx.x == 0) {
+    double tot[3];
+    if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        const double gam = tot[0];
+        const double del = tot[1];
+        const double rho = tot[2];
+        {
             S->counter = 0;
             S->rr_new = rho;
             int reliable = 0;
@@ -663,7 +749,13 @@ void init_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
 int cg_grid_vec(int64_t n) { return grid_for(n); }
 int cg_grid_spmv(int64_t n) { return grid_for(sell_chunks(n) * 32); }
 int64_t cg_partials(int64_t n) {
-    return 3 * static_cast<int64_t>(cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n)) + 64;
+    const int64_t g = cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n);
+    return 3 * (g + (g + 31) / 32) + 64;
+}
+
+int64_t cg_tickets(int64_t n) {
+    const int64_t g = cg_grid_vec(n) > cg_grid_spmv(n) ? cg_grid_vec(n) : cg_grid_spmv(n);
+    return (g + 31) / 32 + 1;
 }
 
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,

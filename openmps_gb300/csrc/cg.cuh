@@ -53,7 +53,8 @@ struct CgOperands {
     double* x2;         // second FP64 solution buffer (reliable updates alternate)
     float *r32, *w32, *s32, *p32, *d32;
     float* u32;         // preconditioned residual u = M r (MIXED_MG, LEARNED)
-    double* partials;   // 3 * max(grid_vec, grid_spmv) doubles
+    double* partials;   // reduction partials (cg_partials doubles)
+    uint32_t* tickets;  // per-group reduction counters (cg_tickets, zero between kernels)
     CgScalars* S;
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
 };
@@ -125,5 +126,6 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s);
 int cg_grid_vec(int64_t n);
 int cg_grid_spmv(int64_t n);
 int64_t cg_partials(int64_t n);
+int64_t cg_tickets(int64_t n);
 
 }  // namespace mpsgb

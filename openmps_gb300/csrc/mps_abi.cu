@@ -53,6 +53,7 @@ struct mps_handle {
     // CG buffers
     CgScalars* S = nullptr;
     double* partials = nullptr;
+    uint32_t* tickets = nullptr;
     double *r = nullptr, *p = nullptr, *Ap = nullptr, *x2 = nullptr;
     float *r32 = nullptr, *w32 = nullptr, *s32 = nullptr, *p32 = nullptr, *d32 = nullptr;
     float* u32 = nullptr;
@@ -293,6 +294,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     h->S = dalloc<CgScalars>(h, 1);
     st.solve_ok = &h->S->converged;
     h->partials = dalloc<double>(h, cg_partials(n));
+    h->tickets = dalloc<uint32_t>(h, cg_tickets(n));
     h->r = dalloc<double>(h, n);
     h->p = dalloc<double>(h, n);
     h->Ap = dalloc<double>(h, n);
@@ -373,6 +375,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(h->S, 0, sizeof(CgScalars), s), "memset");
     check(cudaMemsetAsync(h->d32, 0, sizeof(float) * n, s), "memset");
     check(cudaMemsetAsync(h->S_fb, 0, sizeof(CgScalars), s), "memset");
+    check(cudaMemsetAsync(h->tickets, 0, sizeof(uint32_t) * cg_tickets(n), s), "memset");
     check(cudaMemsetAsync(st.cell_xz, 0xff, sizeof(int32_t) * n, s), "memset");
     check(cudaMemsetAsync(st.ppe_cv32, 0, sizeof(uint2) * sell_cap, s), "memset");
     h->ppe_fp32 = false;
@@ -428,6 +431,7 @@ CgOperands cg_operands(mps_handle* h) {
     o.d32 = h->d32;
     o.u32 = h->u32;
     o.partials = h->partials;
+    o.tickets = h->tickets;
     o.S = h->S;
     o.status = h->st.status;
     return o;
@@ -1460,8 +1464,10 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         o.p32 = loc.get<float>(nn);
         o.d32 = loc.get<float>(nn);
         o.partials = loc.get<double>(static_cast<size_t>(cg_partials(n)));
+        o.tickets = loc.get<uint32_t>(static_cast<size_t>(cg_tickets(n)));
         o.S = loc.get<CgScalars>(1);
         cudaStream_t s = h->stream;
+        check(cudaMemsetAsync(o.tickets, 0, sizeof(uint32_t) * cg_tickets(n), s), "memset");
         auto up = [&](void* d, const void* src, size_t bytes) {
             check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s), "upload");
         };
