@@ -65,7 +65,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cg-launch", choices=("graph", "host"), default="graph",
+    ap.add_argument("--cg-launch", choices=("graph", "host", "persistent"), default="graph",
                     help="host: CG kernels launched one by one (profilers cannot see kernels "
                          "inside conditional CUDA graphs)")
     ap.add_argument("--profile-steps", type=int, default=0,
@@ -229,7 +229,8 @@ def run_ours(args, rank, world, local_rank):
     solver = SOLVERS[args.solver]
     scene = scenes.config_c2()
     dt = scene.meta["dt"]
-    launch = abi.CG_LAUNCH_HOST if args.cg_launch == "host" else abi.CG_LAUNCH_GRAPH
+    launch = {"graph": abi.CG_LAUNCH_GRAPH, "host": abi.CG_LAUNCH_HOST,
+              "persistent": abi.CG_LAUNCH_PERSISTENT}[args.cg_launch]
     params = scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8, cg_launch=launch)
     comp = Computer(params, device=local_rank)
     if solver == abi.SOLVER_LEARNED:

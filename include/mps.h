@@ -76,8 +76,12 @@ extern "C" {
 /* How the CG loop is launched: one CUDA graph with a device-driven while loop, or
  * host-launched kernel batches (the same kernels; for profilers that cannot see
  * kernels inside conditional graphs). */
-#define MPS_CG_LAUNCH_GRAPH 0
+#define MPS_CG_LAUNCH_GRAPH 0   /* one CUDA graph per solve, every phase its own kernel */
 #define MPS_CG_LAUNCH_HOST 1
+#define MPS_CG_LAUNCH_GRAPH_KERNELS 0  /* the same as MPS_CG_LAUNCH_GRAPH */
+#define MPS_CG_LAUNCH_PERSISTENT 2     /* MIXED_MG / LEARNED: the iterations in one persistent
+                                          cooperative kernel (grid barriers between phases);
+                                          per-phase kernels if the device cannot launch it */
 
 /* CG stopping rule */
 #define MPS_CRIT_INITIAL_RESIDUAL 0 /* reference: r_k.r_k < eps^2 r_0.r_0 (Computer.hpp:1386, :1408) */
@@ -107,7 +111,7 @@ typedef struct mps_params {
     int32_t max_cg_iters; /* <= 0: number of unknowns, as the reference (Computer.hpp:1392) */
     double inner_tol;     /* MIXED: relative residual reduction of one FP32 inner solve */
     int32_t max_refinements; /* MIXED: maximum FP64 refinement passes */
-    int32_t cg_launch;       /* MPS_CG_LAUNCH_GRAPH (default) or MPS_CG_LAUNCH_HOST */
+    int32_t cg_launch;       /* MPS_CG_LAUNCH_GRAPH (default), _HOST or _PERSISTENT */
     double reserved[6];
 } mps_params;
 

@@ -47,6 +47,8 @@ MLP_SAMPLE_FLOATS = 18
 
 CG_LAUNCH_GRAPH = 0
 CG_LAUNCH_HOST = 1
+CG_LAUNCH_GRAPH_KERNELS = 0
+CG_LAUNCH_PERSISTENT = 2
 
 CRIT_INITIAL_RESIDUAL = 0
 CRIT_RHS = 1

@@ -685,6 +685,311 @@ __global__ void k_cg_configure(CgScalars* S, double eps, int criterion, int max_
     }
 }
 
+// ------------------------------------------------ persistent preconditioned solve
+// The whole preconditioned iteration loop in one cooperative launch: every phase of an
+// iteration (vector updates + level-1 restriction, each cycle level, the dense coarsest
+// solve, the prolongation, the SpMV with its dot products, the reliable update) runs
+// grid-stride over all resident blocks, and phases are separated by a grid barrier
+// instead of a kernel boundary.  The barrier spins with a clock bound: a wait that
+// exceeds it sets the error word and every block leaves the loop at its next barrier.
+struct GridSync {
+    unsigned* count;
+    unsigned* gen;
+    int32_t* err;
+};
+
+constexpr long long kBarrierClocks = 4000000000LL;  // about two seconds
+
+// Two-level arrival: blocks count in groups of kBarrierGroup, the last block of a group
+// counts at the top, and the last group releases everyone by advancing the generation.
+// `count` holds one counter per group plus the top one (all zero between barriers).
+constexpr int kBarrierGroup = 16;
+
+__device__ __forceinline__ bool grid_barrier(const GridSync& g, unsigned& gen) {
+    __shared__ int err_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned target = gen + 1;
+        const int G = static_cast<int>(gridDim.x);
+        const int NG = (G + kBarrierGroup - 1) / kBarrierGroup;
+        const int grp = static_cast<int>(blockIdx.x) / kBarrierGroup;
+        const int gsize = min(kBarrierGroup, G - grp * kBarrierGroup);
+        __threadfence();
+        if (atomicAdd(g.count + grp, 1u) == static_cast<unsigned>(gsize - 1)) {
+            atomicExch(g.count + grp, 0u);
+            __threadfence();
+            if (atomicAdd(g.count + NG, 1u) == static_cast<unsigned>(NG - 1)) {
+                atomicExch(g.count + NG, 0u);
+                __threadfence();
+                atomicExch(g.gen, target);
+            }
+        }
+        const long long t0 = clock64();
+        while (*reinterpret_cast<volatile unsigned*>(g.gen) != target) {
+            if (clock64() - t0 > kBarrierClocks) {
+                atomicExch(g.err, 1);
+                break;
+            }
+        }
+        __threadfence();
+        err_s = *reinterpret_cast<volatile int32_t*>(g.err);
+    }
+    gen++;
+    __syncthreads();
+    return err_s == 0;
+}
+
+struct PersistentState {
+    unsigned gen;
+    int gtid, nthreads, gwarp, nwarps, lane;
+};
+
+// block sums of three values (lanes park values, warp 0 adds), then one partial per block
+// and, after a barrier, the same fixed-order total in every block (thread 0 valid)
+__device__ __noinline__ bool persistent_sum3(double a, double b, double c, const CgOperands& o, const GridSync& g,
+                                PersistentState& P, double* red, double* out) {
+    red[threadIdx.x] = a;
+    red[kBlock + threadIdx.x] = b;
+    red[2 * kBlock + threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kBlock / 32; w++) {
+            s0 += red[32 * w + threadIdx.x];
+            s1 += red[kBlock + 32 * w + threadIdx.x];
+            s2 += red[2 * kBlock + 32 * w + threadIdx.x];
+        }
+        s0 = warp_sum(s0);
+        s1 = warp_sum(s1);
+        s2 = warp_sum(s2);
+        if (threadIdx.x == 0) {
+            o.partials[blockIdx.x] = s0;
+            o.partials[gridDim.x + blockIdx.x] = s1;
+            o.partials[2 * gridDim.x + blockIdx.x] = s2;
+        }
+    }
+    if (!grid_barrier(g, P.gen)) return false;
+    if (threadIdx.x < 32) {
+        double x = 0.0, y = 0.0, z = 0.0;
+        for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += 32) {
+            x += __ldcg(o.partials + k);
+            y += __ldcg(o.partials + gridDim.x + k);
+            z += __ldcg(o.partials + 2 * gridDim.x + k);
+        }
+        x = warp_sum(x);
+        y = warp_sum(y);
+        z = warp_sum(z);
+        if (threadIdx.x == 0) {
+            out[0] = x;
+            out[1] = y;
+            out[2] = z;
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// u = M r; with `axpy` the iteration's vector updates run in the restriction
+__device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHierarchy& mg, const GridSync& g,
+                                 PersistentState& P, bool axpy, float alpha, float beta) {
+    const MgLevel& L1 = mg.lv[1];
+    for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
+        const int cnt = min(mg.cell_count[c], mg.max_per_cell);
+        const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
+        float sum = 0.0f;
+        for (int s = P.lane; s < cnt; s += 32) {
+            const int i = slots[s];
+            float ri = o.r32[i];
+            if (axpy) {
+                const float si = fmaf(beta, o.s32[i], o.w32[i]);
+                const float pi = fmaf(beta, o.p32[i], o.u32[i]);
+                ri = fmaf(-alpha, si, ri);
+                o.s32[i] = si;
+                o.p32[i] = pi;
+                o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+                o.r32[i] = ri;
+            }
+            sum += ri;
+        }
+        for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(kFull, sum, k);
+        if (P.lane == 0) L1.r[c] = sum;
+    }
+    if (!grid_barrier(g, P.gen)) return false;
+    for (int l = 1; l < mg.levels; l++) {
+        const MgLevel& f = mg.lv[l];
+        const MgLevel& cl = mg.lv[l + 1];
+        for (int I = P.gtid; I < cl.cells; I += P.nthreads)
+            cl.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / cl.nz, I - (I / cl.nz) * cl.nz);
+        if (!grid_barrier(g, P.gen)) return false;
+    }
+    {
+        const MgLevel& Lc = mg.lv[mg.levels];
+        const int m = Lc.cells;
+        for (int row = P.gwarp; row < m; row += P.nwarps) {
+            float v = 0.0f;
+            for (int k = P.lane; k < m; k += 32) v += mg.dense[row * m + k] * Lc.r[k];
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(kFull, v, off);
+            if (P.lane == 0) Lc.e[row] = v;
+        }
+        if (!grid_barrier(g, P.gen)) return false;
+    }
+    for (int l = mg.levels - 1; l >= 2; l--) {
+        const MgLevel& f = mg.lv[l];
+        for (int ch = P.gtid; ch < f.cells; ch += P.nthreads)
+            f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, mg.lv[l + 1].nz, mg.lv[l + 1].e, ch);
+        if (!grid_barrier(g, P.gen)) return false;
+    }
+    if (mg.levels > 1) {
+        const MgLevel& c2 = mg.lv[2];
+        for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
+            const int cnt = min(mg.cell_count[c], mg.max_per_cell);
+            if (cnt == 0) continue;
+            const float e = smoothed_correction(L1.nx, L1.nz, L1.cells, L1.k32, L1.dinv, L1.r, c2.nz, c2.e, c);
+            const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
+            for (int s = P.lane; s < cnt; s += 32) {
+                const int i = slots[s];
+                const float d = mg.dinv0[i];
+                const float scl = mg.scale ? mg.scale[i] : 1.0f;
+                o.u32[i] = d != 0.0f ? scl * d * o.r32[i] + e : 0.0f;
+            }
+        }
+    } else {
+        for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
+            const int cnt = min(mg.cell_count[c], mg.max_per_cell);
+            const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
+            const float e = L1.e[c];
+            for (int s = P.lane; s < cnt; s += 32) {
+                const int i = slots[s];
+                const float d = mg.dinv0[i];
+                const float scl = mg.scale ? mg.scale[i] : 1.0f;
+                o.u32[i] = d != 0.0f ? scl * d * o.r32[i] + e : 0.0f;
+            }
+        }
+    }
+    return grid_barrier(g, P.gen);
+}
+
+// w = A u; gamma = r.u, delta = w.u, rho = r.r (FP64), the same in every block
+__device__ __noinline__ bool persistent_spmv(const CgOperands& o, const GridSync& g, PersistentState& P, double* red,
+                                double* sums) {
+    double vg = 0.0, vd = 0.0, vr = 0.0;
+    for (int c = P.gwarp; c < o.nchunks; c += P.nwarps) {
+        const int i = kSellRows * c + P.lane;
+        const int L = o.len[i];
+        const float wi = row32(o, sell_index(o.off[c], P.lane, 0), L, o.u32);
+        if (i < o.n) {
+            const double ri = o.r32[i], ui = o.u32[i];
+            o.w32[i] = wi;
+            vg += ri * ui;
+            vd += static_cast<double>(wi) * ui;
+            vr += ri * ri;
+        }
+    }
+    return persistent_sum3(vg, vd, vr, o, g, P, red, sums);
+}
+
+// x += d (FP64), d = 0; then r = b - A x with the FP64 matrix into r32; returns r.r
+__device__ __noinline__ bool persistent_true(const CgOperands& o, const GridSync& g, PersistentState& P, double* red,
+                                double* sums) {
+    for (int i = P.gtid; i < o.n; i += P.nthreads) {
+        o.x[i] += static_cast<double>(o.d32[i]);
+        o.d32[i] = 0.0f;
+    }
+    if (!grid_barrier(g, P.gen)) return false;
+    double v = 0.0;
+    for (int c = P.gwarp; c < o.nchunks; c += P.nwarps) {
+        const int i = kSellRows * c + P.lane;
+        const int L = o.len[i];
+        const double* x = o.x;
+        const double ax = row64(o, sell_index(o.off[c], P.lane, 0), L, [&](int j) { return x[j]; });
+        if (i < o.n) {
+            const double ri = o.b[i] - ax;
+            o.r32[i] = static_cast<float>(ri);
+            v += ri * ri;
+        }
+    }
+    return persistent_sum3(v, 0.0, 0.0, o, g, P, red, sums);
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_pcg_persistent(CgOperands o, MgHierarchy mg, GridSync g) {
+    __shared__ double red[3 * kBlock];
+    __shared__ double sums[3];
+    __shared__ unsigned gen0;
+    CgScalars* S = o.S;
+    if (S->converged || S->aborted || S->stalled) return;
+    if (threadIdx.x == 0) gen0 = *reinterpret_cast<volatile unsigned*>(g.gen);
+    __syncthreads();
+    PersistentState P;
+    P.gen = gen0;
+    P.gtid = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    P.nthreads = static_cast<int>(gridDim.x * blockDim.x);
+    P.gwarp = P.gtid >> 5;
+    P.nwarps = P.nthreads >> 5;
+    P.lane = threadIdx.x & 31;
+    double alpha = S->alpha, beta = S->beta, gam_old = S->rr;
+    double rr_upd = S->rr_upd, prev_true = S->prev_true_rr, rho = S->rr_new;
+    const double thr = S->thr, delta2 = S->delta2;
+    int iter = S->iter, updates = S->updates;
+    const int max_iter = S->max_iter;
+    bool conv = false, stalled = false, ok = true;
+    while (iter < max_iter) {
+        ok = persistent_cycle(o, mg, g, P, true, static_cast<float>(alpha), static_cast<float>(beta));
+        if (!ok) break;
+        ok = persistent_spmv(o, g, P, red, sums);
+        if (!ok) break;
+        double gam = sums[0], del = sums[1];
+        rho = sums[2];
+        if (rho < delta2 * rr_upd || rho < thr) {
+            ok = persistent_true(o, g, P, red, sums);
+            if (!ok) break;
+            const double tr = sums[0];
+            updates++;
+            rr_upd = tr;
+            rho = tr;
+            if (tr < thr) {
+                conv = true;
+                iter++;
+                break;
+            }
+            if (tr > 0.25 * prev_true) {
+                stalled = true;
+                break;
+            }
+            prev_true = tr;
+            ok = persistent_cycle(o, mg, g, P, false, 0.0f, 0.0f) && persistent_spmv(o, g, P, red, sums);
+            if (!ok) break;
+            gam = sums[0];
+            del = sums[1];
+            rho = sums[2];
+        }
+        beta = gam / gam_old;
+        alpha = gam / (del - beta * gam / alpha);
+        gam_old = gam;
+        iter++;
+        if (!(isfinite(alpha) && isfinite(beta) && alpha != 0.0)) {
+            stalled = true;
+            break;
+        }
+    }
+    // the pending FP32 correction into x (no reader follows inside this kernel)
+    for (int i = P.gtid; i < o.n; i += P.nthreads) {
+        o.x[i] += static_cast<double>(o.d32[i]);
+        o.d32[i] = 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S->iter = iter;
+        S->updates = updates;
+        S->converged = conv ? 1 : 0;
+        S->stalled = (stalled || !ok) ? 1 : 0;
+        S->rr_new = rho;
+        S->rr_upd = rr_upd;
+        S->alpha = alpha;
+        S->beta = beta;
+        S->rr = gam_old;
+        S->do_update = 1;  // x is current: nothing left to fold
+    }
+}
+
 bool is_pcg(int solver) { return solver == MPS_SOLVER_MIXED_MG || solver == MPS_SOLVER_LEARNED; }
 
 void cg64_body(const CgOperands& ops, cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
@@ -811,6 +1116,7 @@ void CgGraph::reset() {
     graph_ = nullptr;
     solver_ = -1;
     nested_ = false;
+    persistent_ = false;
 }
 
 cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win,
@@ -1009,6 +1315,86 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
         return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t CgGraph::build_persistent(int solver, const CgOperands& ops, cudaStream_t s,
+                                      const MgHierarchy* mg, const CgOperands* fb, const LearnedRun* lrn,
+                                      const PersistentSync& ps) {
+    reset();
+    if (!is_pcg(solver) || !mg || !fb || ps.blocks <= 0) return cudaErrorInvalidValue;
+    ops_ = ops;
+    solver_ = solver;
+    nested_ = false;
+    persistent_ = true;
+    kpi_ = 0;
+    kri_ = 0;
+    const int gs = ops.grid_spmv;
+    cudaError_t e = cudaGraphCreate(&graph_, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h_fb;
+    e = cudaGraphConditionalHandleCreate(&h_fb, graph_, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    init_kernels(solver, ops, mg, 0, 0, s, lrn);
+    cudaMemsetAsync(ps.err, 0, sizeof(int32_t), s);
+    cudaMemsetAsync(ps.count, 0, sizeof(unsigned) * kPersistentCounters, s);  // a timed-out barrier leaves them non-zero
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(ps.blocks);
+        cfg.blockDim = dim3(kBlock);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        GridSync g{ps.count, ps.gen, ps.err};
+        cudaLaunchKernelEx(&cfg, k_pcg_persistent, ops, *mg, g);
+    }
+    k_cg_init<<<gs, kBlock, 0, s>>>(*fb, h_fb, 1, ops.S);
+    e = cudaStreamEndCapture(s, &captured);
+    if (e != cudaSuccess) return e;
+    cudaGraphNode_t fb_init;
+    e = sink_node(graph_, &fb_init);
+    if (e != cudaSuccess) return e;
+    cudaGraphNode_t fb_while;
+    cudaGraph_t fb_body;
+    e = add_while(graph_, &fb_init, h_fb, &fb_while, &fb_body);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(s, fb_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cg64_body(*fb, h_fb, 1, s);
+    e = cudaStreamEndCapture(s, &captured);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(s, graph_, &fb_while, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
+    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    e = cudaStreamEndCapture(s, &captured);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(&exec_, graph_, 0);
+    if (e != cudaSuccess) {
+        exec_ = nullptr;
+        return e;
+    }
+    return cudaSuccess;
+}
+
+static_assert(kPersistentCounters * kBarrierGroup >= 8 * 1024, "barrier counters for 8192 blocks");
+
+int persistent_blocks() {
+    int dev = 0, sms = 0, coop = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent, kBlock, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm * sms;
 }
 
 cudaError_t CgGraph::launch(cudaStream_t s) {

@@ -69,6 +69,16 @@ struct L2Window {
 struct MgHierarchy;
 struct LearnedOps;
 
+// Device words of the persistent solve's grid barrier, and its grid size.
+constexpr int kPersistentCounters = 513;  // barrier group counters + the top one
+
+struct PersistentSync {
+    unsigned* count;  // kPersistentCounters counters, zero between launches
+    unsigned* gen;
+    int32_t* err;     // set when a barrier wait runs out
+    int blocks;
+};
+
 // The learned start of a solve: its device state and the scalars its kernels gate on.
 struct LearnedRun {
     const LearnedOps* L;
@@ -85,8 +95,12 @@ public:
     cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {},
                       const MgHierarchy* mg = nullptr, const CgOperands* fb = nullptr,
                       const LearnedRun* lrn = nullptr);
+    // MIXED_MG / LEARNED with the whole iteration loop in one cooperative kernel
+    cudaError_t build_persistent(int solver, const CgOperands& ops, cudaStream_t s, const MgHierarchy* mg,
+                                 const CgOperands* fb, const LearnedRun* lrn, const PersistentSync& ps);
     cudaError_t launch(cudaStream_t s);
     void reset();
+    bool persistent() const { return persistent_; }
     bool valid() const { return exec_ != nullptr; }
     int solver() const { return solver_; }
     const CgOperands& operands() const { return ops_; }
@@ -103,6 +117,7 @@ private:
     cudaGraphExec_t exec_ = nullptr;
     int solver_ = -1;
     bool nested_ = false;
+    bool persistent_ = false;
     int kpi_ = 0, kri_ = 0;
     CgOperands ops_{};
 };
@@ -113,6 +128,8 @@ private:
 cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, int chunk,
                           cudaStream_t s, int64_t* launches, const MgHierarchy* mg = nullptr,
                           const CgOperands* fb = nullptr, const LearnedRun* lrn = nullptr);
+// Grid size of the persistent solve on the current device (0: cooperative launch unavailable).
+int persistent_blocks();
 // Kernels of one iteration of the solver, and of one reliable update.
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg);
 int cg_kernels_per_update(int solver, const MgHierarchy* mg);

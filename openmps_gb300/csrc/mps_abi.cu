@@ -77,6 +77,8 @@ struct mps_handle {
     int batch_threads = 0, batch_blocks = 0, batch_order = 0;  // tuned launch
     std::vector<float> tune_ms;
     std::vector<int32_t> tune_threads, tune_order;
+    PersistentSync psync{};      // grid barrier words of the persistent solve
+    bool persistent_failed = false;
     cudaGraphExec_t batch_graph = nullptr;
     double batch_graph_dt = 0.0;
     int64_t batch_step_launches = 0;
@@ -184,7 +186,9 @@ void validate(const mps_params& p) {
     if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
         bad("unknown criterion");
     if (p.flags & ~static_cast<uint32_t>(MPS_PRESET_REFERENCE)) bad("unknown method flag");
-    if (p.cg_launch != MPS_CG_LAUNCH_GRAPH && p.cg_launch != MPS_CG_LAUNCH_HOST) bad("unknown cg_launch");
+    if (p.cg_launch != MPS_CG_LAUNCH_GRAPH && p.cg_launch != MPS_CG_LAUNCH_HOST &&
+        p.cg_launch != MPS_CG_LAUNCH_PERSISTENT)
+        bad("unknown cg_launch");
 }
 
 void setup_constants(mps_handle* h) {
@@ -366,6 +370,9 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     L.dinv0 = mg.dinv0;
     L.flags = sc.flags;
     h->S_lrn = dalloc<CgScalars>(h, 1);
+    h->psync.count = dalloc<unsigned>(h, kPersistentCounters);
+    h->psync.gen = dalloc<unsigned>(h, 1);
+    h->psync.err = dalloc<int32_t>(h, 1);
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -380,6 +387,9 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(st.ppe_cv32, 0, sizeof(uint2) * sell_cap, s), "memset");
     h->ppe_fp32 = false;
     check(cudaMemsetAsync(h->S_lrn, 0, sizeof(CgScalars), s), "memset");
+    check(cudaMemsetAsync(h->psync.count, 0, sizeof(unsigned) * kPersistentCounters, s), "memset");
+    check(cudaMemsetAsync(h->psync.gen, 0, sizeof(unsigned), s), "memset");
+    check(cudaMemsetAsync(h->psync.err, 0, sizeof(int32_t), s), "memset");
     check(cudaMemsetAsync(L.counter, 0, sizeof(uint32_t), s), "memset");
     check(cudaMemsetAsync(L.error, 0, sizeof(int32_t), s), "memset");
     check(cudaMemsetAsync(L.active, 0, sizeof(int32_t) * n, s), "memset");
@@ -500,8 +510,9 @@ void read_status(mps_handle* h, bool solve_done) {
             const int kpi = h->cg.kernels_per_iteration(), kpu = h->cg.kernels_per_update();
             if (is_preconditioned(h->prm.solver)) {
                 const int own = S.iter - S.fb_iter;
-                launched(h, mg_setup_launches(h->mg) + 2 + mg_apply_launches(h->mg) + own * kpi +
-                                S.updates * kpu + 4 + 3 * S.fb_iter +
+                // per-phase kernels and the finish kernel, or one persistent kernel
+                const int loop = h->cg.persistent() ? 1 : own * kpi + S.updates * kpu + 1;
+                launched(h, mg_setup_launches(h->mg) + 2 + mg_apply_launches(h->mg) + loop + 3 + 3 * S.fb_iter +
                                 (h->prm.solver == MPS_SOLVER_LEARNED ? 1 + learned_prep_launches(h->mg, true) : 0));
             } else {
                 launched(h, 4 + S.iter * kpi + S.updates * kpu);
@@ -634,10 +645,26 @@ void do_solve(mps_handle* h) {
         h->direct_launches = k;
     } else {
         h->direct_launches = -1;
-        if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n) {
-            check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
-                              pcg ? &mg : nullptr, pcg ? &fb : nullptr, learned ? &run : nullptr),
-                  "CG graph build");
+        const bool want_persistent = pcg && h->prm.cg_launch == MPS_CG_LAUNCH_PERSISTENT && !h->persistent_failed;
+        if (!h->cg.valid() || h->cg.solver() != solver || h->cg.operands().n != h->n ||
+            h->cg.persistent() != want_persistent) {
+            bool built = false;
+            if (want_persistent) {
+                PersistentSync ps = h->psync;
+                ps.blocks = persistent_blocks();
+                built = ps.blocks > 0 &&
+                        h->cg.build_persistent(solver, cg_operands(h), s, &mg, &fb, learned ? &run : nullptr, ps) ==
+                            cudaSuccess;
+                if (!built) {
+                    // no cooperative launch in a graph on this device: per-phase kernels
+                    cudaGetLastError();
+                    h->persistent_failed = true;
+                }
+            }
+            if (!built)
+                check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
+                                  pcg ? &mg : nullptr, pcg ? &fb : nullptr, learned ? &run : nullptr),
+                      "CG graph build");
         }
         check(h->cg.launch(s), "CG graph launch");
     }

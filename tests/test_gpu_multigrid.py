@@ -51,20 +51,36 @@ def test_fallback_after_stall(gpu_lib, oracle_lib):
     assert rel_err(mg.particles()["p"], cpu.particles()["p"]) < 1e-7
 
 
+def _run_launch(s, launch, steps=3):
+    c = Computer(s.params(eps=1e-10, solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS, cg_launch=launch))
+    c.add_scene(s)
+    for _ in range(steps):
+        c.forward_time(s.meta["dt"])
+    return c.particles(), c.stats()
+
+
 def test_host_launch_matches_graph(gpu_lib):
-    # the host-driven loop runs the same kernels in the same order: identical results
+    # the host-driven loop runs the same per-phase kernels in the same order as the graph
+    # of per-phase kernels: identical results
     s = stock_tank()
-    out = []
-    for launch in (abi.CG_LAUNCH_GRAPH, abi.CG_LAUNCH_HOST):
-        c = Computer(s.params(eps=1e-10, solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS,
-                              cg_launch=launch))
-        c.add_scene(s)
-        for _ in range(3):
-            c.forward_time(s.meta["dt"])
-        out.append((c.particles(), c.stats()["cg_iterations"]))
+    a, sa = _run_launch(s, abi.CG_LAUNCH_GRAPH)
+    b, sb = _run_launch(s, abi.CG_LAUNCH_HOST)
     for k in ("x", "z", "u", "w", "p"):
-        np.testing.assert_array_equal(out[0][0][k], out[1][0][k], err_msg=k)
-    assert out[0][1] == out[1][1]
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    assert sa["cg_iterations"] == sb["cg_iterations"]
+
+
+@pytest.mark.parametrize("maker", [stock_tank, reference_tank])
+def test_persistent_kernel_matches_per_phase_kernels(gpu_lib, maker):
+    # the persistent cooperative solve adds its dot products in another order: the same
+    # solution to the solve tolerance, and no fallback
+    s = maker()
+    a, sa = _run_launch(s, abi.CG_LAUNCH_PERSISTENT)
+    b, sb = _run_launch(s, abi.CG_LAUNCH_GRAPH)
+    assert sa["fallback"] == 0 and sa["cg_true_relres"] <= 1e-10
+    assert rel_err(a["p"], b["p"]) < 1e-7
+    assert rel_err(a["x"], b["x"], scale=s.l0) < 1e-9
+    assert abs(sa["cg_iterations"] - sb["cg_iterations"]) <= 2
 
 
 def test_deterministic(gpu_lib):
