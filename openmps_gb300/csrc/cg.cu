@@ -793,7 +793,9 @@ __device__ __noinline__ bool persistent_sum3(double a, double b, double c, const
 __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHierarchy& mg, const GridSync& g,
                                  PersistentState& P, bool axpy, float alpha, float beta) {
     const MgLevel& L1 = mg.lv[1];
-    for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
+    const int nact = *mg.n_active;
+    for (int a = P.gwarp; a < nact; a += P.nwarps) {
+        const int c = mg.active[a];
         const int cnt = min(mg.cell_count[c], mg.max_per_cell);
         const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
         float sum = 0.0f;
@@ -841,9 +843,9 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
     }
     if (mg.levels > 1) {
         const MgLevel& c2 = mg.lv[2];
-        for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
+        for (int a = P.gwarp; a < nact; a += P.nwarps) {
+            const int c = mg.active[a];
             const int cnt = min(mg.cell_count[c], mg.max_per_cell);
-            if (cnt == 0) continue;
             const float e = smoothed_correction(L1.nx, L1.nz, L1.cells, L1.k32, L1.dinv, L1.r, c2.nz, c2.e, c);
             const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
             for (int s = P.lane; s < cnt; s += 32) {

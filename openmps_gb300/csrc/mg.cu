@@ -90,11 +90,13 @@ __device__ __forceinline__ void store_level(const MgLevel& L, int c, const doubl
 // Level-1 operator: per search cell, the bins of its particles in slot order.
 __global__ void k_mg_cells(MgLevel L1, const int32_t* cell_count, const int32_t* cell_slot,
                            int max_per_cell, const double* bins, int n, float omega,
-                           const DevStatus* status) {
+                           const DevStatus* status, int32_t* active, int32_t* n_active) {
     if (setup_failed(status)) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= L1.cells) return;
     const int cnt = min(cell_count[c], max_per_cell);
+    // cells holding particles, in any order (every cell's work below is independent)
+    if (cnt > 0) active[atomicAdd(n_active, 1)] = c;
     const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
     double k[9];
 #pragma unroll
@@ -194,17 +196,21 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
 // cell, lanes over the slots, fixed-order shuffle sum).
 __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_count,
                                                          const int32_t* cell_slot, int max_per_cell,
-                                                         const float* r, const CgScalars* S, int mode) {
+                                                         const float* r, const CgScalars* S, int mode,
+                                                         const int32_t* active, const int32_t* n_active) {
     if (pcg_skip(S, mode)) return;
     const int lane = threadIdx.x & 31;
-    const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (c >= L1.cells) return;
-    const int cnt = min(cell_count[c], max_per_cell);
-    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
-    float sum = 0.0f;
-    for (int s = lane; s < cnt; s += 32) sum += r[slots[s]];
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if (lane == 0) L1.r[c] = sum;
+    const int nact = *n_active;
+    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
+        const int c = active[a];
+        const int cnt = min(cell_count[c], max_per_cell);
+        const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+        float sum = 0.0f;
+        for (int s = lane; s < cnt; s += 32) sum += r[slots[s]];
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) L1.r[c] = sum;
+    }
 }
 
 // An iteration's vector updates fused with the level-1 restriction of the new residual:
@@ -213,29 +219,33 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32
 __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1,
                                                              const int32_t* cell_count,
                                                              const int32_t* cell_slot,
-                                                             int max_per_cell) {
+                                                             int max_per_cell, const int32_t* active,
+                                                             const int32_t* n_active) {
     if (pcg_skip(o.S, 1)) return;
     const int lane = threadIdx.x & 31;
-    const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (c >= L1.cells) return;
     const float alpha = __double2float_rn(o.S->alpha);
     const float beta = __double2float_rn(o.S->beta);
-    const int cnt = min(cell_count[c], max_per_cell);
-    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
-    float sum = 0.0f;
-    for (int s = lane; s < cnt; s += 32) {
-        const int i = slots[s];
-        const float si = fmaf(beta, o.s32[i], o.w32[i]);
-        const float pi = fmaf(beta, o.p32[i], o.u32[i]);
-        const float ri = fmaf(-alpha, si, o.r32[i]);
-        o.s32[i] = si;
-        o.p32[i] = pi;
-        o.d32[i] = fmaf(alpha, pi, o.d32[i]);
-        o.r32[i] = ri;
-        sum += ri;
+    const int nact = *n_active;
+    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
+        const int c = active[a];
+        const int cnt = min(cell_count[c], max_per_cell);
+        const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+        float sum = 0.0f;
+        for (int s = lane; s < cnt; s += 32) {
+            const int i = slots[s];
+            const float si = fmaf(beta, o.s32[i], o.w32[i]);
+            const float pi = fmaf(beta, o.p32[i], o.u32[i]);
+            const float ri = fmaf(-alpha, si, o.r32[i]);
+            o.s32[i] = si;
+            o.p32[i] = pi;
+            o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+            o.r32[i] = ri;
+            sum += ri;
+        }
+        for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, k);
+        if (lane == 0) L1.r[c] = sum;
     }
-    for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, k);
-    if (lane == 0) L1.r[c] = sum;
 }
 
 __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
@@ -258,20 +268,23 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, 
                                                           const int32_t* cell_slot, int max_per_cell,
                                                           const float* dinv0, const float* scale,
                                                           const float* r, float* u,
-                                                          const CgScalars* S, int mode) {
+                                                          const CgScalars* S, int mode,
+                                                          const int32_t* active, const int32_t* n_active) {
     if (pcg_skip(S, mode)) return;
     const int lane = threadIdx.x & 31;
-    const int ch = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (ch >= f.cells) return;
-    const int cnt = min(cell_count[ch], max_per_cell);
-    if (cnt == 0) return;
-    const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
-    const int32_t* slots = cell_slot + static_cast<int64_t>(ch) * max_per_cell;
-    for (int s = lane; s < cnt; s += 32) {
-        const int i = slots[s];
-        const float d = dinv0[i];
-        const float sc = scale ? scale[i] : 1.0f;
-        u[i] = d != 0.0f ? sc * d * r[i] + e : 0.0f;
+    const int nact = *n_active;
+    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
+        const int ch = active[a];
+        const int cnt = min(cell_count[ch], max_per_cell);
+        const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
+        const int32_t* slots = cell_slot + static_cast<int64_t>(ch) * max_per_cell;
+        for (int s = lane; s < cnt; s += 32) {
+            const int i = slots[s];
+            const float d = dinv0[i];
+            const float sc = scale ? scale[i] : 1.0f;
+            u[i] = d != 0.0f ? sc * d * r[i] + e : 0.0f;
+        }
     }
 }
 
@@ -370,6 +383,9 @@ size_t dense_smem(const MgHierarchy& mg) {
 
 int warp_grid(int cells) { return grid_for(static_cast<int64_t>(cells) * 32); }
 
+// grid of the kernels that walk the active level-1 cells (warp per cell, grid-stride)
+int active_grid(int cells) { return std::min(warp_grid(cells), 2048); }
+
 }  // namespace
 
 int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom) {
@@ -398,10 +414,13 @@ cudaError_t mg_prepare_device() {
 }
 
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
+    // cells without particles keep a zero residual through the solve
+    cudaMemsetAsync(mg.n_active, 0, sizeof(int32_t), s);
+    cudaMemsetAsync(mg.lv[1].r, 0, sizeof(float) * mg.lv[1].cells, s);
     k_mg_bins<<<o.grid_spmv, kBlock, 0, s>>>(o, mg.cell_xz, mg.bins, mg.dinv0, kMgOmegaFine, mg.status);
     k_mg_cells<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1], mg.cell_count, mg.cell_slot,
                                                           mg.max_per_cell, mg.bins, mg.n,
-                                                          kMgOmegaCoarse, mg.status);
+                                                          kMgOmegaCoarse, mg.status, mg.active, mg.n_active);
     for (int l = 1; l < mg.levels; l++)
         k_mg_coarsen<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1],
                                                                     kMgOmegaCoarse, mg.status);
@@ -413,12 +432,13 @@ int mg_setup_launches(const MgHierarchy& mg) { return 2 + (mg.levels - 1) + 1; }
 void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
               cudaStream_t s, const CgOperands* fuse_axpy) {
     const MgLevel& L1 = mg.lv[1];
+    const int g1 = active_grid(L1.cells);
     if (fuse_axpy)
-        k_mg_axpy_restrict<<<warp_grid(L1.cells), kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_count,
-                                                                 mg.cell_slot, mg.max_per_cell);
+        k_mg_axpy_restrict<<<g1, kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_count, mg.cell_slot, mg.max_per_cell,
+                                                 mg.active, mg.n_active);
     else
-        k_mg_restrict0<<<warp_grid(L1.cells), kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot,
-                                                             mg.max_per_cell, r, S, mode);
+        k_mg_restrict0<<<g1, kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot, mg.max_per_cell, r, S, mode,
+                                             mg.active, mg.n_active);
     for (int l = 1; l < mg.bottom; l++)
         k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
     MgBottom B{};
@@ -430,9 +450,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     for (int l = mg.bottom - 1; l >= 2; l--)
         k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
     if (mg.bottom > 1)
-        k_mg_up_prolong<<<warp_grid(L1.cells), kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_count, mg.cell_slot,
-                                                              mg.max_per_cell, mg.dinv0, mg.scale,
-                                                              r, u, S, mode);
+        k_mg_up_prolong<<<g1, kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_count, mg.cell_slot, mg.max_per_cell,
+                                              mg.dinv0, mg.scale, r, u, S, mode, mg.active, mg.n_active);
     else
         k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
                                                        r, L1.e, u, S, mode);

@@ -53,6 +53,8 @@ struct MgHierarchy {
     float* dinv0 = nullptr;             // omega_0 / a_ii on active rows, 0 on identity rows
     const float* scale = nullptr;       // per-row scale of the Jacobi term (null: 1)
     double* bins = nullptr;             // 9 * n FP64 scratch of the level-1 product
+    int32_t* active = nullptr;          // level-1 cells holding particles (set up per solve)
+    int32_t* n_active = nullptr;
     DevStatus* status = nullptr;
 };
 

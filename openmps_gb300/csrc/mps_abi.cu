@@ -329,6 +329,8 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         const int64_t m = mg.lv[mg.levels].cells;
         mg.dense = dalloc<float>(h, m * m);
         mg.bins = dalloc<double>(h, 9 * n);
+        mg.active = dalloc<int32_t>(h, mg.lv[1].cells);
+        mg.n_active = dalloc<int32_t>(h, 1);
         mg.dinv0 = dalloc<float>(h, n);
         mg.n = static_cast<int32_t>(n);
         mg.max_per_cell = sc.max_per_cell;
