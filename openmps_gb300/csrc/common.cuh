@@ -44,7 +44,10 @@ struct SceneConst {
     int32_t nchunks;     // PPE chunks of kSellRows rows
     int32_t cells_per_scene;  // gnx * gnz: cells of one scene
     int32_t nscenes;          // scenes of a batch (1 for a single scene)
-    int32_t pad1;
+    // FP32 bounds of the FP64 range tests (range_class below): r^2 surely below nl2_lo
+    // under f32_in_nl, surely above nl2_hi / re^2 / re_lap^2 over the f32_out_* values
+    float f32_in_nl;
+    float f32_out_nl, f32_out_re, f32_out_rl, pad1;
     double l0, re, re2, re_lap, rl2;
     double nl, nl2_lo, nl2_hi;  // neighbour length and a guard band around nl^2
     double n0, lambda, n0_lap, lambda_lap;
@@ -83,6 +86,7 @@ struct DeviceState {
     double *n_wo_spp, *ecs, *ox, *oz, *dux, *duz;
     int32_t *cell_count, *cell_slot;
     int32_t* cell_xz;  // (cx << 16) | cz of each particle's cell at the last search, -1: none
+    float *x32, *z32;  // positions rounded to FP32 (range prefilter), rewritten with x, z
     const int32_t* scene_of;  // batch: scene of each particle (its cells start at
                               // scene * cells_per_scene); null for a single scene
     int32_t *nb_count, *nb;
@@ -109,6 +113,72 @@ __device__ __forceinline__ double weight(double r, double re) {
 }
 
 __device__ __forceinline__ bool has_flag(uint32_t flags, uint32_t f) { return (flags & f) != 0u; }
+
+// ------------------------------------------------- FP32 prefilter of the range tests
+// GB300 issues FP64 arithmetic at a small fraction of its FP32 rate, and most entries
+// of a neighbour row fail the r^2 < r_e^2 test of a stage.  A test on the FP32 copies of
+// the positions settles the clear cases with certainty and leaves only pairs in a thin
+// band around the threshold (its width set by the FP32 rounding of the coordinates) and
+// non-finite positions to the exact FP64 test, so every decision equals the FP64 one.
+//
+// Bound: with u = 2^-24 and x~ = fl32(x), |x - x~| <= u |x~| / (1 - u), and a = fl32(x~j -
+// x~i) gives |(xj - xi)| in [|a|(1 - u) - e, |a| / (1 - u) + e], e = 1.01 u (|x~i| + |x~j|).
+// E = 2^-22 (|x~i| + |z~i| + |x~j| + |z~j|) + 1e-36 covers e + u|a| for both axes (the
+// 1e-36 covers FP32 subnormal rounding), so r^2 lies in [ (|a| - E)+^2 + (|b| - E)+^2,
+// (|a| + E)^2 + (|b| + E)^2 ] up to four FP32 roundings (4 u relative).  The FP64 r^2 of
+// the stages (dx = xj - xi, dot2) is within 2^-50 of the exact value.  With FP32 bounds
+// set 2^-20 inside (in) or outside (out) of the FP64 threshold, "in" implies FP64 r^2 <
+// threshold and "out" implies FP64 r^2 > threshold.  NaN and infinity fall through to
+// the FP64 test (comparisons false, fmaxf drops NaN).
+__device__ __forceinline__ float range_slack(float sum_abs) {
+    return sum_abs * 2.384185791015625e-07f + 1e-36f;  // 2^-22
+}
+
+// Lower bound of r^2 (FP32) for the pair; `out` when it exceeds `out_thr`.
+__device__ __forceinline__ bool surely_out(float xi, float zi, float si, float xj, float zj,
+                                           float out_thr) {
+    const float e = range_slack(si + (fabsf(xj) + fabsf(zj)));
+    const float lx = fmaxf(fabsf(xj - xi) - e, 0.0f);
+    const float lz = fmaxf(fabsf(zj - zi) - e, 0.0f);
+    return lx * lx + lz * lz > out_thr;
+}
+
+// 1: FP64 r^2 < the lower threshold for sure; 0: FP64 r^2 > the upper threshold for
+// sure; 2: undecided (exact FP64 test).
+__device__ __forceinline__ int range_class(float xi, float zi, float si, float xj, float zj,
+                                           float in_thr, float out_thr) {
+    const float e = range_slack(si + (fabsf(xj) + fabsf(zj)));
+    const float ax = fabsf(xj - xi), az = fabsf(zj - zi);
+    const float hx = ax + e, hz = az + e;
+    if (hx * hx + hz * hz < in_thr) return 1;
+    const float lx = fmaxf(ax - e, 0.0f), lz = fmaxf(az - e, 0.0f);
+    return (lx * lx + lz * lz > out_thr) ? 0 : 2;
+}
+
+// Calls f(j) for the entries of row i that may pass the FP64 range test whose FP32
+// upper bound is `out_thr`, in list order.  Entries are screened 32 at a time into a
+// bit mask first, so the FP64 work of a warp runs once per candidate of its busiest lane
+// rather than once per list entry.
+template <class F>
+__device__ __forceinline__ void for_near(const SceneConst& sc, const DeviceState& st, int i,
+                                         float out_thr, F f) {
+    const float xi = st.x32[i], zi = st.z32[i];
+    const float si = fabsf(xi) + fabsf(zi);
+    const int cnt = st.nb_count[i];
+    for (int base = 0; base < cnt; base += 32) {
+        const int m = min(32, cnt - base);
+        unsigned mask = 0u;
+        for (int t = 0; t < m; t++) {
+            const int j = st.nb[static_cast<int64_t>(base + t) * sc.n + i];
+            if (!surely_out(xi, zi, si, st.x32[j], st.z32[j], out_thr)) mask |= 1u << t;
+        }
+        while (mask) {
+            const int t = __ffs(static_cast<int>(mask)) - 1;
+            mask &= mask - 1u;
+            f(st.nb[static_cast<int64_t>(base + t) * sc.n + i]);
+        }
+    }
+}
 
 // A cell overflow or a failed bounds check ends the step after the search
 // (the reference throws from Grid::Store, Grid.hpp:314-318).
@@ -152,6 +222,7 @@ void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s);
+void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // stages.cu
 void launch_set_dt(const SceneConst& sc, const DeviceState& st, double dt, cudaStream_t s);
 void launch_cfl_dt(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

@@ -21,6 +21,8 @@ namespace mpsgb {
 __global__ void k_bucket(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
+    st.x32[i] = __double2float_rn(st.x[i]);
+    st.z32[i] = __double2float_rn(st.z[i]);
     st.cell_xz[i] = -1;
     if (st.type[i] == MPS_TYPE_DISABLED) {
         atomicAdd(&st.status->disabled, 1);
@@ -81,8 +83,11 @@ __global__ void k_cell_sort(SceneConst sc, DeviceState st) {
 
 // Neighbour rows: the nine cells in Grid::Iterator order (Grid.hpp:393-401), each in
 // slot order, keeping j != i with R(x_i, x_j) < NeighborLength (Computer.hpp:740-749).
+// The FP32 range class settles almost every candidate; the rest take the FP64 test.
 __device__ __forceinline__ int neighbor_row(const SceneConst& sc, const DeviceState& st, int i) {
     const double xi = st.x[i], zi = st.z[i];
+    const float xi32 = st.x32[i], zi32 = st.z32[i];
+    const float si32 = fabsf(xi32) + fabsf(zi32);
     const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
     const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
     const int base = st.scene_of ? st.scene_of[i] * sc.cells_per_scene : 0;
@@ -99,16 +104,20 @@ __device__ __forceinline__ int neighbor_row(const SceneConst& sc, const DeviceSt
             for (int l = 0; l < m; l++) {
                 const int j = slots[l];
                 if (j == i) continue;
-                const double dx = __dadd_rn(xi, -st.x[j]);
-                const double dz = __dadd_rn(zi, -st.z[j]);
-                const double r2 = dot2(dx, dz, dx, dz);
-                bool inside;
-                if (r2 < sc.nl2_lo) {
-                    inside = true;
-                } else if (r2 > sc.nl2_hi) {
-                    inside = false;
-                } else {
-                    inside = __dsqrt_rn(r2) < sc.nl;
+                const int cls = range_class(xi32, zi32, si32, st.x32[j], st.z32[j], sc.f32_in_nl,
+                                            sc.f32_out_nl);
+                bool inside = cls == 1;
+                if (cls == 2) {
+                    const double dx = __dadd_rn(xi, -st.x[j]);
+                    const double dz = __dadd_rn(zi, -st.z[j]);
+                    const double r2 = dot2(dx, dz, dx, dz);
+                    if (r2 < sc.nl2_lo) {
+                        inside = true;
+                    } else if (r2 > sc.nl2_hi) {
+                        inside = false;
+                    } else {
+                        inside = __dsqrt_rn(r2) < sc.nl;
+                    }
                 }
                 if (inside) {
                     if (cnt < sc.nb_stride) {
@@ -143,6 +152,18 @@ __global__ void k_status_counters_reset(DevStatus* st) {
 }
 
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s) { k_status_counters_reset<<<1, 32, 0, s>>>(st); }
+
+// FP32 copies of the positions after a host write of x, z.
+__global__ void k_positions_f32(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    st.x32[i] = __double2float_rn(st.x[i]);
+    st.z32[i] = __double2float_rn(st.z[i]);
+}
+
+void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_positions_f32<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
 
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     k_bucket<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);

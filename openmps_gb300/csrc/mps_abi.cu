@@ -191,6 +191,18 @@ void validate(const mps_params& p) {
         bad("unknown cg_launch");
 }
 
+// FP32 bound for the prefilter of an FP64 range threshold t (device side: range_class):
+// t (1 - 2^-20) rounded down, or t (1 + 2^-20) rounded up.  Thresholds outside
+// [1e-30, 1e30] disable the screen (nothing is surely in or surely out).
+float f32_bound(double t, bool upper) {
+    if (!(t >= 1e-30 && t <= 1e30)) return upper ? INFINITY : -1.0f;
+    const double v = upper ? t * (1.0 + 0x1p-20) : t * (1.0 - 0x1p-20);
+    float f = static_cast<float>(v);
+    if (upper && static_cast<double>(f) < v) f = std::nextafter(f, INFINITY);
+    if (!upper && static_cast<double>(f) > v) f = std::nextafter(f, 0.0f);
+    return f;
+}
+
 void setup_constants(mps_handle* h) {
     const mps_params& p = h->prm;
     SceneConst& sc = h->sc;
@@ -205,6 +217,11 @@ void setup_constants(mps_handle* h) {
     sc.nl = std::max(re_by, rl_by) * p.l0 * (1 + p.courant * 2);  // Environment.hpp:161
     sc.nl2_lo = (sc.nl * (1.0 - 1e-12)) * (sc.nl * (1.0 - 1e-12));
     sc.nl2_hi = (sc.nl * (1.0 + 1e-12)) * (sc.nl * (1.0 + 1e-12));
+    sc.f32_in_nl = f32_bound(sc.nl2_lo, false);
+    sc.f32_out_nl = f32_bound(sc.nl2_hi, true);
+    sc.f32_out_re = f32_bound(sc.re2, true);
+    sc.f32_out_rl = f32_bound(sc.rl2, true);
+    sc.pad1 = 0.0f;
     lattice_constants(re_by, p.l0, sc.n0, sc.lambda);
     lattice_constants(rl_by, p.l0, sc.n0_lap, sc.lambda_lap);
     sc.rho = p.rho;
@@ -311,6 +328,8 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     h->u32 = dalloc<float>(h, n);
     h->S_fb = dalloc<CgScalars>(h, 1);
     st.cell_xz = dalloc<int32_t>(h, n);
+    st.x32 = dalloc<float>(h, n);
+    st.z32 = dalloc<float>(h, n);
     // multigrid hierarchy over the search cells (level sizes fixed by the domain)
     MgHierarchy& mg = h->mg;
     mg = MgHierarchy{};
@@ -1081,6 +1100,8 @@ int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const doubl
         upload(h, st.w + old, w, b8, false);
         upload(h, st.p + old, p, b8, false);
         upload(h, st.nd + old, nd, b8, false);
+        launch_positions_f32(h->sc, st, h->stream);
+        launched(h, 1);
         check(cudaStreamSynchronize(h->stream), "add particles");
     });
 }
@@ -1116,6 +1137,8 @@ static int set_particles_impl(mps_handle* h, const int32_t* type, const double* 
         upload(h, st.w, w, sizeof(double) * n, device);
         upload(h, st.p, p, sizeof(double) * n, device);
         upload(h, st.nd, nd, sizeof(double) * n, device);
+        launch_positions_f32(h->sc, st, h->stream);
+        launched(h, 1);
         if (!device) check(cudaStreamSynchronize(h->stream), "set particles");
     });
 }
@@ -1766,6 +1789,8 @@ int mps_batch_set_scene(mps_handle* h, int32_t scene, const int32_t* type, const
         upload(h, st.w + r0, w, b8, false);
         upload(h, st.p + r0, p, b8, false);
         upload(h, st.nd + r0, nd, b8, false);
+        launch_positions_f32(h->sc, st, h->stream);
+        launched(h, 1);
         check(cudaStreamSynchronize(h->stream), "batch scene");
     });
 }

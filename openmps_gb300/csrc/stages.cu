@@ -5,7 +5,9 @@
 //
 // One thread per particle walks its neighbour row in reference order and accumulates
 // exactly like AccumulateNeighbor (Computer.hpp:618-695): the filter r^2 < r_e^2 on
-// current positions, the terms in list order, the SPP virtual particle last.  Every
+// current positions, the terms in list order, the SPP virtual particle last.  The
+// filter runs in two steps (for_near): an FP32 screen that drops entries surely out of
+// range, then the reference's FP64 test on the rest, which decides as before.  Every
 // formula keeps the reference's expression order and this file is compiled with
 // -fmad=false, so each result is bit-identical to the FP64 CPU path.
 #include "common.cuh"
@@ -46,10 +48,8 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
     if (has_flag(sc.flags, MPS_FLAG_HS)) {
         if (has_flag(sc.flags, MPS_FLAG_SPP) && st.n_wo_spp[i] < sc.n0) return 0.0;
         const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
-        const int cnt = st.nb_count[i];
         double sum = 0.0;
-        for (int k = 0; k < cnt; k++) {
-            const int j = st.nb[ell(k, sc.n, i)];
+        for_near(sc, st, i, sc.f32_out_re, [&](int j) {
             const double dx = st.x[j] - xi;
             const double dz = st.z[j] - zi;
             const double r2 = dot2(dx, dz, dx, dz);
@@ -59,7 +59,7 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
                 const double r = __dsqrt_rn(r2);
                 sum += dot2(dx, dz, du, dw) / (r * r * r);
             }
-        }
+        });
         return -sc.re * sum;
     }
     return (st.nd[i] - sc.n0) / dt;
@@ -132,15 +132,13 @@ __global__ void k_density(SceneConst sc, DeviceState st) {
     const int t = st.type[i];
     if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
     const double xi = st.x[i], zi = st.z[i];
-    const int cnt = st.nb_count[i];
     double thisN = 0.0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = st.nb[ell(k, sc.n, i)];
+    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dot2(dx, dz, dx, dz);
         if (r2 < sc.re2) thisN += weight(__dsqrt_rn(r2), sc.re);
-    }
+    });
     if (spp) {
         st.n_wo_spp[i] = thisN;
         st.nd[i] = (thisN < sc.n0) ? sc.n0 : thisN;  // std::max(thisN, n0)
@@ -178,10 +176,8 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     if (st.type[i] != MPS_TYPE_FLUID) return;
     const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
-    const int cnt = st.nb_count[i];
     double vx = 0.0, vz = 0.0, gx = 0.0, gz = 0.0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = st.nb[ell(k, sc.n, i)];
+    for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dot2(dx, dz, dx, dz);
@@ -200,7 +196,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
                 gz += wg * dz;
             }
         }
-    }
+    });
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
@@ -223,14 +219,20 @@ __global__ void k_explicit_update(SceneConst sc, DeviceState st) {
         const double w = st.w[i] + st.duz[i] * dt;
         st.u[i] = u;
         st.w[i] = w;
-        st.x[i] = st.x[i] + u * dt;
-        st.z[i] = st.z[i] + w * dt;
+        const double x = st.x[i] + u * dt;
+        const double z = st.z[i] + w * dt;
+        st.x[i] = x;
+        st.z[i] = z;
+        st.x32[i] = __double2float_rn(x);
+        st.z32[i] = __double2float_rn(z);
     } else {
         const double nx = st.wall_x[i], nz = st.wall_z[i];
         st.u[i] = (nx - st.x[i]) / dt;
         st.w[i] = (nz - st.z[i]) / dt;
         st.x[i] = nx;
         st.z[i] = nz;
+        st.x32[i] = __double2float_rn(nx);
+        st.z32[i] = __double2float_rn(nz);
     }
 }
 
@@ -273,11 +275,9 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     st.ppe_x[i] = st.p[i];
 
     const double xi = st.x[i], zi = st.z[i];
-    const int cnt = st.nb_count[i];
     double a_ii = 0.0, gx = 0.0, gz = 0.0;
     int m = 0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = st.nb[ell(k, n, i)];
+    for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dot2(dx, dz, dx, dz);
@@ -299,7 +299,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
                 gz += wg * dz;
             }
         }
-    }
+    });
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
@@ -368,10 +368,8 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     const double dt = st.step->dt;
     const double factor = -dt / sc.rho * 2.0 / sc.n0;
     const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
-    const int cnt = st.nb_count[i];
     double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = st.nb[ell(k, sc.n, i)];
+    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dot2(dx, dz, dx, dz);
@@ -390,7 +388,7 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
                 gz += wg * dz;
             }
         }
-    }
+    });
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
         const double dx = xs - xi;
@@ -416,10 +414,8 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const double d2 = d * d;
     const double factor = -1.0 / (2 * dt * sc.n0);
     const double xi = st.x[i], zi = st.z[i], oxi = st.ox[i], ozi = st.oz[i];
-    const int cnt = st.nb_count[i];
     double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = st.nb[ell(k, sc.n, i)];
+    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dot2(dx, dz, dx, dz);
@@ -447,7 +443,7 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
                 gz += wg * dz;
             }
         }
-    }
+    });
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
         sx = __dadd_rn(sx, 0.0);  // the virtual particle is excluded (Computer.hpp:1597-1598)
@@ -467,8 +463,12 @@ __global__ void k_apply_du(SceneConst sc, DeviceState st) {
     const double dx = st.dux[i], dz = st.duz[i];
     st.u[i] = st.u[i] + dx;
     st.w[i] = st.w[i] + dz;
-    st.x[i] = st.x[i] + dx * dt;
-    st.z[i] = st.z[i] + dz * dt;
+    const double x = st.x[i] + dx * dt;
+    const double z = st.z[i] + dz * dt;
+    st.x[i] = x;
+    st.z[i] = z;
+    st.x32[i] = __double2float_rn(x);
+    st.z32[i] = __double2float_rn(z);
 }
 
 }  // namespace

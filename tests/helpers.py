@@ -100,3 +100,49 @@ def jittered_tank(l0=0.01, jitter=0.05, seed=7, preset=abi.PRESET_PLAIN):
     s.meta["params"] = params
     s.meta["dt"] = 5e-4
     return s
+
+
+def far_tank(offset=(3071.37, -2047.13)):
+    """The stock two-radius tank moved far from the origin: FP32 copies of its coordinates
+    lose about 1e-4 m, so the FP32 range screen leaves many pairs to the FP64 test."""
+    s = stock_tank()
+    ox, oz = offset
+    s.x = s.x + ox
+    s.z = s.z + oz
+    s.min_x += ox
+    s.max_x += ox
+    s.min_z += oz
+    s.max_z += oz
+    return s
+
+
+def threshold_rings(l0=0.01, seed=5):
+    """A fluid particle with rings of neighbours at distances within a few ulps to 1e-5
+    (relative) of r_e, the Laplacian radius and the neighbour length, on both sides:
+    every range test of the step meets pairs that only the FP64 comparison decides."""
+    base = stock_tank()
+    prm = dict(base.meta["params"])
+    re = prm.get("re_by_l0", 2.1) * l0
+    rl = prm.get("re_lap_by_l0", 4.0) * l0
+    nl = max(re, rl) * (1 + 2 * prm.get("courant", 0.1))
+    rng = np.random.default_rng(seed)
+    deltas = [-1e-5, -1e-7, -1e-9, -1e-12, -4e-16, 0.0, 4e-16, 1e-12, 1e-9, 1e-7, 1e-5]
+    xc, zc = 0.3719, 0.2903
+    xs, zs = [xc], [zc]
+    for radius in (re, rl, nl):
+        k = len(deltas) * 3
+        for a in range(k):
+            th = 2 * np.pi * (a + 0.5 * rng.random()) / k
+            d = radius * (1 + deltas[a % len(deltas)])
+            xs.append(xc + d * np.cos(th))
+            zs.append(zc + d * np.sin(th))
+    n = len(xs)
+    t = np.full(n, abi.TYPE_FLUID, dtype=np.int32)
+    u = rng.normal(size=n) * 0.05
+    w = rng.normal(size=n) * 0.05
+    s = scenes.Scene(name="threshold_rings", type=t, x=np.array(xs), z=np.array(zs), u=u, w=w,
+                     p=np.zeros(n), n=np.zeros(n), l0=l0, min_x=0.0, min_z=0.0, max_x=0.8,
+                     max_z=0.6)
+    s.meta["params"] = prm
+    s.meta["dt"] = base.meta.get("dt", 5e-4)
+    return s

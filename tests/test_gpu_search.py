@@ -9,7 +9,8 @@ disabled because they left the domain.
 import numpy as np
 import pytest
 
-from helpers import assert_same_neighbors, jittered_tank, make_pair, plain_tank, reference_tank
+from helpers import (assert_same_neighbors, far_tank, jittered_tank, make_pair, plain_tank,
+                     reference_tank, threshold_rings)
 from openmps_gb300 import _abi as abi
 from openmps_gb300 import scenes
 
@@ -35,7 +36,7 @@ def test_unit_lattice(gpu_lib, oracle_lib):
     assert counts.reshape(7, 7)[3, 3] == 20
 
 
-@pytest.mark.parametrize("maker", [plain_tank, reference_tank, jittered_tank])
+@pytest.mark.parametrize("maker", [plain_tank, reference_tank, jittered_tank, far_tank, threshold_rings])
 def test_tanks(gpu_lib, oracle_lib, maker):
     s = maker()
     gpu, cpu = make_pair(s, s.params())

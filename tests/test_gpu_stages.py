@@ -11,7 +11,8 @@ import numpy as np
 import pytest
 
 from helpers import (assert_same_neighbors, assert_same_particles, assert_same_ppe, copy_state,
-                     jittered_tank, make_pair, plain_tank, reference_tank, stock_tank)
+                     far_tank, jittered_tank, make_pair, plain_tank, reference_tank, stock_tank,
+                     threshold_rings)
 from openmps_gb300 import _abi as abi
 
 pytestmark = pytest.mark.gpu
@@ -23,6 +24,7 @@ CASES = {
     "jittered_reference": lambda: jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
     "jittered_plain": lambda: jittered_tank(jitter=0.1),
     "stock_two_radii": stock_tank,
+    "stock_far_from_origin": far_tank,
 }
 
 
@@ -98,6 +100,45 @@ def test_stage_chain(gpu_lib, oracle_lib, case, warm_steps):
         for h in (gpu, cpu):
             h.stage("dynamic_stabilize")
         assert_same_particles(gpu, cpu, what="dynamic stabilisation")
+
+
+def test_range_tests_at_thresholds(gpu_lib, oracle_lib):
+    # pairs within 4e-16 .. 1e-5 (relative) of r_e, the Laplacian radius and the
+    # neighbour length: the FP32 screen must leave each of them to the FP64 comparison
+    s = threshold_rings()
+    gpu, cpu = make_pair(s, s.params())
+    dt = s.meta["dt"]
+    for h in (gpu, cpu):
+        h.begin_step(dt)
+        h.stage("search_neighbor")
+    assert_same_neighbors(gpu, cpu, "search")
+    counts, _ = gpu.neighbors()
+    assert counts[0] > 0 and counts[0] < s.count - 1  # the outer ring is split by the test
+    for h in (gpu, cpu):
+        h.stage("density")
+    assert_same_particles(gpu, cpu, what="density")
+    np.testing.assert_array_equal(gpu.density_variation(), cpu.density_variation())
+    for h in (gpu, cpu):
+        h.stage("error_correction")
+    np.testing.assert_array_equal(gpu.aux()["ecs"], cpu.aux()["ecs"])
+    for h in (gpu, cpu):
+        h.stage("explicit")
+    assert_same_particles(gpu, cpu, what="explicit")
+    for h in (gpu, cpu):
+        h.stage("density")
+        h.stage("save_x")
+        h.stage("set_ppe")
+    assert_same_ppe(gpu, cpu, "assembly")
+    # pressure gradient and stabilisation from the same pressure on both sides
+    p = np.linspace(0.0, 50.0, s.count)
+    gpu.set_particles(p=p)
+    cpu.set_particles(p=p)
+    for h in (gpu, cpu):
+        h.stage("pressure_gradient")
+    assert_same_particles(gpu, cpu, what="pressure gradient")
+    for h in (gpu, cpu):
+        h.stage("dynamic_stabilize")
+    assert_same_particles(gpu, cpu, what="dynamic stabilisation")
 
 
 def test_cfl_time_step(gpu_lib, oracle_lib):
