@@ -11,12 +11,15 @@
 //                memory, symmetrised).
 // Cycle, once per iteration (FP32, reads L2-resident planes):
 //   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
-//   and after a reliable update k_mg_restrict0), k_mg_down (levels above the bottom),
-//   k_mg_bottom (the coarsest levels in one block, all in shared memory, __syncthreads
-//   between levels), k_mg_up, k_mg_up_prolong (level-1 post-smoothing + prolongation to
-//   the particles).
+//   and after a reliable update k_mg_restrict0), k_mg_down (level 1 to level 2),
+//   k_mg_middle (levels 2 .. coarsest and back in one thread-block cluster, cluster
+//   barriers between the levels), k_mg_up_prolong (level-1 post-smoothing + prolongation
+//   to the particles).  Hierarchies small enough for one block's shared memory run
+//   k_mg_bottom (all levels, __syncthreads between them) and k_mg_prolong0 instead.
 // Every kernel reads only what the previous kernel wrote, so the sequence captures into
 // the solver's CUDA graph unchanged.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 #include "mg.cuh"
@@ -255,13 +258,6 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
     c.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz, I - (I / c.nz) * c.nz);
 }
 
-__global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
-    if (pcg_skip(S, mode)) return;
-    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ch >= f.cells) return;
-    f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
-}
-
 // Level-1 post-smoothing fused with the prolongation to the particles of the cell:
 // u = s_i dinv0_i r_i + e_1 on active rows, 0 on identity rows (one warp per cell).
 __global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_count,
@@ -293,6 +289,47 @@ struct MgBottom {
     MgLevel lv[kMgMaxLevels + 1];
     const float* dense;
 };
+
+// Levels first..last and back up in one cluster of thread blocks: the levels below the
+// search cells are small (level 2 of a 340k-particle scene has 21k cells), so a cluster
+// barrier between levels replaces a kernel boundary each.  Vectors that other blocks
+// wrote are read through L2; coefficient planes and the dense inverse are read-only here.
+__global__ void __launch_bounds__(kMgMiddleThreads) k_mg_middle(MgBottom B, const CgScalars* S,
+                                                                int mode) {
+    if (pcg_skip(S, mode)) return;  // same decision in every thread of the cluster
+    cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+    const int nt = static_cast<int>(gridDim.x * blockDim.x);
+    const int gt = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    for (int l = B.first; l < B.last; l++) {
+        const MgLevel& f = B.lv[l];
+        const MgLevel& c = B.lv[l + 1];
+        for (int I = gt; I < c.cells; I += nt)
+            c.r[I] = child_residuals<true>(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz,
+                                           I - (I / c.nz) * c.nz);
+        cluster.sync();
+    }
+    {
+        const MgLevel& Lc = B.lv[B.last];
+        const int m = Lc.cells;
+        const int lane = threadIdx.x & 31;
+        for (int row = gt >> 5; row < m; row += nt >> 5) {
+            float v = 0.0f;
+            for (int k = lane; k < m; k += 32) v += B.dense[row * m + k] * __ldcg(Lc.r + k);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) Lc.e[row] = v;
+        }
+    }
+    for (int l = B.last - 1; l >= B.first; l--) {
+        cluster.sync();
+        const MgLevel& f = B.lv[l];
+        const int cnz = B.lv[l + 1].nz;
+        for (int ch = gt; ch < f.cells; ch += nt)
+            f.e[ch] = smoothed_correction<true>(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, cnz,
+                                                B.lv[l + 1].e, ch);
+    }
+}
+
+int g_middle_cluster = 0;  // blocks of the k_mg_middle cluster (set by mg_prepare_device)
 
 // Levels first..last in one block, everything in shared memory: per level the nine
 // coefficient planes, dinv, r and e, then the dense inverse of the last level.
@@ -409,8 +446,32 @@ cudaError_t mg_prepare_device() {
     const int dense_max = (kMgDenseCells * kMgDenseCells + kMgDenseCells + 1) * static_cast<int>(sizeof(float));
     cudaError_t e = cudaFuncSetAttribute(k_mg_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, dense_max);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kMgBottomBytes));
+    e = cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kMgBottomBytes));
+    if (e != cudaSuccess) return e;
+    // the widest cluster that can be resident: 16 blocks (non-portable size), else 8
+    e = cudaFuncSetAttribute(k_mg_middle, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    g_middle_cluster = 0;
+    for (int c : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c);
+        cfg.blockDim = dim3(kMgMiddleThreads);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = c;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_mg_middle, &cfg) == cudaSuccess && clusters > 0) {
+            g_middle_cluster = c;
+            break;
+        }
+        cudaGetLastError();
+    }
+    return g_middle_cluster > 0 ? cudaSuccess : cudaErrorNotSupported;
 }
 
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
@@ -439,16 +500,29 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     else
         k_mg_restrict0<<<g1, kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot, mg.max_per_cell, r, S, mode,
                                              mg.active, mg.n_active);
-    for (int l = 1; l < mg.bottom; l++)
-        k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
     MgBottom B{};
-    B.first = mg.bottom;
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
     B.dense = mg.dense;
-    k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, mg.bottom, mg.levels), s>>>(B, S, mode);
-    for (int l = mg.bottom - 1; l >= 2; l--)
-        k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+    if (mg.bottom > 1) {
+        k_mg_down<<<grid_for(mg.lv[2].cells), kBlock, 0, s>>>(mg.lv[1], mg.lv[2], S, mode);
+        B.first = 2;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g_middle_cluster);
+        cfg.blockDim = dim3(kMgMiddleThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = g_middle_cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_mg_middle, B, S, mode);
+    } else {
+        B.first = 1;
+        k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s>>>(B, S, mode);
+    }
     if (mg.bottom > 1)
         k_mg_up_prolong<<<g1, kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_count, mg.cell_slot, mg.max_per_cell,
                                               mg.dinv0, mg.scale, r, u, S, mode, mg.active, mg.n_active);
@@ -457,6 +531,6 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
                                                        r, L1.e, u, S, mode);
 }
 
-int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * mg.bottom : 3; }
+int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 4 : 3; }
 
 }  // namespace mpsgb

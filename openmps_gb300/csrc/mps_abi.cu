@@ -487,6 +487,10 @@ bool is_preconditioned(int32_t solver) {
 // A preconditioned solve that has not converged after this many iterations has stalled
 // (it needs tens); the FP64 CG fallback then runs with the reference's own limit.
 constexpr int kPcgMaxIter = 400;
+// Reliable-update thresholds on the squared residual norm: the FP32 recurrence is folded
+// into FP64 after a 10x drop in norm (plain FP32 CG, 1000+ iterations per solve) or a
+// ~30x drop (multigrid-preconditioned, ~70 iterations: less drift between updates).
+constexpr double kReliableDelta2 = 1e-2, kReliableDelta2Pcg = 1e-3;
 
 // Iteration limit: the reference stops after as many iterations as unknowns
 // (Computer.hpp:1392).  The mixed solver restarts its FP32 recursion at every reliable
@@ -622,7 +626,8 @@ void do_solve(mps_handle* h) {
         throw StatusError{MPS_ERR_STATE, "the PPE was assembled for the FP64 solver: assemble it again"};
     const bool pcg = is_preconditioned(solver);
     const int max_iter = default_max_iter(h->prm.max_cg_iters, h->n, solver);
-    launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter, 0.01, s);
+    launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, max_iter,
+                        pcg ? kReliableDelta2Pcg : kReliableDelta2, s);
     after_launch("cg configure");
     launched(h, 1);
     CgOperands fb{};
@@ -1277,7 +1282,7 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
         require_particles(h);
         cudaStream_t s = h->stream;
         CgOperands o = cg_operands(h);
-        launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1, 0.01, s);
+        launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1, kReliableDelta2, s);
         if (flush_bytes > 0 && h->flush_bytes < static_cast<size_t>(flush_bytes)) {
             if (h->flush_buf) cudaFree(h->flush_buf);
             h->flush_buf = nullptr;
@@ -1287,7 +1292,7 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
         }
         float total = 0.f;
         for (int32_t k = 0; k < reps; k++) {
-            launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1 << 30, 0.01, s);
+            launch_cg_configure(h->S, h->prm.eps, h->prm.criterion, 1 << 30, kReliableDelta2, s);
             if (flush_bytes > 0)
                 check(cudaMemsetAsync(h->flush_buf, k & 0xff, static_cast<size_t>(flush_bytes), s), "flush");
             check(cudaEventRecord(h->user_events[14], s), "event");
