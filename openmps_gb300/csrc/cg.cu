@@ -796,11 +796,9 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
     const int nact = *mg.n_active;
     for (int a = P.gwarp; a < nact; a += P.nwarps) {
         const int c = mg.active[a];
-        const int cnt = min(mg.cell_count[c], mg.max_per_cell);
-        const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
+        const int end = mg.cell_start[c + 1];
         float sum = 0.0f;
-        for (int s = P.lane; s < cnt; s += 32) {
-            const int i = slots[s];
+        for (int i = mg.cell_start[c] + P.lane; i < end; i += 32) {
             float ri = o.r32[i];
             if (axpy) {
                 const float si = fmaf(beta, o.s32[i], o.w32[i]);
@@ -845,11 +843,9 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
         const MgLevel& c2 = mg.lv[2];
         for (int a = P.gwarp; a < nact; a += P.nwarps) {
             const int c = mg.active[a];
-            const int cnt = min(mg.cell_count[c], mg.max_per_cell);
+            const int end = mg.cell_start[c + 1];
             const float e = smoothed_correction(L1.nx, L1.nz, L1.cells, L1.k32, L1.dinv, L1.r, c2.nz, c2.e, c);
-            const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
-            for (int s = P.lane; s < cnt; s += 32) {
-                const int i = slots[s];
+            for (int i = mg.cell_start[c] + P.lane; i < end; i += 32) {
                 const float d = mg.dinv0[i];
                 const float scl = mg.scale ? mg.scale[i] : 1.0f;
                 o.u32[i] = d != 0.0f ? scl * d * o.r32[i] + e : 0.0f;
@@ -857,11 +853,9 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
         }
     } else {
         for (int c = P.gwarp; c < L1.cells; c += P.nwarps) {
-            const int cnt = min(mg.cell_count[c], mg.max_per_cell);
-            const int32_t* slots = mg.cell_slot + static_cast<int64_t>(c) * mg.max_per_cell;
+            const int end = mg.cell_start[c + 1];
             const float e = L1.e[c];
-            for (int s = P.lane; s < cnt; s += 32) {
-                const int i = slots[s];
+            for (int i = mg.cell_start[c] + P.lane; i < end; i += 32) {
                 const float d = mg.dinv0[i];
                 const float scl = mg.scale ? mg.scale[i] : 1.0f;
                 o.u32[i] = d != 0.0f ? scl * d * o.r32[i] + e : 0.0f;

@@ -87,6 +87,18 @@ struct DeviceState {
     int32_t *cell_count, *cell_slot;
     int32_t* cell_xz;  // (cx << 16) | cz of each particle's cell at the last search, -1: none
     float *x32, *z32;  // positions rounded to FP32 (range prefilter), rewritten with x, z
+    // PPE row order of a single scene: particles sorted by search cell (slot order within
+    // a cell, particles without a cell slot last in index order), so the rows of a cell
+    // are contiguous: coalesced level-1 multigrid work and local SpMV gathers.  Null for a
+    // batch, whose rows stay in particle order.
+    int32_t* row_of;       // particle -> row
+    int32_t* particle_of;  // row -> particle
+    int32_t* row_cell;     // row -> (cx << 16) | cz of its cell, -1: none
+    int32_t* cell_fill;    // per cell: particles stored (count clipped to maxPerCell)
+    int32_t* cell_start;   // exclusive prefix sum of cell_fill (cells + 1 entries)
+    int32_t* unplaced;     // per particle: 1 without a cell slot
+    int32_t* unplaced_pos; // exclusive prefix sum of unplaced (n + 1 entries)
+    int32_t* row_scratch;  // scan scratch of the two prefix sums
     const int32_t* scene_of;  // batch: scene of each particle (its cells start at
                               // scene * cells_per_scene); null for a single scene
     int32_t *nb_count, *nb;
@@ -195,6 +207,9 @@ __device__ __forceinline__ int64_t ell(int k, int n, int i) {
     return static_cast<int64_t>(k) * n + i;
 }
 
+// PPE row of particle i.
+__device__ __forceinline__ int ppe_row(const DeviceState& st, int i) { return st.row_of ? st.row_of[i] : i; }
+
 // SELL-32: rows in chunks of 32 (one warp, one lane per row); entry k of the chunk's row
 // r sits at chunk_off + 32 k + r, so a warp's load at step k reads 32 consecutive
 // entries.  A chunk reserves 32 x (its longest row) entries.
@@ -221,6 +236,8 @@ inline int grid_for(int64_t n, int block = kBlock) {
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// PPE row order from the sorted cells (no-op for a batch); returns the kernels launched.
+int launch_rows(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s);
 void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // stages.cu

@@ -24,6 +24,7 @@ __global__ void k_bucket(SceneConst sc, DeviceState st) {
     st.x32[i] = __double2float_rn(st.x[i]);
     st.z32[i] = __double2float_rn(st.z[i]);
     st.cell_xz[i] = -1;
+    if (st.unplaced) st.unplaced[i] = 1;
     if (st.type[i] == MPS_TYPE_DISABLED) {
         atomicAdd(&st.status->disabled, 1);
         return;
@@ -38,10 +39,11 @@ __global__ void k_bucket(SceneConst sc, DeviceState st) {
     }
     const int base = st.scene_of ? st.scene_of[i] * sc.cells_per_scene : 0;
     const int cell = base + static_cast<int>(fx) * sc.gnz + static_cast<int>(fz);
-    st.cell_xz[i] = (static_cast<int>(fx) << 16) | static_cast<int>(fz);
     const int slot = atomicAdd(&st.cell_count[cell], 1);
     if (slot < sc.max_per_cell) {
         st.cell_slot[static_cast<int64_t>(cell) * sc.max_per_cell + slot] = i;
+        st.cell_xz[i] = (static_cast<int>(fx) << 16) | static_cast<int>(fz);
+        if (st.unplaced) st.unplaced[i] = 0;
     } else {
         atomicOr(&st.status->flags, kStatusCellOverflow);
     }
@@ -52,6 +54,7 @@ __global__ void k_cell_sort(SceneConst sc, DeviceState st) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= sc.cells_per_scene * sc.nscenes) return;
     const int cnt = min(st.cell_count[c], sc.max_per_cell);
+    if (st.cell_fill) st.cell_fill[c] = cnt;
     if (cnt < 2) return;
     int32_t* s = st.cell_slot + static_cast<int64_t>(c) * sc.max_per_cell;
     int buf[64];
@@ -142,6 +145,32 @@ __global__ void k_neighbors(SceneConst sc, DeviceState st) {
     warp_add_u64(&st.status->nb_total, static_cast<unsigned long long>(cnt));
 }
 
+// Rows of the PPE: cell c's particles take rows cell_start[c] .. in slot order, particles
+// without a slot follow all of them in index order.  Threads [0, cells) walk the cells,
+// the rest the particles.
+__global__ void k_rows(SceneConst sc, DeviceState st, int cells) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cells) {
+        const int fill = st.cell_fill[t];
+        const int r0 = st.cell_start[t];
+        const int code = ((t / sc.gnz) << 16) | (t - (t / sc.gnz) * sc.gnz);
+        const int32_t* slots = st.cell_slot + static_cast<int64_t>(t) * sc.max_per_cell;
+        for (int k = 0; k < fill; k++) {
+            const int i = slots[k];
+            st.row_of[i] = r0 + k;
+            st.particle_of[r0 + k] = i;
+            st.row_cell[r0 + k] = code;
+        }
+        return;
+    }
+    const int i = t - cells;
+    if (i >= sc.n || !st.unplaced[i]) return;
+    const int r = st.cell_start[cells] + st.unplaced_pos[i];
+    st.row_of[i] = r;
+    st.particle_of[r] = i;
+    st.row_cell[r] = -1;
+}
+
 // Zeroes the per-step counters of the status block and keeps its failure flags.
 __global__ void k_status_counters_reset(DevStatus* st) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -175,6 +204,15 @@ void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t 
 
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     k_neighbors<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+int launch_rows(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    if (!st.row_of) return 0;
+    const int cells = sc.cells_per_scene;
+    launch_exclusive_scan(st.cell_fill, st.cell_start, cells, st.row_scratch, s);
+    launch_exclusive_scan(st.unplaced, st.unplaced_pos, sc.n, st.row_scratch, s);
+    k_rows<<<grid_for(static_cast<int64_t>(cells) + sc.n), kBlock, 0, s>>>(sc, st, cells);
+    return 7;
 }
 
 }  // namespace mpsgb

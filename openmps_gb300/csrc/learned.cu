@@ -273,19 +273,20 @@ __global__ void __launch_bounds__(kBlock) k_lrn_q(LearnedOps L, CgOperands o, co
     if (lrn_skip(S)) return;
     const double dt = step->dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += gridDim.x * blockDim.x) {
-        const double dev = (L.nd[i] - L.n0) / L.n0;
+        const int q = L.particle_of ? L.particle_of[i] : i;  // row i holds particle q
+        const double dev = (L.nd[q] - L.n0) / L.n0;
         double surf;
         if (L.flags & MPS_FLAG_SPP) {
-            surf = (L.n0 - L.n_wo_spp[i]) / L.n0;
+            surf = (L.n0 - L.n_wo_spp[q]) / L.n0;
         } else {
-            surf = (L.n0 - L.nd[i]) / L.n0;
+            surf = (L.n0 - L.nd[q]) / L.n0;
         }
         surf = surf > 0.0 ? surf : 0.0;
         const float src = static_cast<float>(o.b[i] * dt * dt / L.rho);
-        const float wall = L.type[i] == MPS_TYPE_WALL ? 1.0f : 0.0f;
+        const float wall = L.type[q] == MPS_TYPE_WALL ? 1.0f : 0.0f;
         q4[i] = make_float4(static_cast<float>(dev), src, static_cast<float>(surf), wall);
         const float g = dinv0[i] * o.r32[i];
-        q2[i] = make_float2(g, static_cast<float>(L.p[i] * dt * dt / L.rho_l02));
+        q2[i] = make_float2(g, static_cast<float>(L.p[q] * dt * dt / L.rho_l02));
     }
 }
 
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(kBlock) k_lrn_features(LearnedOps L, CgOperand
             f[12] = static_cast<float>(len) / len_ref - 1.0f;
             f[13] = b.y;
             f[14] = s5 * inv - b.y;
-            f[15] = static_cast<float>(L.ecs[i] * dt);
+            f[15] = static_cast<float>(L.ecs[L.particle_of ? L.particle_of[i] : i] * dt);
             g2 += static_cast<double>(b.x) * b.x;
             cnt += 1.0;
         }

@@ -59,6 +59,7 @@ struct LearnedOps {
     float len_ref = 1;
     const double *nd = nullptr, *n_wo_spp = nullptr, *ecs = nullptr, *p = nullptr;
     const int32_t* type = nullptr;
+    const int32_t* particle_of = nullptr;  // PPE row -> particle (null: the same index)
     const StepScalars* step = nullptr;
     const float* dinv0 = nullptr;  // the multigrid's omega_0 / a_ii
     uint32_t flags = 0;

@@ -90,26 +90,29 @@ __device__ __forceinline__ void store_level(const MgLevel& L, int c, const doubl
     L.dinv[c] = k[4] < 0.0 ? omega / static_cast<float>(k[4]) : 0.0f;
 }
 
-// Level-1 operator: per search cell, the bins of its particles in slot order.
-__global__ void k_mg_cells(MgLevel L1, const int32_t* cell_count, const int32_t* cell_slot,
-                           int max_per_cell, const double* bins, int n, float omega,
-                           const DevStatus* status, int32_t* active, int32_t* n_active) {
-    if (setup_failed(status)) return;
+// Level-1 operator: per search cell, the bins of its rows in order.
+__global__ void k_mg_cells(MgLevel L1, const int32_t* cell_start, const double* bins, int n, float omega,
+                           const DevStatus* status, int32_t* active_flag) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= L1.cells) return;
-    const int cnt = min(cell_count[c], max_per_cell);
-    // cells holding particles, in any order (every cell's work below is independent)
-    if (cnt > 0) active[atomicAdd(n_active, 1)] = c;
-    const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+    const int b = cell_start[c], e = cell_start[c + 1];
+    active_flag[c] = (e > b && !setup_failed(status)) ? 1 : 0;
+    if (setup_failed(status)) return;
     double k[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) k[q] = 0.0;
-    for (int s = 0; s < cnt; s++) {
-        const int i = slots[s];
+    for (int i = b; i < e; i++) {
 #pragma unroll
         for (int q = 0; q < 9; q++) k[q] += bins[static_cast<int64_t>(q) * n + i];
     }
     store_level(L1, c, k, omega);
+}
+
+// The list of level-1 cells holding particles, in ascending cell order (neighbouring
+// warps of the cycle kernels then work on neighbouring cells).
+__global__ void k_mg_active(int cells, const int32_t* flag, const int32_t* pos, int32_t* active) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < cells && flag[c]) active[pos[c]] = c;
 }
 
 // Galerkin product of the 2 x 2 aggregation of level f into level c (FP64).
@@ -195,10 +198,9 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
 }
 
 // --------------------------------------------------------------------- cycle
-// Level-1 residual: per search cell, the sum of its particles' residuals (one warp per
-// cell, lanes over the slots, fixed-order shuffle sum).
-__global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_count,
-                                                         const int32_t* cell_slot, int max_per_cell,
+// Level-1 residual: per search cell, the sum of its rows' residuals (one warp per
+// cell, lanes over the rows, fixed-order shuffle sum).
+__global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_start,
                                                          const float* r, const CgScalars* S, int mode,
                                                          const int32_t* active, const int32_t* n_active) {
     if (pcg_skip(S, mode)) return;
@@ -207,10 +209,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32
     const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
     for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
         const int c = active[a];
-        const int cnt = min(cell_count[c], max_per_cell);
-        const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+        const int e = cell_start[c + 1];
         float sum = 0.0f;
-        for (int s = lane; s < cnt; s += 32) sum += r[slots[s]];
+        for (int i = cell_start[c] + lane; i < e; i += 32) sum += r[i];
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
         if (lane == 0) L1.r[c] = sum;
     }
@@ -220,9 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32
 // s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s for the particles of each
 // cell (particles outside every cell are identity rows whose vectors stay zero).
 __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1,
-                                                             const int32_t* cell_count,
-                                                             const int32_t* cell_slot,
-                                                             int max_per_cell, const int32_t* active,
+                                                             const int32_t* cell_start, const int32_t* active,
                                                              const int32_t* n_active) {
     if (pcg_skip(o.S, 1)) return;
     const int lane = threadIdx.x & 31;
@@ -232,11 +231,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLev
     const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
     for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
         const int c = active[a];
-        const int cnt = min(cell_count[c], max_per_cell);
-        const int32_t* slots = cell_slot + static_cast<int64_t>(c) * max_per_cell;
+        const int e = cell_start[c + 1];
         float sum = 0.0f;
-        for (int s = lane; s < cnt; s += 32) {
-            const int i = slots[s];
+        for (int i = cell_start[c] + lane; i < e; i += 32) {
             const float si = fmaf(beta, o.s32[i], o.w32[i]);
             const float pi = fmaf(beta, o.p32[i], o.u32[i]);
             const float ri = fmaf(-alpha, si, o.r32[i]);
@@ -260,8 +257,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
 
 // Level-1 post-smoothing fused with the prolongation to the particles of the cell:
 // u = s_i dinv0_i r_i + e_1 on active rows, 0 on identity rows (one warp per cell).
-__global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_count,
-                                                          const int32_t* cell_slot, int max_per_cell,
+__global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_start,
                                                           const float* dinv0, const float* scale,
                                                           const float* r, float* u,
                                                           const CgScalars* S, int mode,
@@ -272,11 +268,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, 
     const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
     for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
         const int ch = active[a];
-        const int cnt = min(cell_count[ch], max_per_cell);
+        const int end = cell_start[ch + 1];
         const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
-        const int32_t* slots = cell_slot + static_cast<int64_t>(ch) * max_per_cell;
-        for (int s = lane; s < cnt; s += 32) {
-            const int i = slots[s];
+        for (int i = cell_start[ch] + lane; i < end; i += 32) {
             const float d = dinv0[i];
             const float sc = scale ? scale[i] : 1.0f;
             u[i] = d != 0.0f ? sc * d * r[i] + e : 0.0f;
@@ -476,30 +470,29 @@ cudaError_t mg_prepare_device() {
 
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
     // cells without particles keep a zero residual through the solve
-    cudaMemsetAsync(mg.n_active, 0, sizeof(int32_t), s);
     cudaMemsetAsync(mg.lv[1].r, 0, sizeof(float) * mg.lv[1].cells, s);
     k_mg_bins<<<o.grid_spmv, kBlock, 0, s>>>(o, mg.cell_xz, mg.bins, mg.dinv0, kMgOmegaFine, mg.status);
-    k_mg_cells<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1], mg.cell_count, mg.cell_slot,
-                                                          mg.max_per_cell, mg.bins, mg.n,
-                                                          kMgOmegaCoarse, mg.status, mg.active, mg.n_active);
+    k_mg_cells<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1], mg.cell_start, mg.bins, mg.n,
+                                                          kMgOmegaCoarse, mg.status, mg.active_flag);
+    launch_exclusive_scan(mg.active_flag, mg.active_pos, mg.lv[1].cells, mg.scan_scratch, s);
+    k_mg_active<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1].cells, mg.active_flag, mg.active_pos,
+                                                           mg.active);
     for (int l = 1; l < mg.levels; l++)
         k_mg_coarsen<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1],
                                                                     kMgOmegaCoarse, mg.status);
     k_mg_dense<<<1, kMgBottomThreads, dense_smem(mg), s>>>(mg.lv[mg.levels], mg.dense, mg.status);
 }
 
-int mg_setup_launches(const MgHierarchy& mg) { return 2 + (mg.levels - 1) + 1; }
+int mg_setup_launches(const MgHierarchy& mg) { return 2 + 3 + 1 + (mg.levels - 1) + 1; }
 
 void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* r, float* u,
               cudaStream_t s, const CgOperands* fuse_axpy) {
     const MgLevel& L1 = mg.lv[1];
     const int g1 = active_grid(L1.cells);
     if (fuse_axpy)
-        k_mg_axpy_restrict<<<g1, kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_count, mg.cell_slot, mg.max_per_cell,
-                                                 mg.active, mg.n_active);
+        k_mg_axpy_restrict<<<g1, kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
     else
-        k_mg_restrict0<<<g1, kBlock, 0, s>>>(L1, mg.cell_count, mg.cell_slot, mg.max_per_cell, r, S, mode,
-                                             mg.active, mg.n_active);
+        k_mg_restrict0<<<g1, kBlock, 0, s>>>(L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
     MgBottom B{};
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
@@ -524,8 +517,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
         k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s>>>(B, S, mode);
     }
     if (mg.bottom > 1)
-        k_mg_up_prolong<<<g1, kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_count, mg.cell_slot, mg.max_per_cell,
-                                              mg.dinv0, mg.scale, r, u, S, mode, mg.active, mg.n_active);
+        k_mg_up_prolong<<<g1, kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_start, mg.dinv0, mg.scale, r, u, S,
+                                              mode, mg.active, mg.n_active);
     else
         k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
                                                        r, L1.e, u, S, mode);

@@ -45,17 +45,19 @@ struct MgHierarchy {
     int32_t bottom = 0;  // first level of the single-block kernel
     MgLevel lv[kMgMaxLevels + 1] = {};  // lv[1..levels]
     float* dense = nullptr;             // inverse of the coarsest operator, cells^2
-    // particle level
+    // particle level (PPE rows in cell order: the rows of level-1 cell c are
+    // cell_start[c] .. cell_start[c + 1] - 1)
     int32_t n = 0;
-    int32_t max_per_cell = 0;
-    const int32_t* cell_xz = nullptr;   // (cx << 16) | cz of each particle's cell, -1: none
-    const int32_t* cell_count = nullptr;
-    const int32_t* cell_slot = nullptr;
+    const int32_t* cell_xz = nullptr;   // (cx << 16) | cz of each row's cell, -1: none
+    const int32_t* cell_start = nullptr;
     float* dinv0 = nullptr;             // omega_0 / a_ii on active rows, 0 on identity rows
     const float* scale = nullptr;       // per-row scale of the Jacobi term (null: 1)
     double* bins = nullptr;             // 9 * n FP64 scratch of the level-1 product
-    int32_t* active = nullptr;          // level-1 cells holding particles (set up per solve)
-    int32_t* n_active = nullptr;
+    int32_t* active = nullptr;          // level-1 cells holding particles, ascending (per solve)
+    int32_t* n_active = nullptr;        // their count (the total of the flag scan)
+    int32_t* active_flag = nullptr;     // per level-1 cell: 1 with particles
+    int32_t* active_pos = nullptr;      // exclusive prefix sum of active_flag (cells + 1)
+    int32_t* scan_scratch = nullptr;
     DevStatus* status = nullptr;
 };
 

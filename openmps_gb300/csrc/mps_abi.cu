@@ -330,6 +330,18 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.cell_xz = dalloc<int32_t>(h, n);
     st.x32 = dalloc<float>(h, n);
     st.z32 = dalloc<float>(h, n);
+    st.row_of = st.particle_of = st.row_cell = st.cell_fill = st.cell_start = nullptr;
+    st.unplaced = st.unplaced_pos = st.row_scratch = nullptr;
+    if (h->nscenes == 0) {  // single scene: PPE rows in cell order
+        st.row_of = dalloc<int32_t>(h, n);
+        st.particle_of = dalloc<int32_t>(h, n);
+        st.row_cell = dalloc<int32_t>(h, n);
+        st.cell_fill = dalloc<int32_t>(h, cells);
+        st.cell_start = dalloc<int32_t>(h, cells + 1);
+        st.unplaced = dalloc<int32_t>(h, n);
+        st.unplaced_pos = dalloc<int32_t>(h, n + 1);
+        st.row_scratch = dalloc<int32_t>(h, scan_scratch_ints(static_cast<int>(std::max<int64_t>(cells, n))));
+    }
     // multigrid hierarchy over the search cells (level sizes fixed by the domain)
     MgHierarchy& mg = h->mg;
     mg = MgHierarchy{};
@@ -349,13 +361,15 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         mg.dense = dalloc<float>(h, m * m);
         mg.bins = dalloc<double>(h, 9 * n);
         mg.active = dalloc<int32_t>(h, mg.lv[1].cells);
-        mg.n_active = dalloc<int32_t>(h, 1);
+        mg.active_flag = dalloc<int32_t>(h, mg.lv[1].cells);
+        mg.active_pos = dalloc<int32_t>(h, mg.lv[1].cells + 1);
+        mg.n_active = mg.active_pos + mg.lv[1].cells;
+        mg.scan_scratch = dalloc<int32_t>(h, scan_scratch_ints(mg.lv[1].cells));
+        check(cudaMemsetAsync(mg.active_pos, 0, sizeof(int32_t) * (mg.lv[1].cells + 1), h->stream), "memset");
         mg.dinv0 = dalloc<float>(h, n);
         mg.n = static_cast<int32_t>(n);
-        mg.max_per_cell = sc.max_per_cell;
-        mg.cell_xz = st.cell_xz;
-        mg.cell_count = st.cell_count;
-        mg.cell_slot = st.cell_slot;
+        mg.cell_xz = st.row_cell;
+        mg.cell_start = st.cell_start;
         mg.status = st.status;
     }
     // learned-solve buffers
@@ -387,6 +401,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     L.ecs = st.ecs;
     L.p = st.p;
     L.type = st.type;
+    L.particle_of = st.particle_of;
     L.step = st.step;
     L.dinv0 = mg.dinv0;
     L.flags = sc.flags;
@@ -405,6 +420,14 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     check(cudaMemsetAsync(h->S_fb, 0, sizeof(CgScalars), s), "memset");
     check(cudaMemsetAsync(h->tickets, 0, sizeof(uint32_t) * cg_tickets(n), s), "memset");
     check(cudaMemsetAsync(st.cell_xz, 0xff, sizeof(int32_t) * n, s), "memset");
+    if (st.row_of) {  // identity row order until the first search
+        std::vector<int32_t> iota(static_cast<size_t>(n));
+        for (int64_t i = 0; i < n; i++) iota[static_cast<size_t>(i)] = static_cast<int32_t>(i);
+        check(cudaMemcpy(st.row_of, iota.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemcpy(st.particle_of, iota.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemsetAsync(st.row_cell, 0xff, sizeof(int32_t) * n, s), "memset");
+        check(cudaMemsetAsync(st.cell_start, 0, sizeof(int32_t) * (cells + 1), s), "memset");
+    }
     check(cudaMemsetAsync(st.ppe_cv32, 0, sizeof(uint2) * sell_cap, s), "memset");
     h->ppe_fp32 = false;
     check(cudaMemsetAsync(h->S_lrn, 0, sizeof(CgScalars), s), "memset");
@@ -573,8 +596,9 @@ void do_search(mps_handle* h) {
     launch_bucket(h->sc, h->st, s);
     launch_cell_sort(h->sc, h->st, s);
     launch_neighbors(h->sc, h->st, s);
+    const int k = launch_rows(h->sc, h->st, s);
     after_launch("search");
-    launched(h, kLaunchesSearch);
+    launched(h, kLaunchesSearch + k);
 }
 
 // Keeps as much of the FP32 matrix ({column, value} pairs, read every iteration) in L2
@@ -1388,21 +1412,37 @@ int mps_debug_get_neighbors(mps_handle* h, int32_t* counts, int32_t* list, int64
 
 int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val, double* b,
                       double* x, int64_t capacity, int64_t* nnz) {
+    // the matrix in particle order with ascending columns, as the reference assembles it
+    // (device rows are in cell order: row_of maps particles to rows)
     return guarded(h, [&] {
         const int64_t n = h->n;
         const int64_t nchunks = sell_chunks(n);
         std::vector<int32_t> len(static_cast<size_t>(nchunks * kSellRows)), off(static_cast<size_t>(nchunks + 1));
+        std::vector<int32_t> row_of(static_cast<size_t>(n)), particle_of(static_cast<size_t>(n));
+        std::vector<double> bb(static_cast<size_t>(n)), xx(static_cast<size_t>(n));
         download(h, len.data(), h->st.ppe_len, sizeof(int32_t) * nchunks * kSellRows, false);
         download(h, off.data(), h->st.ppe_off, sizeof(int32_t) * (nchunks + 1), false);
-        download(h, b, h->st.ppe_b, sizeof(double) * n, false);
-        download(h, x, h->st.ppe_x, sizeof(double) * n, false);
+        download(h, bb.data(), h->st.ppe_b, sizeof(double) * n, false);
+        download(h, xx.data(), h->st.ppe_x, sizeof(double) * n, false);
+        if (h->st.row_of) {
+            download(h, row_of.data(), h->st.row_of, sizeof(int32_t) * n, false);
+            download(h, particle_of.data(), h->st.particle_of, sizeof(int32_t) * n, false);
+        }
         check(cudaStreamSynchronize(h->stream), "ppe");
+        if (!h->st.row_of)
+            for (int64_t i = 0; i < n; i++) row_of[static_cast<size_t>(i)] = particle_of[static_cast<size_t>(i)] = static_cast<int32_t>(i);
         int64_t sum = 0;
-        for (int64_t i = 0; i < n; i++) sum += len[static_cast<size_t>(i)];
+        for (int64_t i = 0; i < n; i++) {
+            const size_t r = static_cast<size_t>(row_of[static_cast<size_t>(i)]);
+            sum += len[r];
+            if (b) b[i] = bb[r];
+            if (x) x[i] = xx[r];
+        }
         if (nnz) *nnz = sum;
         if (row_ptr) {
             row_ptr[0] = 0;
-            for (int64_t i = 0; i < n; i++) row_ptr[i + 1] = row_ptr[i] + len[static_cast<size_t>(i)];
+            for (int64_t i = 0; i < n; i++)
+                row_ptr[i + 1] = row_ptr[i] + len[static_cast<size_t>(row_of[static_cast<size_t>(i)])];
         }
         if (!col && !val) return;
         if (sum > capacity) throw StatusError{MPS_ERR_INVALID_ARGUMENT, "PPE capacity too small"};
@@ -1414,13 +1454,21 @@ int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val
             download(h, vbuf.data(), h->st.ppe_val, sizeof(double) * total, false);
         }
         check(cudaStreamSynchronize(h->stream), "ppe");
+        std::vector<std::pair<int32_t, double>> row;
         int64_t o = 0;
         for (int64_t i = 0; i < n; i++) {
-            const int64_t base = off[static_cast<size_t>(i / kSellRows)];
-            for (int32_t k = 0; k < len[static_cast<size_t>(i)]; k++) {
-                const size_t e = static_cast<size_t>(sell_index(base, static_cast<int>(i % kSellRows), k));
-                if (col) col[o] = cbuf[e];
-                if (val) val[o] = vbuf[e];
+            const int64_t r = row_of[static_cast<size_t>(i)];
+            const int64_t base = off[static_cast<size_t>(r / kSellRows)];
+            row.clear();
+            for (int32_t k = 0; k < len[static_cast<size_t>(r)]; k++) {
+                const size_t e = static_cast<size_t>(sell_index(base, static_cast<int>(r % kSellRows), k));
+                row.emplace_back(particle_of[static_cast<size_t>(cbuf[e])], vbuf[e]);
+            }
+            std::sort(row.begin(), row.end(),
+                      [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& c) { return a.first < c.first; });
+            for (const auto& ent : row) {
+                if (col) col[o] = ent.first;
+                if (val) val[o] = ent.second;
                 o++;
             }
         }

@@ -249,18 +249,20 @@ __global__ void k_save_x(SceneConst sc, DeviceState st) {
 
 // SetPressurePoissonEquation (Computer.hpp:1145-1328): right-hand side, initial guess
 // and one matrix row per particle in neighbour order (diagonal last) into the
-// scratch ELL arrays.
+// scratch ELL arrays (column k of particle i at [k n + i]).  Rows and columns are PPE
+// rows (ppe_row); b, x and the row length are stored at the particle's row.
 __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
     const int n = sc.n;
+    const int row = ppe_row(st, i);
     if (!ppe_alive(sc, st, i)) {
-        st.ppe_b[i] = 0;
-        st.ppe_x[i] = 0;
-        st.ppe_col_tmp[ell(0, n, i)] = i;
+        st.ppe_b[row] = 0;
+        st.ppe_x[row] = 0;
+        st.ppe_col_tmp[ell(0, n, i)] = row;
         st.ppe_val_tmp[ell(0, n, i)] = 1.0;
-        st.ppe_len[i] = 1;
+        st.ppe_len[row] = 1;
         return;
     }
     const double dt = st.step->dt;
@@ -268,11 +270,11 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     const double speed = density_variation(sc, st, i, dt);
     if (has_flag(sc.flags, MPS_FLAG_ECS)) {
         const double e = st.ecs[i];
-        st.ppe_b[i] = -sc.rho / (sc.n0 * dt) * (speed + e);
+        st.ppe_b[row] = -sc.rho / (sc.n0 * dt) * (speed + e);
     } else {
-        st.ppe_b[i] = -sc.rho / (sc.n0 * dt) * speed;
+        st.ppe_b[row] = -sc.rho / (sc.n0 * dt) * speed;
     }
-    st.ppe_x[i] = st.p[i];
+    st.ppe_x[row] = st.p[i];
 
     const double xi = st.x[i], zi = st.z[i];
     double a_ii = 0.0, gx = 0.0, gz = 0.0;
@@ -285,7 +287,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double a_ij = ppe_coefficient(sc, __dsqrt_rn(r2));
                 if (spp || !is_surface(sc, st.nd[j])) {
-                    st.ppe_col_tmp[ell(m, n, i)] = j;
+                    st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
                     st.ppe_val_tmp[ell(m, n, i)] = a_ij;
                     m++;
                 }
@@ -305,9 +307,9 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
         const double ddx = xi - xs, ddz = zi - zs;
         a_ii += -ppe_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
-    st.ppe_col_tmp[ell(m, n, i)] = i;
+    st.ppe_col_tmp[ell(m, n, i)] = row;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
-    st.ppe_len[i] = m + 1;
+    st.ppe_len[row] = m + 1;
 }
 
 // Chunk sizes of the SELL-32 layout: one warp per chunk of 32 rows.
@@ -323,16 +325,17 @@ __global__ void k_ppe_chunks(SceneConst sc, DeviceState st) {
 
 // Row entries to ascending column order (uBLAS compressed_matrix, Computer.hpp:1330-1350):
 // each entry goes to its rank among the row's columns (columns are distinct), at its
-// SELL-32 position.
+// SELL-32 position.  One thread per particle (coalesced scratch reads), writing its row.
 __global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (step_failed(sc, st)) return;
     const int n = sc.n;
-    const int len = (i < n) ? st.ppe_len[i] : 0;
+    const int row = (i < n) ? ppe_row(st, i) : 0;
+    const int len = (i < n) ? st.ppe_len[row] : 0;
     warp_add_u64(&st.status->ppe_nnz, static_cast<unsigned long long>(len));
     if (i >= n) return;
-    const int64_t base = st.ppe_off[i / kSellRows];
-    const int r = i % kSellRows;
+    const int64_t base = st.ppe_off[row / kSellRows];
+    const int r = row % kSellRows;
     for (int e = 0; e < len; e++) {
         const int ce = st.ppe_col_tmp[ell(e, n, i)];
         int rank = 0;
@@ -353,7 +356,7 @@ __global__ void k_assign_pressure(SceneConst sc, DeviceState st) {
     if (solve_failed(sc, st)) return;
     const int t = st.type[i];
     if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
-    const double v = st.ppe_x[i];
+    const double v = st.ppe_x[ppe_row(st, i)];
     const bool surface = !has_flag(sc.flags, MPS_FLAG_SPP) && is_surface(sc, st.nd[i]);
     st.p[i] = ((v < 0) || surface) ? 0.0 : v;
 }
