@@ -1115,45 +1115,19 @@ void CgGraph::reset() {
     persistent_ = false;
 }
 
-cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win,
-                           const MgHierarchy* mg, const CgOperands* fb, const LearnedRun* lrn) {
+cudaError_t CgGraph::build(int solver, const CgOperands& ops, cudaStream_t s, const MgHierarchy* mg,
+                           const CgOperands* fb, const LearnedRun* lrn) {
     if (is_pcg(solver) && (!mg || !fb)) return cudaErrorInvalidValue;
     if (solver == MPS_SOLVER_LEARNED && !lrn) return cudaErrorInvalidValue;
     if (solver != MPS_SOLVER_CG64) {
         // preferred: the reliable update under an IF node nested in the WHILE body
-        if (build_impl(solver, ops, s, true, win, mg, fb, lrn) == cudaSuccess) return cudaSuccess;
+        if (build_impl(solver, ops, s, true, mg, fb, lrn) == cudaSuccess) return cudaSuccess;
         cudaGetLastError();
     }
-    return build_impl(solver, ops, s, false, win, mg, fb, lrn);
+    return build_impl(solver, ops, s, false, mg, fb, lrn);
 }
 
 namespace {
-// Sets the L2 access policy window on every kernel node of `g`.
-cudaError_t apply_window(cudaGraph_t g, const L2Window& win) {
-    if (win.num_bytes == 0) return cudaSuccess;
-    size_t nn = 0;
-    cudaError_t e = cudaGraphGetNodes(g, nullptr, &nn);
-    if (e != cudaSuccess) return e;
-    std::vector<cudaGraphNode_t> nodes(nn);
-    e = cudaGraphGetNodes(g, nodes.data(), &nn);
-    if (e != cudaSuccess) return e;
-    cudaKernelNodeAttrValue v = {};
-    v.accessPolicyWindow.base_ptr = win.base;
-    v.accessPolicyWindow.num_bytes = win.num_bytes;
-    v.accessPolicyWindow.hitRatio = win.hit_ratio;
-    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    for (cudaGraphNode_t node : nodes) {
-        cudaGraphNodeType t;
-        e = cudaGraphNodeGetType(node, &t);
-        if (e != cudaSuccess) return e;
-        if (t != cudaGraphNodeTypeKernel) continue;
-        e = cudaGraphKernelNodeSetAttribute(node, cudaKernelNodeAttributeAccessPolicyWindow, &v);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-
 // The one node of a linear chain that has no successor.
 cudaError_t sink_node(cudaGraph_t g, cudaGraphNode_t* out) {
     size_t nn = 0, ne = 0;
@@ -1197,8 +1171,7 @@ cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* dep, cudaGraphConditionalH
 }  // namespace
 
 cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                                const L2Window& win, const MgHierarchy* mg, const CgOperands* fb,
-                                const LearnedRun* lrn) {
+                                const MgHierarchy* mg, const CgOperands* fb, const LearnedRun* lrn) {
     reset();
     ops_ = ops;
     solver_ = solver;
@@ -1243,8 +1216,6 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     body_kernels(solver, ops, mg, h, h_true, 1, !nested, s);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
-    e = apply_window(body, win);
-    if (e != cudaSuccess) return e;
 
     if (nested) {
         // if (reliable update due) { true residual; [u = M r]; w = A u } after the SpMV
@@ -1265,8 +1236,6 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
         if (e != cudaSuccess) return e;
         reliable_kernels(solver, ops, mg, h, 1, s);
         e = cudaStreamEndCapture(s, &captured);
-        if (e != cudaSuccess) return e;
-        e = apply_window(if_body, win);
         if (e != cudaSuccess) return e;
     }
 

@@ -59,13 +59,6 @@ struct CgOperands {
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
 };
 
-// L2 persisting window applied to the kernels of the CG loop (num_bytes 0: none).
-struct L2Window {
-    void* base = nullptr;
-    size_t num_bytes = 0;
-    float hit_ratio = 0.f;
-};
-
 struct MgHierarchy;
 struct LearnedOps;
 
@@ -92,7 +85,7 @@ public:
     ~CgGraph();
     // `mg` and `fb` (operands of the FP64 fallback, own scalars) are required for
     // MPS_SOLVER_MIXED_MG and MPS_SOLVER_LEARNED and ignored otherwise.
-    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s, const L2Window& win = {},
+    cudaError_t build(int solver, const CgOperands& ops, cudaStream_t s,
                       const MgHierarchy* mg = nullptr, const CgOperands* fb = nullptr,
                       const LearnedRun* lrn = nullptr);
     // MIXED_MG / LEARNED with the whole iteration loop in one cooperative kernel
@@ -111,8 +104,7 @@ public:
 
 private:
     cudaError_t build_impl(int solver, const CgOperands& ops, cudaStream_t s, bool nested,
-                           const L2Window& win, const MgHierarchy* mg, const CgOperands* fb,
-                           const LearnedRun* lrn);
+                           const MgHierarchy* mg, const CgOperands* fb, const LearnedRun* lrn);
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int solver_ = -1;

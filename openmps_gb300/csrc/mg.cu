@@ -255,6 +255,14 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
     c.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz, I - (I / c.nz) * c.nz);
 }
 
+// Post-smoothed correction of the level-f cells (levels 2 .. below the cluster kernel).
+__global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+    if (pcg_skip(S, mode)) return;
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= f.cells) return;
+    f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
+}
+
 // Level-1 post-smoothing fused with the prolongation to the particles of the cell:
 // u = s_i dinv0_i r_i + e_1 on active rows, 0 on identity rows (one warp per cell).
 __global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_start,
@@ -324,6 +332,16 @@ __global__ void __launch_bounds__(kMgMiddleThreads) k_mg_middle(MgBottom B, cons
 }
 
 int g_middle_cluster = 0;  // blocks of the k_mg_middle cluster (set by mg_prepare_device)
+
+// First level of the cluster kernel: the levels above it have too many cells for 16
+// SMs (a level-2 pass of a 340k-particle scene, 21k cells, took longer on the cluster
+// than as a kernel of its own) and run as grid-wide kernels.
+constexpr int kMgClusterCells = 8192;
+int middle_first(const MgHierarchy& mg) {
+    int l = 2;
+    while (l < mg.levels && mg.lv[l].cells > kMgClusterCells) l++;
+    return l;
+}
 
 // Levels first..last in one block, everything in shared memory: per level the nine
 // coefficient planes, dinv, r and e, then the dense inverse of the last level.
@@ -497,9 +515,11 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
     B.dense = mg.dense;
+    const int mid = middle_first(mg);
     if (mg.bottom > 1) {
-        k_mg_down<<<grid_for(mg.lv[2].cells), kBlock, 0, s>>>(mg.lv[1], mg.lv[2], S, mode);
-        B.first = 2;
+        for (int l = 1; l < mid; l++)
+            k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+        B.first = mid;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g_middle_cluster);
         cfg.blockDim = dim3(kMgMiddleThreads);
@@ -512,6 +532,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
         cfg.attrs = at;
         cfg.numAttrs = 1;
         cudaLaunchKernelEx(&cfg, k_mg_middle, B, S, mode);
+        for (int l = mid - 1; l >= 2; l--)
+            k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
     } else {
         B.first = 1;
         k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s>>>(B, S, mode);
@@ -524,6 +546,6 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
                                                        r, L1.e, u, S, mode);
 }
 
-int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 4 : 3; }
+int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * middle_first(mg) : 3; }
 
 }  // namespace mpsgb

@@ -85,9 +85,6 @@ struct mps_handle {
     int sm_count = 1;
     CgGraph cg;
     int64_t direct_launches = -1;  // kernels of the last host-driven solve (-1: graph)
-    L2Window l2win;                // persisting window over the FP32 matrix (MIXED)
-    bool l2_limit_changed = false;
-    size_t l2_limit_before = 0;
 
     // pinned host mirrors of the status block
     DevStatus* h_status = nullptr;
@@ -458,7 +455,6 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     for (void* ptr : old_allocs) cudaFree(ptr);
     h->cap = n;
     h->cg.reset();
-    h->l2win = L2Window{};
 }
 
 CgOperands cg_operands(mps_handle* h) {
@@ -601,48 +597,6 @@ void do_search(mps_handle* h) {
     launched(h, kLaunchesSearch + k);
 }
 
-// Keeps as much of the FP32 matrix ({column, value} pairs, read every iteration) in L2
-// as the persisting set-aside allows: the matrix of the 320k-particle scene is about the
-// size of L2.  The set-aside is a limit of this process's context; the handle restores
-// the previous value when it is destroyed.
-void setup_l2_window(mps_handle* h) {
-    if (h->l2win.num_bytes != 0) return;
-    int maxp = 0, maxw = 0;
-    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, h->device) != cudaSuccess ||
-        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, h->device) != cudaSuccess ||
-        maxp <= 0 || maxw <= 0) {
-        cudaGetLastError();
-        return;
-    }
-    const size_t used = static_cast<size_t>(sell_chunks(h->n) * sell_chunk_size(h->sc.ppe_stride)) * sizeof(uint2);
-    const size_t win = std::min(used, static_cast<size_t>(maxw));
-    size_t cur = 0;
-    check(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "L2 limit");
-    const size_t want = std::min(static_cast<size_t>(maxp), win);
-    if (cur < want) {
-        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess) {
-            if (!h->l2_limit_changed) {
-                h->l2_limit_changed = true;
-                h->l2_limit_before = cur;
-            }
-        } else {
-            cudaGetLastError();
-        }
-        check(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "L2 limit");
-    }
-    if (cur == 0) return;
-    h->l2win.base = h->st.ppe_cv32;
-    h->l2win.num_bytes = win;
-    h->l2win.hit_ratio = std::min(1.0f, static_cast<float>(cur) / static_cast<float>(win));
-    cudaStreamAttrValue av = {};
-    av.accessPolicyWindow.base_ptr = h->l2win.base;
-    av.accessPolicyWindow.num_bytes = h->l2win.num_bytes;
-    av.accessPolicyWindow.hitRatio = h->l2win.hit_ratio;
-    av.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    av.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    check(cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &av), "L2 window");
-}
-
 void do_solve(mps_handle* h) {
     cudaStream_t s = h->stream;
     const int solver = h->prm.solver;
@@ -686,7 +640,6 @@ void do_solve(mps_handle* h) {
         fb = cg_operands(h);
         fb.S = h->S_fb;
     }
-    if (solver != MPS_SOLVER_CG64) setup_l2_window(h);
     if (h->prm.cg_launch == MPS_CG_LAUNCH_HOST) {
         int64_t k = 0;
         check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k, pcg ? &mg : nullptr,
@@ -712,8 +665,8 @@ void do_solve(mps_handle* h) {
                 }
             }
             if (!built)
-                check(h->cg.build(solver, cg_operands(h), s, solver != MPS_SOLVER_CG64 ? h->l2win : L2Window{},
-                                  pcg ? &mg : nullptr, pcg ? &fb : nullptr, learned ? &run : nullptr),
+                check(h->cg.build(solver, cg_operands(h), s, pcg ? &mg : nullptr, pcg ? &fb : nullptr,
+                                  learned ? &run : nullptr),
                       "CG graph build");
         }
         check(h->cg.launch(s), "CG graph launch");
@@ -1079,11 +1032,6 @@ int mps_destroy(mps_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->cg.reset();
-    if (h->l2win.num_bytes != 0 || h->l2_limit_changed) {
-        cudaCtxResetPersistingL2Cache();
-        if (h->l2_limit_changed) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_limit_before);
-        cudaGetLastError();
-    }
     if (h->batch_graph) cudaGraphExecDestroy(h->batch_graph);
     dfree_all(h);
     if (h->lrn_packed) cudaFree(h->lrn_packed);
