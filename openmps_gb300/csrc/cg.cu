@@ -594,6 +594,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 __global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
+    pdl_begin();
     __shared__ BlockTicket tk;
     CgScalars* S = o.S;
     if (pcg_skip(S, mode)) return;
@@ -1015,7 +1016,7 @@ void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
     }
     if (is_pcg(solver)) {
         mg_apply(*mg, ops.S, 1, ops.r32, ops.u32, s, &ops);  // vector updates + u = M r
-        k_pmx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
+        launch_pdl(k_pmx_spmv, gs, kBlock, 0, s, ops, 1, h, h_true, use_cond);
     } else {
         k_mx_axpy<<<gv, kBlock, 0, s>>>(ops);
         k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
@@ -1138,9 +1139,11 @@ cudaError_t sink_node(cudaGraph_t g, cudaGraphNode_t* out) {
     if (e != cudaSuccess) return e;
     e = cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &ne);
     if (e != cudaSuccess) return e;
+    // edge data is requested too: programmatic (PDL) edges cannot be listed without it
     std::vector<cudaGraphNode_t> from(ne), to(ne);
+    std::vector<cudaGraphEdgeData> data(ne);
     if (ne > 0) {
-        e = cudaGraphGetEdges(g, from.data(), to.data(), nullptr, &ne);
+        e = cudaGraphGetEdges(g, from.data(), to.data(), data.data(), &ne);
         if (e != cudaSuccess) return e;
     }
     int found = 0;

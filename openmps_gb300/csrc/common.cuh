@@ -231,6 +231,34 @@ inline int grid_for(int64_t n, int block = kBlock) {
     return static_cast<int>((n + block - 1) / block);
 }
 
+// ------------------------------------------- programmatic dependent launch
+// The solver's kernel chains are short kernels back to back; launched with programmatic
+// stream serialization, a kernel's blocks are scheduled while its predecessor drains.
+// Every kernel launched that way starts with pdl_begin(): it waits until the predecessor
+// grid has completed and its writes are visible (griddepcontrol.wait), then lets its own
+// successor start launching (griddepcontrol.launch_dependents).  Both are no-ops for a
+// kernel launched without the attribute.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // ------------------------------------------------------ launchers (host side)
 // grid.cu
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

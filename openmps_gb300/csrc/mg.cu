@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
 __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_start,
                                                          const float* r, const CgScalars* S, int mode,
                                                          const int32_t* active, const int32_t* n_active) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     const int lane = threadIdx.x & 31;
     const int nact = *n_active;
@@ -223,6 +224,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32
 __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1,
                                                              const int32_t* cell_start, const int32_t* active,
                                                              const int32_t* n_active) {
+    pdl_begin();
     if (pcg_skip(o.S, 1)) return;
     const int lane = threadIdx.x & 31;
     const float alpha = __double2float_rn(o.S->alpha);
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLev
 }
 
 __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= c.cells) return;
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
 
 // Post-smoothed correction of the level-f cells (levels 2 .. below the cluster kernel).
 __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     if (ch >= f.cells) return;
@@ -270,6 +274,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, 
                                                           const float* r, float* u,
                                                           const CgScalars* S, int mode,
                                                           const int32_t* active, const int32_t* n_active) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     const int lane = threadIdx.x & 31;
     const int nact = *n_active;
@@ -298,6 +303,7 @@ struct MgBottom {
 // wrote are read through L2; coefficient planes and the dense inverse are read-only here.
 __global__ void __launch_bounds__(kMgMiddleThreads) k_mg_middle(MgBottom B, const CgScalars* S,
                                                                 int mode) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;  // same decision in every thread of the cluster
     cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
     const int nt = static_cast<int>(gridDim.x * blockDim.x);
@@ -347,6 +353,7 @@ int middle_first(const MgHierarchy& mg) {
 // coefficient planes, dinv, r and e, then the dense inverse of the last level.
 __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, const CgScalars* S,
                                                                 int mode) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     extern __shared__ float sm[];
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -405,6 +412,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* ce
                                                         const float* dinv0, const float* scale,
                                                         const float* r, const float* e1, float* u,
                                                         const CgScalars* S, int mode) {
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float d = dinv0[i];
@@ -508,9 +516,9 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     const MgLevel& L1 = mg.lv[1];
     const int g1 = active_grid(L1.cells);
     if (fuse_axpy)
-        k_mg_axpy_restrict<<<g1, kBlock, 0, s>>>(*fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
+        launch_pdl(k_mg_axpy_restrict, g1, kBlock, 0, s, *fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
     else
-        k_mg_restrict0<<<g1, kBlock, 0, s>>>(L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
+        launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
     MgBottom B{};
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
@@ -518,32 +526,34 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     const int mid = middle_first(mg);
     if (mg.bottom > 1) {
         for (int l = 1; l < mid; l++)
-            k_mg_down<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+            launch_pdl(k_mg_down, grid_for(mg.lv[l + 1].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
         B.first = mid;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g_middle_cluster);
         cfg.blockDim = dim3(kMgMiddleThreads);
         cfg.stream = s;
-        cudaLaunchAttribute at[1];
+        cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = g_middle_cluster;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = 2;
         cudaLaunchKernelEx(&cfg, k_mg_middle, B, S, mode);
         for (int l = mid - 1; l >= 2; l--)
-            k_mg_up<<<grid_for(mg.lv[l].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1], S, mode);
+            launch_pdl(k_mg_up, grid_for(mg.lv[l].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
     } else {
         B.first = 1;
-        k_mg_bottom<<<1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s>>>(B, S, mode);
+        launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s, B, S, mode);
     }
     if (mg.bottom > 1)
-        k_mg_up_prolong<<<g1, kBlock, 0, s>>>(L1, mg.lv[2], mg.cell_start, mg.dinv0, mg.scale, r, u, S,
-                                              mode, mg.active, mg.n_active);
+        launch_pdl(k_mg_up_prolong, g1, kBlock, 0, s, L1, mg.lv[2], mg.cell_start, mg.dinv0, mg.scale, r, u, S,
+                   mode, mg.active, mg.n_active);
     else
-        k_mg_prolong0<<<grid_for(mg.n), kBlock, 0, s>>>(mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
-                                                       r, L1.e, u, S, mode);
+        launch_pdl(k_mg_prolong0, grid_for(mg.n), kBlock, 0, s, mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
+                   r, L1.e, u, S, mode);
 }
 
 int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * middle_first(mg) : 3; }
