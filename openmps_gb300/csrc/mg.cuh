@@ -28,7 +28,7 @@ constexpr size_t kMgBottomBytes = 200 * 1024;
 constexpr int kMgBottomThreads = 1024;
 constexpr int kMgMiddleThreads = 1024;  // per thread block of the middle-level cluster
 constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
-constexpr float kMgOmegaCoarse = 0.7f; // Jacobi weight of the cell levels
+constexpr float kMgOmegaCoarse = 0.9f; // Jacobi weight of the cell levels (best of 0.6-0.9 measured)
 
 // One cell level: nine coefficient planes K[d * cells + c], d = 3 (dx + 1) + (dz + 1).
 struct MgLevel {
