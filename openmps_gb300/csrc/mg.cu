@@ -11,15 +11,15 @@
 //                memory, symmetrised).
 // Cycle, once per iteration (FP32, reads L2-resident planes):
 //   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
-//   and after a reliable update k_mg_restrict0), k_mg_down (level 1 to level 2),
-//   k_mg_middle (levels 2 .. coarsest and back in one thread-block cluster, cluster
-//   barriers between the levels), k_mg_up_prolong (level-1 post-smoothing + prolongation
-//   to the particles).  Hierarchies small enough for one block's shared memory run
-//   k_mg_bottom (all levels, __syncthreads between them) and k_mg_prolong0 instead.
+//   and after a reliable update k_mg_restrict0), k_mg_down (levels above the bottom),
+//   k_mg_bottom (the coarsest levels in one block, all in shared memory, __syncthreads
+//   between levels), k_mg_up, k_mg_up_prolong (level-1 post-smoothing + prolongation to
+//   the particles; k_mg_prolong0 when the bottom block covers level 1).
+// A 16-block cluster kernel for levels 2 .. coarsest (cluster barriers between levels)
+// was measured slower: about 4 us per level against well under 1 us per level for one
+// block with __syncthreads, and the grid-wide kernels for the larger levels.
 // Every kernel reads only what the previous kernel wrote, so the sequence captures into
 // the solver's CUDA graph unchanged.
-#include <cooperative_groups.h>
-
 #include <algorithm>
 
 #include "mg.cuh"
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
     c.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz, I - (I / c.nz) * c.nz);
 }
 
-// Post-smoothed correction of the level-f cells (levels 2 .. below the cluster kernel).
+// Post-smoothed correction of the level-f cells (levels 2 .. above the bottom block).
 __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
     pdl_begin();
     if (pcg_skip(S, mode)) return;
@@ -297,56 +297,27 @@ struct MgBottom {
     const float* dense;
 };
 
-// Levels first..last and back up in one cluster of thread blocks: the levels below the
-// search cells are small (level 2 of a 340k-particle scene has 21k cells), so a cluster
-// barrier between levels replaces a kernel boundary each.  Vectors that other blocks
-// wrote are read through L2; coefficient planes and the dense inverse are read-only here.
-__global__ void __launch_bounds__(kMgMiddleThreads) k_mg_middle(MgBottom B, const CgScalars* S,
-                                                                int mode) {
-    pdl_begin();
-    if (pcg_skip(S, mode)) return;  // same decision in every thread of the cluster
-    cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
-    const int nt = static_cast<int>(gridDim.x * blockDim.x);
-    const int gt = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
-    for (int l = B.first; l < B.last; l++) {
-        const MgLevel& f = B.lv[l];
-        const MgLevel& c = B.lv[l + 1];
-        for (int I = gt; I < c.cells; I += nt)
-            c.r[I] = child_residuals<true>(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz,
-                                           I - (I / c.nz) * c.nz);
-        cluster.sync();
-    }
-    {
-        const MgLevel& Lc = B.lv[B.last];
-        const int m = Lc.cells;
-        const int lane = threadIdx.x & 31;
-        for (int row = gt >> 5; row < m; row += nt >> 5) {
-            float v = 0.0f;
-            for (int k = lane; k < m; k += 32) v += B.dense[row * m + k] * __ldcg(Lc.r + k);
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) Lc.e[row] = v;
+// n floats from global memory to shared memory, four independent 16-byte loads in flight
+// per thread where both sides are 16-byte aligned.
+__device__ __forceinline__ void stage_floats(float* dst, const float* __restrict__ src, int n, int tid, int nt) {
+    int done = 0;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const int n4 = n >> 2;
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        int i = tid;
+        for (; i + 3 * nt < n4; i += 4 * nt) {
+            const float4 a = __ldg(s4 + i), b = __ldg(s4 + i + nt), c = __ldg(s4 + i + 2 * nt),
+                         d = __ldg(s4 + i + 3 * nt);
+            d4[i] = a;
+            d4[i + nt] = b;
+            d4[i + 2 * nt] = c;
+            d4[i + 3 * nt] = d;
         }
+        for (; i < n4; i += nt) d4[i] = __ldg(s4 + i);
+        done = 4 * n4;
     }
-    for (int l = B.last - 1; l >= B.first; l--) {
-        cluster.sync();
-        const MgLevel& f = B.lv[l];
-        const int cnz = B.lv[l + 1].nz;
-        for (int ch = gt; ch < f.cells; ch += nt)
-            f.e[ch] = smoothed_correction<true>(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, cnz,
-                                                B.lv[l + 1].e, ch);
-    }
-}
-
-int g_middle_cluster = 0;  // blocks of the k_mg_middle cluster (set by mg_prepare_device)
-
-// First level of the cluster kernel: the levels above it have too many cells for 16
-// SMs (a level-2 pass of a 340k-particle scene, 21k cells, took longer on the cluster
-// than as a kernel of its own) and run as grid-wide kernels.
-constexpr int kMgClusterCells = 8192;
-int middle_first(const MgHierarchy& mg) {
-    int l = 2;
-    while (l < mg.levels && mg.lv[l].cells > kMgClusterCells) l++;
-    return l;
+    for (int k = done + tid; k < n; k += nt) dst[k] = __ldg(src + k);
 }
 
 // Levels first..last in one block, everything in shared memory: per level the nine
@@ -369,13 +340,13 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, cons
         rs[l] = ds[l] + cells;
         es[l] = rs[l] + cells;
         at = es[l] + cells;
-        for (int idx = tid; idx < 9 * cells; idx += nt) ks[l][idx] = B.lv[l].k32[idx];
-        for (int idx = tid; idx < cells; idx += nt) ds[l][idx] = B.lv[l].dinv[idx];
+        stage_floats(ks[l], B.lv[l].k32, 9 * cells, tid, nt);
+        stage_floats(ds[l], B.lv[l].dinv, cells, tid, nt);
     }
     const int m = B.lv[B.last].cells;
     float* dn = at;
-    for (int idx = tid; idx < m * m; idx += nt) dn[idx] = B.dense[idx];
-    for (int c = tid; c < B.lv[B.first].cells; c += nt) rs[B.first][c] = B.lv[B.first].r[c];
+    stage_floats(dn, B.dense, m * m, tid, nt);
+    stage_floats(rs[B.first], B.lv[B.first].r, B.lv[B.first].cells, tid, nt);
     __syncthreads();
     for (int l = B.first; l < B.last; l++) {
         const MgLevel& f = B.lv[l];
@@ -466,32 +437,8 @@ cudaError_t mg_prepare_device() {
     const int dense_max = (kMgDenseCells * kMgDenseCells + kMgDenseCells + 1) * static_cast<int>(sizeof(float));
     cudaError_t e = cudaFuncSetAttribute(k_mg_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, dense_max);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kMgBottomBytes));
-    if (e != cudaSuccess) return e;
-    // the widest cluster that can be resident: 16 blocks (non-portable size), else 8
-    e = cudaFuncSetAttribute(k_mg_middle, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-    g_middle_cluster = 0;
-    for (int c : {16, 8}) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(c);
-        cfg.blockDim = dim3(kMgMiddleThreads);
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = c;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int clusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&clusters, k_mg_middle, &cfg) == cudaSuccess && clusters > 0) {
-            g_middle_cluster = c;
-            break;
-        }
-        cudaGetLastError();
-    }
-    return g_middle_cluster > 0 ? cudaSuccess : cudaErrorNotSupported;
+    return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kMgBottomBytes));
 }
 
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
@@ -519,35 +466,16 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
         launch_pdl(k_mg_axpy_restrict, g1, kBlock, 0, s, *fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
     else
         launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
+    for (int l = 1; l < mg.bottom; l++)
+        launch_pdl(k_mg_down, grid_for(mg.lv[l + 1].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
     MgBottom B{};
+    B.first = mg.bottom;
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
     B.dense = mg.dense;
-    const int mid = middle_first(mg);
-    if (mg.bottom > 1) {
-        for (int l = 1; l < mid; l++)
-            launch_pdl(k_mg_down, grid_for(mg.lv[l + 1].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
-        B.first = mid;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(g_middle_cluster);
-        cfg.blockDim = dim3(kMgMiddleThreads);
-        cfg.stream = s;
-        cudaLaunchAttribute at[2];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = g_middle_cluster;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[1].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 2;
-        cudaLaunchKernelEx(&cfg, k_mg_middle, B, S, mode);
-        for (int l = mid - 1; l >= 2; l--)
-            launch_pdl(k_mg_up, grid_for(mg.lv[l].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
-    } else {
-        B.first = 1;
-        launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_bytes(mg.lv, 1, mg.levels), s, B, S, mode);
-    }
+    launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_bytes(mg.lv, mg.bottom, mg.levels), s, B, S, mode);
+    for (int l = mg.bottom - 1; l >= 2; l--)
+        launch_pdl(k_mg_up, grid_for(mg.lv[l].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
     if (mg.bottom > 1)
         launch_pdl(k_mg_up_prolong, g1, kBlock, 0, s, L1, mg.lv[2], mg.cell_start, mg.dinv0, mg.scale, r, u, S,
                    mode, mg.active, mg.n_active);
@@ -556,6 +484,6 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
                    r, L1.e, u, S, mode);
 }
 
-int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * middle_first(mg) : 3; }
+int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * mg.bottom : 3; }
 
 }  // namespace mpsgb

@@ -26,7 +26,6 @@ constexpr int kMgDenseCells = 128;     // the coarsest level, solved with its de
 // inverse fit this much shared memory.
 constexpr size_t kMgBottomBytes = 200 * 1024;
 constexpr int kMgBottomThreads = 1024;
-constexpr int kMgMiddleThreads = 1024;  // per thread block of the middle-level cluster
 constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
 constexpr float kMgOmegaCoarse = 0.9f; // Jacobi weight of the cell levels (best of 0.6-0.9 measured)
 
@@ -83,17 +82,9 @@ cudaError_t mg_prepare_device();
 // loads of a cell issue at once.
 __device__ __forceinline__ int clampi(int v, int hi) { return min(max(v, 0), hi); }
 
-// Vector loads of the stencils; kL2 bypasses L1 for vectors that other thread blocks of
-// the same launch wrote (the cluster kernel of the middle levels).
-template <bool kL2>
-__device__ __forceinline__ float ldv(const float* p) {
-    if constexpr (kL2) return __ldcg(p);
-    else return *p;
-}
 
 // Residual of level f after the pre-smoothing x = dinv * r, summed over the children of
 // coarse cell (X, Z) (the restriction of the piecewise-constant aggregation).
-template <bool kL2 = false>
 __device__ __forceinline__ float child_residuals(int nx, int nz, int cells, const float* k,
                                                  const float* dinv, const float* r, int X, int Z) {
     float sum = 0.0f;
@@ -105,13 +96,13 @@ __device__ __forceinline__ float child_residuals(int nx, int nz, int cells, cons
             const bool valid = cx < nx && cz < nz;
             const int ccx = min(cx, nx - 1), ccz = min(cz, nz - 1);
             const int ch = ccx * nz + ccz;
-            float res = ldv<kL2>(r + ch);
+            float res = r[ch];
 #pragma unroll
             for (int dx = -1; dx <= 1; dx++) {
 #pragma unroll
                 for (int dz = -1; dz <= 1; dz++) {
                     const int nb = clampi(ccx + dx, nx - 1) * nz + clampi(ccz + dz, nz - 1);
-                    res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * (dinv[nb] * ldv<kL2>(r + nb));
+                    res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * (dinv[nb] * r[nb]);
                 }
             }
             sum += valid ? res : 0.0f;
@@ -121,13 +112,12 @@ __device__ __forceinline__ float child_residuals(int nx, int nz, int cells, cons
 }
 
 // Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
-template <bool kL2 = false>
 __device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
                                                      const float* dinv, const float* r, int cnz,
                                                      const float* ce, int ch) {
     const int cx = ch / nz, cz = ch - (ch / nz) * nz;
-    const float rc = ldv<kL2>(r + ch);
-    const float xc = dinv[ch] * rc + ldv<kL2>(ce + (cx >> 1) * cnz + (cz >> 1));
+    const float rc = r[ch];
+    const float xc = dinv[ch] * rc + ce[(cx >> 1) * cnz + (cz >> 1)];
     float res = rc;
 #pragma unroll
     for (int dx = -1; dx <= 1; dx++) {
@@ -135,7 +125,7 @@ __device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, 
         for (int dz = -1; dz <= 1; dz++) {
             const int nx_ = clampi(cx + dx, nx - 1), nz_ = clampi(cz + dz, nz - 1);
             const int nb = nx_ * nz + nz_;
-            const float xn = dinv[nb] * ldv<kL2>(r + nb) + ldv<kL2>(ce + (nx_ >> 1) * cnz + (nz_ >> 1));
+            const float xn = dinv[nb] * r[nb] + ce[(nx_ >> 1) * cnz + (nz_ >> 1)];
             res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * xn;
         }
     }
