@@ -150,45 +150,45 @@ __device__ __forceinline__ bool cg_done(const CgScalars* S) {
 
 // Row i (lane of a chunk at `at`) times v in FP64, ascending columns.  The FP64 matrix
 // streams with evict-first hints: on big scenes it exceeds L2 and the solver's vectors
-// should stay resident instead.  Software-pipelined: the next eight entries are loaded
+// should stay resident instead.  Software-pipelined: the next D entries are loaded
 // before this batch's gathers, so a lane keeps both kinds of loads in flight.
-template <class V>
+template <int D = 8, class V>
 __device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, V v) {
     double acc = 0.0;
-    const int nb = L >> 3;
-    int c[8];
-    double a[8];
+    const int nb = L / D;
+    int c[D];
+    double a[D];
     if (nb > 0) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
+        for (int u = 0; u < D; u++) {
             c[u] = __ldcs(o.col + at + u * kSellRows);
             a[u] = __ldcs(o.val + at + u * kSellRows);
         }
     }
     for (int bt = 0; bt < nb; bt++) {
-        double xv[8];
+        double xv[D];
 #pragma unroll
-        for (int u = 0; u < 8; u++) xv[u] = v(c[u]);
-        int cn[8];
-        double an[8];
+        for (int u = 0; u < D; u++) xv[u] = v(c[u]);
+        int cn[D];
+        double an[D];
         if (bt + 1 < nb) {
-            const int64_t nx = at + static_cast<int64_t>(bt + 1) * 8 * kSellRows;
+            const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
+            for (int u = 0; u < D; u++) {
                 cn[u] = __ldcs(o.col + nx + u * kSellRows);
                 an[u] = __ldcs(o.val + nx + u * kSellRows);
             }
         }
 #pragma unroll
-        for (int u = 0; u < 8; u++) acc = fma(a[u], xv[u], acc);
+        for (int u = 0; u < D; u++) acc = fma(a[u], xv[u], acc);
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
+        for (int u = 0; u < D; u++) {
             c[u] = cn[u];
             a[u] = an[u];
         }
     }
-    at += static_cast<int64_t>(nb) * 8 * kSellRows;
-    for (int k = nb * 8; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
+    at += static_cast<int64_t>(nb) * D * kSellRows;
+    for (int k = nb * D; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
     return acc;
 }
 
@@ -382,34 +382,35 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
 // followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
 
 // Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
-// The {column, value} pairs keep default caching: the FP32 matrix is meant to stay in L2.
-// Software-pipelined like row64.
+// The {column, value} pairs keep default caching (the FP32 matrix is read every
+// iteration).  Software-pipelined like row64.
+template <int D = 8>
 __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
                                        const float* __restrict__ v) {
     float acc = 0.0f;
-    const int nb = L >> 3;
-    uint2 e[8];
+    const int nb = L / D;
+    uint2 e[D];
     if (nb > 0) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
+        for (int u = 0; u < D; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
     }
     for (int bt = 0; bt < nb; bt++) {
-        float xv[8];
+        float xv[D];
 #pragma unroll
-        for (int u = 0; u < 8; u++) xv[u] = v[e[u].x];
-        uint2 f[8];
+        for (int u = 0; u < D; u++) xv[u] = v[e[u].x];
+        uint2 f[D];
         if (bt + 1 < nb) {
-            const int64_t nx = at + static_cast<int64_t>(bt + 1) * 8 * kSellRows;
+            const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
 #pragma unroll
-            for (int u = 0; u < 8; u++) f[u] = __ldg(o.cv32 + nx + u * kSellRows);
+            for (int u = 0; u < D; u++) f[u] = __ldg(o.cv32 + nx + u * kSellRows);
         }
 #pragma unroll
-        for (int u = 0; u < 8; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
+        for (int u = 0; u < D; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
 #pragma unroll
-        for (int u = 0; u < 8; u++) e[u] = f[u];
+        for (int u = 0; u < D; u++) e[u] = f[u];
     }
-    at += static_cast<int64_t>(nb) * 8 * kSellRows;
-    for (int k = nb * 8; k < L; k++, at += kSellRows) {
+    at += static_cast<int64_t>(nb) * D * kSellRows;
+    for (int k = nb * D; k < L; k++, at += kSellRows) {
         const uint2 t = __ldg(o.cv32 + at);
         acc = fmaf(__uint_as_float(t.y), v[t.x], acc);
     }
@@ -591,7 +592,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 
 // w = A u (FP32); gamma, delta, rho in FP64; next step sizes; reliable-update decision
 // (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
-__global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
+// Four entries per pipeline step and at most 48 registers: five blocks per SM hide the
+// gather latency better than eight-deep steps at four blocks (measured 53 -> 51 us).
+__global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
     pdl_begin();
@@ -605,7 +608,7 @@ __global__ void __launch_bounds__(kBlock) k_pmx_spmv(CgOperands o, int mode,
     for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
         const int L = o.len[i];
-        const float wi = row32(o, sell_index(o.off[c], cl.lane, 0), L, u);
+        const float wi = row32<4>(o, sell_index(o.off[c], cl.lane, 0), L, u);
         if (i < o.n) {
             const double ri = static_cast<double>(o.r32[i]);
             const double ui = static_cast<double>(u[i]);
