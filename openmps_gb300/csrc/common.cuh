@@ -276,6 +276,10 @@ void launch_error_correction(const SceneConst& sc, const DeviceState& st, cudaSt
 void launch_density_variation(const SceneConst& sc, const DeviceState& st, double* out,
                               cudaStream_t s);
 void launch_explicit(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// density + ECS (when flagged) + explicit accelerations in one neighbour walk; then the
+// explicit move (the second loop of ComputeExplicitForces)
+void launch_pre_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_explicit_update(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
@@ -287,6 +291,7 @@ void launch_exclusive_scan(const int* in, int* out, int m, int* scratch, cudaStr
 // number of kernels each launcher issues (for the launch counter)
 constexpr int kLaunchesSearch = 3, kLaunchesDensity = 1, kLaunchesEcs = 1, kLaunchesExplicit = 2,
               kLaunchesSaveX = 1, kLaunchesSetPpe = 6, kLaunchesAssign = 1, kLaunchesGradient = 2,
-              kLaunchesDs = 2, kLaunchesDt = 1, kLaunchesCfl = 2;
+              kLaunchesDs = 2, kLaunchesDt = 1, kLaunchesCfl = 2, kLaunchesPrePressure = 1,
+              kLaunchesExplicitUpdate = 1;
 
 }  // namespace mpsgb

@@ -694,17 +694,15 @@ void forward(mps_handle* h, double dt) {
         launched(h, kLaunchesCfl);
     }
     do_search(h);
+    // density, ECS and the explicit accelerations share one neighbour walk (the
+    // "density" stage time covers all three; "ecs" is empty; "explicit" is the move)
     stage_mark(h, kDensity);
-    launch_density(sc, h->st, s);
-    launched(h, kLaunchesDensity);
+    launch_pre_pressure(sc, h->st, s);
+    launched(h, kLaunchesPrePressure);
     stage_mark(h, kEcs);
-    if (flags & MPS_FLAG_ECS) {
-        launch_error_correction(sc, h->st, s);
-        launched(h, kLaunchesEcs);
-    }
     stage_mark(h, kExplicit);
-    launch_explicit(sc, h->st, s);
-    launched(h, kLaunchesExplicit);
+    launch_explicit_update(sc, h->st, s);
+    launched(h, kLaunchesExplicitUpdate);
     stage_mark(h, kDensity2);
     launch_density(sc, h->st, s);
     launched(h, kLaunchesDensity);
@@ -834,18 +832,16 @@ void batch_stages_pre(mps_handle* h, double dt) {
     sc.guard = 1;
     launch_set_dt(sc, h->st, dt, s);
     do_search(h);
-    launch_density(sc, h->st, s);
-    if (h->prm.flags & MPS_FLAG_ECS) launch_error_correction(sc, h->st, s);
-    launch_explicit(sc, h->st, s);
+    launch_pre_pressure(sc, h->st, s);
+    launch_explicit_update(sc, h->st, s);
     launch_density(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
     launch_set_ppe(sc, h->st, true, s);
     h->ppe_fp32 = true;
     check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
     after_launch("batch stages");
-    launched(h, kLaunchesDt + kLaunchesSearch + 2 * kLaunchesDensity + kLaunchesExplicit + kLaunchesSetPpe +
-                    ((h->prm.flags & MPS_FLAG_ECS) ? kLaunchesEcs : 0) +
-                    ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
+    launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate + kLaunchesDensity +
+                    kLaunchesSetPpe + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
 }
 
 void batch_stages_post(mps_handle* h) {

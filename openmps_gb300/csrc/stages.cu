@@ -208,6 +208,93 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     st.duz[i] = vz + (-sc.g);
 }
 
+// The stages between the search and the move in one walk over each neighbour row:
+// ComputeNeighborDensities, ComputeErrorCorrection (with ECS) and the first loop of
+// ComputeExplicitForces (fluid particles).  All three read positions and velocities that
+// none of them writes, and each writes only its own particle's results, so one walk
+// gives exactly what k_density, k_error_correction and k_explicit_accel give: every
+// accumulator sees the same terms in the same list order, and the square root of a pair
+// is computed once for all of them.
+template <bool kEcs>
+__global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    if (spp) st.n_wo_spp[i] = sc.n0;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
+    const bool fluid = t == MPS_TYPE_FLUID;
+    const bool hs = kEcs && has_flag(sc.flags, MPS_FLAG_HS);
+    const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
+    double thisN = 0.0, hsum = 0.0;
+    double vx = 0.0, vz = 0.0, gx = 0.0, gz = 0.0;
+    const float out_thr = fluid ? fmaxf(sc.f32_out_re, sc.f32_out_rl) : sc.f32_out_re;
+    for_near(sc, st, i, out_thr, [&](int j) {
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        const bool in_re = r2 < sc.re2;
+        const bool in_rl = fluid && r2 < sc.rl2;
+        if (!in_re && !in_rl) return;
+        const double r = __dsqrt_rn(r2);
+        if (in_re) {
+            thisN += weight(r, sc.re);
+            if (hs) {
+                const double du = st.u[j] - ui;
+                const double dw = st.w[j] - wi;
+                hsum += dot2(dx, dz, du, dw) / (r * r * r);
+            }
+        }
+        if (in_rl) {
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double c = viscosity_coefficient(sc, r);
+                vx += c * (st.u[j] - ui);
+                vz += c * (st.w[j] - wi);
+            } else {
+                vx = __dadd_rn(vx, 0.0);
+                vz = __dadd_rn(vz, 0.0);
+            }
+            if (spp) {
+                const double wg = weight(r, sc.re_lap);
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    });
+    // ComputeNeighborDensities
+    double nd;
+    if (spp) {
+        st.n_wo_spp[i] = thisN;
+        nd = (thisN < sc.n0) ? sc.n0 : thisN;
+    } else {
+        nd = thisN;
+    }
+    st.nd[i] = nd;
+    // ComputeErrorCorrection (NeighborDensityVariationSpeed on the same walk)
+    if (kEcs) {
+        double speed;
+        if (has_flag(sc.flags, MPS_FLAG_HS)) {
+            speed = (spp && thisN < sc.n0) ? 0.0 : -sc.re * hsum;
+        } else {
+            speed = (nd - sc.n0) / st.step->dt;
+        }
+        const double error = (nd - sc.n0) / sc.n0;
+        st.ecs[i] = fabs(error) * speed + fabs(speed) * error;
+    }
+    if (!fluid) return;
+    // ComputeExplicitForces, first loop
+    double xs, zs;
+    if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
+        const double ddx = xi - xs, ddz = zi - zs;
+        const double c = viscosity_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        vx += c * (ui - ui);
+        vz += c * (wi - wi);
+    }
+    st.dux[i] = __dadd_rn(vx, 0.0);
+    st.duz[i] = vz + (-sc.g);
+}
+
 // ComputeExplicitForces, second loop (Computer.hpp:995-1020).
 __global__ void k_explicit_update(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -497,6 +584,17 @@ void launch_error_correction(const SceneConst& sc, const DeviceState& st, cudaSt
 void launch_density_variation(const SceneConst& sc, const DeviceState& st, double* out,
                               cudaStream_t s) {
     k_density_variation<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, out);
+}
+
+void launch_pre_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    if ((sc.flags & MPS_FLAG_ECS) != 0u)
+        k_pre_pressure<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    else
+        k_pre_pressure<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_explicit_update(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_explicit_update<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_explicit(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
