@@ -282,6 +282,10 @@ void launch_pre_pressure(const SceneConst& sc, const DeviceState& st, cudaStream
 void launch_explicit_update(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
+// the second number density and the PPE assembly in one neighbour walk (SPP method set:
+// the assembly then needs no neighbour density); same launch count as launch_set_ppe
+bool density_ppe_fusable(const SceneConst& sc);
+void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

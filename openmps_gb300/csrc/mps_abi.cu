@@ -704,14 +704,20 @@ void forward(mps_handle* h, double dt) {
     launch_explicit_update(sc, h->st, s);
     launched(h, kLaunchesExplicitUpdate);
     stage_mark(h, kDensity2);
-    launch_density(sc, h->st, s);
-    launched(h, kLaunchesDensity);
+    const bool fused = density_ppe_fusable(sc);  // the "ppe" stage time then covers density 2
+    if (!fused) {
+        launch_density(sc, h->st, s);
+        launched(h, kLaunchesDensity);
+    }
     if (flags & MPS_FLAG_DS) {
         launch_save_x(sc, h->st, s);
         launched(h, kLaunchesSaveX);
     }
     stage_mark(h, kPpe);
-    launch_set_ppe(sc, h->st, wants_fp32(h), s);
+    if (fused)
+        launch_density_set_ppe(sc, h->st, wants_fp32(h), s);
+    else
+        launch_set_ppe(sc, h->st, wants_fp32(h), s);
     h->ppe_fp32 = wants_fp32(h);
     launched(h, kLaunchesSetPpe);
     after_launch("stages");
@@ -834,14 +840,18 @@ void batch_stages_pre(mps_handle* h, double dt) {
     do_search(h);
     launch_pre_pressure(sc, h->st, s);
     launch_explicit_update(sc, h->st, s);
-    launch_density(sc, h->st, s);
+    const bool fused = density_ppe_fusable(sc);
+    if (!fused) launch_density(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
-    launch_set_ppe(sc, h->st, true, s);
+    if (fused)
+        launch_density_set_ppe(sc, h->st, true, s);
+    else
+        launch_set_ppe(sc, h->st, true, s);
     h->ppe_fp32 = true;
     check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
     after_launch("batch stages");
-    launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate + kLaunchesDensity +
-                    kLaunchesSetPpe + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
+    launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate +
+                    (fused ? 0 : kLaunchesDensity) + kLaunchesSetPpe + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
 }
 
 void batch_stages_post(mps_handle* h) {

@@ -399,6 +399,87 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     st.ppe_len[row] = m + 1;
 }
 
+// Number density after the move (the second ComputeNeighborDensities) and the PPE
+// assembly in one walk over each neighbour row, for the SPP method set: there the
+// assembly reads only the particle's own density (space potential particles replace the
+// surface test on the neighbours' densities), so the two stages fuse.  The density and
+// source terms run on the entries within r_e, the Laplacian on those within the
+// Laplacian radius, each in list order as in k_density and k_ppe_build.
+__global__ void k_density_ppe(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const int n = sc.n;
+    const int row = ppe_row(st, i);
+    st.n_wo_spp[i] = sc.n0;
+    const int t = st.type[i];
+    if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) {
+        st.ppe_b[row] = 0;
+        st.ppe_x[row] = 0;
+        st.ppe_col_tmp[ell(0, n, i)] = row;
+        st.ppe_val_tmp[ell(0, n, i)] = 1.0;
+        st.ppe_len[row] = 1;
+        return;
+    }
+    const bool hs = has_flag(sc.flags, MPS_FLAG_HS);
+    const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
+    double thisN = 0.0, hsum = 0.0, a_ii = 0.0, gx = 0.0, gz = 0.0;
+    int m = 0;
+    for_near(sc, st, i, fmaxf(sc.f32_out_re, sc.f32_out_rl), [&](int j) {
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dot2(dx, dz, dx, dz);
+        const bool in_re = r2 < sc.re2;
+        const bool in_rl = r2 < sc.rl2;
+        if (!in_re && !in_rl) return;
+        const double r = __dsqrt_rn(r2);
+        if (in_re) {
+            thisN += weight(r, sc.re);
+            if (hs) {
+                const double du = st.u[j] - ui;
+                const double dw = st.w[j] - wi;
+                hsum += dot2(dx, dz, du, dw) / (r * r * r);
+            }
+        }
+        if (in_rl) {
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double a_ij = ppe_coefficient(sc, r);
+                st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
+                st.ppe_val_tmp[ell(m, n, i)] = a_ij;
+                m++;
+                a_ii += -a_ij;
+            } else {
+                a_ii = __dadd_rn(a_ii, 0.0);
+            }
+            const double wg = weight(r, sc.re_lap);
+            gx += wg * dx;
+            gz += wg * dz;
+        }
+    });
+    // ComputeNeighborDensities
+    st.n_wo_spp[i] = thisN;
+    const double nd = (thisN < sc.n0) ? sc.n0 : thisN;
+    st.nd[i] = nd;
+    // right-hand side (NeighborDensityVariationSpeed) and initial guess
+    const double dt = st.step->dt;
+    const double speed = hs ? ((thisN < sc.n0) ? 0.0 : -sc.re * hsum) : (nd - sc.n0) / dt;
+    if (has_flag(sc.flags, MPS_FLAG_ECS)) {
+        const double e = st.ecs[i];
+        st.ppe_b[row] = -sc.rho / (sc.n0 * dt) * (speed + e);
+    } else {
+        st.ppe_b[row] = -sc.rho / (sc.n0 * dt) * speed;
+    }
+    st.ppe_x[row] = st.p[i];
+    double xs, zs;
+    if (spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
+        const double ddx = xi - xs, ddz = zi - zs;
+        a_ii += -ppe_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+    }
+    st.ppe_col_tmp[ell(m, n, i)] = row;
+    st.ppe_val_tmp[ell(m, n, i)] = a_ii;
+    st.ppe_len[row] = m + 1;
+}
+
 // Chunk sizes of the SELL-32 layout: one warp per chunk of 32 rows.
 __global__ void k_ppe_chunks(SceneConst sc, DeviceState st) {
     const int c = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -606,11 +687,22 @@ void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s) 
     k_save_x<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
-void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
-    k_ppe_build<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+void launch_ppe_layout(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
     k_ppe_chunks<<<grid_for(static_cast<int64_t>(sc.nchunks) * 32), kBlock, 0, s>>>(sc, st);
     launch_exclusive_scan(st.ppe_chunk, st.ppe_off, sc.nchunks, st.scan_scratch, s);
     k_ppe_sort<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, want_fp32 ? 1 : 0);
+}
+
+void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
+    k_ppe_build<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    launch_ppe_layout(sc, st, want_fp32, s);
+}
+
+bool density_ppe_fusable(const SceneConst& sc) { return (sc.flags & MPS_FLAG_SPP) != 0u; }
+
+void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
+    k_density_ppe<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    launch_ppe_layout(sc, st, want_fp32, s);
 }
 
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {

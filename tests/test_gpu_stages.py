@@ -161,8 +161,9 @@ def test_cfl_time_step(gpu_lib, oracle_lib):
                                   "stock_two_radii", "stock_far_from_origin"])
 def test_step_equals_stage_chain(gpu_lib, oracle_lib, case):
     # mps_forward_time walks each neighbour row once for density, ECS and the explicit
-    # accelerations together; the stage entry points run the three separately.  The
-    # results must be bit-identical (same terms, same order) through a whole step.
+    # accelerations together, and once for the second density and the PPE assembly
+    # (SPP method set); the stage entry points run each stage separately.  The results
+    # must be bit-identical (same terms, same order) through a whole step.
     s = CASES[case]()
     prm = s.params()
     flags = prm.flags
@@ -189,5 +190,9 @@ def test_step_equals_stage_chain(gpu_lib, oracle_lib, case):
     for k in ("type", "x", "z", "u", "w", "p", "n"):
         np.testing.assert_array_equal(A[k], B[k], err_msg="%s %s" % (case, k))
     xa, xb = a.aux(), b.aux()
-    for k in ("n_without_spp", "ecs"):
+    for k in ("n_without_spp", "ecs", "ox", "oz"):
         np.testing.assert_array_equal(xa[k], xb[k], err_msg="%s %s" % (case, k))
+    # the PPE system each path assembled (the step fuses the second density into it
+    # for the SPP method set)
+    for ga, gb, what in zip(a.ppe(), b.ppe(), ("row_ptr", "columns", "values", "rhs", "guess")):
+        np.testing.assert_array_equal(ga, gb, err_msg="%s %s" % (case, what))
