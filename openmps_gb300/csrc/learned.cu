@@ -42,7 +42,7 @@ constexpr int kSmA0 = 0;                        // 128 x 16 BF16
 constexpr int kSmA = kSmA0 + kTile * 16 * 2;    // 128 x 64 BF16
 constexpr int kSmImg = kSmA + kTile * 64 * 2;
 constexpr int kSmBar = (kSmImg + kImgBytes + 15) / 16 * 16;
-constexpr int kSmBytes = 64 * 1024;
+constexpr int kSmBytes = 48 * 1024;  // four CTAs per SM: the whole grid is resident
 
 // byte offset of element (r, k) of a K-major operand with `rows` rows
 __host__ __device__ constexpr int core_offset(int r, int k, int rows) {
@@ -173,18 +173,27 @@ __global__ void __launch_bounds__(kTile) k_mlp_tc(const unsigned char* __restric
     bool bad = false;
     const int ntiles = (n + kTile - 1) / kTile;
 
+    // features of the CTA's next tile are loaded while the current tile runs its layers
+    float4 nxt[4];
+    auto load_tile = [&](int tile) {
+        const int r = tile * kTile + t;
+        if (tile < ntiles && r < n) {
+            const float4* f4 = reinterpret_cast<const float4*>(feat + static_cast<int64_t>(r) * kMlpIn);
+#pragma unroll
+            for (int q = 0; q < 4; q++) nxt[q] = __ldg(f4 + q);
+        }
+    };
+    load_tile(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles && !bad; tile += gridDim.x) {
         const int row = tile * kTile + t;
         float x[16];
         if (row < n) {
-            const float4* f4 = reinterpret_cast<const float4*>(feat + static_cast<int64_t>(row) * kMlpIn);
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const float4 v = f4[q];
-                x[4 * q] = v.x;
-                x[4 * q + 1] = v.y;
-                x[4 * q + 2] = v.z;
-                x[4 * q + 3] = v.w;
+                x[4 * q] = nxt[q].x;
+                x[4 * q + 1] = nxt[q].y;
+                x[4 * q + 2] = nxt[q].z;
+                x[4 * q + 3] = nxt[q].w;
             }
             x[8] *= inv_sigma;
             x[9] *= inv_sigma;
@@ -195,6 +204,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_tc(const unsigned char* __restric
 #pragma unroll
             for (int k = 0; k < 16; k++) x[k] = 0.0f;
         }
+        load_tile(tile + gridDim.x);
         store_row8(A0, kTile, t, 0, x);
         store_row8(A0, kTile, t, 1, x + 8);
         proxy_fence();

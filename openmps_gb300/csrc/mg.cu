@@ -175,6 +175,10 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
             }
         }
     }
+    // elimination: G threads per row, each over the columns g, g + G, ... (no division
+    // in the pivot loop); the block has at least m threads
+    const int G = max(1, static_cast<int>(blockDim.x) / m);
+    const int my_i = threadIdx.x / G, my_g = threadIdx.x - (threadIdx.x / G) * G;
     for (int p = 0; p < m; p++) {
         __syncthreads();
         if (threadIdx.x == 0) piv[0] = 1.0f / A[p * m + p];
@@ -183,10 +187,10 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
         const float ip = piv[0];
         for (int j = threadIdx.x; j < m; j += blockDim.x) A[p * m + j] = (j == p ? 1.0f : A[p * m + j]) * ip;
         __syncthreads();
-        for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
-            const int i = idx / m, j = idx - (idx / m) * m;
-            if (i == p) continue;
-            A[idx] = (j == p ? 0.0f : A[idx]) - colp[i] * A[p * m + j];
+        if (my_i < m && my_i != p) {
+            const float cp = colp[my_i];
+            float* row = A + my_i * m;
+            for (int j = my_g; j < m; j += G) row[j] = (j == p ? 0.0f : row[j]) - cp * A[p * m + j];
         }
     }
     __syncthreads();
