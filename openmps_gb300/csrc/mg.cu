@@ -13,8 +13,9 @@
 //   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
 //   and after a reliable update k_mg_restrict0), k_mg_down (levels above the bottom),
 //   k_mg_bottom (the coarsest levels in one block, all in shared memory, __syncthreads
-//   between levels), k_mg_up, k_mg_up_prolong (level-1 post-smoothing + prolongation to
-//   the particles; k_mg_prolong0 when the bottom block covers level 1).
+//   between levels), k_mg_up, k_mg_up_prolong_rows (level-1 post-smoothing + prolongation
+//   to the particles, one thread per row; k_mg_prolong0 when the bottom block covers
+//   level 1).
 // A 16-block cluster kernel for levels 2 .. coarsest (cluster barriers between levels)
 // was measured slower: about 4 us per level against well under 1 us per level for one
 // block with __syncthreads, and the grid-wide kernels for the larger levels.
@@ -271,28 +272,28 @@ __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const Cg
     f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
 }
 
-// Level-1 post-smoothing fused with the prolongation to the particles of the cell:
-// u = s_i dinv0_i r_i + e_1 on active rows, 0 on identity rows (one warp per cell).
-__global__ void __launch_bounds__(kBlock) k_mg_up_prolong(MgLevel f, MgLevel c, const int32_t* cell_start,
-                                                          const float* dinv0, const float* scale,
-                                                          const float* r, float* u,
-                                                          const CgScalars* S, int mode,
-                                                          const int32_t* active, const int32_t* n_active) {
+// Level-1 post-smoothing fused with the prolongation, one thread per row: the rows of a
+// cell are contiguous, so the threads of a warp mostly share one cell and its stencil
+// loads hit in L1 (the correction is a pure function of the cell: every row of the cell
+// gets the same value).  Rows outside every cell and identity rows get u = 0.
+__global__ void __launch_bounds__(kBlock) k_mg_up_prolong_rows(MgLevel f, MgLevel c, int n, const int32_t* row_cell,
+                                                               const float* dinv0, const float* scale,
+                                                               const float* r, float* u, const CgScalars* S,
+                                                               int mode) {
     pdl_begin();
     if (pcg_skip(S, mode)) return;
-    const int lane = threadIdx.x & 31;
-    const int nact = *n_active;
-    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
-        const int ch = active[a];
-        const int end = cell_start[ch + 1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = dinv0[i];
+    const int code = row_cell[i];
+    float v = 0.0f;
+    if (d != 0.0f && code >= 0) {
+        const int ch = (code >> 16) * f.nz + (code & 0xffff);
         const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
-        for (int i = cell_start[ch] + lane; i < end; i += 32) {
-            const float d = dinv0[i];
-            const float sc = scale ? scale[i] : 1.0f;
-            u[i] = d != 0.0f ? sc * d * r[i] + e : 0.0f;
-        }
+        const float sc = scale ? scale[i] : 1.0f;
+        v = sc * d * r[i] + e;
     }
+    u[i] = v;
 }
 
 struct MgBottom {
@@ -481,8 +482,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     for (int l = mg.bottom - 1; l >= 2; l--)
         launch_pdl(k_mg_up, grid_for(mg.lv[l].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
     if (mg.bottom > 1)
-        launch_pdl(k_mg_up_prolong, g1, kBlock, 0, s, L1, mg.lv[2], mg.cell_start, mg.dinv0, mg.scale, r, u, S,
-                   mode, mg.active, mg.n_active);
+        launch_pdl(k_mg_up_prolong_rows, grid_for(mg.n), kBlock, 0, s, L1, mg.lv[2], mg.n, mg.cell_xz, mg.dinv0,
+                   mg.scale, r, u, S, mode);
     else
         launch_pdl(k_mg_prolong0, grid_for(mg.n), kBlock, 0, s, mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
                    r, L1.e, u, S, mode);
