@@ -255,12 +255,21 @@ __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLev
     }
 }
 
+// Coarse residuals, four threads per coarse cell (one per child, adjacent lanes, summed
+// with two shuffles in a fixed order): four times the parallelism of a thread per cell
+// for these latency-bound stencils.
 __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
     pdl_begin();
     if (pcg_skip(S, mode)) return;
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= c.cells) return;
-    c.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / c.nz, I - (I / c.nz) * c.nz);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = t >> 2;
+    const int cell = min(I, c.cells - 1);  // whole groups of four stay in the shuffles
+    const int X = cell / c.nz, Z = cell - (cell / c.nz) * c.nz;
+    const int a = (t >> 1) & 1, b = t & 1;
+    float v = child_residual(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, 2 * X + a, 2 * Z + b);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    if ((t & 3) == 0 && I < c.cells) c.r[I] = v;
 }
 
 // Post-smoothed correction of the level-f cells (levels 2 .. above the bottom block).
@@ -472,7 +481,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     else
         launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
     for (int l = 1; l < mg.bottom; l++)
-        launch_pdl(k_mg_down, grid_for(mg.lv[l + 1].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
+        launch_pdl(k_mg_down, grid_for(4 * static_cast<int64_t>(mg.lv[l + 1].cells)), kBlock, 0, s, mg.lv[l],
+                   mg.lv[l + 1], S, mode);
     MgBottom B{};
     B.first = mg.bottom;
     B.last = mg.levels;

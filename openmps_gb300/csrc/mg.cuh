@@ -111,6 +111,25 @@ __device__ __forceinline__ float child_residuals(int nx, int nz, int cells, cons
     return sum;
 }
 
+// Residual of fine cell (cx, cz) after the pre-smoothing x = dinv * r (0 outside the grid):
+// one child's share of child_residuals.
+__device__ __forceinline__ float child_residual(int nx, int nz, int cells, const float* k,
+                                                const float* dinv, const float* r, int cx, int cz) {
+    const bool valid = cx < nx && cz < nz;
+    const int ccx = min(cx, nx - 1), ccz = min(cz, nz - 1);
+    const int ch = ccx * nz + ccz;
+    float res = r[ch];
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+        for (int dz = -1; dz <= 1; dz++) {
+            const int nb = clampi(ccx + dx, nx - 1) * nz + clampi(ccz + dz, nz - 1);
+            res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * (dinv[nb] * r[nb]);
+        }
+    }
+    return valid ? res : 0.0f;
+}
+
 // Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
 __device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
                                                      const float* dinv, const float* r, int cnz,
