@@ -272,13 +272,33 @@ __global__ void __launch_bounds__(kBlock) k_mg_down(MgLevel f, MgLevel c, const 
     if ((t & 3) == 0 && I < c.cells) c.r[I] = v;
 }
 
-// Post-smoothed correction of the level-f cells (levels 2 .. above the bottom block).
+// Post-smoothed correction of the level-f cells (levels 2 .. above the bottom block), four
+// threads per cell: each takes a share of the nine stencil terms (3, 2, 2, 2), summed with
+// two shuffles in a fixed order.
 __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const CgScalars* S, int mode) {
     pdl_begin();
     if (pcg_skip(S, mode)) return;
-    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ch >= f.cells) return;
-    f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch0 = t >> 2;
+    const int ch = min(ch0, f.cells - 1);  // whole groups of four stay in the shuffles
+    const int q = t & 3;
+    const int cx = ch / f.nz, cz = ch - (ch / f.nz) * f.nz;
+    const int first = q == 0 ? 0 : 1 + 2 * q, count = q == 0 ? 3 : 2;  // terms 0-2, 3-4, 5-6, 7-8
+    float part = 0.0f;
+    for (int k = first; k < first + count; k++) {
+        const int dx = k / 3 - 1, dz = k - (k / 3) * 3 - 1;
+        const int nx_ = clampi(cx + dx, f.nx - 1), nz_ = clampi(cz + dz, f.nz - 1);
+        const int nb = nx_ * f.nz + nz_;
+        const float xn = f.dinv[nb] * f.r[nb] + c.e[(nx_ >> 1) * c.nz + (nz_ >> 1)];
+        part += f.k32[k * f.cells + ch] * xn;
+    }
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    if (q == 0 && ch0 < f.cells) {
+        const float rc = f.r[ch];
+        const float xc = f.dinv[ch] * rc + c.e[(cx >> 1) * c.nz + (cz >> 1)];
+        f.e[ch] = xc + f.dinv[ch] * (rc - part);
+    }
 }
 
 // Level-1 post-smoothing fused with the prolongation, one thread per row: the rows of a
@@ -490,7 +510,8 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     B.dense = mg.dense;
     launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_bytes(mg.lv, mg.bottom, mg.levels), s, B, S, mode);
     for (int l = mg.bottom - 1; l >= 2; l--)
-        launch_pdl(k_mg_up, grid_for(mg.lv[l].cells), kBlock, 0, s, mg.lv[l], mg.lv[l + 1], S, mode);
+        launch_pdl(k_mg_up, grid_for(4 * static_cast<int64_t>(mg.lv[l].cells)), kBlock, 0, s, mg.lv[l], mg.lv[l + 1],
+                   S, mode);
     if (mg.bottom > 1)
         launch_pdl(k_mg_up_prolong_rows, grid_for(mg.n), kBlock, 0, s, L1, mg.lv[2], mg.n, mg.cell_xz, mg.dinv0,
                    mg.scale, r, u, S, mode);
