@@ -168,26 +168,34 @@ __device__ __forceinline__ int range_class(float xi, float zi, float si, float x
 }
 
 // Calls f(j) for the entries of row i that may pass the FP64 range test whose FP32
-// upper bound is `out_thr`, in list order.  Entries are screened 64 at a time into a
-// bit mask first, so the FP64 work of a warp runs once per candidate of its busiest lane
-// rather than once per list entry (a 64-entry window holds most of a row, so the
-// busiest lane of each window is close to the busiest lane of the row).
+// upper bound is `out_thr`, in list order.  Entries are screened 128 at a time into a
+// bit mask first (two 64-bit words: a whole row of the usual radii), so the FP64 work of
+// a warp runs once per candidate of its busiest lane rather than once per list entry.
 template <class F>
 __device__ __forceinline__ void for_near(const SceneConst& sc, const DeviceState& st, int i,
                                          float out_thr, F f) {
     const float xi = st.x32[i], zi = st.z32[i];
     const float si = fabsf(xi) + fabsf(zi);
     const int cnt = st.nb_count[i];
-    for (int base = 0; base < cnt; base += 64) {
-        const int m = min(64, cnt - base);
-        unsigned long long mask = 0ull;
+    for (int base = 0; base < cnt; base += 128) {
+        const int m = min(128, cnt - base);
+        unsigned long long lo = 0ull, hi = 0ull;
         for (int t = 0; t < m; t++) {
             const int j = st.nb[static_cast<int64_t>(base + t) * sc.n + i];
-            if (!surely_out(xi, zi, si, st.x32[j], st.z32[j], out_thr)) mask |= 1ull << t;
+            if (!surely_out(xi, zi, si, st.x32[j], st.z32[j], out_thr)) {
+                if (t < 64) lo |= 1ull << t;
+                else hi |= 1ull << (t - 64);
+            }
         }
-        while (mask) {
-            const int t = __ffsll(static_cast<long long>(mask)) - 1;
-            mask &= mask - 1ull;
+        while (lo | hi) {
+            int t;
+            if (lo) {
+                t = __ffsll(static_cast<long long>(lo)) - 1;
+                lo &= lo - 1ull;
+            } else {
+                t = 63 + __ffsll(static_cast<long long>(hi));
+                hi &= hi - 1ull;
+            }
             f(st.nb[static_cast<int64_t>(base + t) * sc.n + i]);
         }
     }
