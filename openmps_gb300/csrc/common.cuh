@@ -119,9 +119,28 @@ __device__ __forceinline__ double dot2(double a0, double a1, double b0, double b
     return __dadd_rn(__dadd_rn(0.0, __dmul_rn(a0, b0)), __dmul_rn(a1, b1));
 }
 
-// Particle::W (Particle.hpp:71-75)
+// The stage kernels are bound by GB300's FP64 pipe, so exact FP64 comparisons against a
+// positive finite bound run on the integer pipe: for b > 0 finite, a < b exactly when
+// the bit pattern of a, read as an unsigned integer, is below that of b (non-negative
+// doubles order like their bit patterns; -0, negative values and NaN of either sign
+// compare false, as in IEEE).
+__device__ __forceinline__ bool below(double a, double b) {
+    return static_cast<unsigned long long>(__double_as_longlong(a)) <
+           static_cast<unsigned long long>(__double_as_longlong(b));
+}
+
+// Squared distance: the reference's inner_prod(r, r) = (0 + dx dx) + dz dz.  The 0 + is
+// the identity here (a square is never -0), so it is left out.
+__device__ __forceinline__ double dist2(double dx, double dz) {
+    return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dz, dz));
+}
+
+// Particle::W (Particle.hpp:71-75); the test 0 < r < re on the integer pipe: bits(r) - 1
+// wraps for +0 and lands at or above bits(re) - 1 for r >= re, -0, negatives and NaN.
 __device__ __forceinline__ double weight(double r, double re) {
-    return ((0 < r) && (r < re)) ? __dadd_rn(__ddiv_rn(re, r), -1.0) : 0.0;
+    const unsigned long long br = static_cast<unsigned long long>(__double_as_longlong(r));
+    const unsigned long long be = static_cast<unsigned long long>(__double_as_longlong(re));
+    return (br - 1ull < be - 1ull) ? __dadd_rn(__ddiv_rn(re, r), -1.0) : 0.0;
 }
 
 __device__ __forceinline__ bool has_flag(uint32_t flags, uint32_t f) { return (flags & f) != 0u; }

@@ -52,8 +52,8 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
         for_near(sc, st, i, sc.f32_out_re, [&](int j) {
             const double dx = st.x[j] - xi;
             const double dz = st.z[j] - zi;
-            const double r2 = dot2(dx, dz, dx, dz);
-            if (r2 < sc.re2) {
+            const double r2 = dist2(dx, dz);
+            if (below(r2, sc.re2)) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
                 const double r = __dsqrt_rn(r2);
@@ -136,8 +136,8 @@ __global__ void k_density(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        if (r2 < sc.re2) thisN += weight(__dsqrt_rn(r2), sc.re);
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.re2)) thisN += weight(__dsqrt_rn(r2), sc.re);
     });
     if (spp) {
         st.n_wo_spp[i] = thisN;
@@ -180,8 +180,8 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        if (r2 < sc.rl2) {
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double c = viscosity_coefficient(sc, __dsqrt_rn(r2));
                 vx += c * (st.u[j] - ui);
@@ -233,9 +233,9 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, out_thr, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        const bool in_re = r2 < sc.re2;
-        const bool in_rl = fluid && r2 < sc.rl2;
+        const double r2 = dist2(dx, dz);
+        const bool in_re = below(r2, sc.re2);
+        const bool in_rl = fluid && below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
         const double r = __dsqrt_rn(r2);
         if (in_re) {
@@ -369,8 +369,8 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        if (r2 < sc.rl2) {
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double a_ij = ppe_coefficient(sc, __dsqrt_rn(r2));
                 if (spp || !is_surface(sc, st.nd[j])) {
@@ -428,9 +428,9 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, fmaxf(sc.f32_out_re, sc.f32_out_rl), [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        const bool in_re = r2 < sc.re2;
-        const bool in_rl = r2 < sc.rl2;
+        const double r2 = dist2(dx, dz);
+        const bool in_re = below(r2, sc.re2);
+        const bool in_rl = below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
         const double r = __dsqrt_rn(r2);
         if (in_re) {
@@ -543,8 +543,8 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        if (r2 < sc.re2) {
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.re2)) {
             const double wg = weight(__dsqrt_rn(r2), sc.re);
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double c = (st.p[j] + pi) / r2 * wg;
@@ -564,7 +564,7 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
         const double dx = xs - xi;
         const double dz = zs - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
+        const double r2 = dist2(dx, dz);
         const double c = (0.0 + pi) / r2 * weight(__dsqrt_rn(r2), sc.re);
         sx += c * dx;
         sz += c * dz;
@@ -589,9 +589,9 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
     for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
-        const double r2 = dot2(dx, dz, dx, dz);
-        if (r2 < sc.re2) {
-            if (st.type[j] != MPS_TYPE_DUMMY && r2 < d2) {
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.re2)) {
+            if (st.type[j] != MPS_TYPE_DUMMY && below(r2, d2)) {
                 const double dx0 = st.ox[j] - oxi;
                 const double dz0 = st.oz[j] - ozi;
                 const double nrm = __dsqrt_rn(dot2(dx0, dz0, dx0, dz0));
