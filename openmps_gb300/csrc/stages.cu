@@ -65,18 +65,31 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
     return (st.nd[i] - sc.n0) / dt;
 }
 
+// The constant factors of the Laplacian coefficients, evaluated once per thread in the
+// reference's left-to-right order (so each coefficient is the same rounding chain).
+struct LapFactors {
+    bool hl;
+    double visc;  // HL: ((nu 3) re_lap) / n0_lap; else (((nu 2) 2) / lambda_lap) / n0_lap
+    double ppe;   // HL: (3 re_lap) / n0_lap;       else (4 / lambda_lap) / n0_lap
+};
+__device__ __forceinline__ LapFactors lap_factors(const SceneConst& sc) {
+    LapFactors f;
+    f.hl = has_flag(sc.flags, MPS_FLAG_HL);
+    f.visc = f.hl ? sc.nu * 3.0 * sc.re_lap / sc.n0_lap : sc.nu * 2 * 2.0 / sc.lambda_lap / sc.n0_lap;
+    f.ppe = f.hl ? 3.0 * sc.re_lap / sc.n0_lap : 4.0 / sc.lambda_lap / sc.n0_lap;
+    return f;
+}
+
 // viscosity coefficient (Computer.hpp:963-970) at the Laplacian radius
-__device__ __forceinline__ double viscosity_coefficient(const SceneConst& sc, double r) {
-    if (has_flag(sc.flags, MPS_FLAG_HL)) return sc.nu * 3.0 * sc.re_lap / sc.n0_lap / (r * r * r);
-    const double wgt = weight(r, sc.re_lap);
-    return sc.nu * 2 * 2.0 / sc.lambda_lap / sc.n0_lap * wgt;
+__device__ __forceinline__ double viscosity_coefficient(const SceneConst& sc, const LapFactors& f, double r) {
+    if (f.hl) return f.visc / (r * r * r);
+    return f.visc * weight(r, sc.re_lap);
 }
 
 // PPE off-diagonal coefficient (Computer.hpp:1290-1297)
-__device__ __forceinline__ double ppe_coefficient(const SceneConst& sc, double r) {
-    if (has_flag(sc.flags, MPS_FLAG_HL)) return 3.0 * sc.re_lap / sc.n0_lap / (r * r * r);
-    const double wgt = weight(r, sc.re_lap);
-    return (4.0 / sc.lambda_lap / sc.n0_lap) * wgt;
+__device__ __forceinline__ double ppe_coefficient(const SceneConst& sc, const LapFactors& f, double r) {
+    if (f.hl) return f.ppe / (r * r * r);
+    return f.ppe * weight(r, sc.re_lap);
 }
 
 __device__ __forceinline__ bool ppe_alive(const SceneConst& sc, const DeviceState& st, int i) {
@@ -173,6 +186,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
+    const LapFactors lf = lap_factors(sc);
     if (st.type[i] != MPS_TYPE_FLUID) return;
     const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
@@ -183,7 +197,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double c = viscosity_coefficient(sc, __dsqrt_rn(r2));
+                const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(r2));
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
             } else {
@@ -200,7 +214,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
@@ -220,6 +234,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
+    const LapFactors lf = lap_factors(sc);
     const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     if (spp) st.n_wo_spp[i] = sc.n0;
     const int t = st.type[i];
@@ -248,7 +263,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
         }
         if (in_rl) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double c = viscosity_coefficient(sc, r);
+                const double c = viscosity_coefficient(sc, lf, r);
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
             } else {
@@ -287,7 +302,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
@@ -342,6 +357,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
+    const LapFactors lf = lap_factors(sc);
     const int n = sc.n;
     const int row = ppe_row(st, i);
     if (!ppe_alive(sc, st, i)) {
@@ -372,7 +388,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double a_ij = ppe_coefficient(sc, __dsqrt_rn(r2));
+                const double a_ij = ppe_coefficient(sc, lf, __dsqrt_rn(r2));
                 if (spp || !is_surface(sc, st.nd[j])) {
                     st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
                     st.ppe_val_tmp[ell(m, n, i)] = a_ij;
@@ -392,7 +408,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        a_ii += -ppe_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        a_ii += -ppe_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
     st.ppe_col_tmp[ell(m, n, i)] = row;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
@@ -409,6 +425,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
+    const LapFactors lf = lap_factors(sc);
     const int n = sc.n;
     const int row = ppe_row(st, i);
     st.n_wo_spp[i] = sc.n0;
@@ -443,7 +460,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         }
         if (in_rl) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double a_ij = ppe_coefficient(sc, r);
+                const double a_ij = ppe_coefficient(sc, lf, r);
                 st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
                 st.ppe_val_tmp[ell(m, n, i)] = a_ij;
                 m++;
@@ -473,7 +490,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        a_ii += -ppe_coefficient(sc, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        a_ii += -ppe_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
     st.ppe_col_tmp[ell(m, n, i)] = row;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
