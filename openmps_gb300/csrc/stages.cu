@@ -521,16 +521,37 @@ __global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
     if (i >= n) return;
     const int64_t base = st.ppe_off[row / kSellRows];
     const int r = row % kSellRows;
-    for (int e = 0; e < len; e++) {
+    auto put = [&](int e, int rank) {
         const int ce = st.ppe_col_tmp[ell(e, n, i)];
-        int rank = 0;
-        for (int f = 0; f < len; f++) rank += (st.ppe_col_tmp[ell(f, n, i)] < ce) ? 1 : 0;
         const double v = st.ppe_val_tmp[ell(e, n, i)];
         const int64_t at = sell_index(base, r, rank);
         st.ppe_col[at] = ce;
         st.ppe_val[at] = v;
         if (want_fp32) st.ppe_cv32[at] = make_uint2(static_cast<unsigned>(ce),
                                                      __float_as_uint(__double2float_rn(v)));
+    };
+    // Rows in search-cell order: a neighbour list walks the cells in ascending cell index
+    // and each cell in slot (= row) order, so the off-diagonal columns arrive ascending and
+    // only the diagonal (last) needs its place.  Checked on the way; a row that is not
+    // ascending takes the general rank computation.
+    bool ascending = st.row_of != nullptr;
+    for (int e = 1; ascending && e < len - 1; e++)
+        ascending = st.ppe_col_tmp[ell(e - 1, n, i)] < st.ppe_col_tmp[ell(e, n, i)];
+    if (ascending) {
+        int below_diag = 0;
+        for (int e = 0; e < len - 1; e++) {
+            const bool after = st.ppe_col_tmp[ell(e, n, i)] > row;
+            below_diag += after ? 0 : 1;
+            put(e, e + (after ? 1 : 0));
+        }
+        put(len - 1, below_diag);
+        return;
+    }
+    for (int e = 0; e < len; e++) {
+        const int ce = st.ppe_col_tmp[ell(e, n, i)];
+        int rank = 0;
+        for (int f = 0; f < len; f++) rank += (st.ppe_col_tmp[ell(f, n, i)] < ce) ? 1 : 0;
+        put(e, rank);
     }
 }
 
