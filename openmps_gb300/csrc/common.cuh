@@ -26,6 +26,7 @@
 namespace mpsgb {
 
 constexpr int kBlock = 256;
+constexpr int kReCache = 48;  // cached weights per particle (entries beyond are recomputed)
 
 // device status bits
 constexpr int kStatusCellOverflow = 1;
@@ -99,6 +100,10 @@ struct DeviceState {
     int32_t* unplaced;     // per particle: 1 without a cell slot
     int32_t* unplaced_pos; // exclusive prefix sum of unplaced (n + 1 entries)
     int32_t* row_scratch;  // scan scratch of the two prefix sums
+    // W(r, r_e) of the first kReCache list entries within r_e of each particle, in list
+    // order ([m n + i]), written by the fused density + assembly walk and read by the
+    // pressure gradient on the same positions
+    double* w_re;
     const int32_t* scene_of;  // batch: scene of each particle (its cells start at
                               // scene * cells_per_scene); null for a single scene
     int32_t *nb_count, *nb;
@@ -316,6 +321,8 @@ bool density_ppe_fusable(const SceneConst& sc);
 void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// the same reading the weights launch_density_set_ppe cached (positions unchanged since)
+void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // scan.cu
 int scan_scratch_ints(int m);

@@ -327,6 +327,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.cell_xz = dalloc<int32_t>(h, n);
     st.x32 = dalloc<float>(h, n);
     st.z32 = dalloc<float>(h, n);
+    st.w_re = dalloc<double>(h, n * kReCache);
     st.row_of = st.particle_of = st.row_cell = st.cell_fill = st.cell_start = nullptr;
     st.unplaced = st.unplaced_pos = st.row_scratch = nullptr;
     if (h->nscenes == 0) {  // single scene: PPE rows in cell order
@@ -727,7 +728,10 @@ void forward(mps_handle* h, double dt) {
     launch_assign_pressure(sc, h->st, s);
     launched(h, kLaunchesAssign);
     stage_mark(h, kGradient);
-    launch_pressure_gradient(sc, h->st, s);
+    if (fused)  // the assembly walk cached W(r, r_e) on these positions
+        launch_pressure_gradient_cached(sc, h->st, s);
+    else
+        launch_pressure_gradient(sc, h->st, s);
     launched(h, kLaunchesGradient);
     stage_mark(h, kDs);
     if (flags & MPS_FLAG_DS) {
@@ -859,7 +863,10 @@ void batch_stages_post(mps_handle* h) {
     SceneConst sc = h->sc;
     sc.guard = 1;
     launch_assign_pressure(sc, h->st, s);
-    launch_pressure_gradient(sc, h->st, s);
+    if (density_ppe_fusable(sc))  // batch_stages_pre assembled with the fused walk
+        launch_pressure_gradient_cached(sc, h->st, s);
+    else
+        launch_pressure_gradient(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_dynamic_stabilize(sc, h->st, s);
     after_launch("batch stages");
     launched(h, kLaunchesAssign + kLaunchesGradient + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesDs : 0));

@@ -441,7 +441,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     const bool hs = has_flag(sc.flags, MPS_FLAG_HS);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
     double thisN = 0.0, hsum = 0.0, a_ii = 0.0, gx = 0.0, gz = 0.0;
-    int m = 0;
+    int m = 0, m_re = 0;
     for_near(sc, st, i, fmaxf(sc.f32_out_re, sc.f32_out_rl), [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
@@ -451,7 +451,10 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         if (!in_re && !in_rl) return;
         const double r = __dsqrt_rn(r2);
         if (in_re) {
-            thisN += weight(r, sc.re);
+            const double w = weight(r, sc.re);
+            thisN += w;
+            if (m_re < kReCache) st.w_re[static_cast<int64_t>(m_re) * n + i] = w;
+            m_re++;
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
@@ -568,6 +571,9 @@ __global__ void k_assign_pressure(SceneConst sc, DeviceState st) {
 }
 
 // ModifyByPressureGradient, midpoint branch (Computer.hpp:1501-1521): du only.
+// kCached: W of the entries within r_e comes from st.w_re (the fused density + assembly
+// walk wrote it on the same positions, in the same list order).
+template <bool kCached>
 __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
@@ -578,12 +584,15 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     const double factor = -dt / sc.rho * 2.0 / sc.n0;
     const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
     double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
+    int m_re = 0;
     for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.re2)) {
-            const double wg = weight(__dsqrt_rn(r2), sc.re);
+            const double wg = (kCached && m_re < kReCache) ? st.w_re[static_cast<int64_t>(m_re) * sc.n + i]
+                                                           : weight(__dsqrt_rn(r2), sc.re);
+            m_re++;
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double c = (st.p[j] + pi) / r2 * wg;
                 sx += c * dx;
@@ -748,7 +757,12 @@ void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStr
 }
 
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_pressure_gradient<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_pressure_gradient<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+}
+
+void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_pressure_gradient<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
