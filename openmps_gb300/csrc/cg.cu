@@ -349,9 +349,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_pupdate(CgOperands o) {
 }
 
 // |b - A x|^2 in FP64 into S->true_rr (reported as the true relative residual)
-__global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o) {
+// |b - A x|^2 in FP64 for the statistics.  With `after_update` (the mixed-precision
+// solves) a solve that converged on its own already holds it: convergence is only ever
+// declared by a reliable update, on the true residual of the x it leaves.
+__global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o, int after_update) {
     __shared__ BlockTicket tk;
     if (o.S->aborted) return;
+    if (after_update && o.S->converged && !o.S->fallback) return;
     ticket_init(tk);
     const ChunkLoop cl;
     const double* x = o.x;
@@ -1253,7 +1257,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     if (is_pcg(solver)) {
         k_cg_init<<<gs, kBlock, 0, s>>>(*fb, h_fb, 1, ops.S);
     } else {
-        k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+        k_true_residual<<<gs, kBlock, 0, s>>>(ops, solver != MPS_SOLVER_CG64 ? 1 : 0);
     }
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
@@ -1275,7 +1279,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
                                           cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
         k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
-        k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+        k_true_residual<<<gs, kBlock, 0, s>>>(ops, 1);
         e = cudaStreamEndCapture(s, &captured);
         if (e != cudaSuccess) return e;
     }
@@ -1343,7 +1347,7 @@ cudaError_t CgGraph::build_persistent(int solver, const CgOperands& ops, cudaStr
     e = cudaStreamBeginCaptureToGraph(s, graph_, &fb_while, nullptr, 1, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
-    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    k_true_residual<<<gs, kBlock, 0, s>>>(ops, 0);  // the persistent loop does not record it
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
     e = cudaGraphInstantiate(&exec_, graph_, 0);
@@ -1422,7 +1426,7 @@ cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, 
         k_fb_merge<<<1, 32, 0, s>>>(ops.S, fb->S);
         k++;
     }
-    k_true_residual<<<gs, kBlock, 0, s>>>(ops);
+    k_true_residual<<<gs, kBlock, 0, s>>>(ops, solver != MPS_SOLVER_CG64 ? 1 : 0);
     k++;
     if (launches) *launches = k;
     return cudaGetLastError();
