@@ -1031,21 +1031,66 @@ void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
     if (with_true) reliable_kernels(solver, ops, mg, h, use_cond, s);
 }
 
+// The learned start in two parts: r0 of the previous pressure and the per-particle
+// feature quantities (no use of the hierarchy), then the first preconditioned step,
+// the features, the network and the warm start.
+void learned_prep_head(const LearnedOps& L, const CgOperands& o, CgScalars* S, cudaStream_t s) {
+    CgOperands p = o;
+    p.S = S;
+    k_mx_init<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0);  // r0 = b - A x0 in FP64, into r32
+    launch_learned_q(L, p, S, s);
+}
+
+void learned_prep_tail(const LearnedOps& L, const CgOperands& o, const MgHierarchy& mg, CgScalars* S,
+                       bool infer, cudaStream_t s) {
+    CgOperands p = o;
+    p.S = S;
+    MgHierarchy plain = mg;
+    plain.scale = nullptr;
+    mg_apply(plain, S, 0, o.r32, o.u32, s);
+    k_pmx_spmv<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0, 0, 0);  // alpha0 = r0.u0 / (A u0).u0
+    launch_learned_feature_rows(L, p, S, s);
+    if (infer) {
+        launch_mlp_infer(L.packed, L.feat, L.n, L.sigma, L.out, L.error, s);
+        launch_learned_apply(L, p, S, s);
+    }
+}
+
+// With `fk` (graph capture), the coarse half of the multigrid setup runs on a side
+// stream beside the initial residual (and the learned start's first kernels), joining
+// before the first use of the hierarchy.  The two branches share no buffers.
 void init_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
                   cudaGraphConditionalHandle h, int use_cond, cudaStream_t s,
-                  const LearnedRun* lrn) {
+                  const LearnedRun* lrn, const SetupFork* fk = nullptr) {
     const int gs = ops.grid_spmv;
     if (solver == MPS_SOLVER_CG64) {
         k_cg_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond, nullptr);
         return;
     }
-    if (is_pcg(solver)) mg_setup(*mg, ops, s);
+    const bool pcg = is_pcg(solver);
+    const bool forked = pcg && fk != nullptr;
+    if (pcg) {
+        mg_setup_level1(*mg, ops, s);
+        if (forked) {
+            cudaEventRecord(fk->fork, s);
+            cudaStreamWaitEvent(fk->side, fk->fork, 0);
+            mg_setup_coarse(*mg, fk->side);
+            cudaEventRecord(fk->join, fk->side);
+        } else {
+            mg_setup_coarse(*mg, s);
+        }
+    }
     if (solver == MPS_SOLVER_LEARNED && lrn) {
         k_cg_configure<<<1, 32, 0, s>>>(lrn->S, 0.0, MPS_CRIT_RHS, 1, 0.0);
-        learned_prep(*lrn->L, ops, *mg, lrn->S, true, s);
+        learned_prep_head(*lrn->L, ops, lrn->S, s);
+        if (forked) cudaStreamWaitEvent(s, fk->join, 0);
+        learned_prep_tail(*lrn->L, ops, *mg, lrn->S, true, s);
+        k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
+    } else {
+        k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
+        if (forked) cudaStreamWaitEvent(s, fk->join, 0);
     }
-    k_mx_init<<<gs, kBlock, 0, s>>>(ops, h, use_cond);
-    if (is_pcg(solver)) {
+    if (pcg) {
         mg_apply(*mg, ops.S, 0, ops.r32, ops.u32, s);
         k_pmx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, use_cond);
     } else {
@@ -1083,18 +1128,8 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
 
 void learned_prep(const LearnedOps& L, const CgOperands& o, const MgHierarchy& mg, CgScalars* S,
                   bool infer, cudaStream_t s) {
-    CgOperands p = o;
-    p.S = S;
-    k_mx_init<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0);  // r0 = b - A x0 in FP64, into r32
-    MgHierarchy plain = mg;
-    plain.scale = nullptr;
-    mg_apply(plain, S, 0, o.r32, o.u32, s);
-    k_pmx_spmv<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0, 0, 0);  // alpha0 = r0.u0 / (A u0).u0
-    launch_learned_features(L, p, S, s);
-    if (infer) {
-        launch_mlp_infer(L.packed, L.feat, L.n, L.sigma, L.out, L.error, s);
-        launch_learned_apply(L, p, S, s);
-    }
+    learned_prep_head(L, o, S, s);
+    learned_prep_tail(L, o, mg, S, infer, s);
 }
 
 int learned_prep_launches(const MgHierarchy& mg, bool infer) {
@@ -1111,7 +1146,12 @@ int cg_kernels_per_update(int solver, const MgHierarchy* mg) {
     return is_pcg(solver) && mg ? 2 + mg_apply_launches(*mg) : 2;
 }
 
-CgGraph::~CgGraph() { reset(); }
+CgGraph::~CgGraph() {
+    reset();
+    if (fork_.fork) cudaEventDestroy(fork_.fork);
+    if (fork_.join) cudaEventDestroy(fork_.join);
+    if (fork_.side) cudaStreamDestroy(fork_.side);
+}
 
 void CgGraph::reset() {
     if (exec_) cudaGraphExecDestroy(exec_);
@@ -1200,11 +1240,17 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     }
     cudaGraph_t captured = nullptr;
 
-    // init chain
+    // init chain (the multigrid's coarse setup on a side branch)
+    if (!fork_.side) {
+        e = cudaStreamCreateWithFlags(&fork_.side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork_.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork_.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
     e = cudaStreamBeginCaptureToGraph(s, graph_, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    init_kernels(solver, ops, mg, h, 1, s, lrn);
+    init_kernels(solver, ops, mg, h, 1, s, lrn, &fork_);
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
     cudaGraphNode_t init_node;

@@ -80,6 +80,12 @@ struct LearnedRun {
 
 // A CUDA graph running one whole solve: init kernels + device-driven while loop (+ for
 // the preconditioned solvers the FP64 CG fallback loop, which runs only after a failure).
+// Side stream and events of a fork/join inside a captured graph.
+struct SetupFork {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
 class CgGraph {
 public:
     ~CgGraph();
@@ -112,6 +118,7 @@ private:
     bool persistent_ = false;
     int kpi_ = 0, kri_ = 0;
     CgOperands ops_{};
+    SetupFork fork_;  // created at the first build, kept across rebuilds
 };
 
 // The same solve with host-launched kernels: `chunk` iterations per launch batch, the

@@ -688,10 +688,18 @@ cudaError_t mlp_train_prepare_device() {
                                 static_cast<int>(kTrBytes));
 }
 
+void launch_learned_q(const LearnedOps& L, const CgOperands& o, const CgScalars* S, cudaStream_t s) {
+    k_lrn_q<<<grid_for(L.n), kBlock, 0, s>>>(L, o, L.dinv0, L.step, S, L.q4, L.q2);
+}
+
+void launch_learned_feature_rows(const LearnedOps& L, const CgOperands& o, const CgScalars* S, cudaStream_t s) {
+    k_lrn_features<<<o.grid_spmv, kBlock, 0, s>>>(L, o, L.dinv0, L.step, S, L.q4, L.q2, L.len_ref);
+}
+
 void launch_learned_features(const LearnedOps& L, const CgOperands& o, const CgScalars* S,
                              cudaStream_t s) {
-    k_lrn_q<<<grid_for(L.n), kBlock, 0, s>>>(L, o, L.dinv0, L.step, S, L.q4, L.q2);
-    k_lrn_features<<<o.grid_spmv, kBlock, 0, s>>>(L, o, L.dinv0, L.step, S, L.q4, L.q2, L.len_ref);
+    launch_learned_q(L, o, S, s);
+    launch_learned_feature_rows(L, o, S, s);
 }
 
 void launch_learned_apply(const LearnedOps& L, const CgOperands& o, const CgScalars* S, cudaStream_t s) {

@@ -74,6 +74,10 @@ void mlp_pack_weights(const float* blob, void* image);
 // raw features, c = alpha0 u0, sigma.
 void launch_learned_features(const LearnedOps& L, const CgOperands& o, const CgScalars* S,
                              cudaStream_t s);
+// its two kernels: per-particle quantities (need r0 only), then the per-row features
+// (need the first preconditioned step)
+void launch_learned_q(const LearnedOps& L, const CgOperands& o, const CgScalars* S, cudaStream_t s);
+void launch_learned_feature_rows(const LearnedOps& L, const CgOperands& o, const CgScalars* S, cudaStream_t s);
 // Network inference on the tensor cores: out = MLP(features).  The residual features
 // (8, 9, 10) are divided by sigma[0] (sigma null: used as given).
 void launch_mlp_infer(const void* packed, const float* feat, int n, const double* sigma,

@@ -475,7 +475,7 @@ cudaError_t mg_prepare_device() {
                                 static_cast<int>(kMgBottomBytes));
 }
 
-void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
+void mg_setup_level1(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
     // cells without particles keep a zero residual through the solve
     cudaMemsetAsync(mg.lv[1].r, 0, sizeof(float) * mg.lv[1].cells, s);
     k_mg_bins<<<o.grid_spmv, kBlock, 0, s>>>(o, mg.cell_xz, mg.bins, mg.dinv0, kMgOmegaFine, mg.status);
@@ -484,10 +484,18 @@ void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
     launch_exclusive_scan(mg.active_flag, mg.active_pos, mg.lv[1].cells, mg.scan_scratch, s);
     k_mg_active<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1].cells, mg.active_flag, mg.active_pos,
                                                            mg.active);
+}
+
+void mg_setup_coarse(const MgHierarchy& mg, cudaStream_t s) {
     for (int l = 1; l < mg.levels; l++)
         k_mg_coarsen<<<grid_for(mg.lv[l + 1].cells), kBlock, 0, s>>>(mg.lv[l], mg.lv[l + 1],
                                                                     kMgOmegaCoarse, mg.status);
     k_mg_dense<<<1, kMgBottomThreads, dense_smem(mg), s>>>(mg.lv[mg.levels], mg.dense, mg.status);
+}
+
+void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s) {
+    mg_setup_level1(mg, o, s);
+    mg_setup_coarse(mg, s);
 }
 
 int mg_setup_launches(const MgHierarchy& mg) { return 2 + 3 + 1 + (mg.levels - 1) + 1; }

@@ -66,6 +66,11 @@ int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom);
 // Setup of one solve: level-1 operator from the FP64 matrix, the coarser Galerkin
 // operators and the dense inverse.  Skips itself when the step already failed.
 void mg_setup(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s);
+// The two halves of mg_setup: the level-1 operator (reads the matrix), then the coarser
+// Galerkin operators and the dense inverse (read only the level-1 operator), which can
+// run beside other work that does not use the hierarchy.
+void mg_setup_level1(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s);
+void mg_setup_coarse(const MgHierarchy& mg, cudaStream_t s);
 int mg_setup_launches(const MgHierarchy& mg);
 // u = M r.  `mode` gates the kernels on the solve state like the PCG kernels: 0 init,
 // 1 iteration, 2 after a reliable update (see pcg_skip).  With `fuse_axpy` (mode 1) the
