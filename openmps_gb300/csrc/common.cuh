@@ -300,7 +300,9 @@ void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t 
 // PPE row order from the sorted cells (no-op for a batch); returns the kernels launched.
 int launch_rows(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s);
-void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// FP32 position copies of particles [first, first + count) (count < 0: to the end)
+void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s, int first = 0,
+                          int count = -1);
 // stages.cu
 void launch_set_dt(const SceneConst& sc, const DeviceState& st, double dt, cudaStream_t s);
 void launch_cfl_dt(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

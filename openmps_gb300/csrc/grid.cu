@@ -182,16 +182,20 @@ __global__ void k_status_counters_reset(DevStatus* st) {
 
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s) { k_status_counters_reset<<<1, 32, 0, s>>>(st); }
 
-// FP32 copies of the positions after a host write of x, z.
-__global__ void k_positions_f32(SceneConst sc, DeviceState st) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.n) return;
+// FP32 copies of the positions of particles [first, first + count) after a host write of
+// x, z.
+__global__ void k_positions_f32(DeviceState st, int first, int count) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int i = first + k;
     st.x32[i] = __double2float_rn(st.x[i]);
     st.z32[i] = __double2float_rn(st.z[i]);
 }
 
-void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_positions_f32<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s, int first, int count) {
+    if (count < 0) count = sc.n - first;
+    if (count <= 0) return;
+    k_positions_f32<<<grid_for(count), kBlock, 0, s>>>(st, first, count);
 }
 
 void launch_bucket(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {

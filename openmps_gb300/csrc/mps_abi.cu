@@ -1090,7 +1090,7 @@ int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const doubl
         upload(h, st.w + old, w, b8, false);
         upload(h, st.p + old, p, b8, false);
         upload(h, st.nd + old, nd, b8, false);
-        launch_positions_f32(h->sc, st, h->stream);
+        launch_positions_f32(h->sc, st, h->stream, static_cast<int>(old), static_cast<int>(n));
         launched(h, 1);
         check(cudaStreamSynchronize(h->stream), "add particles");
     });
@@ -1803,7 +1803,7 @@ int mps_batch_set_scene(mps_handle* h, int32_t scene, const int32_t* type, const
         upload(h, st.w + r0, w, b8, false);
         upload(h, st.p + r0, p, b8, false);
         upload(h, st.nd + r0, nd, b8, false);
-        launch_positions_f32(h->sc, st, h->stream);
+        launch_positions_f32(h->sc, st, h->stream, static_cast<int>(r0), static_cast<int>(n));
         launched(h, 1);
         check(cudaStreamSynchronize(h->stream), "batch scene");
     });
