@@ -9,12 +9,14 @@
 // uneven chunks);
 // each warp load reads 32 consecutive matrix entries and a row is summed by its own lane
 // in ascending column order (no cross-lane reduction: in FP64 every instruction counts,
-// the FP64 pipe bounds this kernel on GB300).  Loads are unrolled 8 deep so that each
-// lane keeps that many matrix loads and gathers in flight.
+// the FP64 pipe bounds this kernel on GB300).  Row loads are software-pipelined (eight
+// entries per step for the FP64 rows, four for the preconditioned FP32 SpMV) so that each
+// lane keeps matrix loads and gathers in flight.
 //
-// Reductions: each block sums its part with warp shuffles, writes one partial, and the
-// last block to finish (atomic ticket, no waiting) sums the partials in a fixed order.
-// Results are deterministic run to run.
+// Reductions (grid_sum): lanes park their values in shared memory and the block's last
+// warp adds them; blocks publish partials in groups of 32, the last block of a group adds
+// the group's, and the last group adds the group sums (atomic tickets, no waiting).  Every
+// addition has a fixed order, so results are deterministic run to run.
 //
 // MPS_SOLVER_CG64: the reference CG in FP64 (3 kernels per iteration).
 // MPS_SOLVER_MIXED: CG whose iterations run in FP32 (FP32 matrix, FP32 SpMV and axpy with
