@@ -57,8 +57,20 @@ extern "C" {
 #define MPS_FLAG_ECS 0x04u /* MPS_ECS  error-compensating source       (defines.hpp:41) */
 #define MPS_FLAG_DS 0x08u  /* MPS_DS   dynamic stabilisation           (defines.hpp:51) */
 #define MPS_FLAG_SPP 0x10u /* MPS_SPP  space-potential (surface) particle (defines.hpp:56) */
+/* MPS_GC gradient corrective matrix (defines.hpp:46): the pressure gradient of a fluid
+ * particle is multiplied by C_i = (sum_j W/r^2 dx dx^T)^-1 (Computer.hpp:1457-1499). */
+#define MPS_FLAG_GC 0x20u
+/* PRESSURE_EXPLICIT (defines.hpp:26): no PPE; p = c^2 (rho0/n0 n - rho0) where that is
+ * positive, from the second number density (Computer.hpp:1046-1067), and MaxDt =
+ * min(maxDt, courant l0 / c) (Environment.hpp:131-135).  Needs mps_params.sound_speed. */
+#define MPS_FLAG_PRESSURE_EXPLICIT 0x40u
 /* PRESSURE_GRADIENT_MIDPOINT (defines.hpp:21) is always on: the other branch does
- * not compile in the reference (Computer.hpp:1522-1537). */
+ * not compile in the reference (Computer.hpp:1522-1537).  ARTIFICIAL_COLLISION_FORCE
+ * (defines.hpp:16) has no flag: its stage calls a Particle member that does not exist
+ * (Computer.hpp:1104-1134), so no build of the reference can enable it. */
+/* Every method flag. */
+#define MPS_FLAGS_ALL (MPS_FLAG_HS | MPS_FLAG_HL | MPS_FLAG_ECS | MPS_FLAG_DS | MPS_FLAG_SPP | \
+                       MPS_FLAG_GC | MPS_FLAG_PRESSURE_EXPLICIT)
 /* The stock build of the reference (defines.hpp as shipped). */
 #define MPS_PRESET_REFERENCE (MPS_FLAG_HS | MPS_FLAG_HL | MPS_FLAG_ECS | MPS_FLAG_DS | MPS_FLAG_SPP)
 /* Plain MPS: standard source/Laplacian, free-surface flag n/n0 < surface_ratio. */
@@ -112,7 +124,8 @@ typedef struct mps_params {
     double inner_tol;     /* MIXED: relative residual reduction of one FP32 inner solve */
     int32_t max_refinements; /* MIXED: maximum FP64 refinement passes */
     int32_t cg_launch;       /* MPS_CG_LAUNCH_GRAPH (default), _HOST or _PERSISTENT */
-    double reserved[6];
+    double sound_speed;      /* Environment(..., c, ...): used only with MPS_FLAG_PRESSURE_EXPLICIT */
+    double reserved[5];
 } mps_params;
 
 /* Derived constants of Environment (Environment.hpp:129-216) and Grid (Grid.hpp:137-150). */

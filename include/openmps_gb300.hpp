@@ -89,6 +89,11 @@ struct Environment {
         params.re_lap_by_l0 = re_lap_by_l0;
         return *this;
     }
+    // Environment(..., c, ...) of PRESSURE_EXPLICIT (Environment.hpp:115-117)
+    Environment& SoundSpeed(double c) {
+        params.sound_speed = c;
+        return *this;
+    }
     Environment& Solver(int32_t solver, int32_t criterion = MPS_CRIT_INITIAL_RESIDUAL) {
         params.solver = solver;
         params.criterion = criterion;

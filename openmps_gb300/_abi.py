@@ -34,6 +34,9 @@ FLAG_HL = 0x02
 FLAG_ECS = 0x04
 FLAG_DS = 0x08
 FLAG_SPP = 0x10
+FLAG_GC = 0x20
+FLAG_PRESSURE_EXPLICIT = 0x40
+FLAGS_ALL = FLAG_HS | FLAG_HL | FLAG_ECS | FLAG_DS | FLAG_SPP | FLAG_GC | FLAG_PRESSURE_EXPLICIT
 PRESET_REFERENCE = FLAG_HS | FLAG_HL | FLAG_ECS | FLAG_DS | FLAG_SPP
 PRESET_PLAIN = 0
 
@@ -77,7 +80,8 @@ class MpsParams(C.Structure):
         ("inner_tol", C.c_double),
         ("max_refinements", C.c_int32),
         ("cg_launch", C.c_int32),
-        ("reserved", C.c_double * 6),
+        ("sound_speed", C.c_double),
+        ("reserved", C.c_double * 5),
     ]
 
 

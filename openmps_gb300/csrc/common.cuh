@@ -54,6 +54,7 @@ struct SceneConst {
     double n0, lambda, n0_lap, lambda_lap;
     double rho, nu, g, surface_ratio, max_dt, max_dx;
     double min_x, min_z;
+    double sound_speed;  // c of the explicit pressure (MPS_FLAG_PRESSURE_EXPLICIT)
 };
 
 // Time of the step in flight (Environment::t, ::dt); lives in device memory so that
@@ -322,6 +323,10 @@ void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32,
 bool density_ppe_fusable(const SceneConst& sc);
 void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
 void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// the explicit pressure of every particle from its number density; sets *ok (the solve
+// flag the later stages test) to 1 when given
+void launch_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok, cudaStream_t s);
+// the midpoint gradient, or with MPS_FLAG_GC the corrected one (two walks of each row)
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // the same reading the weights launch_density_set_ppe cached (positions unchanged since)
 void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
@@ -333,6 +338,6 @@ void launch_exclusive_scan(const int* in, int* out, int m, int* scratch, cudaStr
 constexpr int kLaunchesSearch = 3, kLaunchesDensity = 1, kLaunchesEcs = 1, kLaunchesExplicit = 2,
               kLaunchesSaveX = 1, kLaunchesSetPpe = 6, kLaunchesAssign = 1, kLaunchesGradient = 2,
               kLaunchesDs = 2, kLaunchesDt = 1, kLaunchesCfl = 2, kLaunchesPrePressure = 1,
-              kLaunchesExplicitUpdate = 1;
+              kLaunchesExplicitUpdate = 1, kLaunchesExplicitPressure = 1;
 
 }  // namespace mpsgb

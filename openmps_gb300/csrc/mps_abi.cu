@@ -182,7 +182,9 @@ void validate(const mps_params& p) {
     if (p.solver < MPS_SOLVER_CG64 || p.solver > MPS_SOLVER_MIXED_MG) bad("unknown solver");
     if (p.criterion != MPS_CRIT_INITIAL_RESIDUAL && p.criterion != MPS_CRIT_RHS)
         bad("unknown criterion");
-    if (p.flags & ~static_cast<uint32_t>(MPS_PRESET_REFERENCE)) bad("unknown method flag");
+    if (p.flags & ~static_cast<uint32_t>(MPS_FLAGS_ALL)) bad("unknown method flag");
+    if ((p.flags & MPS_FLAG_PRESSURE_EXPLICIT) && !(p.sound_speed > 0))
+        bad("MPS_FLAG_PRESSURE_EXPLICIT needs a positive sound_speed");
     if (p.cg_launch != MPS_CG_LAUNCH_GRAPH && p.cg_launch != MPS_CG_LAUNCH_HOST &&
         p.cg_launch != MPS_CG_LAUNCH_PERSISTENT)
         bad("unknown cg_launch");
@@ -225,7 +227,11 @@ void setup_constants(mps_handle* h) {
     sc.nu = p.nu;
     sc.g = p.g;
     sc.surface_ratio = p.surface_ratio;
-    sc.max_dt = std::min(p.max_dt, std::sqrt(2 * (p.courant * p.l0) / p.g));  // :138
+    sc.sound_speed = p.sound_speed;
+    if (p.flags & MPS_FLAG_PRESSURE_EXPLICIT)
+        sc.max_dt = std::min(p.max_dt, (p.courant * p.l0) / p.sound_speed);  // Environment.hpp:135
+    else
+        sc.max_dt = std::min(p.max_dt, std::sqrt(2 * (p.courant * p.l0) / p.g));  // :138
     sc.max_dx = p.courant * p.l0;                                             // :143
     sc.min_x = p.min_x;
     sc.min_z = p.min_z;
@@ -714,19 +720,29 @@ void forward(mps_handle* h, double dt) {
         launch_save_x(sc, h->st, s);
         launched(h, kLaunchesSaveX);
     }
+    const bool implicit = (flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u;
     stage_mark(h, kPpe);
-    if (fused)
-        launch_density_set_ppe(sc, h->st, wants_fp32(h), s);
-    else
-        launch_set_ppe(sc, h->st, wants_fp32(h), s);
-    h->ppe_fp32 = wants_fp32(h);
-    launched(h, kLaunchesSetPpe);
-    after_launch("stages");
+    if (implicit) {
+        if (fused)
+            launch_density_set_ppe(sc, h->st, wants_fp32(h), s);
+        else
+            launch_set_ppe(sc, h->st, wants_fp32(h), s);
+        h->ppe_fp32 = wants_fp32(h);
+        launched(h, kLaunchesSetPpe);
+        after_launch("stages");
+    }
     stage_mark(h, kSolve);
-    do_solve(h);
+    if (implicit) do_solve(h);
     stage_mark(h, kPressure);
-    launch_assign_pressure(sc, h->st, s);
-    launched(h, kLaunchesAssign);
+    if (implicit) {
+        launch_assign_pressure(sc, h->st, s);
+        launched(h, kLaunchesAssign);
+    } else {
+        // no PPE: the pressure follows from the number density; the solve flag the
+        // later stages test is set
+        launch_explicit_pressure(sc, h->st, &h->S->converged, s);
+        launched(h, kLaunchesExplicitPressure);
+    }
     stage_mark(h, kGradient);
     if (fused)  // the assembly walk cached W(r, r_e) on these positions
         launch_pressure_gradient_cached(sc, h->st, s);
@@ -740,7 +756,7 @@ void forward(mps_handle* h, double dt) {
     }
     stage_mark(h, kNumStages);
     after_launch("step");
-    read_status(h, true);
+    read_status(h, implicit);
     h->stats.steps += 1;
     if (h->stage_timing) {
         float total = 0.f;
@@ -835,6 +851,8 @@ BatchOps batch_ops(mps_handle* h) {
     return B;
 }
 
+bool batch_implicit(const mps_handle* h) { return (h->prm.flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u; }
+
 // The stages of a batch step before the solve (fixed dt), stream-ordered and capturable.
 void batch_stages_pre(mps_handle* h, double dt) {
     cudaStream_t s = h->stream;
@@ -847,32 +865,40 @@ void batch_stages_pre(mps_handle* h, double dt) {
     const bool fused = density_ppe_fusable(sc);
     if (!fused) launch_density(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
-    if (fused)
+    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
+    const bool implicit = batch_implicit(h);
+    if (!implicit)
+        launch_explicit_pressure(sc, h->st, nullptr, s);
+    else if (fused)
         launch_density_set_ppe(sc, h->st, true, s);
     else
         launch_set_ppe(sc, h->st, true, s);
     h->ppe_fp32 = true;
-    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
     after_launch("batch stages");
     launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate +
-                    (fused ? 0 : kLaunchesDensity) + kLaunchesSetPpe + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
+                    (fused ? 0 : kLaunchesDensity) + (implicit ? kLaunchesSetPpe : kLaunchesExplicitPressure) +
+                    ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
 }
 
 void batch_stages_post(mps_handle* h) {
     cudaStream_t s = h->stream;
     SceneConst sc = h->sc;
     sc.guard = 1;
-    launch_assign_pressure(sc, h->st, s);
+    const bool implicit = batch_implicit(h);
+    if (implicit) launch_assign_pressure(sc, h->st, s);
     if (density_ppe_fusable(sc))  // batch_stages_pre assembled with the fused walk
         launch_pressure_gradient_cached(sc, h->st, s);
     else
         launch_pressure_gradient(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_dynamic_stabilize(sc, h->st, s);
     after_launch("batch stages");
-    launched(h, kLaunchesAssign + kLaunchesGradient + ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesDs : 0));
+    launched(h, (implicit ? kLaunchesAssign : 0) + kLaunchesGradient +
+                    ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesDs : 0));
 }
 
+// The batched PPE solve (nothing with the explicit pressure).
 void batch_solve(mps_handle* h) {
+    if (!batch_implicit(h)) return;
     check(launch_batch_solve(batch_ops(h), h->batch_blocks, h->batch_threads, h->stream), "batch solve");
     launched(h, 1);
 }
@@ -1295,6 +1321,12 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
 }
 
 // ---------------------------------------------------------------- stages
+// The reference has no PPE with PRESSURE_EXPLICIT (Computer.hpp:1143).
+void require_implicit(const mps_handle* h) {
+    if (h->prm.flags & MPS_FLAG_PRESSURE_EXPLICIT)
+        throw StatusError{MPS_ERR_STATE, "no PPE with MPS_FLAG_PRESSURE_EXPLICIT"};
+}
+
 #define MPS_STAGE(name, body)                              \
     int name(mps_handle* h) {                              \
         return guarded(h, [&] {                            \
@@ -1310,10 +1342,15 @@ MPS_STAGE(mps_stage_density, launch_density(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_error_correction, launch_error_correction(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_explicit, launch_explicit(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_save_x, launch_save_x(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_set_ppe, launch_set_ppe(h->sc, h->st, wants_fp32(h), h->stream);
+MPS_STAGE(mps_stage_set_ppe, require_implicit(h); launch_set_ppe(h->sc, h->st, wants_fp32(h), h->stream);
           h->ppe_fp32 = wants_fp32(h))
-MPS_STAGE(mps_stage_solve_ppe, do_solve(h); read_status(h, true))
-MPS_STAGE(mps_stage_assign_pressure, launch_assign_pressure(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_solve_ppe, require_implicit(h); do_solve(h); read_status(h, true))
+// the pressure of ComputeImplicitForces: from the PPE solution, or explicit
+MPS_STAGE(mps_stage_assign_pressure,
+          if (h->prm.flags & MPS_FLAG_PRESSURE_EXPLICIT)
+              launch_explicit_pressure(h->sc, h->st, nullptr, h->stream);
+          else
+              launch_assign_pressure(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_pressure_gradient, launch_pressure_gradient(h->sc, h->st, h->stream))
 MPS_STAGE(mps_stage_dynamic_stabilize, launch_dynamic_stabilize(h->sc, h->st, h->stream))
 
@@ -1841,7 +1878,7 @@ int mps_batch_forward(mps_handle* h, double dt, int32_t nsteps) {
         cudaStream_t s = h->stream;
         check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
         int32_t left = nsteps;
-        if (h->batch_threads == 0) {
+        if (h->batch_threads == 0 && batch_implicit(h)) {
             // first step: eager, with the autotuner between assembly and solve
             batch_stages_pre(h, dt);
             batch_autotune(h);

@@ -1,7 +1,8 @@
 // stages.cu - the per-particle stages of Computer::ForwardTime (Computer.hpp:1700-1742):
 // number density, error-compensating source, explicit forces, PPE right-hand side and
-// matrix assembly, pressure assignment, midpoint pressure gradient, dynamic
-// stabilisation and the CFL time step.
+// matrix assembly, pressure assignment (or the explicit pressure), midpoint pressure
+// gradient (plain or with the GC corrective matrix), dynamic stabilisation and the CFL
+// time step.
 //
 // One thread per particle walks its neighbour row in reference order and accumulates
 // exactly like AccumulateNeighbor (Computer.hpp:618-695): the filter r^2 < r_e^2 on
@@ -620,6 +621,123 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     st.duz[i] = factor * sz;
 }
 
+// ComputeImplicitForces with PRESSURE_EXPLICIT (Computer.hpp:1046-1067): the virtual
+// density rho0 / n0 n of every particle (dummy and disabled ones included, from the
+// number density they carry) and p = c^2 (rho - rho0) above rho0, else 0.
+__global__ void k_explicit_pressure(SceneConst sc, DeviceState st, int32_t* ok) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && ok) *ok = 1;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const double rho0 = sc.rho;
+    const double c = sc.sound_speed;
+    const double rho = rho0 / sc.n0 * st.nd[i];
+    st.p[i] = (rho <= rho0) ? 0.0 : c * c * (rho - rho0);
+}
+
+// Detail::InvertMatrix<2> (Computer.hpp:323-347): the inverse of [[a, b], [b, d]], or
+// val times the identity when the determinant is exactly zero.
+__device__ __forceinline__ void gc_invert(double a, double b, double d, double val, double* m) {
+    const double det = a * d - b * b;
+    if (det == 0) {
+        m[0] = val;
+        m[1] = 0.0;
+        m[2] = 0.0;
+        m[3] = val;
+        return;
+    }
+    m[0] = d / det;
+    m[1] = -b / det;
+    m[2] = -b / det;
+    m[3] = a / det;
+}
+
+// prod(C, dx) of uBLAS: each row summed from 0 (0 + c0 dx) + c1 dz.
+__device__ __forceinline__ double row_dot(double c0, double c1, double dx, double dz) {
+    return __dadd_rn(__dadd_rn(0.0, __dmul_rn(c0, dx)), __dmul_rn(c1, dz));
+}
+
+// ModifyByPressureGradient with MPS_GC (Computer.hpp:1457-1499): du only.  The first
+// walk sums C^-1 = sum W / r^2 dx dx^T over every neighbour within r_e and the SPP
+// particle; the second sums (p_ij / r^2 W) C dx over the non-dummy ones in the same
+// order.  The two off-diagonal sums of C^-1 add the same products (dx dz = dz dx
+// exactly), so one accumulator holds both.
+template <bool kCached>
+__global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.n) return;
+    if (solve_failed(sc, st)) return;
+    if (st.type[i] != MPS_TYPE_FLUID) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
+    auto w_of = [&](int m, double r2) {
+        return (kCached && m < kReCache) ? st.w_re[static_cast<int64_t>(m) * sc.n + i]
+                                         : weight(__dsqrt_rn(r2), sc.re);
+    };
+    double m00 = 0.0, m01 = 0.0, m11 = 0.0, gx = 0.0, gz = 0.0;
+    int m_re = 0;
+    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.re2)) {
+            const double wg = w_of(m_re, r2);
+            m_re++;
+            const double t = wg / r2;
+            m00 += t * (dx * dx);
+            m01 += t * (dx * dz);
+            m11 += t * (dz * dz);
+            if (spp) {
+                gx += wg * dx;
+                gz += wg * dz;
+            }
+        }
+    });
+    double xs = 0.0, zs = 0.0;
+    const bool has_spp = spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs);
+    double sdx = 0.0, sdz = 0.0, sr2 = 0.0, sw = 0.0;
+    if (has_spp) {
+        sdx = xs - xi;
+        sdz = zs - zi;
+        sr2 = dist2(sdx, sdz);
+        sw = weight(__dsqrt_rn(sr2), sc.re);
+        const double t = sw / sr2;
+        m00 += t * (sdx * sdx);
+        m01 += t * (sdx * sdz);
+        m11 += t * (sdz * sdz);
+    }
+    double C[4];
+    gc_invert(m00, m01, m11, 2.0 / sc.n0, C);  // InvertMatrix(invC, DIM / n0)
+    double sx = 0.0, sz = 0.0;
+    m_re = 0;
+    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
+        const double dx = st.x[j] - xi;
+        const double dz = st.z[j] - zi;
+        const double r2 = dist2(dx, dz);
+        if (below(r2, sc.re2)) {
+            const double wg = w_of(m_re, r2);
+            m_re++;
+            if (st.type[j] != MPS_TYPE_DUMMY) {
+                const double c = (st.p[j] + pi) / r2 * wg;
+                sx += c * row_dot(C[0], C[1], dx, dz);
+                sz += c * row_dot(C[2], C[3], dx, dz);
+            } else {
+                sx = __dadd_rn(sx, 0.0);
+                sz = __dadd_rn(sz, 0.0);
+            }
+        }
+    });
+    if (has_spp) {
+        const double c = (0.0 + pi) / sr2 * sw;
+        sx += c * row_dot(C[0], C[1], sdx, sdz);
+        sz += c * row_dot(C[2], C[3], sdx, sdz);
+    }
+    const double dt = st.step->dt;
+    const double factor = -dt * st.nd[i] / (sc.rho * sc.n0);
+    st.dux[i] = factor * sx;
+    st.duz[i] = factor * sz;
+}
+
 // DynamicStabilize (Computer.hpp:1568-1635): du only.
 __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -745,7 +863,9 @@ void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32,
     launch_ppe_layout(sc, st, want_fp32, s);
 }
 
-bool density_ppe_fusable(const SceneConst& sc) { return (sc.flags & MPS_FLAG_SPP) != 0u; }
+bool density_ppe_fusable(const SceneConst& sc) {
+    return (sc.flags & MPS_FLAG_SPP) != 0u && (sc.flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u;
+}
 
 void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
     k_density_ppe<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
@@ -756,13 +876,23 @@ void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStr
     k_assign_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
+void launch_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok, cudaStream_t s) {
+    k_explicit_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, ok);
+}
+
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_pressure_gradient<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    if (sc.flags & MPS_FLAG_GC)
+        k_pressure_gradient_gc<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    else
+        k_pressure_gradient<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_pressure_gradient<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    if (sc.flags & MPS_FLAG_GC)
+        k_pressure_gradient_gc<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    else
+        k_pressure_gradient<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 

@@ -12,6 +12,8 @@
 //     outputInterval of simulated time, stepping with ForwardTime() (CFL time step, at
 //     most outputInterval / minStepCountPerOutput) (Main.cpp:320-395);
 //   * a Computer::Exception prints "!!!!ERROR!!!!" and stops the run (Main.cpp:380-388).
+// With MPS_FLAG_PRESSURE_EXPLICIT among the flags, <environment> holds the sound speed c
+// and <condition> needs no eps, as in the reference built with PRESSURE_EXPLICIT.
 // Extensions (optional elements of <environment>): r_lapByl_0 (Laplacian radius),
 // flags (method bit set, default the reference's stock set) and solver (cg64, mixed,
 // mg, learned; default cg64 like the reference), weights (network file for "learned",
@@ -148,7 +150,7 @@ int solver_code(const std::string& s) {
 
 }  // namespace
 
-int main(int argc, char** argv) {
+int run(int argc, char** argv) {
     std::string file;
     bool parse_only = false;
     for (int i = 1; i < argc; i++) {
@@ -177,7 +179,10 @@ int main(int argc, char** argv) {
     const double start = xml.num("condition", "startTime");
     const double end = xml.num("condition", "endTime");
     const double interval = xml.num("condition", "outputInterval");
-    const double eps = xml.num("condition", "eps");
+    const uint32_t flags = static_cast<uint32_t>(xml.num_or("environment", "flags", MPS_PRESET_REFERENCE));
+    const bool explicit_pressure = (flags & MPS_FLAG_PRESSURE_EXPLICIT) != 0u;
+    // with PRESSURE_EXPLICIT there is no eps and the sound speed c is read (Main.cpp:215-217, :263-265)
+    const double eps = explicit_pressure ? xml.num_or("condition", "eps", 0.0) : xml.num("condition", "eps");
     const double steps_per_output = xml.num("environment", "minStepCountPerOutput");
     openmps_gb300::Environment env(interval / steps_per_output, xml.num("environment", "courant"),
                                    xml.num("environment", "g"), xml.num("environment", "rho"),
@@ -185,8 +190,9 @@ int main(int argc, char** argv) {
                                    xml.num("environment", "r_eByl_0"), xml.num("environment", "l_0"),
                                    xml.num("environment", "minX"), xml.num("environment", "minZ"),
                                    xml.num("environment", "maxX"), xml.num("environment", "maxZ"),
-                                   static_cast<uint32_t>(xml.num_or("environment", "flags", MPS_PRESET_REFERENCE)));
+                                   flags);
     env.LaplacianRadius(xml.num_or("environment", "r_lapByl_0", 0.0));
+    if (explicit_pressure) env.SoundSpeed(xml.num("environment", "c"));
     std::string solver = "cg64", weights;
     xml.attr("environment", "solver", &solver);
     xml.attr("environment", "weights", &weights);
@@ -196,9 +202,9 @@ int main(int argc, char** argv) {
         const mps_params& p = env.params;
         std::printf("maxDt=%.17g courant=%.17g g=%.17g rho=%.17g nu=%.17g surfaceRatio=%.17g r_eByl_0=%.17g "
                     "l_0=%.17g min=(%.17g,%.17g) max=(%.17g,%.17g) flags=%u solver=%d eps=%.17g "
-                    "start=%.17g end=%.17g interval=%.17g\n",
+                    "start=%.17g end=%.17g interval=%.17g c=%.17g\n",
                     p.max_dt, p.courant, p.g, p.rho, p.nu, p.surface_ratio, p.re_by_l0, p.l0, p.min_x, p.min_z,
-                    p.max_x, p.max_z, p.flags, p.solver, eps, start, end, interval);
+                    p.max_x, p.max_z, p.flags, p.solver, eps, start, end, interval, p.sound_speed);
         return 0;
     }
     mkdir("result", 0755);
@@ -243,4 +249,13 @@ int main(int argc, char** argv) {
     }
     std::cout << "finished" << std::endl;
     return 0;
+}
+
+int main(int argc, char** argv) {
+    try {
+        return run(argc, argv);
+    } catch (const std::exception& ex) {  // a malformed input (missing item, bad number)
+        std::cerr << ex.what() << std::endl;
+        return 1;
+    }
 }

@@ -86,6 +86,23 @@ void lattice_constants(double re_by_l0, double l0, double& n0, double& lambda) {
 
 inline bool has(uint32_t flags, uint32_t f) { return (flags & f) != 0; }
 
+/* Detail::InvertMatrix<2> (Computer.hpp:323-347): the inverse of [[a, b], [c, d]], or
+ * val times the identity when the determinant is exactly zero.  out = {m00, m01, m10, m11}. */
+void gc_invert(double a, double b, double c, double d, double val, double* out) {
+    const double det = a * d - b * c;
+    if (det == 0) {
+        out[0] = val;
+        out[1] = 0;
+        out[2] = 0;
+        out[3] = val;
+        return;
+    }
+    out[0] = d / det;
+    out[1] = -b / det;
+    out[2] = -c / det;
+    out[3] = a / det;
+}
+
 class Oracle {
 public:
     mps_params prm;
@@ -122,7 +139,10 @@ public:
         l0 = prm.l0;
         re = re_by * l0;                                               /* Environment.hpp:145 */
         re_lap = rl_by * l0;
-        max_dt = std::min(prm.max_dt, std::sqrt(2 * (prm.courant * l0) / prm.g)); /* :138 */
+        if (has(prm.flags, MPS_FLAG_PRESSURE_EXPLICIT))
+            max_dt = std::min(prm.max_dt, (prm.courant * l0) / prm.sound_speed); /* :135 */
+        else
+            max_dt = std::min(prm.max_dt, std::sqrt(2 * (prm.courant * l0) / prm.g)); /* :138 */
         max_dx = prm.courant * l0;                                     /* :143 */
         nl = std::max(re_by, rl_by) * l0 * (1 + prm.courant * 2);      /* :161 */
         lattice_constants(re_by, l0, n0, lambda);
@@ -511,8 +531,124 @@ public:
         }
     }
 
+    /* ComputeImplicitForces with PRESSURE_EXPLICIT (Computer.hpp:1046-1067): every particle */
+    void explicit_pressure() {
+        const size_t n = count();
+        const double c = prm.sound_speed;
+        const double rho0 = prm.rho;
+        ORACLE_PARALLEL_FOR
+        for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {
+            const size_t i = static_cast<size_t>(ii);
+            const double rho = rho0 / n0 * nd[i];
+            p[i] = (rho <= rho0) ? 0 : c * c * (rho - rho0);
+        }
+    }
+
+    /* ModifyByPressureGradient, MPS_GC branch (Computer.hpp:1457-1499, :1543-1563) */
+    void pressure_gradient_gc() {
+        const size_t n = count();
+        const double re2 = re * re;
+        const bool use_spp = spp();
+        ORACLE_PARALLEL_FOR
+        for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {
+            const size_t i = static_cast<size_t>(ii);
+            if (type[i] != MPS_TYPE_FLUID) continue;
+            const int32_t* row = &nb[i * static_cast<size_t>(nb_stride)];
+            /* C^-1 = sum (W / r^2) dx dx^T over every neighbour within r_e, then the SPP
+             * particle (a first AccumulateNeighbor, :1459-1470) */
+            double m00 = 0.0, m01 = 0.0, m10 = 0.0, m11 = 0.0, gx = 0.0, gz = 0.0;
+            for (int32_t k = 0; k < nb_count[i]; k++) {
+                const int32_t j = row[k];
+                if (static_cast<size_t>(j) == i) continue;
+                const double dx = x[j] - x[i];
+                const double dz = z[j] - z[i];
+                const double r2 = dot2(dx, dz, dx, dz);
+                if (r2 < re2) {
+                    const double wg = weight(std::sqrt(r2), re);
+                    const double t = wg / r2;
+                    m00 += t * (dx * dx);
+                    m01 += t * (dx * dz);
+                    m10 += t * (dz * dx);
+                    m11 += t * (dz * dz);
+                    if (use_spp) {
+                        gx += wg * dx;
+                        gz += wg * dz;
+                    }
+                }
+            }
+            double sxp = 0.0, szp = 0.0;
+            const bool has_spp = use_spp && spp_particle(i, re, gx, gz, sxp, szp);
+            if (has_spp) {
+                const double dx = sxp - x[i];
+                const double dz = szp - z[i];
+                const double r2 = dot2(dx, dz, dx, dz);
+                const double t = weight(std::sqrt(r2), re) / r2;
+                m00 += t * (dx * dx);
+                m01 += t * (dx * dz);
+                m10 += t * (dz * dx);
+                m11 += t * (dz * dz);
+            }
+            double C[4];
+            gc_invert(m00, m01, m10, m11, 2.0 / n0, C); /* InvertMatrix(invC, DIM / n0) :1472 */
+            /* sum over non-dummy neighbours of (p_ij / r^2 W) C dx, prod(C, dx) row by row
+             * from 0 (:1475-1496) */
+            double sx = 0.0, sz = 0.0;
+            for (int32_t k = 0; k < nb_count[i]; k++) {
+                const int32_t j = row[k];
+                if (static_cast<size_t>(j) == i) continue;
+                const double dx = x[j] - x[i];
+                const double dz = z[j] - z[i];
+                const double r2 = dot2(dx, dz, dx, dz);
+                if (r2 < re2) {
+                    if (type[j] != MPS_TYPE_DUMMY) {
+                        const double c = (p[j] + p[i]) / r2 * weight(std::sqrt(r2), re);
+                        const double cx = (0.0 + C[0] * dx) + C[1] * dz;
+                        const double cz = (0.0 + C[2] * dx) + C[3] * dz;
+                        sx += c * cx;
+                        sz += c * cz;
+                    } else {
+                        sx += 0.0;
+                        sz += 0.0;
+                    }
+                }
+            }
+            if (has_spp) {
+                const double dx = sxp - x[i];
+                const double dz = szp - z[i];
+                const double r2 = dot2(dx, dz, dx, dz);
+                const double c = (0.0 + p[i]) / r2 * weight(std::sqrt(r2), re);
+                const double cx = (0.0 + C[0] * dx) + C[1] * dz;
+                const double cz = (0.0 + C[2] * dx) + C[3] * dz;
+                sx += c * cx;
+                sz += c * cz;
+            }
+            const double factor = -dt * nd[i] / (prm.rho * n0);
+            dux[i] = factor * sx;
+            duz[i] = factor * sz;
+        }
+        apply_du();
+    }
+
+    /* u += du; x += du dt for fluid particles (Computer.hpp:1543-1563) */
+    void apply_du() {
+        const size_t n = count();
+        ORACLE_PARALLEL_FOR
+        for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {
+            const size_t i = static_cast<size_t>(ii);
+            if (type[i] != MPS_TYPE_FLUID) continue;
+            u[i] += dux[i];
+            w[i] += duz[i];
+            x[i] += dux[i] * dt;
+            z[i] += duz[i] * dt;
+        }
+    }
+
     /* ModifyByPressureGradient, midpoint branch (Computer.hpp:1433-1521, :1543-1563) */
     void pressure_gradient() {
+        if (has(prm.flags, MPS_FLAG_GC)) {
+            pressure_gradient_gc();
+            return;
+        }
         const size_t n = count();
         const double re2 = re * re;
         const bool use_spp = spp();
@@ -558,15 +694,7 @@ public:
             dux[i] = factor * sx;
             duz[i] = factor * sz;
         }
-        ORACLE_PARALLEL_FOR
-        for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {
-            const size_t i = static_cast<size_t>(ii);
-            if (type[i] != MPS_TYPE_FLUID) continue;
-            u[i] += dux[i];
-            w[i] += duz[i];
-            x[i] += dux[i] * dt;
-            z[i] += duz[i] * dt;
-        }
+        apply_du();
     }
 
     /* DynamicStabilize (Computer.hpp:1568-1656) */
@@ -662,9 +790,13 @@ public:
         explicit_forces();
         density();
         if (has(prm.flags, MPS_FLAG_DS)) save_x();
-        set_ppe();
-        solve_ppe();
-        assign_pressure();
+        if (has(prm.flags, MPS_FLAG_PRESSURE_EXPLICIT)) {
+            explicit_pressure();
+        } else {
+            set_ppe();
+            solve_ppe();
+            assign_pressure();
+        }
         pressure_gradient();
         if (has(prm.flags, MPS_FLAG_DS)) dynamic_stabilize();
     }
@@ -941,8 +1073,14 @@ int oracle_stage_solve_ppe(oracle_handle* h) {
     return guarded(h, [&](Oracle& o) { o.solve_ppe(); });
 }
 int oracle_stage_assign_pressure(oracle_handle* h) {
-    return guarded(h, [&](Oracle& o) { o.assign_pressure(); });
+    return guarded(h, [&](Oracle& o) {
+        if (has(o.prm.flags, MPS_FLAG_PRESSURE_EXPLICIT))
+            o.explicit_pressure();
+        else
+            o.assign_pressure();
+    });
 }
+void oracle_gc_invert(const double* m, double val, double* out) { gc_invert(m[0], m[1], m[2], m[3], val, out); }
 int oracle_stage_pressure_gradient(oracle_handle* h) {
     return guarded(h, [&](Oracle& o) { o.pressure_gradient(); });
 }

@@ -64,6 +64,9 @@ int oracle_get_aux(const oracle_handle* h, double* n_without_spp, double* ecs, d
 int oracle_set_aux(oracle_handle* h, const double* n_without_spp, const double* ecs,
                    const double* ox, const double* oz);
 
+/* Detail::InvertMatrix<2> (Computer.hpp:323-347): m and out row-major {00, 01, 10, 11}. */
+void oracle_gc_invert(const double* m, double val, double* out);
+
 /* Reference CG (Computer.hpp:1359-1429) on a caller CSR system; x: guess in, solution out. */
 int oracle_cg_solve_csr(int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val,
                         const double* b, double* x, double eps, int32_t criterion,

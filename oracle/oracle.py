@@ -69,6 +69,8 @@ def load(openmp: bool = False) -> C.CDLL:
     lib.oracle_cg_solve_csr.argtypes = [C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int32,
                                         C.c_int32, _I32, _D, _D]
     lib.oracle_num_threads.restype = C.c_int
+    lib.oracle_gc_invert.argtypes = [_D, C.c_double, _D]
+    lib.oracle_gc_invert.restype = None
     _LIBS[name] = lib
     return lib
 
@@ -231,3 +233,11 @@ def cg_solve_csr(row_ptr, col, val, b, x0, eps, criterion=abi.CRIT_INITIAL_RESID
 
 def num_threads(openmp=True) -> int:
     return int(load(openmp).oracle_num_threads())
+
+
+def gc_invert(m, val):
+    """Detail::InvertMatrix<2> of the row-major 2x2 matrix m (4 values)."""
+    a = np.ascontiguousarray(m, dtype=np.float64).reshape(4)
+    out = np.zeros(4)
+    load(False).oracle_gc_invert(_ptr(a), float(val), _ptr(out))
+    return out

@@ -17,8 +17,11 @@ from openmps_gb300 import build, scenes
 DRIVER = build.DRIVER
 
 
-def write_case(path, scene, end=0.004, interval=0.002, eps=1e-10, steps_per_output=4, extra=""):
+def write_case(path, scene, end=0.004, interval=0.002, eps=1e-10, steps_per_output=4, extra="",
+               flags=None):
     P = dict(scene.meta["params"])
+    if flags is not None:
+        P["flags"] = flags
     rows = ["Type, x, z, u, w, p, n"]
     for k in range(scene.count):
         rows.append("%d, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g" % (
@@ -31,9 +34,10 @@ def write_case(path, scene, end=0.004, interval=0.002, eps=1e-10, steps_per_outp
         ("flags", P["flags"])))
     xml = ('<?xml version="1.0" encoding="utf-8"?>\n<openmps>\n  <condition>\n'
            '    <startTime value="0" />\n    <endTime value="%r" />\n    <outputInterval value="%r" />\n'
-           '    <eps value="%r" />\n  </condition>\n  <environment>\n%s\n%s  </environment>\n'
+           '%s  </condition>\n  <environment>\n%s\n%s  </environment>\n'
            '  <particles type="csv">\n%s\n  </particles>\n</openmps>\n'
-           % (end, interval, eps, env, extra, "\n".join(rows)))
+           % (end, interval, "" if eps is None else '    <eps value="%r" />\n' % eps, env, extra,
+              "\n".join(rows)))
     with open(path, "w") as f:
         f.write(xml)
 
@@ -58,6 +62,25 @@ def test_parse_only(driver, tmp_path):
     assert float(kv["r_eByl_0"]) == s.meta["params"]["re_by_l0"]
     assert int(kv["flags"]) == abi.PRESET_REFERENCE
     assert float(kv["eps"]) == 1e-10
+
+
+def test_parse_only_explicit_pressure(driver, tmp_path):
+    # a PRESSURE_EXPLICIT input: no eps in <condition>, the sound speed c in <environment>
+    # (Main.cpp:215-217, :263-265)
+    s = scenes.config_c0()
+    xml = tmp_path / "explicit.xml"
+    flags = abi.PRESET_REFERENCE | abi.FLAG_PRESSURE_EXPLICIT
+    write_case(xml, s, eps=None, flags=flags, extra='    <c value="27.5" />\n')
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode == 0, out.stderr
+    kv = dict(item.split("=", 1) for item in out.stdout.strip().splitlines()[-1].split()
+              if "=" in item and not item.startswith(("min=", "max=")))
+    assert int(kv["flags"]) == flags
+    assert float(kv["c"]) == 27.5
+    # without c the input is rejected, as the reference's xml.get throws
+    write_case(xml, s, eps=None, flags=flags)
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode != 0
 
 
 def test_rejects_bad_header(driver, tmp_path):

@@ -293,3 +293,28 @@ def test_density_variation(oracle_lib, case):
             idx = i + 35 * j
             analy = -div(float(i), float(j))
             assert abs((speed[idx] / n[idx] - analy) / analy) < 0.10
+
+
+# ------------------------------------------------------ test_ComputerMatrix.cpp
+@pytest.mark.parametrize("m, inv", [
+    # test_ComputerMatrix.cpp:19-33: diagonal
+    ((1.0, 0.0, 0.0, 2.0), (1.0, 0.0, 0.0, 0.5)),
+    # :35-49: anti-diagonal
+    ((0.0, 1.0, 2.0, 0.0), (0.0, 0.5, 1.0, 0.0)),
+    # :51-66: full, asymmetric
+    ((1.0, 2.0, 3.0, 4.0), (-2.0, 1.0, 1.5, -0.5)),
+])
+def test_invert_matrix_known_answers(oracle_lib, m, inv):
+    # the reference asserts the Frobenius distance is 0 with ASSERT_DOUBLE_EQ (4 ulps)
+    from oracle.oracle import gc_invert
+
+    got = gc_invert(m, 1.0)
+    assert math.sqrt(float(np.sum((got - np.array(inv)) ** 2))) <= 4 * np.finfo(float).eps
+
+
+def test_invert_matrix_singular_gives_scaled_identity(oracle_lib):
+    # Detail::InvertMatrix<2> returns IdentityMatrix(val) when det == 0 (Computer.hpp:337-340)
+    from oracle.oracle import gc_invert
+
+    np.testing.assert_array_equal(gc_invert((1.0, 2.0, 2.0, 4.0), 0.25), [0.25, 0.0, 0.0, 0.25])
+    np.testing.assert_array_equal(gc_invert((0.0, 0.0, 0.0, 0.0), 3.0), [3.0, 0.0, 0.0, 3.0])
