@@ -323,9 +323,10 @@ def run_ours(args, rank, world, local_rank):
     comp.set_stage_timing(False)
 
     # ---- the PPE solvers on the same state (a few steps each from a snapshot)
-    compare = None
+    compare = variants = None
     if not args.no_compare and rank == 0:
         compare = compare_solvers(comp, scene, dt, local_rank)
+        variants = method_variants(comp, scene, dt, local_rank)
 
     # ---- the batched workload: 256 uneven dam breaks in one handle
     batched = None
@@ -402,6 +403,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if compare is not None:
         line["ppe_solvers_same_state"] = compare
+    if variants is not None:
+        line["method_variants"] = variants
     if batched is not None:
         line["batched"] = batched
     if not args.no_cpu_baseline and world == 1:
@@ -451,6 +454,53 @@ def compare_solvers(comp, scene, dt, device, steps=3):
         v["ppe_speedup_vs_cg64"] = base["ppe_ms"] / v["ppe_ms"]
     out["note"] = ("same snapshot for every solver, %d steps each, L2 flushed before each step; "
                    "step_ms includes the per-stage events" % steps)
+    return out
+
+
+VARIANT_SOUND_SPEED = 28.0  # about ten times sqrt(2 g h) of the 0.4 m water column
+
+
+def method_variants(comp, scene, dt, device, steps=3):
+    """The workload's step with the other method flags, from the same snapshot: the GC
+    corrective-matrix gradient (multigrid solver), and the explicit pressure (no PPE; its
+    own CFL time step courant l0 / c) with and without GC.  Per-stage CUDA events."""
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300.computer import Computer
+
+    P = comp.particles()
+    A = comp.aux()
+    stock = abi.PRESET_REFERENCE
+    l0 = scene.l0
+    dt_explicit = 0.1 * l0 / VARIANT_SOUND_SPEED
+    cases = {
+        "stock_mg": (stock, dt),
+        "gc_mg": (stock | abi.FLAG_GC, dt),
+        "explicit": (stock | abi.FLAG_PRESSURE_EXPLICIT, dt_explicit),
+        "explicit_gc": (stock | abi.FLAG_PRESSURE_EXPLICIT | abi.FLAG_GC, dt_explicit),
+    }
+    out = {}
+    for name, (flags, step_dt) in cases.items():
+        c = Computer(scene.params(solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS, eps=1e-8,
+                                  flags=flags, sound_speed=VARIANT_SOUND_SPEED), device=device)
+        c.add_particles(P["type"], P["x"], P["z"], P["u"], P["w"], P["p"], P["n"])
+        c.set_aux(A["n_without_spp"], A["ecs"], A["ox"], A["oz"])
+        c.set_stage_timing(True)
+        step_ms, grad_ms, pres_ms = [], [], []
+        for _ in range(steps):
+            c.flush_l2(FLUSH_BYTES)
+            c.event_record(0)
+            c.forward_time(step_dt)
+            c.event_record(1)
+            step_ms.append(c.event_elapsed(0, 1))
+            st = c.stats()["stage_ms"]
+            grad_ms.append(st["gradient"])
+            pres_ms.append(st["pressure"])
+        c.close()
+        ms = statistics.mean(step_ms)
+        out[name] = {"flags": flags, "dt": step_dt, "step_ms": ms, "gradient_ms": statistics.mean(grad_ms),
+                     "pressure_ms": statistics.mean(pres_ms), "particle_steps_per_s": scene.count / (ms * 1e-3)}
+    out["note"] = ("same snapshot, %d steps each, L2 flushed before each step; explicit: c = %g m/s, "
+                   "dt = courant l0 / c" % (steps, VARIANT_SOUND_SPEED))
     return out
 
 
