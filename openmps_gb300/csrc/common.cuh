@@ -326,9 +326,14 @@ void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStr
 // the explicit pressure of every particle from its number density; sets *ok (the solve
 // flag the later stages test) to 1 when given
 void launch_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok, cudaStream_t s);
+// the second number density and the explicit pressure in one walk, caching W(r, r_e) for
+// launch_pressure_gradient_cached (one launch)
+void launch_density_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok,
+                                      cudaStream_t s);
 // the midpoint gradient, or with MPS_FLAG_GC the corrected one (two walks of each row)
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
-// the same reading the weights launch_density_set_ppe cached (positions unchanged since)
+// the same reading the weights launch_density_set_ppe or launch_density_explicit_pressure
+// cached (positions unchanged since)
 void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // scan.cu
@@ -338,6 +343,6 @@ void launch_exclusive_scan(const int* in, int* out, int m, int* scratch, cudaStr
 constexpr int kLaunchesSearch = 3, kLaunchesDensity = 1, kLaunchesEcs = 1, kLaunchesExplicit = 2,
               kLaunchesSaveX = 1, kLaunchesSetPpe = 6, kLaunchesAssign = 1, kLaunchesGradient = 2,
               kLaunchesDs = 2, kLaunchesDt = 1, kLaunchesCfl = 2, kLaunchesPrePressure = 1,
-              kLaunchesExplicitUpdate = 1, kLaunchesExplicitPressure = 1;
+              kLaunchesExplicitUpdate = 1;
 
 }  // namespace mpsgb

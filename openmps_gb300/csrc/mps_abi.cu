@@ -711,8 +711,14 @@ void forward(mps_handle* h, double dt) {
     launch_explicit_update(sc, h->st, s);
     launched(h, kLaunchesExplicitUpdate);
     stage_mark(h, kDensity2);
+    const bool implicit = (flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u;
     const bool fused = density_ppe_fusable(sc);  // the "ppe" stage time then covers density 2
-    if (!fused) {
+    if (!implicit) {
+        // no PPE: the second density and the pressure in one walk (the "density2" stage
+        // time covers the pressure); the solve flag the later stages test is set
+        launch_density_explicit_pressure(sc, h->st, &h->S->converged, s);
+        launched(h, kLaunchesDensity);
+    } else if (!fused) {
         launch_density(sc, h->st, s);
         launched(h, kLaunchesDensity);
     }
@@ -720,7 +726,6 @@ void forward(mps_handle* h, double dt) {
         launch_save_x(sc, h->st, s);
         launched(h, kLaunchesSaveX);
     }
-    const bool implicit = (flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u;
     stage_mark(h, kPpe);
     if (implicit) {
         if (fused)
@@ -737,14 +742,9 @@ void forward(mps_handle* h, double dt) {
     if (implicit) {
         launch_assign_pressure(sc, h->st, s);
         launched(h, kLaunchesAssign);
-    } else {
-        // no PPE: the pressure follows from the number density; the solve flag the
-        // later stages test is set
-        launch_explicit_pressure(sc, h->st, &h->S->converged, s);
-        launched(h, kLaunchesExplicitPressure);
     }
     stage_mark(h, kGradient);
-    if (fused)  // the assembly walk cached W(r, r_e) on these positions
+    if (fused || !implicit)  // the density walk cached W(r, r_e) on these positions
         launch_pressure_gradient_cached(sc, h->st, s);
     else
         launch_pressure_gradient(sc, h->st, s);
@@ -862,21 +862,24 @@ void batch_stages_pre(mps_handle* h, double dt) {
     do_search(h);
     launch_pre_pressure(sc, h->st, s);
     launch_explicit_update(sc, h->st, s);
-    const bool fused = density_ppe_fusable(sc);
-    if (!fused) launch_density(sc, h->st, s);
-    if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
-    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
     const bool implicit = batch_implicit(h);
+    const bool fused = density_ppe_fusable(sc);
+    check(cudaMemsetAsync(h->d_all_ok, 1, sizeof(int32_t), s), "memset");
     if (!implicit)
-        launch_explicit_pressure(sc, h->st, nullptr, s);
-    else if (fused)
-        launch_density_set_ppe(sc, h->st, true, s);
-    else
-        launch_set_ppe(sc, h->st, true, s);
+        launch_density_explicit_pressure(sc, h->st, nullptr, s);  // no PPE
+    else if (!fused)
+        launch_density(sc, h->st, s);
+    if (h->prm.flags & MPS_FLAG_DS) launch_save_x(sc, h->st, s);
+    if (implicit) {
+        if (fused)
+            launch_density_set_ppe(sc, h->st, true, s);
+        else
+            launch_set_ppe(sc, h->st, true, s);
+    }
     h->ppe_fp32 = true;
     after_launch("batch stages");
     launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate +
-                    (fused ? 0 : kLaunchesDensity) + (implicit ? kLaunchesSetPpe : kLaunchesExplicitPressure) +
+                    (fused ? 0 : kLaunchesDensity) + (implicit ? kLaunchesSetPpe : 0) +
                     ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
 }
 
@@ -886,7 +889,7 @@ void batch_stages_post(mps_handle* h) {
     sc.guard = 1;
     const bool implicit = batch_implicit(h);
     if (implicit) launch_assign_pressure(sc, h->st, s);
-    if (density_ppe_fusable(sc))  // batch_stages_pre assembled with the fused walk
+    if (density_ppe_fusable(sc) || !implicit)  // batch_stages_pre's density walk cached W
         launch_pressure_gradient_cached(sc, h->st, s);
     else
         launch_pressure_gradient(sc, h->st, s);

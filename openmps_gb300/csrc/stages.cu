@@ -161,6 +161,50 @@ __global__ void k_density(SceneConst sc, DeviceState st) {
     }
 }
 
+// With PRESSURE_EXPLICIT: the second ComputeNeighborDensities and the pressure of
+// ComputeImplicitForces (Computer.hpp:1046-1067) in one pass.  The pressure reads only
+// the particle's own density, and SaveX between the two stages touches neither, so the
+// results equal the separate kernels.  W(r, r_e) of the entries in range is cached for
+// the pressure gradient (same positions, same list order), as k_density_ppe does.
+__global__ void k_density_explicit_pressure(SceneConst sc, DeviceState st, int32_t* ok) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && ok) *ok = 1;
+    if (i >= sc.n) return;
+    if (step_failed(sc, st)) return;
+    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
+    if (spp) st.n_wo_spp[i] = sc.n0;
+    const int t = st.type[i];
+    double nd = st.nd[i];  // dummy and disabled particles keep theirs
+    if (t != MPS_TYPE_DUMMY && t != MPS_TYPE_DISABLED) {
+        const int n = sc.n;
+        const double xi = st.x[i], zi = st.z[i];
+        double thisN = 0.0;
+        int m_re = 0;
+        for_near(sc, st, i, sc.f32_out_re, [&](int j) {
+            const double dx = st.x[j] - xi;
+            const double dz = st.z[j] - zi;
+            const double r2 = dist2(dx, dz);
+            if (below(r2, sc.re2)) {
+                const double w = weight(__dsqrt_rn(r2), sc.re);
+                thisN += w;
+                if (m_re < kReCache) st.w_re[static_cast<int64_t>(m_re) * n + i] = w;
+                m_re++;
+            }
+        });
+        if (spp) {
+            st.n_wo_spp[i] = thisN;
+            nd = (thisN < sc.n0) ? sc.n0 : thisN;
+        } else {
+            nd = thisN;
+        }
+        st.nd[i] = nd;
+    }
+    const double rho0 = sc.rho;
+    const double c = sc.sound_speed;
+    const double rho = rho0 / sc.n0 * nd;
+    st.p[i] = (rho <= rho0) ? 0.0 : c * c * (rho - rho0);
+}
+
 // ComputeErrorCorrection (Computer.hpp:877-910)
 __global__ void k_error_correction(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -878,6 +922,11 @@ void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStr
 
 void launch_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok, cudaStream_t s) {
     k_explicit_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, ok);
+}
+
+void launch_density_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok,
+                                      cudaStream_t s) {
+    k_density_explicit_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, ok);
 }
 
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
