@@ -125,7 +125,12 @@ typedef struct mps_params {
     int32_t max_refinements; /* MIXED: maximum FP64 refinement passes */
     int32_t cg_launch;       /* MPS_CG_LAUNCH_GRAPH (default), _HOST or _PERSISTENT */
     double sound_speed;      /* Environment(..., c, ...): used only with MPS_FLAG_PRESSURE_EXPLICIT */
-    double reserved[5];
+    int32_t dim;             /* 2 (default; 0 means 2) or 3 (DIM3, defines.hpp:9-11): three-
+                                dimensional scenes take the *3 particle calls below and the
+                                MPS_SOLVER_CG64 or MPS_SOLVER_MIXED solver; no batches */
+    int32_t pad0;
+    double min_y, max_y;     /* domain along y (DIM3: Environment(..., minY, ..., maxY, ...)) */
+    double reserved[2];
 } mps_params;
 
 /* Derived constants of Environment (Environment.hpp:129-216) and Grid (Grid.hpp:137-150). */
@@ -137,6 +142,9 @@ typedef struct mps_environment {
     double rho, nu, g;
     double min_x, min_z, max_x, max_z;
     int64_t grid_nx, grid_nz, grid_max_per_cell;
+    double min_y, max_y;  /* DIM3 */
+    int64_t grid_ny;      /* 1 in 2D */
+    int64_t dim;
 } mps_environment;
 
 /* Per-step solver statistics and counters. */
@@ -202,6 +210,20 @@ int mps_set_particles_device(mps_handle* h, const int32_t* type, const double* x
  * particle takes in the explicit step.  Host arrays of n elements. */
 int mps_set_wall_positions(mps_handle* h, const double* wx, const double* wz);
 
+/* Three-dimensional scenes (mps_params.dim = 3): the same calls with the y axis, in the
+ * reference's DIM3 argument order (position x, y, z; velocity u, v, w).  The
+ * two-dimensional particle calls return MPS_ERR_STATE on such a handle, and these on a
+ * two-dimensional one. */
+int mps_add_particles3(mps_handle* h, int64_t n, const int32_t* type, const double* x,
+                       const double* y, const double* z, const double* u, const double* v,
+                       const double* w, const double* p, const double* nd);
+int mps_get_particles3(mps_handle* h, int32_t* type, double* x, double* y, double* z, double* u,
+                       double* v, double* w, double* p, double* nd);
+int mps_set_particles3(mps_handle* h, const int32_t* type, const double* x, const double* y,
+                       const double* z, const double* u, const double* v, const double* w,
+                       const double* p, const double* nd);
+int mps_set_wall_positions3(mps_handle* h, const double* wx, const double* wy, const double* wz);
+
 /* ForwardTime(double dt) (Computer.hpp:1700-1742); dt <= 0 selects ForwardTime()
  * (Computer.hpp:1745-1751) with the CFL time step of DetermineDt (:759-777). */
 int mps_forward_time(mps_handle* h, double dt);
@@ -264,6 +286,11 @@ int mps_debug_get_ppe(mps_handle* h, int64_t* row_ptr, int32_t* col, double* val
 int mps_debug_get_aux(mps_handle* h, double* n_without_spp, double* ecs, double* ox, double* oz);
 int mps_debug_set_aux(mps_handle* h, const double* n_without_spp, const double* ecs,
                       const double* ox, const double* oz);
+/* The same with originalX's y component (DIM3 handles). */
+int mps_debug_get_aux3(mps_handle* h, double* n_without_spp, double* ecs, double* ox, double* oy,
+                       double* oz);
+int mps_debug_set_aux3(mps_handle* h, const double* n_without_spp, const double* ecs,
+                       const double* ox, const double* oy, const double* oz);
 
 /* SolvePressurePoissonEquation on a caller-supplied CSR system (host arrays), the
  * entry the reference's CG tests drive (test_ComputerConjugateGradient.cpp).

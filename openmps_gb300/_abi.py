@@ -81,7 +81,11 @@ class MpsParams(C.Structure):
         ("max_refinements", C.c_int32),
         ("cg_launch", C.c_int32),
         ("sound_speed", C.c_double),
-        ("reserved", C.c_double * 5),
+        ("dim", C.c_int32),
+        ("pad0", C.c_int32),
+        ("min_y", C.c_double),
+        ("max_y", C.c_double),
+        ("reserved", C.c_double * 2),
     ]
 
 
@@ -109,6 +113,10 @@ class MpsEnvironment(C.Structure):
         ("grid_nx", C.c_int64),
         ("grid_nz", C.c_int64),
         ("grid_max_per_cell", C.c_int64),
+        ("min_y", C.c_double),
+        ("max_y", C.c_double),
+        ("grid_ny", C.c_int64),
+        ("dim", C.c_int64),
     ]
 
 

@@ -3,7 +3,7 @@
 Each CUDA translation unit is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo`` and linked into
 ``openmps_gb300/libopenmps_gb300.so``.  The per-particle stage kernels
-(``grid.cu``, ``stages.cu``) are compiled with ``-fmad=false`` so that every
+(``grid.cu``, ``stages.cu``, ``dim3.cu``) are compiled with ``-fmad=false`` so that every
 floating-point operation rounds like the reference's FP64 CPU path; the solver
 (``cg.cu``) uses fused multiply-adds.  Host code never contracts either
 (``-ffp-contract=off``), so x86 and Arm hosts compute the same constants.
@@ -30,6 +30,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "grid.cu": ["-fmad=false"],
     "stages.cu": ["-fmad=false"],
+    "dim3.cu": ["-fmad=false"],
     "cg.cu": [],
     "mg.cu": [],
     "learned.cu": [],

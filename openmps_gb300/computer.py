@@ -48,6 +48,12 @@ PROTOTYPES = {
     "mps_get_particles_device": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "mps_set_particles_device": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "mps_set_wall_positions": (C.c_int, [_P, _D, _D]),
+    "mps_add_particles3": (C.c_int, [_P, C.c_int64, _I32, _D, _D, _D, _D, _D, _D, _D, _D]),
+    "mps_get_particles3": (C.c_int, [_P, _I32, _D, _D, _D, _D, _D, _D, _D, _D]),
+    "mps_set_particles3": (C.c_int, [_P, _I32, _D, _D, _D, _D, _D, _D, _D, _D]),
+    "mps_set_wall_positions3": (C.c_int, [_P, _D, _D, _D]),
+    "mps_debug_get_aux3": (C.c_int, [_P, _D, _D, _D, _D, _D]),
+    "mps_debug_set_aux3": (C.c_int, [_P, _D, _D, _D, _D, _D]),
     "mps_forward_time": (C.c_int, [_P, C.c_double]),
     "mps_forward_steps": (C.c_int, [_P, C.c_double, C.c_int32]),
     "mps_get_environment": (C.c_int, [_P, C.POINTER(abi.MpsEnvironment)]),
@@ -211,6 +217,42 @@ class Computer:
 
     def set_wall_positions(self, wx, wz):
         self._check(self.lib.mps_set_wall_positions(self.h, _ptr(_f64(wx)), _ptr(_f64(wz))))
+
+    # ------------------------------------------- three-dimensional scenes (dim = 3)
+    FIELDS3 = ("x", "y", "z", "u", "v", "w", "p", "n")
+
+    def add_particles3(self, t, x, y, z, u=None, v=None, w=None, p=None, n=None):
+        t = np.ascontiguousarray(t, dtype=np.int32)
+        arrs = [_f64(a) for a in (x, y, z, u, v, w, p, n)]
+        self._check(self.lib.mps_add_particles3(self.h, len(t), _ptr(t, C.c_int32),
+                                                *[_ptr(a) for a in arrs]))
+
+    def particles3(self) -> dict:
+        n = self.count
+        out = {k: np.empty(n) for k in self.FIELDS3}
+        out["type"] = np.empty(n, dtype=np.int32)
+        self._check(self.lib.mps_get_particles3(self.h, _ptr(out["type"], C.c_int32),
+                                                *[_ptr(out[k]) for k in self.FIELDS3]))
+        return out
+
+    def set_particles3(self, t=None, x=None, y=None, z=None, u=None, v=None, w=None, p=None, n=None):
+        t = None if t is None else np.ascontiguousarray(t, dtype=np.int32)
+        self._check(self.lib.mps_set_particles3(self.h, _ptr(t, C.c_int32),
+                                                *[_ptr(_f64(a)) for a in (x, y, z, u, v, w, p, n)]))
+
+    def set_wall_positions3(self, wx, wy, wz):
+        self._check(self.lib.mps_set_wall_positions3(self.h, _ptr(_f64(wx)), _ptr(_f64(wy)), _ptr(_f64(wz))))
+
+    def aux3(self) -> dict:
+        n = self.count
+        out = {k: np.zeros(n) for k in ("n_without_spp", "ecs", "ox", "oy", "oz")}
+        self._check(self.lib.mps_debug_get_aux3(self.h, *[_ptr(out[k]) for k in
+                                                          ("n_without_spp", "ecs", "ox", "oy", "oz")]))
+        return out
+
+    def set_aux3(self, n_without_spp=None, ecs=None, ox=None, oy=None, oz=None):
+        self._check(self.lib.mps_debug_set_aux3(self.h, *[_ptr(_f64(a)) for a in
+                                                          (n_without_spp, ecs, ox, oy, oz)]))
 
     # ---------------------------------------------------------------- steps
     def forward_time(self, dt: float | None = None):

@@ -55,6 +55,10 @@ struct SceneConst {
     double rho, nu, g, surface_ratio, max_dt, max_dx;
     double min_x, min_z;
     double sound_speed;  // c of the explicit pressure (MPS_FLAG_PRESSURE_EXPLICIT)
+    // three-dimensional scenes (DIM3): cells (x, y, z) at ((cx gny) + cy) gnz + cz
+    int32_t dim;  // 2 or 3
+    int32_t gny;  // cells along y (1 in 2D)
+    double min_y;
 };
 
 // Time of the step in flight (Environment::t, ::dt); lives in device memory so that
@@ -117,6 +121,9 @@ struct DeviceState {
     StepScalars* step;
     DevStatus* status;
     const int32_t* solve_ok;  // converged flag of the last PPE solve
+    // the y axis of three-dimensional scenes (null in 2D): position, velocity, wall
+    // target, SaveX copy and velocity change
+    double *y, *v, *wall_y, *oy, *duy;
 };
 
 // --------------------------------------------------------------- helpers
@@ -336,6 +343,22 @@ void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaS
 // cached (positions unchanged since)
 void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// part 2 of the CFL step (dt from the max |u|^2 a launch before it gathered)
+void launch_cfl_dt_finish(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// dim3.cu: the stages of a three-dimensional scene (same names and counts as above)
+void launch_search3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_cfl_dt3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_density3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_error_correction3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_density_variation3(const SceneConst& sc, const DeviceState& st, double* out, cudaStream_t s);
+void launch_explicit3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_save_x3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_set_ppe3(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
+void launch_pressure_gradient3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_dynamic_stabilize3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+// the PPE layout kernels (stages.cu) after a row assembly: chunk sizes, offsets, SELL sort
+void launch_ppe_layout(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
+constexpr int kLaunchesSearch3 = 3;
 // scan.cu
 int scan_scratch_ints(int m);
 void launch_exclusive_scan(const int* in, int* out, int m, int* scratch, cudaStream_t s);

@@ -171,6 +171,46 @@ void lattice_constants(double re_by_l0, double l0, double& n0, double& lambda) {
     lambda /= n0;
 }
 
+// The DIM3 branch of the same loops (Environment.hpp:166-215): x outer, then y, then z.
+void lattice_constants3(double re_by_l0, double l0, double& n0, double& lambda) {
+    const double re = re_by_l0 * l0;
+    const int range = static_cast<int>(std::ceil(re_by_l0));
+    n0 = 0;
+    lambda = 0;
+    volatile double t0, t1, t2;
+    for (int i = -range; i < range; i++) {
+        for (int j = -range; j < range; j++) {
+            for (int k = -range; k < range; k++) {
+                if (!((i == 0) && (j == 0) && (k == 0))) {
+                    const double x0 = i * l0;
+                    const double x1 = j * l0;
+                    const double x2 = k * l0;
+                    t0 = x0 * x0;
+                    t1 = x1 * x1;
+                    t2 = x2 * x2;
+                    const double r = std::sqrt(((0.0 + t0) + t1) + t2);
+                    if (r < re) {
+                        const double w = ((0 < r) && (r < re)) ? (re / r - 1) : 0;
+                        n0 += w;
+                        t0 = r * r;
+                        t1 = t0 * w;
+                        lambda += t1;
+                    }
+                }
+            }
+        }
+    }
+    lambda /= n0;
+}
+
+bool is3(const mps_handle* h) { return h->sc.dim == 3; }
+
+void require_dim(const mps_handle* h, int dim) {
+    if (h->sc.dim != dim)
+        throw StatusError{MPS_ERR_STATE, dim == 3 ? "two-dimensional handle: use the 2D particle calls"
+                                                  : "three-dimensional handle: use the *3 particle calls"};
+}
+
 void validate(const mps_params& p) {
     auto bad = [](const char* m) { throw StatusError{MPS_ERR_INVALID_ARGUMENT, m}; };
     if (!(p.l0 > 0)) bad("l0 must be positive");
@@ -185,6 +225,13 @@ void validate(const mps_params& p) {
     if (p.flags & ~static_cast<uint32_t>(MPS_FLAGS_ALL)) bad("unknown method flag");
     if ((p.flags & MPS_FLAG_PRESSURE_EXPLICIT) && !(p.sound_speed > 0))
         bad("MPS_FLAG_PRESSURE_EXPLICIT needs a positive sound_speed");
+    if (p.dim != 0 && p.dim != 2 && p.dim != 3) bad("dim must be 2 or 3");
+    if (p.dim == 3) {
+        if (!(p.max_y > p.min_y)) bad("empty domain along y");
+        if (p.solver != MPS_SOLVER_CG64 && p.solver != MPS_SOLVER_MIXED)
+            throw StatusError{MPS_ERR_NOT_SUPPORTED,
+                              "three-dimensional scenes take MPS_SOLVER_CG64 or MPS_SOLVER_MIXED"};
+    }
     if (p.cg_launch != MPS_CG_LAUNCH_GRAPH && p.cg_launch != MPS_CG_LAUNCH_HOST &&
         p.cg_launch != MPS_CG_LAUNCH_PERSISTENT)
         bad("unknown cg_launch");
@@ -221,8 +268,15 @@ void setup_constants(mps_handle* h) {
     sc.f32_out_re = f32_bound(sc.re2, true);
     sc.f32_out_rl = f32_bound(sc.rl2, true);
     sc.pad1 = 0.0f;
-    lattice_constants(re_by, p.l0, sc.n0, sc.lambda);
-    lattice_constants(rl_by, p.l0, sc.n0_lap, sc.lambda_lap);
+    sc.dim = (p.dim == 3) ? 3 : 2;
+    const bool d3 = sc.dim == 3;
+    if (d3) {
+        lattice_constants3(re_by, p.l0, sc.n0, sc.lambda);
+        lattice_constants3(rl_by, p.l0, sc.n0_lap, sc.lambda_lap);
+    } else {
+        lattice_constants(re_by, p.l0, sc.n0, sc.lambda);
+        lattice_constants(rl_by, p.l0, sc.n0_lap, sc.lambda_lap);
+    }
     sc.rho = p.rho;
     sc.nu = p.nu;
     sc.g = p.g;
@@ -235,17 +289,21 @@ void setup_constants(mps_handle* h) {
     sc.max_dx = p.courant * p.l0;                                             // :143
     sc.min_x = p.min_x;
     sc.min_z = p.min_z;
+    sc.min_y = d3 ? p.min_y : 0.0;
     // Grid.hpp:137-150
     const double cx = std::ceil((p.max_x - p.min_x) / sc.nl);
     const double cz = std::ceil((p.max_z - p.min_z) / sc.nl);
-    if (!(cx < 1e6 && cz < 1e6 && cx * cz < 2e8))
+    const double cy = d3 ? std::ceil((p.max_y - p.min_y) / sc.nl) : -1.0;
+    if (!(cx < 1e6 && cz < 1e6 && cy < 1e6 && (cx + 2) * (cz + 2) * (cy + 2) < 2e8))
         throw StatusError{MPS_ERR_INVALID_ARGUMENT, "domain has too many cells"};
     sc.gnx = static_cast<int32_t>(cx) + 2;
     sc.gnz = static_cast<int32_t>(cz) + 2;
-    sc.cells_per_scene = sc.gnx * sc.gnz;
+    sc.gny = static_cast<int32_t>(cy) + 2;  // 1 in 2D
+    sc.cells_per_scene = sc.gnx * sc.gny * sc.gnz;
     sc.nscenes = 1;
     const int c = static_cast<int>(std::ceil(sc.nl / p.l0));
-    sc.max_per_cell = (c + 1) * (c + 1);
+    sc.max_per_cell = d3 ? (c + 1) * (c + 1) * (c + 1) : (c + 1) * (c + 1);
+    // Computer::MaxNeighborCount (Computer.hpp:1136-1140): 9 maxPerCell in both dimensions
     sc.nb_stride = sc.max_per_cell * 9;
     sc.ppe_stride = sc.nb_stride + 1;
 }
@@ -290,11 +348,17 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     DeviceState& st = h->st;
     const int64_t cells = static_cast<int64_t>(sc.cells_per_scene) * sc.nscenes;
     st.type = dalloc<int32_t>(h, n);
-    double** dbl[] = {&st.x, &st.z, &st.u, &st.w, &st.p, &st.nd, &st.wall_x, &st.wall_z,
-                      &st.n_wo_spp, &st.ecs, &st.ox, &st.oz, &st.dux, &st.duz};
-    double* const* old_dbl[] = {&old.x, &old.z, &old.u, &old.w, &old.p, &old.nd, &old.wall_x,
-                                &old.wall_z, &old.n_wo_spp, &old.ecs, &old.ox, &old.oz,
-                                &old.dux, &old.duz};
+    std::vector<double**> dbl = {&st.x, &st.z, &st.u, &st.w, &st.p, &st.nd, &st.wall_x, &st.wall_z,
+                                 &st.n_wo_spp, &st.ecs, &st.ox, &st.oz, &st.dux, &st.duz};
+    std::vector<double* const*> old_dbl = {&old.x, &old.z, &old.u, &old.w, &old.p, &old.nd, &old.wall_x,
+                                           &old.wall_z, &old.n_wo_spp, &old.ecs, &old.ox, &old.oz,
+                                           &old.dux, &old.duz};
+    const bool d3 = sc.dim == 3;
+    st.y = st.v = st.wall_y = st.oy = st.duy = nullptr;
+    if (d3) {  // the y axis
+        for (double** a : {&st.y, &st.v, &st.wall_y, &st.oy, &st.duy}) dbl.push_back(a);
+        for (double* const* a : {&old.y, &old.v, &old.wall_y, &old.oy, &old.duy}) old_dbl.push_back(a);
+    }
     for (double** a : dbl) *a = dalloc<double>(h, n);
     st.cell_count = dalloc<int32_t>(h, cells);
     st.cell_slot = dalloc<int32_t>(h, cells * sc.max_per_cell);
@@ -336,7 +400,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.w_re = dalloc<double>(h, n * kReCache);
     st.row_of = st.particle_of = st.row_cell = st.cell_fill = st.cell_start = nullptr;
     st.unplaced = st.unplaced_pos = st.row_scratch = nullptr;
-    if (h->nscenes == 0) {  // single scene: PPE rows in cell order
+    if (h->nscenes == 0 && !d3) {  // single 2D scene: PPE rows in cell order
         st.row_of = dalloc<int32_t>(h, n);
         st.particle_of = dalloc<int32_t>(h, n);
         st.row_cell = dalloc<int32_t>(h, n);
@@ -350,7 +414,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     MgHierarchy& mg = h->mg;
     mg = MgHierarchy{};
     int bottom = 0;
-    mg.levels = mg_plan(sc.gnx, sc.gnz, mg.lv, &bottom);
+    mg.levels = d3 ? 0 : mg_plan(sc.gnx, sc.gnz, mg.lv, &bottom);  // no 3D hierarchy
     mg.bottom = bottom;
     if (mg.levels > 0) {
         for (int l = 1; l <= mg.levels; l++) {
@@ -448,7 +512,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     if (keep > 0) {
         check(cudaMemcpyAsync(st.type, old.type, sizeof(int32_t) * keep, cudaMemcpyDeviceToDevice, s),
               "copy");
-        for (size_t k = 0; k < sizeof(dbl) / sizeof(dbl[0]); k++)
+        for (size_t k = 0; k < dbl.size(); k++)
             check(cudaMemcpyAsync(*dbl[k], *old_dbl[k], sizeof(double) * keep,
                                   cudaMemcpyDeviceToDevice, s),
                   "copy");
@@ -596,6 +660,12 @@ void do_search(mps_handle* h) {
         launch_status_counters_reset(h->st.status, s);  // batch: failures stay flagged across steps
     else
         check(cudaMemsetAsync(h->st.status, 0, sizeof(DevStatus), s), "memset");
+    if (is3(h)) {
+        launch_search3(h->sc, h->st, s);
+        after_launch("search");
+        launched(h, kLaunchesSearch3);
+        return;
+    }
     launch_bucket(h->sc, h->st, s);
     launch_cell_sort(h->sc, h->st, s);
     launch_neighbors(h->sc, h->st, s);
@@ -685,9 +755,91 @@ void do_solve(mps_handle* h) {
     }
 }
 
+// ForwardTime of a three-dimensional scene (Computer.hpp:1700-1742), the stage kernels of
+// dim3.cu in the reference's order with the dimension-free PPE layout, solvers and
+// pressure kernels.
+void forward3(mps_handle* h, double dt) {
+    cudaStream_t s = h->stream;
+    const uint32_t flags = h->prm.flags;
+    SceneConst sc = h->sc;
+    sc.guard = 1;
+    stage_mark(h, kSearch);
+    if (dt > 0) {
+        launch_set_dt(sc, h->st, dt, s);
+        launched(h, kLaunchesDt);
+    } else {
+        launch_cfl_dt3(sc, h->st, s);
+        launched(h, kLaunchesCfl);
+    }
+    do_search(h);
+    stage_mark(h, kDensity);
+    launch_density3(sc, h->st, s);
+    launched(h, kLaunchesDensity);
+    stage_mark(h, kEcs);
+    if (flags & MPS_FLAG_ECS) {
+        launch_error_correction3(sc, h->st, s);
+        launched(h, kLaunchesEcs);
+    }
+    stage_mark(h, kExplicit);
+    launch_explicit3(sc, h->st, s);
+    launched(h, kLaunchesExplicit);
+    stage_mark(h, kDensity2);
+    launch_density3(sc, h->st, s);
+    launched(h, kLaunchesDensity);
+    if (flags & MPS_FLAG_DS) {
+        launch_save_x3(sc, h->st, s);
+        launched(h, kLaunchesSaveX);
+    }
+    const bool implicit = (flags & MPS_FLAG_PRESSURE_EXPLICIT) == 0u;
+    stage_mark(h, kPpe);
+    if (implicit) {
+        launch_set_ppe3(sc, h->st, wants_fp32(h), s);
+        h->ppe_fp32 = wants_fp32(h);
+        launched(h, kLaunchesSetPpe);
+        after_launch("stages");
+    }
+    stage_mark(h, kSolve);
+    if (implicit) do_solve(h);
+    stage_mark(h, kPressure);
+    if (implicit) {
+        launch_assign_pressure(sc, h->st, s);
+        launched(h, kLaunchesAssign);
+    } else {
+        launch_explicit_pressure(sc, h->st, &h->S->converged, s);
+        launched(h, 1);
+    }
+    stage_mark(h, kGradient);
+    launch_pressure_gradient3(sc, h->st, s);
+    launched(h, kLaunchesGradient);
+    stage_mark(h, kDs);
+    if (flags & MPS_FLAG_DS) {
+        launch_dynamic_stabilize3(sc, h->st, s);
+        launched(h, kLaunchesDs);
+    }
+    stage_mark(h, kNumStages);
+    after_launch("step");
+    read_status(h, implicit);
+    h->stats.steps += 1;
+    if (h->stage_timing) {
+        float total = 0.f;
+        for (int k = 0; k < kNumStages; k++) {
+            float ms = 0.f;
+            check(cudaEventElapsedTime(&ms, h->stage_events[k], h->stage_events[k + 1]), "elapsed");
+            h->stats.stage_ms[k] = ms;
+            total += ms;
+        }
+        h->stats.stage_ms[10] = 0.0;
+        h->stats.stage_ms[11] = total;
+    }
+}
+
 void forward(mps_handle* h, double dt) {
     require_particles(h);
     if (h->nscenes > 0) throw StatusError{MPS_ERR_STATE, "batch handle: use mps_batch_forward"};
+    if (is3(h)) {
+        forward3(h, dt);
+        return;
+    }
     cudaStream_t s = h->stream;
     const uint32_t flags = h->prm.flags;
     SceneConst sc = h->sc;
@@ -1090,11 +1242,12 @@ int mps_destroy(mps_handle* h) {
     return MPS_OK;
 }
 
-int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const double* x,
-                      const double* z, const double* u, const double* w, const double* p,
-                      const double* nd) {
-    if (!h || n < 0 || (n > 0 && (!type || !x || !z))) return MPS_ERR_INVALID_ARGUMENT;
+static int add_particles_impl(mps_handle* h, int dim, int64_t n, const int32_t* type, const double* x,
+                              const double* y, const double* z, const double* u, const double* v,
+                              const double* w, const double* p, const double* nd) {
+    if (!h || n < 0 || (n > 0 && (!type || !x || !z || (dim == 3 && !y)))) return MPS_ERR_INVALID_ARGUMENT;
     return guarded(h, [&] {
+        require_dim(h, dim);
         if (n == 0) return;
         for (int64_t i = 0; i < n; i++)
             if (type[i] < MPS_TYPE_FLUID || type[i] > MPS_TYPE_DISABLED)
@@ -1119,19 +1272,42 @@ int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const doubl
         upload(h, st.w + old, w, b8, false);
         upload(h, st.p + old, p, b8, false);
         upload(h, st.nd + old, nd, b8, false);
+        if (dim == 3) {
+            upload(h, st.y + old, y, b8, false);
+            upload(h, st.wall_y + old, y, b8, false);
+            upload(h, st.v + old, v, b8, false);
+        }
         launch_positions_f32(h->sc, st, h->stream, static_cast<int>(old), static_cast<int>(n));
         launched(h, 1);
         check(cudaStreamSynchronize(h->stream), "add particles");
     });
 }
 
+int mps_add_particles(mps_handle* h, int64_t n, const int32_t* type, const double* x,
+                      const double* z, const double* u, const double* w, const double* p,
+                      const double* nd) {
+    return add_particles_impl(h, 2, n, type, x, nullptr, z, u, nullptr, w, p, nd);
+}
+
+int mps_add_particles3(mps_handle* h, int64_t n, const int32_t* type, const double* x,
+                       const double* y, const double* z, const double* u, const double* v,
+                       const double* w, const double* p, const double* nd) {
+    return add_particles_impl(h, 3, n, type, x, y, z, u, v, w, p, nd);
+}
+
 int64_t mps_particle_count(const mps_handle* h) { return h ? h->n : -1; }
 
 static int get_particles_impl(mps_handle* h, int32_t* type, double* x, double* z, double* u,
-                              double* w, double* p, double* nd, bool device) {
+                              double* w, double* p, double* nd, bool device, int dim = 2,
+                              double* y = nullptr, double* v = nullptr) {
     return guarded(h, [&] {
+        require_dim(h, dim);
         const int64_t n = h->n;
         const DeviceState& st = h->st;
+        if (dim == 3) {
+            download(h, y, st.y, sizeof(double) * n, device);
+            download(h, v, st.v, sizeof(double) * n, device);
+        }
         download(h, type, st.type, sizeof(int32_t) * n, device);
         download(h, x, st.x, sizeof(double) * n, device);
         download(h, z, st.z, sizeof(double) * n, device);
@@ -1145,10 +1321,16 @@ static int get_particles_impl(mps_handle* h, int32_t* type, double* x, double* z
 
 static int set_particles_impl(mps_handle* h, const int32_t* type, const double* x, const double* z,
                               const double* u, const double* w, const double* p, const double* nd,
-                              bool device) {
+                              bool device, int dim = 2, const double* y = nullptr,
+                              const double* v = nullptr) {
     return guarded(h, [&] {
+        require_dim(h, dim);
         const int64_t n = h->n;
         DeviceState& st = h->st;
+        if (dim == 3) {
+            upload(h, st.y, y, sizeof(double) * n, device);
+            upload(h, st.v, v, sizeof(double) * n, device);
+        }
         upload(h, st.type, type, sizeof(int32_t) * n, device);
         upload(h, st.x, x, sizeof(double) * n, device);
         upload(h, st.z, z, sizeof(double) * n, device);
@@ -1183,8 +1365,30 @@ int mps_set_particles_device(mps_handle* h, const int32_t* type, const double* x
     return set_particles_impl(h, type, x, z, u, w, p, nd, true);
 }
 
+int mps_get_particles3(mps_handle* h, int32_t* type, double* x, double* y, double* z, double* u,
+                       double* v, double* w, double* p, double* nd) {
+    return get_particles_impl(h, type, x, z, u, w, p, nd, false, 3, y, v);
+}
+
+int mps_set_particles3(mps_handle* h, const int32_t* type, const double* x, const double* y,
+                       const double* z, const double* u, const double* v, const double* w,
+                       const double* p, const double* nd) {
+    return set_particles_impl(h, type, x, z, u, w, p, nd, false, 3, y, v);
+}
+
+int mps_set_wall_positions3(mps_handle* h, const double* wx, const double* wy, const double* wz) {
+    return guarded(h, [&] {
+        require_dim(h, 3);
+        upload(h, h->st.wall_x, wx, sizeof(double) * h->n, false);
+        upload(h, h->st.wall_y, wy, sizeof(double) * h->n, false);
+        upload(h, h->st.wall_z, wz, sizeof(double) * h->n, false);
+        check(cudaStreamSynchronize(h->stream), "wall positions");
+    });
+}
+
 int mps_set_wall_positions(mps_handle* h, const double* wx, const double* wz) {
     return guarded(h, [&] {
+        require_dim(h, 2);
         upload(h, h->st.wall_x, wx, sizeof(double) * h->n, false);
         upload(h, h->st.wall_z, wz, sizeof(double) * h->n, false);
         check(cudaStreamSynchronize(h->stream), "wall positions");
@@ -1228,6 +1432,10 @@ int mps_get_environment(const mps_handle* h, mps_environment* env) {
     env->grid_nx = sc.gnx;
     env->grid_nz = sc.gnz;
     env->grid_max_per_cell = sc.max_per_cell;
+    env->min_y = sc.dim == 3 ? h->prm.min_y : 0.0;
+    env->max_y = sc.dim == 3 ? h->prm.max_y : 0.0;
+    env->grid_ny = sc.gny;
+    env->dim = sc.dim;
     return MPS_OK;
 }
 
@@ -1340,12 +1548,23 @@ void require_implicit(const mps_handle* h) {
         });                                                \
     }
 
+// each hook runs the 2D or the 3D kernel of its stage
 MPS_STAGE(mps_stage_search_neighbor, do_search(h); read_status(h, false))
-MPS_STAGE(mps_stage_density, launch_density(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_error_correction, launch_error_correction(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_explicit, launch_explicit(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_save_x, launch_save_x(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_set_ppe, require_implicit(h); launch_set_ppe(h->sc, h->st, wants_fp32(h), h->stream);
+MPS_STAGE(mps_stage_density,
+          if (is3(h)) launch_density3(h->sc, h->st, h->stream);
+          else launch_density(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_error_correction,
+          if (is3(h)) launch_error_correction3(h->sc, h->st, h->stream);
+          else launch_error_correction(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_explicit,
+          if (is3(h)) launch_explicit3(h->sc, h->st, h->stream);
+          else launch_explicit(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_save_x,
+          if (is3(h)) launch_save_x3(h->sc, h->st, h->stream);
+          else launch_save_x(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_set_ppe, require_implicit(h);
+          if (is3(h)) launch_set_ppe3(h->sc, h->st, wants_fp32(h), h->stream);
+          else launch_set_ppe(h->sc, h->st, wants_fp32(h), h->stream);
           h->ppe_fp32 = wants_fp32(h))
 MPS_STAGE(mps_stage_solve_ppe, require_implicit(h); do_solve(h); read_status(h, true))
 // the pressure of ComputeImplicitForces: from the PPE solution, or explicit
@@ -1354,8 +1573,12 @@ MPS_STAGE(mps_stage_assign_pressure,
               launch_explicit_pressure(h->sc, h->st, nullptr, h->stream);
           else
               launch_assign_pressure(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_pressure_gradient, launch_pressure_gradient(h->sc, h->st, h->stream))
-MPS_STAGE(mps_stage_dynamic_stabilize, launch_dynamic_stabilize(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_pressure_gradient,
+          if (is3(h)) launch_pressure_gradient3(h->sc, h->st, h->stream);
+          else launch_pressure_gradient(h->sc, h->st, h->stream))
+MPS_STAGE(mps_stage_dynamic_stabilize,
+          if (is3(h)) launch_dynamic_stabilize3(h->sc, h->st, h->stream);
+          else launch_dynamic_stabilize(h->sc, h->st, h->stream))
 
 #undef MPS_STAGE
 
@@ -1364,6 +1587,8 @@ int mps_stage_begin_step(mps_handle* h, double dt) {
         require_particles(h);
         if (dt > 0)
             launch_set_dt(h->sc, h->st, dt, h->stream);
+        else if (is3(h))
+            launch_cfl_dt3(h->sc, h->st, h->stream);
         else
             launch_cfl_dt(h->sc, h->st, h->stream);
         after_launch("begin step");
@@ -1377,7 +1602,10 @@ int mps_stage_density_variation(mps_handle* h, double* speed_host) {
     return guarded(h, [&] {
         require_particles(h);
         double* out = h->r;  // scratch vector of n doubles
-        launch_density_variation(h->sc, h->st, out, h->stream);
+        if (is3(h))
+            launch_density_variation3(h->sc, h->st, out, h->stream);
+        else
+            launch_density_variation(h->sc, h->st, out, h->stream);
         after_launch("density variation");
         download(h, speed_host, out, sizeof(double) * h->n, false);
         check(cudaStreamSynchronize(h->stream), "density variation");
@@ -1494,6 +1722,34 @@ int mps_debug_set_aux(mps_handle* h, const double* n_without_spp, const double* 
         upload(h, h->st.n_wo_spp, n_without_spp, b, false);
         upload(h, h->st.ecs, ecs, b, false);
         upload(h, h->st.ox, ox, b, false);
+        upload(h, h->st.oz, oz, b, false);
+        check(cudaStreamSynchronize(h->stream), "aux");
+    });
+}
+
+int mps_debug_get_aux3(mps_handle* h, double* n_without_spp, double* ecs, double* ox, double* oy,
+                       double* oz) {
+    return guarded(h, [&] {
+        require_dim(h, 3);
+        const size_t b = sizeof(double) * h->n;
+        download(h, n_without_spp, h->st.n_wo_spp, b, false);
+        download(h, ecs, h->st.ecs, b, false);
+        download(h, ox, h->st.ox, b, false);
+        download(h, oy, h->st.oy, b, false);
+        download(h, oz, h->st.oz, b, false);
+        check(cudaStreamSynchronize(h->stream), "aux");
+    });
+}
+
+int mps_debug_set_aux3(mps_handle* h, const double* n_without_spp, const double* ecs,
+                       const double* ox, const double* oy, const double* oz) {
+    return guarded(h, [&] {
+        require_dim(h, 3);
+        const size_t b = sizeof(double) * h->n;
+        upload(h, h->st.n_wo_spp, n_without_spp, b, false);
+        upload(h, h->st.ecs, ecs, b, false);
+        upload(h, h->st.ox, ox, b, false);
+        upload(h, h->st.oy, oy, b, false);
         upload(h, h->st.oz, oz, b, false);
         check(cudaStreamSynchronize(h->stream), "aux");
     });
@@ -1755,6 +2011,7 @@ int mps_mlp_train(int32_t device, float* blob, const float* samples, int64_t n, 
 int mps_batch_create(const mps_params* prm, int device, int32_t nscenes, const int64_t* counts,
                      mps_handle** out) {
     if (!prm || !out || nscenes <= 0 || !counts) return MPS_ERR_INVALID_ARGUMENT;
+    if (prm->dim == 3) return MPS_ERR_NOT_SUPPORTED;  // batches are two-dimensional
     for (int32_t k = 0; k < nscenes; k++)
         if (counts[k] <= 0) return MPS_ERR_INVALID_ARGUMENT;
     mps_handle* h = nullptr;

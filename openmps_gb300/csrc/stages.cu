@@ -863,6 +863,10 @@ void launch_cfl_dt(const SceneConst& sc, const DeviceState& st, cudaStream_t s) 
     k_cfl_dt<<<1, 32, 0, s>>>(sc, st);
 }
 
+void launch_cfl_dt_finish(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
+    k_cfl_dt<<<1, 32, 0, s>>>(sc, st);
+}
+
 void launch_density(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     k_density<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }

@@ -166,6 +166,89 @@ def lattice(nx: int, nz: int, l0: float, bounds, ptype: int = abi.TYPE_FLUID, u_
     return s
 
 
+# ------------------------------------------------------ three-dimensional scenes
+@dataclasses.dataclass
+class Scene3:
+    """A three-dimensional particle set (DIM3): positions (x, y, z), velocities (u, v, w)."""
+
+    name: str
+    type: np.ndarray
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+    w: np.ndarray
+    p: np.ndarray
+    n: np.ndarray
+    l0: float
+    bounds: tuple  # (min_x, min_y, min_z, max_x, max_y, max_z)
+    meta: dict = dataclasses.field(default_factory=dict)
+
+    @property
+    def count(self) -> int:
+        return int(self.type.shape[0])
+
+    def params(self, **kw) -> abi.MpsParams:
+        b = self.bounds
+        base = dict(l0=self.l0, min_x=b[0], min_y=b[1], min_z=b[2], max_x=b[3], max_y=b[4], max_z=b[5],
+                    dim=3)
+        base.update(self.meta.get("params", {}))
+        base.update(kw)
+        return abi.make_params(**base)
+
+    def arrays3(self):
+        return (self.type, self.x, self.y, self.z, self.u, self.v, self.w, self.p, self.n)
+
+    def copy(self) -> "Scene3":
+        return dataclasses.replace(self, **{k: getattr(self, k).copy() for k in
+                                            ("type", "x", "y", "z", "u", "v", "w", "p", "n")},
+                                   meta=dict(self.meta))
+
+
+def tank3d(l0: float, water: tuple, tank: tuple, wall_layers: int = 1, dummy_layers: int = 2,
+           jitter: float = 0.0, seed: int = 0, name: str = "tank3d") -> Scene3:
+    """Water block ``water = (nx, ny, nz)`` lattice points in the corner of an open box
+    ``tank = (nx, ny, nz)``: fluid at ``(i l0, j l0, k l0)``; boundary particles at every
+    lattice point within ``wall_layers + dummy_layers`` layers outside the interior (floor
+    and four side walls), layer = Chebyshev distance, the first ``wall_layers`` wall and
+    the rest dummy.  ``jitter`` (units of l0) moves the fluid by seeded U(-jitter, jitter)."""
+    layers = wall_layers + dummy_layers
+    wi, wj, wk = np.meshgrid(*(np.arange(m) for m in water), indexing="ij")
+    fx, fy, fz = (a.ravel() * l0 for a in (wi, wj, wk))
+    if jitter:
+        rnd = uniform01(seed, 3 * fx.size)
+        fx = fx + (2.0 * rnd[0::3] - 1.0) * jitter * l0
+        fy = fy + (2.0 * rnd[1::3] - 1.0) * jitter * l0
+        fz = fz + (2.0 * rnd[2::3] - 1.0) * jitter * l0
+    tx, ty, tz = tank
+    bi, bj, bk = (a.ravel() for a in np.meshgrid(np.arange(-layers, tx + layers), np.arange(-layers, ty + layers),
+                                                 np.arange(-layers, tz), indexing="ij"))
+    out = lambda a, m: np.where(a < 0, -a, np.where(a >= m, a - m + 1, 0))
+    layer = np.maximum(np.maximum(out(bi, tx), out(bj, ty)), np.where(bk < 0, -bk, 0))
+    keep = layer > 0
+    bi, bj, bk, layer = bi[keep], bj[keep], bk[keep], layer[keep]
+    btype = np.where(layer <= wall_layers, abi.TYPE_WALL, abi.TYPE_DUMMY)
+    t = np.concatenate([np.full(fx.size, abi.TYPE_FLUID), btype]).astype(np.int32)
+    x = np.concatenate([fx, bi * l0])
+    y = np.concatenate([fy, bj * l0])
+    z = np.concatenate([fz, bk * l0])
+    n = t.size
+    bounds = (-layers * l0, -layers * l0, -layers * l0, (tx + layers - 1) * l0, (ty + layers - 1) * l0, tz * l0)
+    return Scene3(name=name, type=t, x=x, y=y, z=z, u=np.zeros(n), v=np.zeros(n), w=np.zeros(n), p=np.zeros(n),
+                  n=np.zeros(n), l0=l0, bounds=bounds,
+                  meta={"water": tuple(water), "tank": tuple(tank), "wall_layers": wall_layers,
+                        "dummy_layers": dummy_layers, "jitter": jitter, "seed": seed})
+
+
+def dam_break3d(l0: float, water=(0.2, 0.1, 0.4), tank=(0.8, 0.1, 0.6), **kw) -> Scene3:
+    """3D dam break: a ``water`` (x, y, z in m) column in the corner of a ``tank`` box."""
+    r = lambda v: int(round(v / l0))
+    s = tank3d(l0, tuple(r(a) for a in water), tuple(r(a) for a in tank), name="dam_break3d", **kw)
+    s.meta.update(water_m=tuple(water), tank_m=tuple(tank))
+    return s
+
+
 # ----------------------------------------------------------------- workloads
 PLAIN_PHYSICS = dict(rho=1000.0, nu=1e-6, g=9.8, surface_ratio=0.97, re_by_l0=2.1,
                      re_lap_by_l0=4.0, courant=0.1, flags=abi.PRESET_PLAIN)

@@ -1,6 +1,7 @@
 """Build recipe of the CPU oracle (test infrastructure only).
 
-Compiles ``oracle/mps_oracle.cpp`` twice into ``oracle/_build/``:
+Compiles ``oracle/mps_oracle.cpp`` (2D) and ``oracle/mps_oracle3.cpp`` (3D) twice into
+``oracle/_build/``:
 
 * ``libmps_oracle.so``      serial, ``-O2 -ffp-contract=off``: the parity oracle;
 * ``libmps_oracle_omp.so``  ``-O3 -fopenmp -ffp-contract=off``: the timed CPU baseline.
@@ -18,7 +19,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
-SRC = os.path.join(HERE, "mps_oracle.cpp")
+SRCS = [os.path.join(HERE, "mps_oracle.cpp"), os.path.join(HERE, "mps_oracle3.cpp")]
 
 VARIANTS = {
     "libmps_oracle.so": ["-O2", "-ffp-contract=off"],
@@ -30,7 +31,7 @@ def _needs_build(out: str) -> bool:
     if not os.path.exists(out):
         return True
     mtime = os.path.getmtime(out)
-    deps = [SRC, os.path.join(HERE, "mps_oracle.h"), os.path.join(HERE, "..", "include", "mps.h")]
+    deps = [*SRCS, os.path.join(HERE, "mps_oracle.h"), os.path.join(HERE, "..", "include", "mps.h")]
     return any(os.path.getmtime(d) > mtime for d in deps)
 
 
@@ -39,7 +40,7 @@ def _compile(name: str, flags: list[str]) -> str:
     if not _needs_build(out):
         return out
     tmp = out + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-std=c++17", "-shared", "-fPIC", "-Wall", "-Wextra", *flags, SRC, "-o", tmp]
+    cmd = ["g++", "-std=c++17", "-shared", "-fPIC", "-Wall", "-Wextra", *flags, *SRCS, "-o", tmp]
     subprocess.run(cmd, check=True)
     os.replace(tmp, out)
     return out

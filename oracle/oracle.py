@@ -71,6 +71,28 @@ def load(openmp: bool = False) -> C.CDLL:
     lib.oracle_num_threads.restype = C.c_int
     lib.oracle_gc_invert.argtypes = [_D, C.c_double, _D]
     lib.oracle_gc_invert.restype = None
+    # three-dimensional oracle
+    lib.oracle3_create.argtypes = [C.POINTER(abi.MpsParams), C.POINTER(P)]
+    lib.oracle3_destroy.argtypes = [P]
+    lib.oracle3_destroy.restype = None
+    lib.oracle3_last_error.argtypes = [P]
+    lib.oracle3_last_error.restype = C.c_char_p
+    lib.oracle3_add_particles.argtypes = [P, C.c_int64, _I32] + [_D] * 8
+    lib.oracle3_particle_count.argtypes = [P]
+    lib.oracle3_particle_count.restype = C.c_int64
+    lib.oracle3_get_particles.argtypes = [P, _I32] + [_D] * 8
+    lib.oracle3_set_particles.argtypes = [P, _I32] + [_D] * 8
+    lib.oracle3_forward_time.argtypes = [P, C.c_double]
+    lib.oracle3_get_environment.argtypes = [P, C.POINTER(abi.MpsEnvironment)]
+    lib.oracle3_stage.argtypes = [P, C.c_int32, C.c_double]
+    lib.oracle3_density_variation.argtypes = [P, _D]
+    lib.oracle3_get_neighbors.argtypes = [P, _I32, _I32, C.c_int64, _I64]
+    lib.oracle3_get_ppe.argtypes = [P, _I64, _I32, _D, _D, _D, C.c_int64, _I64]
+    lib.oracle3_get_aux.argtypes = [P] + [_D] * 5
+    lib.oracle3_set_aux.argtypes = [P] + [_D] * 5
+    lib.oracle3_get_stats.argtypes = [P, _I32]
+    lib.oracle3_gc_invert.argtypes = [_D, C.c_double, _D]
+    lib.oracle3_gc_invert.restype = None
     _LIBS[name] = lib
     return lib
 
@@ -241,3 +263,126 @@ def gc_invert(m, val):
     out = np.zeros(4)
     load(False).oracle_gc_invert(_ptr(a), float(val), _ptr(out))
     return out
+
+
+def gc_invert3(m, val):
+    """Detail::InvertMatrix<3> of the row-major 3x3 matrix m (9 values)."""
+    a = np.ascontiguousarray(m, dtype=np.float64).reshape(9)
+    out = np.zeros(9)
+    load(False).oracle3_gc_invert(_ptr(a), float(val), _ptr(out))
+    return out
+
+
+class Oracle3:
+    """CPU restatement of the DIM3 build of ``Computer`` (one scene)."""
+
+    FIELDS = ("x", "y", "z", "u", "v", "w", "p", "n")
+    STAGES = {"search_neighbor": 1, "density": 2, "error_correction": 3, "explicit": 4, "save_x": 5,
+              "set_ppe": 6, "solve_ppe": 7, "assign_pressure": 8, "pressure_gradient": 9,
+              "dynamic_stabilize": 10}
+
+    def __init__(self, params: abi.MpsParams, openmp: bool = False):
+        self.lib = load(openmp)
+        self.params = params
+        h = C.c_void_p()
+        rc = self.lib.oracle3_create(C.byref(params), C.byref(h))
+        if rc:
+            raise OracleError(rc, "create")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.lib.oracle3_destroy(h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc:
+            raise OracleError(rc, self.lib.oracle3_last_error(self.h).decode())
+
+    def add_particles(self, t, x, y, z, u=None, v=None, w=None, p=None, n=None):
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.int32)
+        self._check(self.lib.oracle3_add_particles(self.h, len(t), _ptr(t, C.c_int32),
+                                                   *[_ptr(conv(a)) for a in (x, y, z, u, v, w, p, n)]))
+
+    def add_scene(self, scene):
+        self.add_particles(*scene.arrays3())
+
+    @property
+    def count(self) -> int:
+        return int(self.lib.oracle3_particle_count(self.h))
+
+    def particles(self) -> dict:
+        n = self.count
+        out = {k: np.empty(n) for k in self.FIELDS}
+        out["type"] = np.empty(n, dtype=np.int32)
+        self._check(self.lib.oracle3_get_particles(self.h, _ptr(out["type"], C.c_int32),
+                                                   *[_ptr(out[k]) for k in self.FIELDS]))
+        return out
+
+    def set_particles(self, t=None, x=None, y=None, z=None, u=None, v=None, w=None, p=None, n=None):
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        t = None if t is None else np.ascontiguousarray(t, dtype=np.int32)
+        self._check(self.lib.oracle3_set_particles(self.h, _ptr(t, C.c_int32),
+                                                   *[_ptr(conv(a)) for a in (x, y, z, u, v, w, p, n)]))
+
+    def forward_time(self, dt: float):
+        self._check(self.lib.oracle3_forward_time(self.h, dt))
+
+    def begin_step(self, dt: float):
+        self._check(self.lib.oracle3_stage(self.h, 0, dt))
+
+    def stage(self, name: str):
+        self._check(self.lib.oracle3_stage(self.h, self.STAGES[name], 0.0))
+
+    def environment(self) -> abi.MpsEnvironment:
+        env = abi.MpsEnvironment()
+        self._check(self.lib.oracle3_get_environment(self.h, C.byref(env)))
+        return env
+
+    def density_variation(self) -> np.ndarray:
+        out = np.zeros(self.count)
+        self._check(self.lib.oracle3_density_variation(self.h, _ptr(out)))
+        return out
+
+    def neighbors(self):
+        n = self.count
+        counts = np.zeros(n, dtype=np.int32)
+        total = C.c_int64()
+        self._check(self.lib.oracle3_get_neighbors(self.h, _ptr(counts, C.c_int32), None, 0, C.byref(total)))
+        lst = np.zeros(max(total.value, 1), dtype=np.int32)
+        self._check(self.lib.oracle3_get_neighbors(self.h, _ptr(counts, C.c_int32), _ptr(lst, C.c_int32),
+                                                   lst.size, C.byref(total)))
+        return counts, lst[: total.value]
+
+    def ppe(self):
+        n = self.count
+        nnz = C.c_int64()
+        rp = np.zeros(n + 1, dtype=np.int64)
+        self._check(self.lib.oracle3_get_ppe(self.h, _ptr(rp, C.c_int64), None, None, None, None, 0,
+                                             C.byref(nnz)))
+        col = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        val = np.zeros(max(nnz.value, 1))
+        b = np.zeros(n)
+        x = np.zeros(n)
+        self._check(self.lib.oracle3_get_ppe(self.h, _ptr(rp, C.c_int64), _ptr(col, C.c_int32), _ptr(val),
+                                             _ptr(b), _ptr(x), col.size, C.byref(nnz)))
+        return rp, col[: nnz.value], val[: nnz.value], b, x
+
+    def aux(self) -> dict:
+        n = self.count
+        out = {k: np.zeros(n) for k in ("n_without_spp", "ecs", "ox", "oy", "oz")}
+        self._check(self.lib.oracle3_get_aux(self.h, *[_ptr(out[k]) for k in
+                                                       ("n_without_spp", "ecs", "ox", "oy", "oz")]))
+        return out
+
+    def set_aux(self, n_without_spp=None, ecs=None, ox=None, oy=None, oz=None):
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        self._check(self.lib.oracle3_set_aux(self.h, *[_ptr(conv(a)) for a in
+                                                       (n_without_spp, ecs, ox, oy, oz)]))
+
+    def stats(self) -> dict:
+        it = C.c_int32()
+        self._check(self.lib.oracle3_get_stats(self.h, C.byref(it)))
+        return {"cg_iterations": it.value}
