@@ -501,6 +501,44 @@ def method_variants(comp, scene, dt, device, steps=3):
                      "pressure_ms": statistics.mean(pres_ms), "particle_steps_per_s": scene.count / (ms * 1e-3)}
     out["note"] = ("same snapshot, %d steps each, L2 flushed before each step; explicit: c = %g m/s, "
                    "dt = courant l0 / c" % (steps, VARIANT_SOUND_SPEED))
+    out["dim3"] = dim3_workload(device)
+    return out
+
+
+def dim3_workload(device, warmup=2, steps=3):
+    """A three-dimensional dam break (DIM3): a 0.1 x 0.2 x 0.2 m column in a 0.4 x 0.2 x 0.4 m
+    box at l0 = 5 mm, the reference's stock method set at r_e = 2.4 l0 (Sample.xml), dt =
+    2.5e-4 s, PPE to |b - Ax| <= 1e-8 |b| with the FP64 CG and the mixed-precision CG."""
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import scenes
+    from openmps_gb300.computer import Computer
+
+    scene = scenes.dam_break3d(5e-3, water=(0.1, 0.2, 0.2), tank=(0.4, 0.2, 0.4))
+    scene.meta["params"] = dict(scenes.STOCK_PHYSICS, re_by_l0=2.4, re_lap_by_l0=0.0, max_dt=1.0)
+    dt = 2.5e-4
+    out = {"workload": "3D dam break, %d fluid + %d wall/dummy particles, l0=5e-3 m, HS HL ECS DS SPP, "
+                       "re=2.4 l0, dt=%g s" % (int((scene.type == 0).sum()), int((scene.type != 0).sum()), dt),
+           "particles": scene.count}
+    for name, solver in (("cg64", abi.SOLVER_CG64), ("mixed", abi.SOLVER_MIXED)):
+        c = Computer(scene.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8), device=device)
+        c.add_particles3(*scene.arrays3())
+        for _ in range(warmup):
+            c.forward_time(dt)
+        c.set_stage_timing(True)
+        step_ms, ppe_ms, its = [], [], []
+        for _ in range(steps):
+            c.flush_l2(FLUSH_BYTES)
+            c.event_record(0)
+            c.forward_time(dt)
+            c.event_record(1)
+            step_ms.append(c.event_elapsed(0, 1))
+            st = c.stats()
+            ppe_ms.append(st["stage_ms"]["solve"])
+            its.append(st["cg_iterations"])
+        out[name] = {"step_ms": statistics.mean(step_ms), "ppe_ms": statistics.mean(ppe_ms),
+                     "iterations": statistics.mean(its), "ppe_nnz": c.stats()["ppe_nnz"],
+                     "particle_steps_per_s": scene.count / (statistics.mean(step_ms) * 1e-3)}
+        c.close()
     return out
 
 
