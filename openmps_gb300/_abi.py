@@ -36,7 +36,9 @@ FLAG_DS = 0x08
 FLAG_SPP = 0x10
 FLAG_GC = 0x20
 FLAG_PRESSURE_EXPLICIT = 0x40
-FLAGS_ALL = FLAG_HS | FLAG_HL | FLAG_ECS | FLAG_DS | FLAG_SPP | FLAG_GC | FLAG_PRESSURE_EXPLICIT
+FLAG_CENTRAL_GRAVITY = 0x80
+FLAGS_ALL = (FLAG_HS | FLAG_HL | FLAG_ECS | FLAG_DS | FLAG_SPP | FLAG_GC | FLAG_PRESSURE_EXPLICIT
+             | FLAG_CENTRAL_GRAVITY)
 PRESET_REFERENCE = FLAG_HS | FLAG_HL | FLAG_ECS | FLAG_DS | FLAG_SPP
 PRESET_PLAIN = 0
 

@@ -124,6 +124,7 @@ struct DeviceState {
     // the y axis of three-dimensional scenes (null in 2D): position, velocity, wall
     // target, SaveX copy and velocity change
     double *y, *v, *wall_y, *oy, *duy;
+    float* y32;  // FP32 copy of y (range prefilter), rewritten with y
 };
 
 // --------------------------------------------------------------- helpers
@@ -199,6 +200,28 @@ __device__ __forceinline__ int range_class(float xi, float zi, float si, float x
     return (lx * lx + lz * lz > out_thr) ? 0 : 2;
 }
 
+// The same for three coordinates.  Each axis's error bound above only grows with the
+// sum of absolute coordinates, so E = 2^-22 (sum of the six |coordinates|) + 1e-36
+// covers every axis; the bounds of r^2 take six FP32 roundings (6 u relative), still
+// inside the 2^-20 margin of the thresholds, and the FP64 r^2 of dist3 is within 2^-50.
+__device__ __forceinline__ bool surely_out3(float xi, float yi, float zi, float si, float xj, float yj,
+                                            float zj, float out_thr) {
+    const float e = range_slack(si + ((fabsf(xj) + fabsf(yj)) + fabsf(zj)));
+    const float lx = fmaxf(fabsf(xj - xi) - e, 0.0f);
+    const float ly = fmaxf(fabsf(yj - yi) - e, 0.0f);
+    const float lz = fmaxf(fabsf(zj - zi) - e, 0.0f);
+    return (lx * lx + ly * ly) + lz * lz > out_thr;
+}
+__device__ __forceinline__ int range_class3(float xi, float yi, float zi, float si, float xj, float yj,
+                                            float zj, float in_thr, float out_thr) {
+    const float e = range_slack(si + ((fabsf(xj) + fabsf(yj)) + fabsf(zj)));
+    const float ax = fabsf(xj - xi), ay = fabsf(yj - yi), az = fabsf(zj - zi);
+    const float hx = ax + e, hy = ay + e, hz = az + e;
+    if ((hx * hx + hy * hy) + hz * hz < in_thr) return 1;
+    const float lx = fmaxf(ax - e, 0.0f), ly = fmaxf(ay - e, 0.0f), lz = fmaxf(az - e, 0.0f);
+    return ((lx * lx + ly * ly) + lz * lz > out_thr) ? 0 : 2;
+}
+
 // Calls f(j) for the entries of row i that may pass the FP64 range test whose FP32
 // upper bound is `out_thr`, in list order.  Entries are screened 128 at a time into a
 // bit mask first (two 64-bit words: a whole row of the usual radii), so the FP64 work of
@@ -215,6 +238,37 @@ __device__ __forceinline__ void for_near(const SceneConst& sc, const DeviceState
         for (int t = 0; t < m; t++) {
             const int j = st.nb[static_cast<int64_t>(base + t) * sc.n + i];
             if (!surely_out(xi, zi, si, st.x32[j], st.z32[j], out_thr)) {
+                if (t < 64) lo |= 1ull << t;
+                else hi |= 1ull << (t - 64);
+            }
+        }
+        while (lo | hi) {
+            int t;
+            if (lo) {
+                t = __ffsll(static_cast<long long>(lo)) - 1;
+                lo &= lo - 1ull;
+            } else {
+                t = 63 + __ffsll(static_cast<long long>(hi));
+                hi &= hi - 1ull;
+            }
+            f(st.nb[static_cast<int64_t>(base + t) * sc.n + i]);
+        }
+    }
+}
+
+// for_near for three-dimensional scenes (surely_out3 on x32, y32, z32).
+template <class F>
+__device__ __forceinline__ void for_near3(const SceneConst& sc, const DeviceState& st, int i,
+                                          float out_thr, F f) {
+    const float xi = st.x32[i], yi = st.y32[i], zi = st.z32[i];
+    const float si = (fabsf(xi) + fabsf(yi)) + fabsf(zi);
+    const int cnt = st.nb_count[i];
+    for (int base = 0; base < cnt; base += 128) {
+        const int m = min(128, cnt - base);
+        unsigned long long lo = 0ull, hi = 0ull;
+        for (int t = 0; t < m; t++) {
+            const int j = st.nb[static_cast<int64_t>(base + t) * sc.n + i];
+            if (!surely_out3(xi, yi, zi, si, st.x32[j], st.y32[j], st.z32[j], out_thr)) {
                 if (t < 64) lo |= 1ull << t;
                 else hi |= 1ull << (t - 64);
             }

@@ -10,9 +10,11 @@
 // list order and the SPP particle last.  Vectors have three components, summed in the
 // reference's order (uBLAS inner_prod and prod run each sum from 0), and DIM = 3 enters
 // the coefficients as in the reference: nu (5 - DIM) r_e / n0 / r^3, 2 DIM / lambda / n0,
-// -dt / rho DIM / n0, DIM / n0 for the GC identity.  Every range test is the FP64 one
-// (no FP32 screen).  Compiled with -fmad=false: results are bit-identical to the FP64
-// CPU path.  The PPE rows are the particles in index order; the layout kernels, the
+// -dt / rho DIM / n0, DIM / n0 for the GC identity.  The range tests take the FP32
+// screen of the 2D kernels on three coordinates (range_class3 / for_near3: surely-in and
+// surely-out pairs settled in FP32, the rest by the reference's FP64 test, so every
+// decision is the FP64 one).  Compiled with -fmad=false: results are bit-identical to the
+// FP64 CPU path.  The PPE rows are the particles in index order; the layout kernels, the
 // pressure assignment, the explicit pressure and the solvers are the dimension-free
 // ones.
 #include "common.cuh"
@@ -35,9 +37,11 @@ __device__ __forceinline__ bool is_surface3(const SceneConst& sc, double nd) {
     return __ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
 }
 
-// Neighbour row k of particle i.
-__device__ __forceinline__ int nb_at(const SceneConst& sc, const DeviceState& st, int k, int i) {
-    return st.nb[ell(k, sc.n, i)];
+// FP32 copies of particle i's position (the range screen reads them).
+__device__ __forceinline__ void positions_f32(const DeviceState& st, int i) {
+    st.x32[i] = __double2float_rn(st.x[i]);
+    st.y32[i] = __double2float_rn(st.y[i]);
+    st.z32[i] = __double2float_rn(st.z[i]);
 }
 
 // ------------------------------------------------------------------ search
@@ -46,6 +50,9 @@ __device__ __forceinline__ int nb_at(const SceneConst& sc, const DeviceState& st
 __global__ void k3_bucket(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
+    st.x32[i] = __double2float_rn(st.x[i]);
+    st.y32[i] = __double2float_rn(st.y[i]);
+    st.z32[i] = __double2float_rn(st.z[i]);
     if (st.type[i] == MPS_TYPE_DISABLED) {
         atomicAdd(&st.status->disabled, 1);
         return;
@@ -77,6 +84,8 @@ __global__ void k3_neighbors(SceneConst sc, DeviceState st) {
     int cnt = 0;
     if (i < sc.n && st.type[i] != MPS_TYPE_DISABLED) {
         const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
+        const float xi32 = st.x32[i], yi32 = st.y32[i], zi32 = st.z32[i];
+        const float si32 = (fabsf(xi32) + fabsf(yi32)) + fabsf(zi32);
         const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
         const int by = static_cast<int>(floor(__ddiv_rn(__dadd_rn(yi, -sc.min_y), sc.nl)));
         const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
@@ -95,10 +104,17 @@ __global__ void k3_neighbors(SceneConst sc, DeviceState st) {
                     for (int l = 0; l < m; l++) {
                         const int j = slots[l];
                         if (j == i) continue;
-                        const double dx = __dadd_rn(xi, -st.x[j]);
-                        const double dy = __dadd_rn(yi, -st.y[j]);
-                        const double dz = __dadd_rn(zi, -st.z[j]);
-                        if (__dsqrt_rn(dist3(dx, dy, dz)) < sc.nl) {
+                        const int cls = range_class3(xi32, yi32, zi32, si32, st.x32[j], st.y32[j], st.z32[j],
+                                                     sc.f32_in_nl, sc.f32_out_nl);
+                        bool inside = cls == 1;
+                        if (cls == 2) {  // the FP64 test, the square root only near NL
+                            const double dx = __dadd_rn(xi, -st.x[j]);
+                            const double dy = __dadd_rn(yi, -st.y[j]);
+                            const double dz = __dadd_rn(zi, -st.z[j]);
+                            const double r2 = dist3(dx, dy, dz);
+                            inside = (r2 < sc.nl2_lo) ? true : (r2 > sc.nl2_hi) ? false : __dsqrt_rn(r2) < sc.nl;
+                        }
+                        if (inside) {
                             if (cnt < sc.nb_stride) {
                                 st.nb[ell(cnt, sc.n, i)] = j;
                             } else {
@@ -172,9 +188,7 @@ __device__ double density_variation3(const SceneConst& sc, const DeviceState& st
         const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
         const double ui = st.u[i], vi = st.v[i], wi = st.w[i];
         double sum = 0.0;
-        const int cnt = st.nb_count[i];
-        for (int k = 0; k < cnt; k++) {
-            const int j = nb_at(sc, st, k, i);
+            for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
             const double dx = st.x[j] - xi;
             const double dy = st.y[j] - yi;
             const double dz = st.z[j] - zi;
@@ -186,7 +200,7 @@ __device__ double density_variation3(const SceneConst& sc, const DeviceState& st
                 const double r = __dsqrt_rn(r2);
                 sum += dot3(dx, dy, dz, du, dv, dw) / (r * r * r);
             }
-        }
+        });
         return -sc.re * sum;
     }
     return (st.nd[i] - sc.n0) / dt;
@@ -214,12 +228,10 @@ __global__ void k3_density(SceneConst sc, DeviceState st) {
     if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) return;
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     double thisN = 0.0;
-    const int cnt = st.nb_count[i];
-    for (int k = 0; k < cnt; k++) {
-        const int j = nb_at(sc, st, k, i);
+    for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
         const double r2 = dist3(st.x[j] - xi, st.y[j] - yi, st.z[j] - zi);
         if (below(r2, sc.re2)) thisN += weight(__dsqrt_rn(r2), sc.re);
-    }
+    });
     if (spp) {
         st.n_wo_spp[i] = thisN;
         st.nd[i] = (thisN < sc.n0) ? sc.n0 : thisN;
@@ -258,14 +270,12 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     const double ui = st.u[i], vi = st.v[i], wi = st.w[i];
     double ax = 0.0, ay = 0.0, az = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-    const int cnt = st.nb_count[i];
-    for (int k = 0; k < cnt; k++) {
-        const int j = nb_at(sc, st, k, i);
+    for_near3(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
         const double dz = st.z[j] - zi;
         const double r2 = dist3(dx, dy, dz);
-        if (!below(r2, sc.rl2)) continue;
+        if (!below(r2, sc.rl2)) return;
         if (st.type[j] != MPS_TYPE_DUMMY) {
             const double c = viscosity_coefficient3(sc, lf, __dsqrt_rn(r2));
             ax += c * (st.u[j] - ui);
@@ -282,7 +292,7 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
             gy += wg * dy;
             gz += wg * dz;
         }
-    }
+    });
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re_lap, gx, gy, gz, xs, ys, zs)) {
         const double ddx = xi - xs, ddy = yi - ys, ddz = zi - zs;
@@ -291,9 +301,23 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
         ay += c * (vi - vi);
         az += c * (wi - wi);
     }
-    st.dux[i] = __dadd_rn(ax, 0.0);
-    st.duy[i] = __dadd_rn(ay, 0.0);
-    st.duz[i] = az + (-sc.g);
+    if (has_flag(sc.flags, MPS_FLAG_CENTRAL_GRAVITY)) {  // Computer.hpp:981-988
+        const double g = -sc.g;
+        const double r = __dsqrt_rn(dot3(xi, yi, zi, xi, yi, zi));
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        if (!(r < sc.l0 * 0.01)) {
+            cx = xi / r;
+            cy = yi / r;
+            cz = zi / r;
+        }
+        st.dux[i] = ax + g * cx;
+        st.duy[i] = ay + g * cy;
+        st.duz[i] = az + g * cz;
+    } else {
+        st.dux[i] = __dadd_rn(ax, 0.0);
+        st.duy[i] = __dadd_rn(ay, 0.0);
+        st.duz[i] = az + (-sc.g);
+    }
 }
 
 // ComputeExplicitForces, second loop (Computer.hpp:995-1020).
@@ -321,6 +345,7 @@ __global__ void k3_explicit_update(SceneConst sc, DeviceState st) {
         st.y[i] = ny;
         st.z[i] = nz;
     }
+    positions_f32(st, i);
 }
 
 // SaveX (Computer.hpp:1025-1039)
@@ -365,14 +390,12 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     double a_ii = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
     int m = 0;
-    const int cnt = st.nb_count[i];
-    for (int k = 0; k < cnt; k++) {
-        const int j = nb_at(sc, st, k, i);
+    for_near3(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
         const double dz = st.z[j] - zi;
         const double r2 = dist3(dx, dy, dz);
-        if (!below(r2, sc.rl2)) continue;
+        if (!below(r2, sc.rl2)) return;
         if (st.type[j] != MPS_TYPE_DUMMY) {
             const double a_ij = ppe_coefficient3(sc, lf, __dsqrt_rn(r2));
             if (spp || !is_surface3(sc, st.nd[j])) {
@@ -390,7 +413,7 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
             gy += wg * dy;
             gz += wg * dz;
         }
-    }
+    });
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re_lap, gx, gy, gz, xs, ys, zs)) {
         const double ddx = xi - xs, ddy = yi - ys, ddz = zi - zs;
@@ -446,18 +469,16 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
     if (st.type[i] != MPS_TYPE_FLUID) return;
     const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i], pi = st.p[i];
-    const int cnt = st.nb_count[i];
     double gx = 0.0, gy = 0.0, gz = 0.0;
     double C[9];
     if (kGc) {
         double m00 = 0.0, m01 = 0.0, m02 = 0.0, m11 = 0.0, m12 = 0.0, m22 = 0.0;
-        for (int k = 0; k < cnt; k++) {
-            const int j = nb_at(sc, st, k, i);
+        for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
             const double dx = st.x[j] - xi;
             const double dy = st.y[j] - yi;
             const double dz = st.z[j] - zi;
             const double r2 = dist3(dx, dy, dz);
-            if (!below(r2, sc.re2)) continue;
+            if (!below(r2, sc.re2)) return;
             const double wg = weight(__dsqrt_rn(r2), sc.re);
             const double t = wg / r2;
             m00 += t * (dx * dx);
@@ -471,7 +492,7 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
                 gy += wg * dy;
                 gz += wg * dz;
             }
-        }
+        });
         double xs, ys, zs;
         if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
             const double dx = xs - xi, dy = ys - yi, dz = zs - zi;
@@ -489,13 +510,12 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
         gx = gy = gz = 0.0;
     }
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int k = 0; k < cnt; k++) {
-        const int j = nb_at(sc, st, k, i);
+    for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
         const double dz = st.z[j] - zi;
         const double r2 = dist3(dx, dy, dz);
-        if (!below(r2, sc.re2)) continue;
+        if (!below(r2, sc.re2)) return;
         const double wg = weight(__dsqrt_rn(r2), sc.re);
         if (st.type[j] != MPS_TYPE_DUMMY) {
             const double c = (st.p[j] + pi) / r2 * wg;
@@ -518,7 +538,7 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
             gy += wg * dy;
             gz += wg * dz;
         }
-    }
+    });
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
         const double dx = xs - xi, dy = ys - yi, dz = zs - zi;
@@ -555,14 +575,12 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     const double oxi = st.ox[i], oyi = st.oy[i], ozi = st.oz[i];
     double sx = 0.0, sy = 0.0, sz = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-    const int cnt = st.nb_count[i];
-    for (int k = 0; k < cnt; k++) {
-        const int j = nb_at(sc, st, k, i);
+    for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
         const double dz = st.z[j] - zi;
         const double r2 = dist3(dx, dy, dz);
-        if (!below(r2, sc.re2)) continue;
+        if (!below(r2, sc.re2)) return;
         if (st.type[j] != MPS_TYPE_DUMMY && below(r2, d2)) {
             const double dx0 = st.ox[j] - oxi;
             const double dy0 = st.oy[j] - oyi;
@@ -589,7 +607,7 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
             gy += wg * dy;
             gz += wg * dz;
         }
-    }
+    });
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
         sx = __dadd_rn(sx, 0.0);  // the SPP particle is excluded (Computer.hpp:1597-1598)
@@ -615,6 +633,7 @@ __global__ void k3_apply_du(SceneConst sc, DeviceState st) {
     st.x[i] = st.x[i] + dx * dt;
     st.y[i] = st.y[i] + dy * dt;
     st.z[i] = st.z[i] + dz * dt;
+    positions_f32(st, i);
 }
 
 }  // namespace

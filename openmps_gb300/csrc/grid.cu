@@ -183,13 +183,14 @@ __global__ void k_status_counters_reset(DevStatus* st) {
 void launch_status_counters_reset(DevStatus* st, cudaStream_t s) { k_status_counters_reset<<<1, 32, 0, s>>>(st); }
 
 // FP32 copies of the positions of particles [first, first + count) after a host write of
-// x, z.
+// x, z (and y in 3D).
 __global__ void k_positions_f32(DeviceState st, int first, int count) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     const int i = first + k;
     st.x32[i] = __double2float_rn(st.x[i]);
     st.z32[i] = __double2float_rn(st.z[i]);
+    if (st.y32) st.y32[i] = __double2float_rn(st.y[i]);
 }
 
 void launch_positions_f32(const SceneConst& sc, const DeviceState& st, cudaStream_t s, int first, int count) {

@@ -397,6 +397,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.cell_xz = dalloc<int32_t>(h, n);
     st.x32 = dalloc<float>(h, n);
     st.z32 = dalloc<float>(h, n);
+    st.y32 = d3 ? dalloc<float>(h, n) : nullptr;
     st.w_re = dalloc<double>(h, n * kReCache);
     st.row_of = st.particle_of = st.row_cell = st.cell_fill = st.cell_start = nullptr;
     st.unplaced = st.unplaced_pos = st.row_scratch = nullptr;

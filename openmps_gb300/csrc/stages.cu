@@ -43,6 +43,26 @@ __device__ __forceinline__ bool spp_particle(const SceneConst& sc, const DeviceS
     return false;
 }
 
+// a = viscosity + G (Computer.hpp:980-988): G = (0, -g), or with MPS_FLAG_CENTRAL_GRAVITY
+// G_z c with c = x / |x|, c = 0 within l0 / 100 of the origin.
+__device__ __forceinline__ void add_gravity(const SceneConst& sc, double xi, double zi, double vx, double vz,
+                                            double& ax, double& az) {
+    if (has_flag(sc.flags, MPS_FLAG_CENTRAL_GRAVITY)) {
+        const double g = -sc.g;
+        const double r = __dsqrt_rn(dot2(xi, zi, xi, zi));
+        double cx = 0.0, cz = 0.0;
+        if (!(r < sc.l0 * 0.01)) {
+            cx = xi / r;
+            cz = zi / r;
+        }
+        ax = vx + g * cx;
+        az = vz + g * cz;
+    } else {
+        ax = __dadd_rn(vx, 0.0);
+        az = vz + (-sc.g);
+    }
+}
+
 // NeighborDensityVariationSpeed (Computer.hpp:838-872)
 __device__ double density_variation(const SceneConst& sc, const DeviceState& st, int i,
                                     double dt) {
@@ -263,8 +283,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
-    st.dux[i] = __dadd_rn(vx, 0.0);  // a += G, G = (0, -g) (Environment.hpp:149)
-    st.duz[i] = vz + (-sc.g);
+    add_gravity(sc, xi, zi, vx, vz, st.dux[i], st.duz[i]);  // a += G (Environment.hpp:149)
 }
 
 // The stages between the search and the move in one walk over each neighbour row:
@@ -351,8 +370,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
-    st.dux[i] = __dadd_rn(vx, 0.0);
-    st.duz[i] = vz + (-sc.g);
+    add_gravity(sc, xi, zi, vx, vz, st.dux[i], st.duz[i]);
 }
 
 // ComputeExplicitForces, second loop (Computer.hpp:995-1020).

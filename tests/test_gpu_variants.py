@@ -260,3 +260,71 @@ def test_explicit_batch_matches_oracle(gpu_lib, oracle_lib):
         P, Q = b.scene(k), o.particles()
         for f in ("type", "x", "z", "u", "w", "p", "n"):
             np.testing.assert_array_equal(P[f], Q[f], err_msg="scene %d %s" % (k, f))
+
+
+# ------------------------------------------------------------- central gravity
+def _central(scene, dx, dz):
+    """The scene moved by (dx, dz) around the origin, with the fluid particle nearest to it
+    placed exactly at the origin (the c = 0 branch)."""
+    s = scene
+    s.x = s.x + dx
+    s.z = s.z + dz
+    s.min_x += dx
+    s.max_x += dx
+    s.min_z += dz
+    s.max_z += dz
+    fluid = np.flatnonzero(s.type == abi.TYPE_FLUID)
+    k = fluid[np.argmin(s.x[fluid] ** 2 + s.z[fluid] ** 2)]
+    s.x[k] = 0.0
+    s.z[k] = 0.0
+    s = _explicit(_with_flags(s, abi.FLAG_CENTRAL_GRAVITY))
+    return s
+
+
+def test_central_gravity_2d(gpu_lib, oracle_lib):
+    # CENTRAL_GRAVITY (Computer.hpp:925-932, :981-988) through the step's fused walk and
+    # through the stage hooks, both bit-identical to the oracle
+    s = _central(stock_tank(), -0.1, -0.2)
+    gpu, cpu = make_pair(s, s.params())
+    hooks, _ = make_pair(s, s.params())
+    for _ in range(6):
+        gpu.forward_time(s.meta["dt"])
+        cpu.forward_time(s.meta["dt"])
+        hooks.begin_step(s.meta["dt"])
+        for name in ("search_neighbor", "density", "error_correction", "explicit", "density", "save_x",
+                     "assign_pressure", "pressure_gradient", "dynamic_stabilize"):
+            hooks.stage(name)
+    _assert_bitwise(gpu, cpu, "central gravity")
+    assert_same_particles(hooks, cpu, what="central gravity, stage hooks")
+    # gravity points to the origin: the fluid above it moves down, the fluid below it up
+    P = gpu.particles()
+    f = P["type"] == abi.TYPE_FLUID
+    assert np.mean(P["w"][f & (P["z"] > 0.05)]) < 0 < np.mean(P["w"][f & (P["z"] < -0.05)])
+
+
+def test_central_gravity_3d(gpu_lib, oracle_lib):
+    from openmps_gb300.computer import Computer
+    from oracle.oracle import Oracle3
+
+    s = scenes.tank3d(0.01, (6, 5, 8), (14, 8, 12))
+    off = (-0.03, -0.02, -0.04)
+    s.x, s.y, s.z = s.x + off[0], s.y + off[1], s.z + off[2]
+    b = s.bounds
+    s.bounds = (b[0] + off[0], b[1] + off[1], b[2] + off[2], b[3] + off[0], b[4] + off[1], b[5] + off[2])
+    fluid = np.flatnonzero(s.type == abi.TYPE_FLUID)
+    k = fluid[np.argmin(s.x[fluid] ** 2 + s.y[fluid] ** 2 + s.z[fluid] ** 2)]
+    s.x[k] = s.y[k] = s.z[k] = 0.0
+    s.meta["params"] = dict(scenes.STOCK_PHYSICS, re_lap_by_l0=0.0, max_dt=1.0, sound_speed=SOUND_SPEED,
+                            flags=abi.PRESET_REFERENCE | abi.FLAG_PRESSURE_EXPLICIT | abi.FLAG_CENTRAL_GRAVITY)
+    prm = s.params()
+    gpu = Computer(prm)
+    gpu.add_particles3(*s.arrays3())
+    cpu = Oracle3(prm)
+    cpu.add_scene(s)
+    dt = 0.1 * s.l0 / SOUND_SPEED
+    for _ in range(6):
+        gpu.forward_time(dt)
+        cpu.forward_time(dt)
+    G, C = gpu.particles3(), cpu.particles()
+    for f in ("type", "x", "y", "z", "u", "v", "w", "p", "n"):
+        np.testing.assert_array_equal(G[f], C[f], err_msg=f)
