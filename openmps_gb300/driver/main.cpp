@@ -14,6 +14,8 @@
 //   * a Computer::Exception prints "!!!!ERROR!!!!" and stops the run (Main.cpp:380-388).
 // With MPS_FLAG_PRESSURE_EXPLICIT among the flags, <environment> holds the sound speed c
 // and <condition> needs no eps, as in the reference built with PRESSURE_EXPLICIT.
+// A DIM3 input (minY and maxY in <environment>) runs a three-dimensional scene: its CSV
+// holds Type, x, y, z, u, v, w, p, n.
 // Extensions (optional elements of <environment>): r_lapByl_0 (Laplacian radius),
 // flags (method bit set, default the reference's stock set) and solver (cg64, mixed,
 // mg, learned; default cg64 like the reference), weights (network file for "learned",
@@ -92,8 +94,14 @@ std::vector<std::string> items(std::string line) {
     return out;
 }
 
-std::vector<openmps_gb300::Particle> read_csv(const std::string& csv) {
-    using openmps_gb300::Particle;
+// Particle columns of the CSV (y and v only in 3D).
+struct Columns {
+    std::vector<int32_t> type;
+    std::vector<double> x, y, z, u, v, w, p, n;
+};
+
+// The header items Type, x, z, u, w, p, n (with y, v in 3D) in any order (Main.cpp:63-170).
+Columns read_csv(const std::string& csv, int dim) {
     std::stringstream ss(csv);
     std::string line;
     std::vector<std::string> header;
@@ -102,6 +110,7 @@ std::vector<openmps_gb300::Particle> read_csv(const std::string& csv) {
         if (!header.empty()) break;
     }
     std::map<std::string, int> col = {{"Type", -1}, {"x", -1}, {"z", -1}, {"u", -1}, {"w", -1}, {"p", -1}, {"n", -1}};
+    if (dim == 3) col.insert({{"y", -1}, {"v", -1}});
     for (size_t i = 0; i < header.size(); i++) {
         auto f = col.find(header[i]);
         if (f == col.end()) throw std::runtime_error("Illegal header item in input csv");
@@ -109,33 +118,65 @@ std::vector<openmps_gb300::Particle> read_csv(const std::string& csv) {
     }
     for (const auto& c : col)
         if (c.second < 0) throw std::runtime_error("Some header item doesn't exist");
-    std::vector<Particle> out;
+    Columns out;
     while (std::getline(ss, line)) {
         const auto d = items(line);
         if (d.empty()) continue;
-        Particle q(static_cast<Particle::Type>(std::stoi(d.at(col["Type"]))));
-        q.X()(0) = std::stod(d.at(col["x"]));
-        q.X()(1) = std::stod(d.at(col["z"]));
-        q.U()(0) = std::stod(d.at(col["u"]));
-        q.U()(1) = std::stod(d.at(col["w"]));
-        q.P() = std::stod(d.at(col["p"]));
-        q.N() = std::stod(d.at(col["n"]));
-        out.push_back(q);
+        out.type.push_back(static_cast<int32_t>(std::stoi(d.at(col["Type"]))));
+        out.x.push_back(std::stod(d.at(col["x"])));
+        out.z.push_back(std::stod(d.at(col["z"])));
+        out.u.push_back(std::stod(d.at(col["u"])));
+        out.w.push_back(std::stod(d.at(col["w"])));
+        out.p.push_back(std::stod(d.at(col["p"])));
+        out.n.push_back(std::stod(d.at(col["n"])));
+        if (dim == 3) {
+            out.y.push_back(std::stod(d.at(col["y"])));
+            out.v.push_back(std::stod(d.at(col["v"])));
+        }
     }
-    std::cout << out.size() << " particles" << std::endl;
+    std::cout << out.type.size() << " particles" << std::endl;
     return out;
 }
 
-size_t write_csv(openmps_gb300::Computer& c, size_t count) {
+void check_status(mps_handle* h, int rc) {
+    if (rc != MPS_OK) throw openmps_gb300::Computer::Exception(rc, mps_last_error(h));
+}
+
+void add_columns(mps_handle* h, const Columns& c, int dim) {
+    const int64_t n = static_cast<int64_t>(c.type.size());
+    if (dim == 3)
+        check_status(h, mps_add_particles3(h, n, c.type.data(), c.x.data(), c.y.data(), c.z.data(), c.u.data(),
+                                           c.v.data(), c.w.data(), c.p.data(), c.n.data()));
+    else
+        check_status(h, mps_add_particles(h, n, c.type.data(), c.x.data(), c.z.data(), c.u.data(), c.w.data(),
+                                          c.p.data(), c.n.data()));
+}
+
+// result/particles_%05d.csv with the reference's header and default ostream formatting
+// (Main.cpp:30-61); returns the particles that are not disabled.
+size_t write_csv(mps_handle* h, int dim, size_t count) {
+    const int64_t n = mps_particle_count(h);
+    Columns c;
+    c.type.resize(static_cast<size_t>(n));
+    for (auto* a : {&c.x, &c.y, &c.z, &c.u, &c.v, &c.w, &c.p, &c.n}) a->resize(static_cast<size_t>(n));
+    if (dim == 3)
+        check_status(h, mps_get_particles3(h, c.type.data(), c.x.data(), c.y.data(), c.z.data(), c.u.data(),
+                                           c.v.data(), c.w.data(), c.p.data(), c.n.data()));
+    else
+        check_status(h, mps_get_particles(h, c.type.data(), c.x.data(), c.z.data(), c.u.data(), c.w.data(),
+                                          c.p.data(), c.n.data()));
     char name[64];
     std::snprintf(name, sizeof(name), "result/particles_%05zu.csv", count);
     std::ofstream out(name);
-    out << "Type, x, z, u, w, p, n" << std::endl;
+    out << (dim == 3 ? "Type, x, y, z, u, v, w, p, n" : "Type, x, z, u, w, p, n") << std::endl;
     size_t alive = 0;
-    for (const auto& q : c.Particles()) {
-        out << static_cast<int>(q.TYPE()) << ", " << q.X()[0] << ", " << q.X()[1] << ", " << q.U()[0] << ", "
-            << q.U()[1] << ", " << q.P() << ", " << q.N() << std::endl;
-        if (q.TYPE() != openmps_gb300::Particle::Type::Disabled) alive++;
+    for (size_t i = 0; i < static_cast<size_t>(n); i++) {
+        out << c.type[i] << ", " << c.x[i] << ", ";
+        if (dim == 3) out << c.y[i] << ", ";
+        out << c.z[i] << ", " << c.u[i] << ", ";
+        if (dim == 3) out << c.v[i] << ", ";
+        out << c.w[i] << ", " << c.p[i] << ", " << c.n[i] << std::endl;
+        if (c.type[i] != MPS_TYPE_DISABLED) alive++;
     }
     return alive;
 }
@@ -193,18 +234,27 @@ int run(int argc, char** argv) {
                                    flags);
     env.LaplacianRadius(xml.num_or("environment", "r_lapByl_0", 0.0));
     if (explicit_pressure) env.SoundSpeed(xml.num("environment", "c"));
+    // DIM3 inputs hold minY and maxY (Main.cpp:224-232)
+    std::string probe;
+    const int dim = static_cast<int>(xml.num_or("environment", "dim", xml.attr("environment", "minY", &probe) ? 3 : 2));
+    if (dim == 3) {
+        env.params.dim = 3;
+        env.params.min_y = xml.num("environment", "minY");
+        env.params.max_y = xml.num("environment", "maxY");
+    }
     std::string solver = "cg64", weights;
     xml.attr("environment", "solver", &solver);
     xml.attr("environment", "weights", &weights);
     env.Solver(solver_code(solver));
-    auto particles = read_csv(xml.particles_csv());
+    const Columns particles = read_csv(xml.particles_csv(), dim);
     if (parse_only) {
         const mps_params& p = env.params;
         std::printf("maxDt=%.17g courant=%.17g g=%.17g rho=%.17g nu=%.17g surfaceRatio=%.17g r_eByl_0=%.17g "
                     "l_0=%.17g min=(%.17g,%.17g) max=(%.17g,%.17g) flags=%u solver=%d eps=%.17g "
-                    "start=%.17g end=%.17g interval=%.17g c=%.17g\n",
+                    "start=%.17g end=%.17g interval=%.17g c=%.17g dim=%d minY=%.17g maxY=%.17g\n",
                     p.max_dt, p.courant, p.g, p.rho, p.nu, p.surface_ratio, p.re_by_l0, p.l0, p.min_x, p.min_z,
-                    p.max_x, p.max_z, p.flags, p.solver, eps, start, end, interval, p.sound_speed);
+                    p.max_x, p.max_z, p.flags, p.solver, eps, start, end, interval, p.sound_speed, dim, p.min_y,
+                    p.max_y);
         return 0;
     }
     mkdir("result", 0755);
@@ -218,9 +268,9 @@ int run(int argc, char** argv) {
             if (mps_learned_set_weights(computer.Handle(), blob.data(), MPS_MLP_BLOB_FLOATS) != MPS_OK)
                 throw std::runtime_error(mps_last_error(computer.Handle()));
         }
-        computer.AddParticles(std::move(particles));
+        add_columns(computer.Handle(), particles, dim);
         const size_t offset = static_cast<size_t>(std::ceil(start / interval));
-        size_t alive = write_csv(computer, offset);
+        size_t alive = write_csv(computer.Handle(), dim, offset);
         std::printf("#%05zu: t=%8.4f (%05d), %12zu particles\n", offset, start, 0, alive);
         double next = 0.0;
         size_t iteration = 0;
@@ -234,7 +284,7 @@ int run(int argc, char** argv) {
                     t = computer.GetEnvironment().t;
                     iteration++;
                 }
-                alive = write_csv(computer, out + offset);
+                alive = write_csv(computer.Handle(), dim, out + offset);
                 std::printf("#%05zu: t=%8.4f (%05zu), %12zu particles\n", out + offset, t + start, iteration, alive);
             } catch (const openmps_gb300::Computer::Exception& ex) {
                 std::cout << "!!!!ERROR!!!!" << std::endl

@@ -127,3 +127,74 @@ def test_run_matches_python_binding(driver, tmp_path):
         # the driver prints six significant digits (default ostream formatting): up to half
         # a unit of the sixth digit, 5e-6 relative
         np.testing.assert_allclose(got, ref, rtol=5.01e-6, atol=1e-12)
+
+
+def write_case3(path, scene, end=0.004, interval=0.002, eps=1e-10, steps_per_output=4):
+    """A DIM3 input: minY/maxY in <environment>, the CSV with y and v (Main.cpp:38-50, :104-164)."""
+    P = dict(scene.meta["params"])
+    b = scene.bounds
+    rows = ["Type, x, y, z, u, v, w, p, n"]
+    for k in range(scene.count):
+        rows.append("%d, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g, %.17g" % (
+            scene.type[k], scene.x[k], scene.y[k], scene.z[k], scene.u[k], scene.v[k], scene.w[k], scene.p[k],
+            scene.n[k]))
+    env = "\n".join('    <%s value="%r" />' % (k, v) for k, v in (
+        ("l_0", scene.l0), ("minStepCountPerOutput", steps_per_output), ("courant", P["courant"]),
+        ("g", P["g"]), ("rho", P["rho"]), ("nu", P["nu"]), ("r_eByl_0", P["re_by_l0"]),
+        ("surfaceRatio", P["surface_ratio"]), ("minX", b[0]), ("minY", b[1]), ("minZ", b[2]), ("maxX", b[3]),
+        ("maxY", b[4]), ("maxZ", b[5]), ("flags", P["flags"])))
+    xml = ('<?xml version="1.0" encoding="utf-8"?>\n<openmps>\n  <condition>\n'
+           '    <startTime value="0" />\n    <endTime value="%r" />\n    <outputInterval value="%r" />\n'
+           '    <eps value="%r" />\n  </condition>\n  <environment>\n%s\n  </environment>\n'
+           '  <particles type="csv">\n%s\n  </particles>\n</openmps>\n' % (end, interval, eps, env, "\n".join(rows)))
+    with open(path, "w") as f:
+        f.write(xml)
+
+
+def _scene3():
+    s = scenes.tank3d(0.01, (5, 4, 6), (10, 6, 9))
+    s.meta["params"] = dict(scenes.STOCK_PHYSICS, re_by_l0=2.1, re_lap_by_l0=0.0)
+    return s
+
+
+def test_parse_only_3d(driver, tmp_path):
+    s = _scene3()
+    xml = tmp_path / "case3.xml"
+    write_case3(xml, s)
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode == 0, out.stderr
+    assert "%d particles" % s.count in out.stdout
+    kv = dict(item.split("=", 1) for item in out.stdout.strip().splitlines()[-1].split()
+              if "=" in item and not item.startswith(("min=", "max=")))
+    assert int(kv["dim"]) == 3
+    assert float(kv["minY"]) == s.bounds[1] and float(kv["maxY"]) == s.bounds[4]
+    # a 2D header in a DIM3 input misses y and v
+    text = xml.read_text().replace("Type, x, y, z, u, v, w, p, n", "Type, x, z, u, w, p, n")
+    xml.write_text(text)
+    out = subprocess.run([driver, str(xml), "--parse-only"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode != 0
+
+
+@pytest.mark.gpu
+def test_run_3d_matches_python_binding(driver, tmp_path):
+    from openmps_gb300.computer import Computer
+
+    s = _scene3()
+    xml = tmp_path / "case3.xml"
+    write_case3(xml, s, end=0.004, interval=0.002, steps_per_output=4)
+    out = subprocess.run([driver, str(xml)], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert out.returncode == 0, out.stdout + out.stderr
+    c = Computer(s.params(eps=1e-10, max_dt=0.002 / 4))
+    c.add_particles3(*s.arrays3())
+    nxt = 0.0
+    for k in (1, 2):
+        nxt += 0.002
+        while c.environment().t < nxt:
+            c.forward_time()
+        path = tmp_path / "result" / ("particles_%05d.csv" % k)
+        with open(path) as f:
+            assert f.readline().strip() == "Type, x, y, z, u, v, w, p, n"
+        got = np.loadtxt(path, delimiter=",", skiprows=1)
+        P = c.particles3()
+        ref = np.stack([P[f] for f in ("type", "x", "y", "z", "u", "v", "w", "p", "n")], axis=1)
+        np.testing.assert_allclose(got, ref, rtol=5.01e-6, atol=1e-12)
