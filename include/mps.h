@@ -64,13 +64,17 @@ extern "C" {
  * positive, from the second number density (Computer.hpp:1046-1067), and MaxDt =
  * min(maxDt, courant l0 / c) (Environment.hpp:131-135).  Needs mps_params.sound_speed. */
 #define MPS_FLAG_PRESSURE_EXPLICIT 0x40u
+/* CENTRAL_GRAVITY (a switch of Computer.hpp that defines.hpp does not list): gravity
+ * points to the origin, a += G_z x / |x|, and vanishes within l0 / 100 of it
+ * (Computer.hpp:925-932, :981-988). */
+#define MPS_FLAG_CENTRAL_GRAVITY 0x80u
 /* PRESSURE_GRADIENT_MIDPOINT (defines.hpp:21) is always on: the other branch does
  * not compile in the reference (Computer.hpp:1522-1537).  ARTIFICIAL_COLLISION_FORCE
  * (defines.hpp:16) has no flag: its stage calls a Particle member that does not exist
  * (Computer.hpp:1104-1134), so no build of the reference can enable it. */
 /* Every method flag. */
 #define MPS_FLAGS_ALL (MPS_FLAG_HS | MPS_FLAG_HL | MPS_FLAG_ECS | MPS_FLAG_DS | MPS_FLAG_SPP | \
-                       MPS_FLAG_GC | MPS_FLAG_PRESSURE_EXPLICIT)
+                       MPS_FLAG_GC | MPS_FLAG_PRESSURE_EXPLICIT | MPS_FLAG_CENTRAL_GRAVITY)
 /* The stock build of the reference (defines.hpp as shipped). */
 #define MPS_PRESET_REFERENCE (MPS_FLAG_HS | MPS_FLAG_HL | MPS_FLAG_ECS | MPS_FLAG_DS | MPS_FLAG_SPP)
 /* Plain MPS: standard source/Laplacian, free-surface flag n/n0 < surface_ratio. */

@@ -9,6 +9,9 @@
  * reference switches by changing the include and the namespace.  The reference's
  * compile-time method switches are runtime flags here (Environment::flags); walls are
  * static unless SetWallPositions is called (the positionWall callback of the reference).
+ * With DIM3 defined (the reference's switch, defines.hpp:9-11) or OPENMPS_GB300_DIM3,
+ * vectors have three components, Environment takes minY and maxY in the reference's
+ * DIM3 order (Environment.hpp:101-128) and the computer is three-dimensional.
  */
 #ifndef OPENMPS_GB300_HPP
 #define OPENMPS_GB300_HPP
@@ -23,9 +26,17 @@
 
 namespace openmps_gb300 {
 
-// 2-vector indexed like the reference's uBLAS c_vector: v(0), v(1)
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+constexpr int kDim = 3;
+constexpr int AXIS_X = 0, AXIS_Y = 1, AXIS_Z = 2;
+#else
+constexpr int kDim = 2;
+constexpr int AXIS_X = 0, AXIS_Z = 1;
+#endif
+
+// kDim-vector indexed like the reference's uBLAS c_vector: v(0), v(1)[, v(2)]
 struct Vector {
-    double v[2] = {0.0, 0.0};
+    double v[kDim] = {};
     double& operator()(int i) { return v[i]; }
     double operator()(int i) const { return v[i]; }
     double& operator[](int i) { return v[i]; }
@@ -58,30 +69,28 @@ private:
     Type type_;
 };
 
-// Environment(maxDt, courant, g, rho, nu, surfaceRatio, r_eByl_0, l_0, minX, minZ, maxX, maxZ)
-// in the reference's argument order; method flags, the Laplacian radius and the solver
-// are members.
+// Environment(maxDt, courant, g, rho, nu, surfaceRatio, r_eByl_0, l_0, minX, [minY,] minZ,
+// maxX, [maxY,] maxZ) in the reference's argument order; method flags, the Laplacian
+// radius and the solver are members.
 struct Environment {
     mps_params params;
 
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+    Environment(double maxDt, double courant, double g, double rho, double nu, double surfaceRatio,
+                double r_eByl_0, double l_0, double minX, double minY, double minZ, double maxX, double maxY,
+                double maxZ, uint32_t flags = MPS_PRESET_REFERENCE) {
+        fill(maxDt, courant, g, rho, nu, surfaceRatio, r_eByl_0, l_0, minX, minZ, maxX, maxZ, flags);
+        params.dim = 3;
+        params.min_y = minY;
+        params.max_y = maxY;
+    }
+#else
     Environment(double maxDt, double courant, double g, double rho, double nu, double surfaceRatio,
                 double r_eByl_0, double l_0, double minX, double minZ, double maxX, double maxZ,
                 uint32_t flags = MPS_PRESET_REFERENCE) {
-        mps_default_params(&params);
-        params.max_dt = maxDt;
-        params.courant = courant;
-        params.g = g;
-        params.rho = rho;
-        params.nu = nu;
-        params.surface_ratio = surfaceRatio;
-        params.re_by_l0 = r_eByl_0;
-        params.l0 = l_0;
-        params.min_x = minX;
-        params.min_z = minZ;
-        params.max_x = maxX;
-        params.max_z = maxZ;
-        params.flags = flags;
+        fill(maxDt, courant, g, rho, nu, surfaceRatio, r_eByl_0, l_0, minX, minZ, maxX, maxZ, flags);
     }
+#endif
     explicit Environment(const mps_params& p) : params(p) {}
 
     // two-radius extension: the Laplacian radius / l0 (0: same as r_e)
@@ -98,6 +107,25 @@ struct Environment {
         params.solver = solver;
         params.criterion = criterion;
         return *this;
+    }
+
+private:
+    void fill(double maxDt, double courant, double g, double rho, double nu, double surfaceRatio, double r_eByl_0,
+              double l_0, double minX, double minZ, double maxX, double maxZ, uint32_t flags) {
+        mps_default_params(&params);
+        params.max_dt = maxDt;
+        params.courant = courant;
+        params.g = g;
+        params.rho = rho;
+        params.nu = nu;
+        params.surface_ratio = surfaceRatio;
+        params.re_by_l0 = r_eByl_0;
+        params.l0 = l_0;
+        params.min_x = minX;
+        params.min_z = minZ;
+        params.max_x = maxX;
+        params.max_z = maxZ;
+        params.flags = flags;
     }
 };
 
@@ -136,20 +164,30 @@ public:
     void AddParticles(std::vector<Particle>&& src) {
         const size_t n = src.size();
         std::vector<int32_t> t(n);
-        std::vector<double> x(n), z(n), u(n), w(n), p(n), nd(n);
+        std::vector<double> x(n), y(n), z(n), u(n), v(n), w(n), p(n), nd(n);
         for (size_t i = 0; i < n; i++) {
             const Particle& q = src[i];
             t[i] = static_cast<int32_t>(q.TYPE());
-            x[i] = q.X()(0);
-            z[i] = q.X()(1);
-            u[i] = q.U()(0);
-            w[i] = q.U()(1);
+            x[i] = q.X()(AXIS_X);
+            z[i] = q.X()(AXIS_Z);
+            u[i] = q.U()(AXIS_X);
+            w[i] = q.U()(AXIS_Z);
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+            y[i] = q.X()(AXIS_Y);
+            v[i] = q.U()(AXIS_Y);
+#endif
             p[i] = q.P();
             nd[i] = q.N();
         }
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+        check(mps_add_particles3(h_, static_cast<int64_t>(n), t.data(), x.data(), y.data(), z.data(), u.data(),
+                                 v.data(), w.data(), p.data(), nd.data()),
+              h_);
+#else
         check(mps_add_particles(h_, static_cast<int64_t>(n), t.data(), x.data(), z.data(), u.data(), w.data(),
                                 p.data(), nd.data()),
               h_);
+#endif
         src.clear();
         fresh_ = false;
     }
@@ -159,16 +197,26 @@ public:
         if (fresh_) return cache_;
         const int64_t n = mps_particle_count(h_);
         std::vector<int32_t> t(n);
-        std::vector<double> x(n), z(n), u(n), w(n), p(n), nd(n);
+        std::vector<double> x(n), y(n), z(n), u(n), v(n), w(n), p(n), nd(n);
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+        check(mps_get_particles3(h_, t.data(), x.data(), y.data(), z.data(), u.data(), v.data(), w.data(), p.data(),
+                                 nd.data()),
+              h_);
+#else
         check(mps_get_particles(h_, t.data(), x.data(), z.data(), u.data(), w.data(), p.data(), nd.data()), h_);
+#endif
         cache_.clear();
         cache_.reserve(n);
         for (int64_t i = 0; i < n; i++) {
             Particle q(static_cast<Particle::Type>(t[i]));
-            q.X()(0) = x[i];
-            q.X()(1) = z[i];
-            q.U()(0) = u[i];
-            q.U()(1) = w[i];
+            q.X()(AXIS_X) = x[i];
+            q.X()(AXIS_Z) = z[i];
+            q.U()(AXIS_X) = u[i];
+            q.U()(AXIS_Z) = w[i];
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+            q.X()(AXIS_Y) = y[i];
+            q.U()(AXIS_Y) = v[i];
+#endif
             q.P() = p[i];
             q.N() = nd[i];
             cache_.push_back(q);
@@ -188,9 +236,16 @@ public:
         return s;
     }
     // positions of every non-fluid particle for the next steps (positionWall)
+#if defined(DIM3) || defined(OPENMPS_GB300_DIM3)
+    void SetWallPositions(const std::vector<double>& wx, const std::vector<double>& wy,
+                          const std::vector<double>& wz) {
+        check(mps_set_wall_positions3(h_, wx.data(), wy.data(), wz.data()), h_);
+    }
+#else
     void SetWallPositions(const std::vector<double>& wx, const std::vector<double>& wz) {
         check(mps_set_wall_positions(h_, wx.data(), wz.data()), h_);
     }
+#endif
     mps_handle* Handle() const { return h_; }
 
 private:

@@ -198,3 +198,92 @@ def test_run_3d_matches_python_binding(driver, tmp_path):
         P = c.particles3()
         ref = np.stack([P[f] for f in ("type", "x", "y", "z", "u", "v", "w", "p", "n")], axis=1)
         np.testing.assert_allclose(got, ref, rtol=5.01e-6, atol=1e-12)
+
+
+# ------------------------------------------------- the header-only C++ wrapper
+CPP_PROGRAM = r"""
+#include <cstdio>
+#include <vector>
+#include "openmps_gb300.hpp"
+namespace OpenMps = openmps_gb300;  // a caller of the reference swaps its include and namespace
+int main() {
+    std::vector<OpenMps::Particle> ps;
+    int n = 0;
+    double t, x, y, z;
+    while (std::scanf("%d %lf %lf %lf", &n, &x, &y, &z) == 4) {
+        OpenMps::Particle q(static_cast<OpenMps::Particle::Type>(n));
+        q.X()[OpenMps::AXIS_X] = x;
+#ifdef DIM3
+        q.X()[OpenMps::AXIS_Y] = y;
+#endif
+        q.X()[OpenMps::AXIS_Z] = z;
+        ps.push_back(q);
+    }
+#ifdef DIM3
+    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 0.97, 2.1, 0.01, MINX, MINY, MINZ, MAXX, MAXY, MAXZ);
+#else
+    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 0.97, 2.1, 0.01, MINX, MINZ, MAXX, MAXZ);
+#endif
+    auto computer = OpenMps::CreateComputer(1e-10, env);
+    computer.AddParticles(std::move(ps));
+    for (int k = 0; k < 3; k++) computer.ForwardTime(5e-4);
+    t = computer.GetEnvironment().t;
+    std::printf("%.17g\n", t);
+    for (const auto& q : computer.Particles()) {
+        for (int a = 0; a < OpenMps::kDim; a++) std::printf("%.17g ", q.X()[a]);
+        for (int a = 0; a < OpenMps::kDim; a++) std::printf("%.17g ", q.U()[a]);
+        std::printf("%.17g %.17g\n", q.P(), q.N());
+    }
+    return 0;
+}
+"""
+
+
+def _cpp_flags(dim, b):
+    d = ["-DMINX=%r" % b[0], "-DMAXX=%r" % b[3 if dim == 3 else 2]]
+    if dim == 3:
+        d += ["-DDIM3", "-DMINY=%r" % b[1], "-DMINZ=%r" % b[2], "-DMAXY=%r" % b[4], "-DMAXZ=%r" % b[5]]
+    else:
+        d += ["-DMINZ=%r" % b[1], "-DMAXZ=%r" % b[3]]
+    return d
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cpp_wrapper_compiles(tmp_path, dim):
+    src = tmp_path / "prog.cpp"
+    src.write_text(CPP_PROGRAM)
+    res = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                          "-I", os.path.join(build.HERE, "..", "include"), str(src)]
+                         + _cpp_flags(dim, (0.0, 0.0, 0.0, 1.0, 1.0, 1.0)), capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_wrapper_dim3_run(driver, tmp_path):
+    # the wrapper compiled with the reference's DIM3 switch, against the Python binding
+    from openmps_gb300.computer import Computer
+
+    s = _scene3()
+    s.meta["params"] = dict(scenes.STOCK_PHYSICS, re_by_l0=2.1, re_lap_by_l0=0.0, rho=1000.0, nu=1e-6,
+                            surface_ratio=0.97, courant=0.1, g=9.8, max_dt=5e-4, eps=1e-10)
+    src = tmp_path / "prog.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "prog"
+    res = subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I",
+                          os.path.join(build.HERE, "..", "include"), str(src), "-o", str(exe), "-L", build.HERE,
+                          "-lopenmps_gb300", "-Wl,-rpath," + build.HERE] + _cpp_flags(3, s.bounds),
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    stdin = "\n".join("%d %.17g %.17g %.17g" % (s.type[k], s.x[k], s.y[k], s.z[k]) for k in range(s.count))
+    out = subprocess.run([str(exe)], input=stdin, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    got = np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
+    c = Computer(s.params())
+    c.add_particles3(*s.arrays3())
+    for _ in range(3):
+        c.forward_time(5e-4)
+    assert float(lines[0]) == c.environment().t
+    P = c.particles3()
+    ref = np.stack([P[f] for f in ("x", "y", "z", "u", "v", "w", "p", "n")], axis=1)
+    np.testing.assert_array_equal(got, ref)
