@@ -209,3 +209,62 @@ def test_environment_and_errors(gpu_lib, oracle_lib):
     with pytest.raises(ComputerError) as err:
         Batch(s.params(), [scenes.batch_scene(0)])
     assert err.value.code == abi.MPS_ERR_NOT_SUPPORTED
+
+
+# ------------------------------------------------------------------ failures
+def test_cell_overflow_and_recovery(gpu_lib, oracle_lib):
+    from openmps_gb300.computer import ComputerError
+    from oracle.oracle import OracleError
+
+    s = _scene()
+    bad = s.copy()
+    bad.x[:80] = 0.021  # 80 particles in one cell (maxPerCell is 64 at r_e = 2.1 l0)
+    bad.y[:80] = 0.021
+    bad.z[:80] = 0.021 + np.arange(80) * 1e-6
+    gpu, cpu = _pair(bad)
+    with pytest.raises(ComputerError) as e:
+        gpu.forward_time(DT)
+    assert e.value.code == abi.MPS_ERR_CELL_OVERFLOW
+    with pytest.raises(OracleError) as e:
+        cpu.forward_time(DT)
+    assert e.value.code == abi.MPS_ERR_CELL_OVERFLOW
+    gpu.set_particles3(*s.arrays3())  # the handle stays usable
+    gpu.forward_time(DT)
+
+
+def test_out_of_domain_disabled(gpu_lib, oracle_lib):
+    s = _scene()
+    s.y[3] = 5.0  # beyond maxY: Grid::Store fails, the particle is disabled (Computer.hpp:710-715)
+    s.x[4] = -7.0
+    gpu, cpu = _pair(s, eps=1e-13)
+    gpu.forward_time(DT)
+    cpu.forward_time(DT)
+    G, C = gpu.particles3(), cpu.particles()
+    assert G["type"][3] == abi.TYPE_DISABLED and G["type"][4] == abi.TYPE_DISABLED
+    np.testing.assert_array_equal(G["type"], C["type"])
+    assert gpu.stats()["disabled"] == 2
+
+
+def test_neighbor_row_overflow_is_an_error(gpu_lib):
+    from openmps_gb300.computer import Computer, ComputerError
+    from test_oracle_dim3 import packed_cluster
+
+    s = packed_cluster()
+    gpu = Computer(s.params())
+    gpu.add_particles3(*s.arrays3())
+    gpu.begin_step(DT)
+    with pytest.raises(ComputerError) as e:
+        gpu.stage("search_neighbor")
+    assert e.value.code == abi.MPS_ERR_DEVICE_CHECK
+
+
+def test_cg_not_converged(gpu_lib):
+    from openmps_gb300.computer import Computer, ComputerError
+
+    s = _scene()
+    c = Computer(s.params(max_cg_iters=2, eps=1e-12))
+    c.add_particles3(*s.arrays3())
+    with pytest.raises(ComputerError) as e:
+        c.forward_time(DT)
+    assert e.value.code == abi.MPS_ERR_CG_NOT_CONVERGED
+    assert np.all(c.particles3()["p"] == 0.0)

@@ -90,3 +90,37 @@ def test_single_layer_equals_2d(oracle_lib):
     np.testing.assert_array_equal(c3, c2)
     np.testing.assert_array_equal(l3, l2)
     np.testing.assert_array_equal(o3.particles()["n"], o2.particles()["n"])
+
+
+def packed_cluster(l0=0.01, re_by=2.1):
+    """27 particles in each of the 27 cells around a particle at a cell centre, all within
+    NeighborLength of it: no cell holds more than maxPerCell (64) particles, but the
+    centre's row needs 728 entries against the reference's 9 maxPerCell = 576."""
+    nl = re_by * l0 * 1.2
+    c = np.array([10.5, 10.5, 10.5]) * nl  # a cell centre with the domain origin at 0
+    pts = []
+    for d in np.ndindex(3, 3, 3):
+        d = np.array(d) - 1
+        for k in np.ndindex(3, 3, 3):
+            k = np.array(k)
+            off = np.where(d != 0, d * (0.52 + 0.02 * k), (k - 1) * 0.02)
+            pts.append(c + nl * off)
+    pts = np.array(pts)
+    n = len(pts)
+    s = scenes.Scene3(name="packed", type=np.zeros(n, dtype=np.int32), x=pts[:, 0].copy(), y=pts[:, 1].copy(),
+                      z=pts[:, 2].copy(), u=np.zeros(n), v=np.zeros(n), w=np.zeros(n), p=np.zeros(n),
+                      n=np.zeros(n), l0=l0, bounds=(0.0, 0.0, 0.0, 21 * nl, 21 * nl, 21 * nl))
+    s.meta["params"] = dict(scenes.PLAIN_PHYSICS, re_by_l0=re_by, re_lap_by_l0=0.0, eps=1e-10, max_dt=5e-4)
+    return s
+
+
+def test_neighbor_row_overflow(oracle_lib):
+    from oracle.oracle import Oracle3, OracleError
+
+    s = packed_cluster()
+    o = Oracle3(s.params())
+    o.add_scene(s)
+    o.begin_step(5e-4)
+    with pytest.raises(OracleError) as e:
+        o.stage("search_neighbor")
+    assert e.value.code == abi.MPS_ERR_DEVICE_CHECK
