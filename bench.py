@@ -20,6 +20,10 @@ from, since later steps of the dam break need more PPE iterations);
 ``roofline`` reports the PPE solver's SpMV kernel (the dominant kernel) against
 the measured HBM bandwidth; ``cpu_baseline`` times the CPU restatement of the
 reference step (OpenMP, all host cores) on a bounded sample of the same scene.
+Further blocks: ``ppe_solvers_same_state`` (every PPE solver from one snapshot),
+``method_variants`` (GC, explicit pressure, and a 104k-particle 3D dam break),
+``configs`` (the other configurations: throughput and SpMV GB/s, cache-resident
+matrices tagged) and ``batched`` (256 independent scenes in one handle).
 
 ``--impl reference`` times that CPU path alone (rank 0 only) on the same
 workload and metric.  With ``--gpus N`` (one process per GPU under torchrun)
@@ -323,10 +327,11 @@ def run_ours(args, rank, world, local_rank):
     comp.set_stage_timing(False)
 
     # ---- the PPE solvers on the same state (a few steps each from a snapshot)
-    compare = variants = None
+    compare = variants = sweep = None
     if not args.no_compare and rank == 0:
         compare = compare_solvers(comp, scene, dt, local_rank)
         variants = method_variants(comp, scene, dt, local_rank)
+        sweep = config_sweep(local_rank, load_peak()[0])
 
     # ---- the batched workload: 256 uneven dam breaks in one handle
     batched = None
@@ -405,6 +410,8 @@ def run_ours(args, rank, world, local_rank):
         line["ppe_solvers_same_state"] = compare
     if variants is not None:
         line["method_variants"] = variants
+    if sweep is not None:
+        line["configs"] = sweep
     if batched is not None:
         line["batched"] = batched
     if not args.no_cpu_baseline and world == 1:
@@ -502,6 +509,54 @@ def method_variants(comp, scene, dt, device, steps=3):
     out["note"] = ("same snapshot, %d steps each, L2 flushed before each step; explicit: c = %g m/s, "
                    "dt = courant l0 / c" % (steps, VARIANT_SOUND_SPEED))
     out["dim3"] = dim3_workload(device)
+    return out
+
+
+def config_sweep(device, peak, warmup=3, steps=5):
+    """Throughput and SpMV bandwidth of the other configurations: C0 (the l0 = 0.01 dam
+    break, 800 fluid), C1 (the 80,000-fluid hydrostatic tank) and the 320k dam break at
+    one radius (r_e = re_lap = 2.1 l0), each with the multigrid mixed-precision solver to
+    |b - Ax| <= 1e-8 |b|, L2 flushed before every timed step.  The SpMVs are timed alone,
+    L2 flushed before each launch; a matrix that fits in L2 is tagged, because there the
+    GB/s exceed what HBM alone delivers when L2 is warm."""
+    from openmps_gb300 import _abi as abi
+    from openmps_gb300 import scenes
+    from openmps_gb300.computer import Computer
+
+    c2_one = scenes.config_c2()
+    c2_one.meta["params"] = dict(c2_one.meta["params"], re_lap_by_l0=0.0)
+    cases = (("C0 dam break, 800 fluid, l0=1e-2 m, dt=5e-4 s", scenes.config_c0()),
+             ("C1 hydrostatic tank, 80,000 fluid, l0=2.5e-3 m, dt=1e-4 s", scenes.config_c1()),
+             ("C2 320k dam break at one radius r_e = re_lap = 2.1 l0, dt=2.5e-5 s", c2_one))
+    out = []
+    for name, sc in cases:
+        dt = sc.meta["dt"]
+        c = Computer(sc.params(solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS, eps=1e-8), device=device)
+        c.add_scene(sc)
+        for _ in range(warmup):
+            c.forward_time(dt)
+        ms, its = [], []
+        for _ in range(steps):
+            c.flush_l2(FLUSH_BYTES)
+            c.event_record(0)
+            c.forward_time(dt)
+            c.event_record(1)
+            ms.append(c.event_elapsed(0, 1))
+            its.append(c.stats()["cg_iterations"])
+        st = c.stats()
+        n, nnz = sc.count, st["ppe_nnz"]
+        b32 = 8 * nnz + 4 * (n + 1) + 12 * n
+        b64 = 12 * nnz + 4 * (n + 1) + 16 * n
+        t32 = c.bench_spmv(abi.SOLVER_MIXED, reps=20, flush_bytes=FLUSH_BYTES)
+        t64 = c.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
+        c.close()
+        out.append({"workload": name, "particles": n, "ppe_nnz": nnz, "ms_per_step": statistics.mean(ms),
+                    "particle_steps_per_s": n / (statistics.mean(ms) * 1e-3),
+                    "ppe_iterations": statistics.mean(its),
+                    "spmv32": {"ms": t32, "gbs": b32 / (t32 * 1e-3) / 1e9, "frac": b32 / (t32 * 1e-3) / 1e9 / peak,
+                               "bytes": b32, "l2_resident": b32 < 100e6},
+                    "spmv64": {"ms": t64, "gbs": b64 / (t64 * 1e-3) / 1e9, "frac": b64 / (t64 * 1e-3) / 1e9 / peak,
+                               "bytes": b64, "l2_resident": b64 < 100e6}})
     return out
 
 
