@@ -14,8 +14,8 @@
 //   * a Computer::Exception prints "!!!!ERROR!!!!" and stops the run (Main.cpp:380-388).
 // With MPS_FLAG_PRESSURE_EXPLICIT among the flags, <environment> holds the sound speed c
 // and <condition> needs no eps, as in the reference built with PRESSURE_EXPLICIT.
-// A DIM3 input (minY and maxY in <environment>) runs a three-dimensional scene: its CSV
-// holds Type, x, y, z, u, v, w, p, n.
+// A DIM3 input (minY < maxY in <environment>, or dim = 3) runs a three-dimensional
+// scene: its CSV holds Type, x, y, z, u, v, w, p, n.
 // Extensions (optional elements of <environment>): r_lapByl_0 (Laplacian radius),
 // flags (method bit set, default the reference's stock set) and solver (cg64, mixed,
 // mg, learned; default cg64 like the reference), weights (network file for "learned",
@@ -234,9 +234,10 @@ int run(int argc, char** argv) {
                                    flags);
     env.LaplacianRadius(xml.num_or("environment", "r_lapByl_0", 0.0));
     if (explicit_pressure) env.SoundSpeed(xml.num("environment", "c"));
-    // DIM3 inputs hold minY and maxY (Main.cpp:224-232)
-    std::string probe;
-    const int dim = static_cast<int>(xml.num_or("environment", "dim", xml.attr("environment", "minY", &probe) ? 3 : 2));
+    // A DIM3 input spans a y range (minY < maxY, Main.cpp:224-232); the reference's 2D
+    // inputs may carry minY = maxY (Benchmark/Sample/Sample.xml), read only by DIM3 builds.
+    const bool y_range = xml.num_or("environment", "maxY", 0.0) > xml.num_or("environment", "minY", 0.0);
+    const int dim = static_cast<int>(xml.num_or("environment", "dim", y_range ? 3 : 2));
     if (dim == 3) {
         env.params.dim = 3;
         env.params.min_y = xml.num("environment", "minY");
