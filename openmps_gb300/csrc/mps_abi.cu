@@ -1881,6 +1881,7 @@ int mps_learned_set_weights(mps_handle* h, const float* blob, int64_t count) {
 
 int mps_learned_collect(mps_handle* h, int32_t enable) {
     if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    if (enable && h->sc.dim == 3) return MPS_ERR_NOT_SUPPORTED;  // the learned features are 2D
     h->lrn_collect = enable != 0;
     return MPS_OK;
 }

@@ -206,6 +206,10 @@ def test_environment_and_errors(gpu_lib, oracle_lib):
     with pytest.raises(ComputerError) as err:
         Computer(s.params(solver=abi.SOLVER_MIXED_MG))
     assert err.value.code == abi.MPS_ERR_NOT_SUPPORTED
+    with pytest.raises(ComputerError) as err:  # switching an existing 3D handle
+        gpu.set_solver(abi.SOLVER_LEARNED, abi.CRIT_RHS, 1e-8)
+    assert err.value.code == abi.MPS_ERR_NOT_SUPPORTED
+    assert gpu.lib.mps_learned_collect(gpu.h, 1) == abi.MPS_ERR_NOT_SUPPORTED
     with pytest.raises(ComputerError) as err:
         Batch(s.params(), [scenes.batch_scene(0)])
     assert err.value.code == abi.MPS_ERR_NOT_SUPPORTED
