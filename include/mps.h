@@ -346,7 +346,8 @@ int mps_cg_solve_csr_device_noalloc(int64_t n, const int64_t* row_ptr, const int
 /* Loads the network used by MPS_SOLVER_LEARNED (converted to the tensor-core image). */
 int mps_learned_set_weights(mps_handle* h, const float* blob, int64_t count);
 /* When enabled, every solve also records one training sample per particle: the
- * features of the step and the targets from the solution (any solver). */
+ * features of the step and the targets from the solution (any solver).  Two-dimensional
+ * scenes only (MPS_ERR_NOT_SUPPORTED on a DIM3 handle). */
 int mps_learned_collect(mps_handle* h, int32_t enable);
 /* The last step's samples (n x MPS_MLP_SAMPLE_FLOATS) and active-row flags (n);
  * with both pointers null only *count (= n) is returned. */
