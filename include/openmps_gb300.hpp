@@ -155,7 +155,8 @@ public:
         check(mps_forward_time(h_, dt), h_);
     }
     void ForwardTime() { ForwardTime(-1.0); }
-    // nsteps steps with a fixed dt replayed from one captured graph
+    // nsteps ForwardTime(dt) calls in one library call (each step still ends with its
+    // status check, so a failure stops at the step that failed)
     void ForwardSteps(const double dt, int32_t nsteps) {
         fresh_ = false;
         check(mps_forward_steps(h_, dt, nsteps), h_);
