@@ -381,8 +381,18 @@ public:
                 vx += c * (u[i] - u[i]);
                 vz += c * (w[i] - w[i]);
             }
-            dux[i] = vx + 0.0;        /* a = vis; a += G, G = (0, -g) (Environment.hpp:149) */
-            duz[i] = vz + (-prm.g);
+            if (has(prm.flags, MPS_FLAG_CENTRAL_GRAVITY)) {
+                /* CENTRAL_GRAVITY (Computer.hpp:925-932, :981-988): a += G_z c, c = x / |x| */
+                const double g = -prm.g;
+                const double r = std::sqrt(dot2(x[i], z[i], x[i], z[i]));
+                const double cx = (r < l0 * 0.01) ? 0.0 : x[i] / r;
+                const double cz = (r < l0 * 0.01) ? 0.0 : z[i] / r;
+                dux[i] = vx + g * cx;
+                duz[i] = vz + g * cz;
+            } else {
+                dux[i] = vx + 0.0; /* a = vis; a += G, G = (0, -g) (Environment.hpp:149) */
+                duz[i] = vz + (-prm.g);
+            }
         }
         ORACLE_PARALLEL_FOR
         for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {

@@ -331,9 +331,18 @@ public:
                 ay += c * (v[i] - v[i]);
                 az += c * (w[i] - w[i]);
             }
-            dux[i] = ax + 0.0;
-            duy[i] = ay + 0.0;
-            duz[i] = az + (-prm.g);
+            if (flag(prm.flags, MPS_FLAG_CENTRAL_GRAVITY)) { /* Computer.hpp:925-932, :981-988 */
+                const double g = -prm.g;
+                const double r = std::sqrt(dot3(x[i], y[i], z[i], x[i], y[i], z[i]));
+                const bool zero = r < l0 * 0.01;
+                dux[i] = ax + g * (zero ? 0.0 : x[i] / r);
+                duy[i] = ay + g * (zero ? 0.0 : y[i] / r);
+                duz[i] = az + g * (zero ? 0.0 : z[i] / r);
+            } else {
+                dux[i] = ax + 0.0;
+                duy[i] = ay + 0.0;
+                duz[i] = az + (-prm.g);
+            }
         }
         ORACLE3_PARALLEL_FOR
         for (int64_t ii = 0; ii < static_cast<int64_t>(n); ii++) {
