@@ -191,7 +191,11 @@ class Computer:
                                                *[_ptr(a) for a in arrs]))
 
     def add_scene(self, scene):
-        self.add_particles(*scene.arrays())
+        """Adds a ``scenes.Scene`` (2D) or ``scenes.Scene3`` (3D handle) particle set."""
+        if hasattr(scene, "arrays3"):
+            self.add_particles3(*scene.arrays3())
+        else:
+            self.add_particles(*scene.arrays())
 
     @property
     def count(self) -> int:
