@@ -91,6 +91,7 @@ int oracle3_get_particles(const oracle3_handle* h, int32_t* type, double* x, dou
 int oracle3_set_particles(oracle3_handle* h, const int32_t* type, const double* x, const double* y,
                           const double* z, const double* u, const double* v, const double* w, const double* p,
                           const double* nd);
+int oracle3_set_wall_positions(oracle3_handle* h, const double* wx, const double* wy, const double* wz);
 int oracle3_forward_time(oracle3_handle* h, double dt);
 int oracle3_get_environment(const oracle3_handle* h, mps_environment* env);
 int oracle3_stage(oracle3_handle* h, int32_t stage, double dt);

@@ -785,6 +785,15 @@ int oracle3_set_particles(oracle3_handle* h, const int32_t* type, const double* 
     });
 }
 
+/* positionWall targets of every non-fluid particle for the next steps (Computer.hpp:1015) */
+int oracle3_set_wall_positions(oracle3_handle* h, const double* wx, const double* wy, const double* wz) {
+    return guarded3(h, [&](Oracle3& o) {
+        in3(o.wall_x, wx);
+        in3(o.wall_y, wy);
+        in3(o.wall_z, wz);
+    });
+}
+
 int oracle3_forward_time(oracle3_handle* h, double dt) {
     return guarded3(h, [&](Oracle3& o) { o.forward_time(dt); });
 }

@@ -83,6 +83,7 @@ def load(openmp: bool = False) -> C.CDLL:
     lib.oracle3_get_particles.argtypes = [P, _I32] + [_D] * 8
     lib.oracle3_set_particles.argtypes = [P, _I32] + [_D] * 8
     lib.oracle3_forward_time.argtypes = [P, C.c_double]
+    lib.oracle3_set_wall_positions.argtypes = [P, _D, _D, _D]
     lib.oracle3_get_environment.argtypes = [P, C.POINTER(abi.MpsEnvironment)]
     lib.oracle3_stage.argtypes = [P, C.c_int32, C.c_double]
     lib.oracle3_density_variation.argtypes = [P, _D]
@@ -329,6 +330,10 @@ class Oracle3:
 
     def forward_time(self, dt: float):
         self._check(self.lib.oracle3_forward_time(self.h, dt))
+
+    def set_wall_positions(self, wx, wy, wz):
+        conv = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self._check(self.lib.oracle3_set_wall_positions(self.h, _ptr(conv(wx)), _ptr(conv(wy)), _ptr(conv(wz))))
 
     def begin_step(self, dt: float):
         self._check(self.lib.oracle3_stage(self.h, 0, dt))
