@@ -124,3 +124,30 @@ def test_neighbor_row_overflow(oracle_lib):
     with pytest.raises(OracleError) as e:
         o.stage("search_neighbor")
     assert e.value.code == abi.MPS_ERR_DEVICE_CHECK
+
+
+def test_single_layer_ppe_against_2d(oracle_lib):
+    # with the SPP method set (no surface test) the one-layer scene's PPE has the 2D
+    # pattern, and its off-diagonal HL coefficients (5 - D) r_e / n0 / r^3 differ from the
+    # 2D ones only by the factor (2 / n0_3D) / (3 / n0_2D)
+    from oracle.oracle import Oracle, Oracle3
+
+    s2, s3 = single_layer_pair()
+    for s in (s2, s3):
+        s.meta["params"]["flags"] = abi.PRESET_REFERENCE
+    o2 = Oracle(s2.params())
+    o2.add_scene(s2)
+    o3 = Oracle3(s3.params())
+    o3.add_scene(s3)
+    for o in (o2, o3):
+        o.begin_step(5e-4)
+        for name in ("search_neighbor", "density", "error_correction", "explicit", "density", "set_ppe"):
+            o.stage(name)
+    rp2, col2, val2, _, _ = o2.ppe()
+    rp3, col3, val3, _, _ = o3.ppe()
+    np.testing.assert_array_equal(rp3, rp2)
+    np.testing.assert_array_equal(col3, col2)
+    rows = np.repeat(np.arange(rp2.size - 1), np.diff(rp2))
+    off = col2 != rows
+    ratio = (2.0 / o3.environment().n0) / (3.0 / o2.environment().n0)
+    np.testing.assert_allclose(val3[off], val2[off] * ratio, rtol=1e-14)
