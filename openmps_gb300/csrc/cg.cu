@@ -387,9 +387,18 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o, int afte
 // reduction.  An iteration is an elementwise kernel (s, p, d, r updates, no reduction)
 // followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
 
+// A {column, FP32 value} pair of the SELL stream, loaded without allocating in L1: each
+// pair is read once per SpMV, so L1 stays with the gathered entries of v, which
+// neighbouring rows share.  The L2 policy stays the default (the FP32 matrix is read
+// every iteration and may stay resident).
+__device__ __forceinline__ uint2 ld_sell_pair(const uint2* p) {
+    uint2 e;
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(e.x), "=r"(e.y) : "l"(p));
+    return e;
+}
+
 // Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
-// The {column, value} pairs keep default caching (the FP32 matrix is read every
-// iteration).  Software-pipelined like row64.
+// Software-pipelined like row64.
 template <int D = 8>
 __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
                                        const float* __restrict__ v) {
@@ -398,7 +407,7 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
     uint2 e[D];
     if (nb > 0) {
 #pragma unroll
-        for (int u = 0; u < D; u++) e[u] = __ldg(o.cv32 + at + u * kSellRows);
+        for (int u = 0; u < D; u++) e[u] = ld_sell_pair(o.cv32 + at + u * kSellRows);
     }
     for (int bt = 0; bt < nb; bt++) {
         float xv[D];
@@ -408,7 +417,7 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
         if (bt + 1 < nb) {
             const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
 #pragma unroll
-            for (int u = 0; u < D; u++) f[u] = __ldg(o.cv32 + nx + u * kSellRows);
+            for (int u = 0; u < D; u++) f[u] = ld_sell_pair(o.cv32 + nx + u * kSellRows);
         }
 #pragma unroll
         for (int u = 0; u < D; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
@@ -417,7 +426,7 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
     }
     at += static_cast<int64_t>(nb) * D * kSellRows;
     for (int k = nb * D; k < L; k++, at += kSellRows) {
-        const uint2 t = __ldg(o.cv32 + at);
+        const uint2 t = ld_sell_pair(o.cv32 + at);
         acc = fmaf(__uint_as_float(t.y), v[t.x], acc);
     }
     return acc;
