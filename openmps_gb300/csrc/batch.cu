@@ -284,7 +284,7 @@ __device__ void spmv_dots(const BatchOps& B, const Smem& S, const BatchScene& sc
         int64_t at = sell_index(o.off[i >> 5], i & 31, 0);
         float acc = 0.0f;
         for (int k = 0; k < L; k++, at += kSellRows) {
-            const uint2 e = o.cv32[at];
+            const uint2 e = ld_sell_pair(o.cv32 + at);
             acc = fmaf(__uint_as_float(e.y), o.u32[e.x], acc);
         }
         o.w32[i] = acc;

@@ -387,16 +387,6 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o, int afte
 // reduction.  An iteration is an elementwise kernel (s, p, d, r updates, no reduction)
 // followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
 
-// A {column, FP32 value} pair of the SELL stream, loaded without allocating in L1: each
-// pair is read once per SpMV, so L1 stays with the gathered entries of v, which
-// neighbouring rows share.  The L2 policy stays the default (the FP32 matrix is read
-// every iteration and may stay resident).
-__device__ __forceinline__ uint2 ld_sell_pair(const uint2* p) {
-    uint2 e;
-    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(e.x), "=r"(e.y) : "l"(p));
-    return e;
-}
-
 // Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
 // Software-pipelined like row64.
 template <int D = 8>

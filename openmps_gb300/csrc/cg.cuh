@@ -5,6 +5,16 @@
 
 namespace mpsgb {
 
+// A {column, FP32 value} pair of the SELL stream, loaded without allocating in L1: each
+// pair is read once per SpMV, so L1 stays with the gathered entries of the vector, which
+// neighbouring rows share.  The L2 policy stays the default (the FP32 matrix is read
+// every iteration and may stay resident).  The matrix is read-only while a solve runs.
+__device__ __forceinline__ uint2 ld_sell_pair(const uint2* p) {
+    uint2 e;
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(e.x), "=r"(e.y) : "l"(p));
+    return e;
+}
+
 // Scalars of one solve, in device memory (read back once per step).
 struct CgScalars {
     double rr;        // r.r of the current direction update
