@@ -26,7 +26,10 @@ Further blocks: ``ppe_solvers_same_state`` (every PPE solver from one snapshot),
 matrices tagged) and ``batched`` (256 independent scenes in one handle).
 
 ``--impl reference`` times that CPU path alone (rank 0 only) on the same
-workload and metric.  With ``--gpus N`` (one process per GPU under torchrun)
+workload and metric, over the same simulation steps (``--warmup`` untimed steps
+from the initial state, then ``--steps`` timed ones).  The headline solver is the
+multigrid-preconditioned mixed-precision CG (``--solver mg``); the learned solver's
+result stands beside it in ``ppe_solvers_same_state``.  With ``--gpus N`` (one process per GPU under torchrun)
 every rank advances its own independent replica of the scene (replicas only: the
 step has no data-parallel exchange), and ``value`` sums all ranks.
 """
@@ -45,7 +48,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s, 320k dam break"
+METRIC_FULL = METRIC + "; PPE ms to 1e-8 rel: learned vs plain CG"
 UNIT = "particle-steps/s"
+WORKLOAD = ("2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, reference MPS scheme "
+            "(HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s")
+
+
+def workload_config(particles: int, world: int) -> dict:
+    """The `config` block, identical in both arms."""
+    return {"workload": WORKLOAD, "particles": particles, "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
+            "l2": "GPU arm: L2 flushed between timed steps (512 MiB write); working set > L2 in both arms",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 512 << 20
 SOLVERS = {"cg64": 0, "mixed": 1, "mg": 3, "learned": 2}
@@ -60,7 +73,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--solver", choices=("cg64", "mixed", "mg", "learned"), default="learned")
+    ap.add_argument("--solver", choices=("cg64", "mixed", "mg", "learned"), default="mg")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the same-state comparison of the PPE solvers")
     ap.add_argument("--no-batch", action="store_true",
@@ -148,8 +161,33 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(scene, params, dt, budget_s: float, max_steps: int | None = None) -> dict:
-    """The CPU restatement of the reference step (OpenMP, all host threads)."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu on Arm hosts, whose /proc/cpuinfo names none)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+        name = fields.get("Model name", "").strip()
+        vendor = fields.get("Vendor ID", "").strip()
+        if name:
+            return (vendor + " " + name).strip()
+    except (OSError, subprocess.SubprocessError, ValueError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(scene, params, dt, budget_s: float, warmup: int = 0, max_steps: int | None = None) -> dict:
+    """The CPU restatement of the reference step (OpenMP, all host threads): `warmup`
+    untimed steps from the scene's initial state, then timed steps until `max_steps` or
+    the time budget."""
     from oracle import build_oracle
     from oracle import oracle as orc
 
@@ -157,24 +195,27 @@ def cpu_baseline(scene, params, dt, budget_s: float, max_steps: int | None = Non
     o = orc.Oracle(params, openmp=True)
     o.add_scene(scene)
     threads = orc.num_threads(True)
-    times = []
-    n_active = scene.count
+    for _ in range(warmup):
+        o.forward_time(dt)
+    times, its = [], []
     t_all = time.perf_counter()
     while True:
         t0 = time.perf_counter()
         o.forward_time(dt)
         times.append(time.perf_counter() - t0)
+        its.append(o.stats()["cg_iterations"])
         if max_steps is not None and len(times) >= max_steps:
             break
-        if time.perf_counter() - t_all + times[-1] > budget_s or len(times) >= 50:
+        if max_steps is None and (time.perf_counter() - t_all + times[-1] > budget_s or len(times) >= 50):
             break
     n_active = int((o.particles()["type"] != 3).sum())
     sec = sum(times)
     return {"value": n_active * len(times) / sec, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d step(s) of the same scene from its initial state (%.1f s of CPU time), "
-                      "CG iterations of the last step %d" % (len(times), sec,
-                                                            o.stats()["cg_iterations"]),
-            "seconds_per_step": sec / len(times)}
+            "cpu_model": cpu_model(),
+            "sample": "steps %d-%d of the same scene (%d untimed before them), %.1f s of CPU time; "
+                      "FP64 CG, %.0f iterations per step" % (warmup + 1, warmup + len(times), warmup, sec,
+                                                             statistics.mean(its)),
+            "seconds_per_step": sec / len(times), "cg_iterations_per_step": statistics.mean(its)}
 
 
 def reduce_max(values, dist):
@@ -372,7 +413,7 @@ def run_ours(args, rank, world, local_rank):
         return
 
     line = {
-        "metric": METRIC,
+        "metric": METRIC_FULL,
         "value": value,
         "unit": UNIT,
         "n_gpus": world,
@@ -385,13 +426,11 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f64" if solver == abi.SOLVER_CG64 else "f64 (PPE iterations f32, f64 residual/refinement)",
         "ppe_solver": SOLVER_DESC[solver],
         "data": "synthetic (seeded lattice dam break)",
-        "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
-                               "reference MPS scheme (HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
-                   "particles": n, "active_particles": n_active, "ppe_nnz": nnz,
-                   "solver": args.solver, "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
-                   "l2": "flushed between timed steps (512 MiB write); working set > L2",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(n, world),
         "impl": "ours",
+        "solver": args.solver,
+        "active_particles": n_active,
+        "ppe_nnz": nnz,
         "cg_iterations_per_step": statistics.mean(iters) if iters else None,
         "ppe_true_relres": relres,
         "stage_ms": stage_ms,
@@ -406,17 +445,18 @@ def run_ours(args, rank, world, local_rank):
                      "spmv64_ms_per_launch": spmv64_ms,
                      "spmv64_achieved_gbs": (12 * nnz + 4 * (n + 1) + 16 * n) / (spmv64_ms * 1e-3) / 1e9},
     }
-    if compare is not None:
-        line["ppe_solvers_same_state"] = compare
-    if variants is not None:
-        line["method_variants"] = variants
+    # the long blocks first; the compact solver comparison closes the line
     if sweep is not None:
         line["configs"] = sweep
+    if variants is not None:
+        line["method_variants"] = variants
     if batched is not None:
         line["batched"] = batched
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, scene.params(criterion=abi.CRIT_RHS, eps=1e-8), dt,
-                                            args.cpu_seconds)
+                                            args.cpu_seconds, warmup=max(args.warmup, 0))
+    if compare is not None:
+        line["ppe_solvers_same_state"] = compare
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
@@ -453,14 +493,15 @@ def compare_solvers(comp, scene, dt, device, steps=3):
             its.append(st["cg_iterations"])
             assert st["cg_true_relres"] <= 1e-8
         c.close()
-        out[name] = {"step_ms": statistics.mean(step_ms), "ppe_ms": statistics.mean(solve_ms),
-                     "iterations": statistics.mean(its), "solver": SOLVER_DESC[sv]}
+        out[name] = {"step_ms": round(statistics.mean(step_ms), 3), "ppe_ms": round(statistics.mean(solve_ms), 3),
+                     "iterations": round(statistics.mean(its), 1)}
     base = out["cg64"]
-    for name, v in out.items():
-        v["step_speedup_vs_cg64"] = base["step_ms"] / v["step_ms"]
-        v["ppe_speedup_vs_cg64"] = base["ppe_ms"] / v["ppe_ms"]
-    out["note"] = ("same snapshot for every solver, %d steps each, L2 flushed before each step; "
-                   "step_ms includes the per-stage events" % steps)
+    for name, v in list(out.items()):
+        v["step_x_vs_cg64"] = round(base["step_ms"] / v["step_ms"], 2)
+        v["ppe_x_vs_cg64"] = round(base["ppe_ms"] / v["ppe_ms"], 2)
+    out["note"] = ("one snapshot, %d steps per solver, L2 flushed before each step, PPE to 1e-8 |b|: cg64 = FP64 CG "
+                   "(reference algorithm), mixed = FP32 CG + FP64 reliable updates, mg = mixed preconditioned by "
+                   "the cell multigrid, learned = mg started from the network's guess and Jacobi scale" % steps)
     return out
 
 
@@ -647,7 +688,9 @@ def batched_workload(device, nscenes, steps):
 
 # ------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
-    """The CPU restatement of the reference step (OpenMP, all host threads)."""
+    """The CPU restatement of the reference step (OpenMP, all host threads), over the same
+    simulation steps as the GPU arm: `--warmup` untimed steps from the initial state, then
+    `--steps` timed ones."""
     if rank != 0:
         return
     from openmps_gb300 import _abi as abi
@@ -656,21 +699,20 @@ def run_reference(args, rank, world):
     scene = scenes.config_c2()
     dt = scene.meta["dt"]
     params = scene.params(criterion=abi.CRIT_RHS, eps=1e-8)
-    steps = max(1, min(args.steps, 5))
-    cb = cpu_baseline(scene, params, dt, budget_s=1e9, max_steps=steps)
+    warmup = max(args.warmup, 0)
+    cb = cpu_baseline(scene, params, dt, budget_s=1e9, warmup=warmup, max_steps=max(1, args.steps))
     line = {
-        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world, "steps": steps,
-        "warmup": 0, "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
+        "metric": METRIC_FULL, "value": cb["value"], "unit": UNIT, "n_gpus": world, "steps": max(1, args.steps),
+        "warmup": warmup, "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded lattice dam break)",
-        "config": {"workload": "2D dam break, 320,000 fluid + 20,050 wall/dummy particles, l0=5e-4 m, "
-                               "reference MPS scheme (HS, HL, ECS, DS, SPP), re=2.1 l0 / re_lap=4.0 l0, dt=2.5e-5 s",
-                   "ppe_tolerance": "|b-Ax| <= 1e-8 |b|",
-                   "note": "the reference (header-only C++ with Boost/ViennaCL) cannot be built here; "
-                           "this arm runs its C++ restatement with OpenMP"},
+        "config": workload_config(scene.count, world),
         "impl": "reference",
+        "solver": "cg64",
+        "note": "the reference (header-only C++ with Boost/ViennaCL) cannot be built here; this arm runs its "
+                "C++ restatement (the oracle) with OpenMP on all host cores",
         "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
-                         "sample": cb["sample"]},
+                         "cpu_model": cb["cpu_model"], "sample": cb["sample"]},
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

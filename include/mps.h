@@ -241,6 +241,16 @@ int mps_get_stats(const mps_handle* h, mps_stats* st);
 int mps_set_solver(mps_handle* h, int32_t solver, int32_t criterion, double eps);
 /* Enables per-stage CUDA-event timing (stats.stage_ms). */
 int mps_set_stage_timing(mps_handle* h, int32_t enable);
+/* Bounds of the handle's device-side waits, in SM clock cycles (negative: the default).
+ * No counterpart in the reference, which has no device waits.  barrier_clocks bounds
+ * each grid-barrier wait of the persistent preconditioned solve (MPS_CG_LAUNCH_PERSISTENT;
+ * default 4e9, about two seconds); mma_clocks bounds each tensor-core completion wait of
+ * the learned solve's network inference (default 2e9).  A wait that runs out sets an
+ * error word and lets its kernel return: the step still completes (the network's
+ * output is not used, or the FP64 CG finishes the solve), and mps_forward_time returns
+ * MPS_ERR_TIMEOUT.  The handle stays usable.  0 makes every such wait give up at its
+ * first check, which tests use to exercise this path. */
+int mps_set_wait_limits(mps_handle* h, int64_t barrier_clocks, int64_t mma_clocks);
 
 /* ------------------------------------------------- timing on the handle's stream */
 int mps_synchronize(mps_handle* h);
@@ -317,10 +327,13 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
  *
  * All pointers are device pointers on the current device; `stream` is a
  * cudaStream_t (NULL: the default stream); x holds the initial guess on entry and the
- * solution on return.  The first call on a device resolves the scratch array's
- * address (cudaGetSymbolAddress) and should come before any stream capture.  Every
- * call shares the one array: calls that overlap on the GPU (other streams or host
- * threads at the same time) race.  The call returns when the solve is complete.
+ * solution on return.  Every call looks up the scratch array's address in the current
+ * context (cudaGetSymbolAddress, which allocates nothing), so a device reset or another
+ * context on the same device never leaves it a stale address; the first call in a
+ * context may load the library's module and should come before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (other streams or
+ * host threads at the same time) race.  The call returns when the solve is complete.
+ * NULL pointers return MPS_ERR_INVALID_ARGUMENT.
  * ---------------------------------------------------------------------- */
 #define MPS_NOALLOC_MAX_ROWS 262144
 int mps_cg_solve_csr_device_noalloc(int64_t n, const int64_t* row_ptr, const int32_t* col,

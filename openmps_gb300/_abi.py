@@ -46,6 +46,8 @@ SOLVER_CG64 = 0
 SOLVER_MIXED = 1
 SOLVER_LEARNED = 2
 SOLVER_MIXED_MG = 3
+SOLVER_NAMES = {SOLVER_CG64: "cg64", SOLVER_MIXED: "mixed", SOLVER_LEARNED: "learned",
+                SOLVER_MIXED_MG: "mixed_mg"}
 
 MLP_BLOB_FLOATS = 9570
 MLP_SAMPLE_FLOATS = 18

@@ -60,6 +60,7 @@ PROTOTYPES = {
     "mps_get_stats": (C.c_int, [_P, C.POINTER(abi.MpsStats)]),
     "mps_set_solver": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double]),
     "mps_set_stage_timing": (C.c_int, [_P, C.c_int32]),
+    "mps_set_wait_limits": (C.c_int, [_P, C.c_int64, C.c_int64]),
     "mps_synchronize": (C.c_int, [_P]),
     "mps_event_record": (C.c_int, [_P, C.c_int32]),
     "mps_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
@@ -283,6 +284,10 @@ class Computer:
 
     def set_stage_timing(self, enable: bool):
         self._check(self.lib.mps_set_stage_timing(self.h, 1 if enable else 0))
+
+    def set_wait_limits(self, barrier_clocks: int = -1, mma_clocks: int = -1):
+        """Bounds of the device-side waits in SM clocks (negative: the default)."""
+        self._check(self.lib.mps_set_wait_limits(self.h, barrier_clocks, mma_clocks))
 
     # --------------------------------------------------------------- timing
     def synchronize(self):

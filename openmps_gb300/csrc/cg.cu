@@ -705,16 +705,15 @@ struct GridSync {
     unsigned* count;
     unsigned* gen;
     int32_t* err;
+    const WaitLimits* limits;  // null: kDefaultBarrierClocks
 };
-
-constexpr long long kBarrierClocks = 4000000000LL;  // about two seconds
 
 // Two-level arrival: blocks count in groups of kBarrierGroup, the last block of a group
 // counts at the top, and the last group releases everyone by advancing the generation.
 // `count` holds one counter per group plus the top one (all zero between barriers).
 constexpr int kBarrierGroup = 16;
 
-__device__ __forceinline__ bool grid_barrier(const GridSync& g, unsigned& gen) {
+__device__ __forceinline__ bool grid_barrier(const GridSync& g, unsigned& gen, long long limit) {
     __shared__ int err_s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -735,7 +734,7 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& g, unsigned& gen) {
         }
         const long long t0 = clock64();
         while (*reinterpret_cast<volatile unsigned*>(g.gen) != target) {
-            if (clock64() - t0 > kBarrierClocks) {
+            if (clock64() - t0 >= limit) {
                 atomicExch(g.err, 1);
                 break;
             }
@@ -750,6 +749,7 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& g, unsigned& gen) {
 
 struct PersistentState {
     unsigned gen;
+    long long limit;  // barrier wait bound in SM clocks
     int gtid, nthreads, gwarp, nwarps, lane;
 };
 
@@ -777,7 +777,7 @@ __device__ __noinline__ bool persistent_sum3(double a, double b, double c, const
             o.partials[2 * gridDim.x + blockIdx.x] = s2;
         }
     }
-    if (!grid_barrier(g, P.gen)) return false;
+    if (!grid_barrier(g, P.gen, P.limit)) return false;
     if (threadIdx.x < 32) {
         double x = 0.0, y = 0.0, z = 0.0;
         for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += 32) {
@@ -823,13 +823,13 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
         for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(kFull, sum, k);
         if (P.lane == 0) L1.r[c] = sum;
     }
-    if (!grid_barrier(g, P.gen)) return false;
+    if (!grid_barrier(g, P.gen, P.limit)) return false;
     for (int l = 1; l < mg.levels; l++) {
         const MgLevel& f = mg.lv[l];
         const MgLevel& cl = mg.lv[l + 1];
         for (int I = P.gtid; I < cl.cells; I += P.nthreads)
             cl.r[I] = child_residuals(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, I / cl.nz, I - (I / cl.nz) * cl.nz);
-        if (!grid_barrier(g, P.gen)) return false;
+        if (!grid_barrier(g, P.gen, P.limit)) return false;
     }
     {
         const MgLevel& Lc = mg.lv[mg.levels];
@@ -840,13 +840,13 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
             for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(kFull, v, off);
             if (P.lane == 0) Lc.e[row] = v;
         }
-        if (!grid_barrier(g, P.gen)) return false;
+        if (!grid_barrier(g, P.gen, P.limit)) return false;
     }
     for (int l = mg.levels - 1; l >= 2; l--) {
         const MgLevel& f = mg.lv[l];
         for (int ch = P.gtid; ch < f.cells; ch += P.nthreads)
             f.e[ch] = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, mg.lv[l + 1].nz, mg.lv[l + 1].e, ch);
-        if (!grid_barrier(g, P.gen)) return false;
+        if (!grid_barrier(g, P.gen, P.limit)) return false;
     }
     if (mg.levels > 1) {
         const MgLevel& c2 = mg.lv[2];
@@ -871,7 +871,7 @@ __device__ __noinline__ bool persistent_cycle(const CgOperands& o, const MgHiera
             }
         }
     }
-    return grid_barrier(g, P.gen);
+    return grid_barrier(g, P.gen, P.limit);
 }
 
 // w = A u; gamma = r.u, delta = w.u, rho = r.r (FP64), the same in every block
@@ -900,7 +900,7 @@ __device__ __noinline__ bool persistent_true(const CgOperands& o, const GridSync
         o.x[i] += static_cast<double>(o.d32[i]);
         o.d32[i] = 0.0f;
     }
-    if (!grid_barrier(g, P.gen)) return false;
+    if (!grid_barrier(g, P.gen, P.limit)) return false;
     double v = 0.0;
     for (int c = P.gwarp; c < o.nchunks; c += P.nwarps) {
         const int i = kSellRows * c + P.lane;
@@ -926,6 +926,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_pcg_persistent(CgOperands o, MgHi
     __syncthreads();
     PersistentState P;
     P.gen = gen0;
+    P.limit = g.limits ? g.limits->barrier_clocks : kDefaultBarrierClocks;
     P.gtid = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
     P.nthreads = static_cast<int>(gridDim.x * blockDim.x);
     P.gwarp = P.gtid >> 5;
@@ -1052,7 +1053,7 @@ void learned_prep_tail(const LearnedOps& L, const CgOperands& o, const MgHierarc
     k_pmx_spmv<<<o.grid_spmv, kBlock, 0, s>>>(p, 0, 0, 0, 0);  // alpha0 = r0.u0 / (A u0).u0
     launch_learned_feature_rows(L, p, S, s);
     if (infer) {
-        launch_mlp_infer(L.packed, L.feat, L.n, L.sigma, L.out, L.error, s);
+        launch_mlp_infer(L.packed, L.feat, L.n, L.sigma, L.out, L.error, s, L.limits);
         launch_learned_apply(L, p, S, s);
     }
 }
@@ -1373,7 +1374,7 @@ cudaError_t CgGraph::build_persistent(int solver, const CgOperands& ops, cudaStr
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        GridSync g{ps.count, ps.gen, ps.err};
+        GridSync g{ps.count, ps.gen, ps.err, ps.limits};
         cudaLaunchKernelEx(&cfg, k_pcg_persistent, ops, *mg, g);
     }
     k_cg_init<<<gs, kBlock, 0, s>>>(*fb, h_fb, 1, ops.S);

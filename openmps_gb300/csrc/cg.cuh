@@ -72,6 +72,20 @@ struct CgOperands {
 struct MgHierarchy;
 struct LearnedOps;
 
+// Bounds of the device-side waits, in SM clock cycles, kept in device memory per handle
+// so that captured graphs read the current values.  A wait gives up once this many
+// cycles have passed since it began (0: at its first check), sets an error word and
+// lets its kernel return; the host turns the word into MPS_ERR_TIMEOUT.
+struct WaitLimits {
+    long long barrier_clocks;  // grid barrier of the persistent preconditioned solve
+    long long mma_clocks;      // tensor-core completion wait of the network inference
+};
+constexpr long long kDefaultBarrierClocks = 4000000000LL;  // about two seconds
+constexpr long long kDefaultMmaClocks = 2000000000LL;      // about one second
+// After a tensor-core wait gave up, the MMAs it waited for may still write TMEM: the
+// kernel waits this long again for their completion before it frees TMEM.
+constexpr long long kMmaDrainClocks = 2000000000LL;
+
 // Device words of the persistent solve's grid barrier, and its grid size.
 constexpr int kPersistentCounters = 513;  // barrier group counters + the top one
 
@@ -80,6 +94,7 @@ struct PersistentSync {
     unsigned* gen;
     int32_t* err;     // set when a barrier wait runs out
     int blocks;
+    const WaitLimits* limits;  // null: the defaults
 };
 
 // The learned start of a solve: its device state and the scalars its kernels gate on.

@@ -10,8 +10,10 @@
 // padded output layer) into 64 TMEM columns and commits them to an mbarrier; every
 // thread then reads its own row of the accumulator (tcgen05.ld 32x32b: warp w owns TMEM
 // lanes 32w..32w+31), adds the bias, applies GELU, rounds to BF16 and writes the row
-// back as the next layer's A operand.  Waits are bounded: a wait that gives up sets an
-// error word, the CTA frees its TMEM and returns, and the solve uses no network output.
+// back as the next layer's A operand.  Waits are bounded (WaitLimits::mma_clocks): a
+// wait that gives up waits once more, within kMmaDrainClocks, for the MMAs it issued to
+// complete, sets an error word, frees its TMEM and returns; the solve then uses no
+// network output.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -25,7 +27,6 @@ namespace {
 
 constexpr int kTile = 128;
 constexpr int kTmemCols = 64;
-constexpr uint32_t kWaitLimit = 1u << 20;
 
 // tensor-core weight image (bytes)
 constexpr int kImgW1 = 0;                       // N 64 x K 16
@@ -138,7 +139,7 @@ __device__ __forceinline__ void store_row8(unsigned char* base, int rows, int r,
 __global__ void __launch_bounds__(kTile) k_mlp_tc(const unsigned char* __restrict__ image,
                                                   const float* __restrict__ feat, int n,
                                                   const double* sigma, float* __restrict__ out,
-                                                  int32_t* error) {
+                                                  int32_t* error, const WaitLimits* limits) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int t = threadIdx.x, warp = t >> 5;
     unsigned char* A0 = sm + kSmA0;
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_tc(const unsigned char* __restric
     const float* mu = reinterpret_cast<const float*>(img + kImgNorm);
     const float* sd = mu + 16;
     const float inv_sigma = sigma ? static_cast<float>(1.0 / sigma[0]) : 1.0f;
+    const long long wait_clocks = limits ? limits->mma_clocks : kDefaultMmaClocks;
     const uint32_t aA0 = smem_u32(A0), aA = smem_u32(A), aImg = smem_u32(img);
     uint32_t phase = 0;
     bool bad = false;
@@ -228,11 +230,20 @@ __global__ void __launch_bounds__(kTile) k_mlp_tc(const unsigned char* __restric
                 }
                 mma_commit(bar);
             }
-            uint32_t spins = 0;
-            while (!bar_try_wait(bar, phase)) {
-                if (++spins > kWaitLimit) {
+            // the bound is checked before each poll, so a bound of 0 gives up at once
+            const long long t0 = clock64();
+            for (;;) {
+                if (clock64() - t0 >= wait_clocks) {
                     bad = true;
                     break;
+                }
+                if (bar_try_wait(bar, phase)) break;
+            }
+            if (bad) {
+                // the layer's MMAs may still be writing TMEM: wait for their commit
+                // (bounded) before the CTA frees TMEM below
+                const long long t1 = clock64();
+                while (!bar_try_wait(bar, phase) && clock64() - t1 < kMmaDrainClocks) {
                 }
             }
             phase ^= 1u;
@@ -280,6 +291,8 @@ __device__ __forceinline__ bool lrn_skip(const CgScalars* S) { return S->aborted
 __global__ void __launch_bounds__(kBlock) k_lrn_q(LearnedOps L, CgOperands o, const float* dinv0,
                                                   const StepScalars* step, const CgScalars* S,
                                                   float4* q4, float2* q2) {
+    // each solve starts with a clear tensor-core error word (read by the host after it)
+    if (blockIdx.x == 0 && threadIdx.x == 0) *L.error = 0;
     if (lrn_skip(S)) return;
     const double dt = step->dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += gridDim.x * blockDim.x) {
@@ -712,10 +725,11 @@ void launch_learned_targets(const LearnedOps& L, const CgOperands& o, const CgSc
 }
 
 void launch_mlp_infer(const void* packed, const float* feat, int n, const double* sigma, float* out,
-                      int32_t* error, cudaStream_t s) {
+                      int32_t* error, cudaStream_t s, const WaitLimits* limits) {
     const int tiles = (n + kTile - 1) / kTile;
     const int grid = tiles < 4 * 152 ? (tiles > 0 ? tiles : 1) : 4 * 152;
-    k_mlp_tc<<<grid, kTile, kSmBytes, s>>>(static_cast<const unsigned char*>(packed), feat, n, sigma, out, error);
+    k_mlp_tc<<<grid, kTile, kSmBytes, s>>>(static_cast<const unsigned char*>(packed), feat, n, sigma, out, error,
+                                           limits);
 }
 
 int mlp_train_blocks(int64_t n) {

@@ -49,7 +49,8 @@ struct LearnedOps {
     double* sigma = nullptr;       // [0] sigma, [1] partial scratch count
     double* partials = nullptr;    // per-block partial sums
     uint32_t* counter = nullptr;   // last-block ticket
-    int32_t* error = nullptr;      // tensor-core wait timed out (1)
+    int32_t* error = nullptr;      // tensor-core wait timed out (1), cleared by each solve
+    const WaitLimits* limits = nullptr;  // the handle's wait bounds (null: defaults)
     float4* q4 = nullptr;          // n per-particle quantities averaged over neighbours
     float2* q2 = nullptr;
     double* x0d = nullptr;         // n FP64 copy of the assembled initial guess
@@ -81,7 +82,7 @@ void launch_learned_feature_rows(const LearnedOps& L, const CgOperands& o, const
 // Network inference on the tensor cores: out = MLP(features).  The residual features
 // (8, 9, 10) are divided by sigma[0] (sigma null: used as given).
 void launch_mlp_infer(const void* packed, const float* feat, int n, const double* sigma,
-                      float* out, int32_t* error, cudaStream_t s);
+                      float* out, int32_t* error, cudaStream_t s, const WaitLimits* limits = nullptr);
 // The whole learned start of a solve: r0 (FP64, into o.r32 with S as scratch scalars),
 // u0 = M r0 without learned scales, the CG step size alpha0 of u0, features, and with
 // `infer` the network, the warm start and the scales.

@@ -79,6 +79,8 @@ struct mps_handle {
     std::vector<int32_t> tune_threads, tune_order;
     PersistentSync psync{};      // grid barrier words of the persistent solve
     bool persistent_failed = false;
+    WaitLimits* d_limits = nullptr;  // bounds of the device-side waits (mps_set_wait_limits)
+    int32_t* h_wait_err = nullptr;   // pinned: [0] tensor-core wait, [1] grid barrier gave up
     cudaGraphExec_t batch_graph = nullptr;
     double batch_graph_dt = 0.0;
     int64_t batch_step_launches = 0;
@@ -474,10 +476,12 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     L.step = st.step;
     L.dinv0 = mg.dinv0;
     L.flags = sc.flags;
+    L.limits = h->d_limits;
     h->S_lrn = dalloc<CgScalars>(h, 1);
     h->psync.count = dalloc<unsigned>(h, kPersistentCounters);
     h->psync.gen = dalloc<unsigned>(h, 1);
     h->psync.err = dalloc<int32_t>(h, 1);
+    h->psync.limits = h->d_limits;
     cudaStream_t s = h->stream;
     // zero everything persistent, then carry the old contents over
     check(cudaMemsetAsync(st.type, 0, sizeof(int32_t) * n, s), "memset");
@@ -602,8 +606,17 @@ void read_status(mps_handle* h, bool solve_done) {
           "status");
     check(cudaMemcpyAsync(h->h_step, h->st.step, sizeof(StepScalars), cudaMemcpyDeviceToHost, s),
           "status");
+    const bool learned_ran = solve_done && h->prm.solver == MPS_SOLVER_LEARNED && h->lrn.error;
+    const bool persistent_ran = solve_done && is_preconditioned(h->prm.solver) && h->cg.persistent() &&
+                                h->direct_launches < 0 && h->psync.err;
+    h->h_wait_err[0] = h->h_wait_err[1] = 0;
     if (solve_done)
         check(cudaMemcpyAsync(h->h_S, h->S, sizeof(CgScalars), cudaMemcpyDeviceToHost, s), "status");
+    if (learned_ran)
+        check(cudaMemcpyAsync(h->h_wait_err, h->lrn.error, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "status");
+    if (persistent_ran)
+        check(cudaMemcpyAsync(h->h_wait_err + 1, h->psync.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+              "status");
     check(cudaStreamSynchronize(s), "step");
     h->t = h->h_step->t;
     h->dt = h->h_step->dt;
@@ -643,6 +656,13 @@ void read_status(mps_handle* h, bool solve_done) {
                       h->h_status->check_index);
         throw StatusError{MPS_ERR_DEVICE_CHECK, buf};
     }
+    // a bounded wait that gave up: the solve went on without what it waited for (the
+    // network's output, or the persistent iteration, which the FP64 CG replaced)
+    if (h->h_wait_err[0])
+        throw StatusError{MPS_ERR_TIMEOUT, "tensor-core wait timed out: the solve ran without the network"};
+    if (h->h_wait_err[1])
+        throw StatusError{MPS_ERR_TIMEOUT,
+                          "grid barrier wait timed out: the FP64 CG finished the persistent solve"};
     if (solve_done && !h->h_S->converged)
         throw StatusError{MPS_ERR_CG_NOT_CONVERGED,
                           "Conjugate Gradient method couldn't solve Pressure Poison Equation"};
@@ -1213,6 +1233,11 @@ int mps_create(const mps_params* prm, int device, mps_handle** out) {
         check(cudaMallocHost(reinterpret_cast<void**>(&h->h_status), sizeof(DevStatus)), "pinned");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->h_S), sizeof(CgScalars)), "pinned");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->h_step), sizeof(StepScalars)), "pinned");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->h_wait_err), 2 * sizeof(int32_t)), "pinned");
+        h->h_wait_err[0] = h->h_wait_err[1] = 0;
+        check(cudaMalloc(reinterpret_cast<void**>(&h->d_limits), sizeof(WaitLimits)), "wait limits");
+        const WaitLimits defaults{kDefaultBarrierClocks, kDefaultMmaClocks};
+        check(cudaMemcpy(h->d_limits, &defaults, sizeof(defaults), cudaMemcpyHostToDevice), "wait limits");
     });
     if (rc != MPS_OK) {
         mps_destroy(h);
@@ -1238,6 +1263,8 @@ int mps_destroy(mps_handle* h) {
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->h_S) cudaFreeHost(h->h_S);
     if (h->h_step) cudaFreeHost(h->h_step);
+    if (h->h_wait_err) cudaFreeHost(h->h_wait_err);
+    if (h->d_limits) cudaFree(h->d_limits);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return MPS_OK;
@@ -1454,6 +1481,16 @@ int mps_set_solver(mps_handle* h, int32_t solver, int32_t criterion, double eps)
         p.eps = eps;
         validate(p);
         h->prm = p;
+    });
+}
+
+int mps_set_wait_limits(mps_handle* h, int64_t barrier_clocks, int64_t mma_clocks) {
+    if (!h) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        const WaitLimits w{barrier_clocks < 0 ? kDefaultBarrierClocks : static_cast<long long>(barrier_clocks),
+                           mma_clocks < 0 ? kDefaultMmaClocks : static_cast<long long>(mma_clocks)};
+        check(cudaMemcpyAsync(h->d_limits, &w, sizeof(w), cudaMemcpyHostToDevice, h->stream), "wait limits");
+        check(cudaStreamSynchronize(h->stream), "wait limits");
     });
 }
 

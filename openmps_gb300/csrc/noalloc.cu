@@ -13,14 +13,18 @@
 // device array of fixed size (kNoallocMaxRows rows).  Every GPU that loads the library
 // holds that array until the process exits.
 //
-// The host obtains the array's device address with cudaGetSymbolAddress once per
-// device, on the first call made with that device current, and passes it to the
-// kernels.  Every call shares the array and finds the previous call's contents; the
-// parts that must start at zero are cleared at the start of each call.  Calls that
-// overlap on the GPU (different streams or host threads at the same time) race on
-// the array.
+// In host code the array's name stands for a host-side shadow, not a device address.
+// Each call therefore asks the runtime for the array's address in the current device's
+// context (cudaGetSymbolAddress, a lookup that allocates nothing) and passes it to the
+// kernels.  The address is not cached: after cudaDeviceReset, or with another context
+// current on the same device, the module is loaded again and the array can move, so a
+// cached address would point at memory this context does not own.  The first call in a
+// context may load the library's module (lazy module loading), so make that first call
+// before any stream capture.  Every call shares the array and finds the previous
+// call's contents; the parts that must start at zero are cleared at the start of each
+// call.  Calls that overlap on the GPU (different streams or host threads at the same
+// time) race on the array.
 #include <cmath>
-#include <mutex>
 
 #include "common.cuh"
 
@@ -227,24 +231,14 @@ __global__ void k_na_true(double* base, int64_t n, const int64_t* rp, const int3
     }
 }
 
-// Device address of g_noalloc_scratch per device, resolved on the first call.
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-double* g_scratch_addr[kMaxDevices] = {};
-
-int scratch_for_current_device(double** out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MPS_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
-            cudaGetLastError();
-            return MPS_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = static_cast<double*>(ptr);
+// Device address of g_noalloc_scratch in the current context, looked up on every call.
+int scratch_for_current_context(double** out) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return MPS_ERR_CUDA;
     }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<double*>(ptr);
     return MPS_OK;
 }
 
@@ -259,11 +253,11 @@ extern "C" int mps_cg_solve_csr_device_noalloc(int64_t n, const int64_t* row_ptr
                                                void* stream, int32_t* iterations,
                                                double* true_relres) {
     using namespace mpsgb;
-    if (n <= 0 || !row_ptr || !b || !x) return MPS_ERR_INVALID_ARGUMENT;
+    if (n <= 0 || !row_ptr || !col || !val || !b || !x) return MPS_ERR_INVALID_ARGUMENT;
     if (n > kNoallocMaxRows) return MPS_ERR_NOALLOC_TOO_LARGE;
     if (criterion != MPS_CRIT_INITIAL_RESIDUAL && criterion != MPS_CRIT_RHS) return MPS_ERR_INVALID_ARGUMENT;
     double* base = nullptr;
-    const int rc = scratch_for_current_device(&base);
+    const int rc = scratch_for_current_context(&base);
     if (rc != MPS_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int grid = static_cast<int>((n + kBlock - 1) / kBlock);

@@ -8,7 +8,7 @@ holds the reference source tree; the GPU tests only read the .npz files).
   l0 = 0.001 m (the CSV shipped beside the reference's sources).
 
 Particle arrays keep the parsed doubles as they are.  Usage:
-    python tests/golden/make_reference_fixtures.py /root/reference
+    python tests/golden/make_reference_fixtures.py <root of the OpenMps source tree>
 """
 import os
 import re

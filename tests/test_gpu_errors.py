@@ -51,3 +51,49 @@ def test_invalid_arguments(gpu_lib):
         c.forward_time(1e-3)  # no particles yet
     with pytest.raises(ComputerError):
         c.add_particles(np.array([7]), np.zeros(1), np.zeros(1))  # bad type
+
+
+def _wait_limit_case(solver, launch):
+    from helpers import stock_tank
+    from openmps_gb300 import learned
+
+    s = stock_tank()
+    c = Computer(s.params(eps=1e-10, solver=solver, criterion=abi.CRIT_RHS, cg_launch=launch))
+    if solver == abi.SOLVER_LEARNED:
+        c.learned_set_weights(learned.load())
+    c.add_scene(s)
+    c.forward_time(s.meta["dt"])  # one ordinary step first
+    return s, c
+
+
+@pytest.mark.parametrize("which", ["mma", "barrier"])
+def test_bounded_wait_runs_out(gpu_lib, which):
+    # A wait bound of 0 cycles makes every tensor-core completion wait (learned solve) or
+    # every grid-barrier wait that is not already released (persistent solve) give up at
+    # its first check.  The kernel records the timeout and returns (the tensor-core
+    # kernel first waits, bounded, for the MMAs it issued, then frees TMEM); the step
+    # completes without the part that waited and the call reports MPS_ERR_TIMEOUT.
+    # With the default bounds restored the same handle steps normally.
+    if which == "mma":
+        s, c = _wait_limit_case(abi.SOLVER_LEARNED, abi.CG_LAUNCH_GRAPH)
+        c.set_wait_limits(mma_clocks=0)
+    else:
+        s, c = _wait_limit_case(abi.SOLVER_MIXED_MG, abi.CG_LAUNCH_PERSISTENT)
+        c.set_wait_limits(barrier_clocks=0)
+    t0 = c.environment().t
+    with pytest.raises(ComputerError) as e:
+        c.forward_time(s.meta["dt"])
+    assert e.value.code == abi.MPS_ERR_TIMEOUT, e.value
+    st = c.stats()
+    # the step finished: time advanced and the FP64 true residual meets the tolerance
+    assert c.environment().t > t0
+    assert st["cg_true_relres"] <= 1e-10
+    if which == "barrier":
+        assert st["fallback"] == 1
+    P = c.particles()
+    assert all(np.all(np.isfinite(P[k])) for k in ("x", "z", "u", "w", "p"))
+    c.set_wait_limits()
+    for _ in range(2):
+        c.forward_time(s.meta["dt"])
+    st = c.stats()
+    assert st["fallback"] == 0 and st["cg_true_relres"] <= 1e-10
