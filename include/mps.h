@@ -231,6 +231,11 @@ int mps_set_wall_positions3(mps_handle* h, const double* wx, const double* wy, c
 /* ForwardTime(double dt) (Computer.hpp:1700-1742); dt <= 0 selects ForwardTime()
  * (Computer.hpp:1745-1751) with the CFL time step of DetermineDt (:759-777). */
 int mps_forward_time(mps_handle* h, double dt);
+/* DetermineDt (Computer.hpp:759-777): the CFL time step mps_forward_time(h, 0) would take
+ * from the current state, without advancing.  A caller that evaluates moving-wall
+ * positions on the host for the step (positionWall(i, t, dt), Computer.hpp:1015) needs
+ * dt first; mps_forward_time(h, *dt) then takes exactly that step. */
+int mps_determine_dt(mps_handle* h, double* dt);
 /* nsteps calls of mps_forward_time(h, dt). */
 int mps_forward_steps(mps_handle* h, double dt, int32_t nsteps);
 

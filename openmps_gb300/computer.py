@@ -56,6 +56,7 @@ PROTOTYPES = {
     "mps_debug_set_aux3": (C.c_int, [_P, _D, _D, _D, _D, _D]),
     "mps_forward_time": (C.c_int, [_P, C.c_double]),
     "mps_forward_steps": (C.c_int, [_P, C.c_double, C.c_int32]),
+    "mps_determine_dt": (C.c_int, [_P, _D]),
     "mps_get_environment": (C.c_int, [_P, C.POINTER(abi.MpsEnvironment)]),
     "mps_get_stats": (C.c_int, [_P, C.POINTER(abi.MpsStats)]),
     "mps_set_solver": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double]),
@@ -263,6 +264,12 @@ class Computer:
     def forward_time(self, dt: float | None = None):
         """``ForwardTime(dt)``; ``dt=None`` is ``ForwardTime()`` with the CFL time step."""
         self._check(self.lib.mps_forward_time(self.h, -1.0 if dt is None else float(dt)))
+
+    def determine_dt(self) -> float:
+        """The CFL time step ``ForwardTime()`` would take from the current state."""
+        dt = C.c_double()
+        self._check(self.lib.mps_determine_dt(self.h, C.byref(dt)))
+        return float(dt.value)
 
     def forward_steps(self, dt: float, nsteps: int):
         self._check(self.lib.mps_forward_steps(self.h, float(dt), int(nsteps)))

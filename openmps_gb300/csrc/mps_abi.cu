@@ -1423,6 +1423,31 @@ int mps_set_wall_positions(mps_handle* h, const double* wx, const double* wz) {
     });
 }
 
+int mps_determine_dt(mps_handle* h, double* dt) {
+    if (!dt) return MPS_ERR_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        require_particles(h);
+        if (h->nscenes > 0) throw StatusError{MPS_ERR_STATE, "a batch advances with a fixed dt"};
+        cudaStream_t s = h->stream;
+        // the CFL kernels also advance t: keep the step scalars and put them back
+        check(cudaMemcpyAsync(h->h_step, h->st.step, sizeof(StepScalars), cudaMemcpyDeviceToHost, s), "step");
+        check(cudaStreamSynchronize(s), "step");
+        const StepScalars saved = *h->h_step;
+        if (is3(h))
+            launch_cfl_dt3(h->sc, h->st, s);
+        else
+            launch_cfl_dt(h->sc, h->st, s);
+        after_launch("determine dt");
+        launched(h, kLaunchesCfl);
+        check(cudaMemcpyAsync(h->h_step, h->st.step, sizeof(StepScalars), cudaMemcpyDeviceToHost, s), "step");
+        check(cudaStreamSynchronize(s), "step");
+        *dt = h->h_step->dt;
+        *h->h_step = saved;
+        check(cudaMemcpyAsync(h->st.step, h->h_step, sizeof(StepScalars), cudaMemcpyHostToDevice, s), "step");
+        check(cudaStreamSynchronize(s), "step");
+    });
+}
+
 int mps_forward_time(mps_handle* h, double dt) {
     return guarded(h, [&] { forward(h, dt); });
 }

@@ -225,13 +225,24 @@ int run(int argc, char** argv) {
     // with PRESSURE_EXPLICIT there is no eps and the sound speed c is read (Main.cpp:215-217, :263-265)
     const double eps = explicit_pressure ? xml.num_or("condition", "eps", 0.0) : xml.num("condition", "eps");
     const double steps_per_output = xml.num("environment", "minStepCountPerOutput");
-    openmps_gb300::Environment env(interval / steps_per_output, xml.num("environment", "courant"),
-                                   xml.num("environment", "g"), xml.num("environment", "rho"),
-                                   xml.num("environment", "nu"), xml.num_or("environment", "surfaceRatio", 0.97),
-                                   xml.num("environment", "r_eByl_0"), xml.num("environment", "l_0"),
-                                   xml.num("environment", "minX"), xml.num("environment", "minZ"),
-                                   xml.num("environment", "maxX"), xml.num("environment", "maxZ"),
-                                   flags);
+    // the method set is read at run time, so the environment is built from mps_params
+    // (the Environment(...) constructor takes the reference's compile-time argument list)
+    mps_params prm;
+    mps_default_params(&prm);
+    prm.max_dt = interval / steps_per_output;
+    prm.courant = xml.num("environment", "courant");
+    prm.g = xml.num("environment", "g");
+    prm.rho = xml.num("environment", "rho");
+    prm.nu = xml.num("environment", "nu");
+    prm.surface_ratio = xml.num_or("environment", "surfaceRatio", 0.97);
+    prm.re_by_l0 = xml.num("environment", "r_eByl_0");
+    prm.l0 = xml.num("environment", "l_0");
+    prm.min_x = xml.num("environment", "minX");
+    prm.min_z = xml.num("environment", "minZ");
+    prm.max_x = xml.num("environment", "maxX");
+    prm.max_z = xml.num("environment", "maxZ");
+    prm.flags = flags;
+    openmps_gb300::Environment env(prm);
     env.LaplacianRadius(xml.num_or("environment", "r_lapByl_0", 0.0));
     if (explicit_pressure) env.SoundSpeed(xml.num("environment", "c"));
     // A DIM3 input spans a y range (minY < maxY, Main.cpp:224-232); the reference's 2D
@@ -277,12 +288,12 @@ int run(int argc, char** argv) {
         size_t iteration = 0;
         const size_t end_count = static_cast<size_t>(std::ceil((end - start) / interval));
         for (size_t out = 1; out <= end_count; out++) {
-            double t = computer.GetEnvironment().t;
+            double t = computer.GetEnvironment().T();
             try {
                 next += interval;
                 while (t < next) {
                     computer.ForwardTime();
-                    t = computer.GetEnvironment().t;
+                    t = computer.GetEnvironment().T();
                     iteration++;
                 }
                 alive = write_csv(computer.Handle(), dim, out + offset);

@@ -219,15 +219,16 @@ int main() {
         q.X()[OpenMps::AXIS_Z] = z;
         ps.push_back(q);
     }
+    // the reference's argument list with the shipped switches (MPS_SPP: no surfaceRatio)
 #ifdef DIM3
-    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 0.97, 2.1, 0.01, MINX, MINY, MINZ, MAXX, MAXY, MAXZ);
+    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 2.1, 0.01, MINX, MINY, MINZ, MAXX, MAXY, MAXZ);
 #else
-    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 0.97, 2.1, 0.01, MINX, MINZ, MAXX, MAXZ);
+    OpenMps::Environment env(5e-4, 0.1, 9.8, 1000.0, 1e-6, 2.1, 0.01, MINX, MINZ, MAXX, MAXZ);
 #endif
     auto computer = OpenMps::CreateComputer(1e-10, env);
     computer.AddParticles(std::move(ps));
     for (int k = 0; k < 3; k++) computer.ForwardTime(5e-4);
-    t = computer.GetEnvironment().t;
+    t = computer.GetEnvironment().T();
     std::printf("%.17g\n", t);
     for (const auto& q : computer.Particles()) {
         for (int a = 0; a < OpenMps::kDim; a++) std::printf("%.17g ", q.X()[a]);

@@ -1,0 +1,137 @@
+"""The benchmark configurations run for their full step counts.
+
+* the 80k-fluid hydrostatic tank (84,450 particles, l0 = 2.5e-3 m, seeded lattice
+  jitter of 1e-4 l0, dt = 1e-4 s): 2000 steps with the FP64 CG and with the
+  mixed-precision (FP32 inner, FP64 refined) multigrid solver.  Averaged over the last
+  200 steps, the pressure of every fluid particle in the bulk is within 1 % of rho g h
+  of the hydrostatic rho g (h - z), for both solvers;
+* the 320k-fluid dam break (340,050 particles): 500 steps, every PPE solved to
+  |b - A x| <= 1e-8 |b| without the FP64 fallback, the state finite;
+* 256 independent dam breaks in one batch: 1000 steps, every scene converged at every
+  step without a fallback;
+* the l0 = 0.01 dam break with plain MPS (standard source and Laplacian, free-surface
+  flag n/n0 < 0.97, no DS or SPP) and the reference's CG to 1e-10: the method diverges
+  and the CG fails within the 1000 steps; the oracle, run the same way, fails with the
+  same error a few steps apart, and the two trajectories agree before the divergence.
+"""
+import numpy as np
+import pytest
+
+from helpers import rel_err
+from openmps_gb300 import _abi as abi
+from openmps_gb300 import scenes
+from openmps_gb300.computer import Batch, Computer, ComputerError
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("solver", [abi.SOLVER_MIXED_MG, abi.SOLVER_CG64])
+def test_c1_hydrostatic_pressure_2000_steps(gpu_lib, solver):
+    s = scenes.config_c1()
+    dt = s.meta["dt"]
+    steps, avg = s.meta["steps"], 200
+    c = Computer(s.params(solver=solver, criterion=abi.CRIT_RHS, eps=1e-8))
+    c.add_scene(s)
+    fluid = s.type == abi.TYPE_FLUID
+    psum = np.zeros(s.count)
+    for k in range(steps):
+        c.forward_time(dt)
+        assert c.stats()["cg_true_relres"] <= 1e-8
+        if k >= steps - avg:
+            psum += c.particles()["p"]
+    P = c.particles()
+    pbar = psum / avg
+    P0 = s.params()
+    rho, g, l0 = P0.rho, P0.g, s.l0
+    rows = s.meta["water_rows"]
+    h = (rows - 0.5) * l0  # half a spacing above the top layer
+    width = s.meta["water_cols"] * l0
+    ref = rho * g * (h - P["z"])
+    # the bulk: 10 layers below the surface, 5 from the floor and the side walls
+    bulk = fluid & (P["z"] < h - 10 * l0) & (P["z"] > 5 * l0) & (P["x"] > 5 * l0) & (P["x"] < width - 6 * l0)
+    err = np.abs(pbar - ref)[bulk] / (rho * g * h)
+    drift = float(np.max(np.hypot(P["x"] - s.x, P["z"] - s.z)[fluid]))
+    print("C1 %s: %d steps, bulk particles %d, |p - rho g (h - z)| / (rho g h): max %.3e, rms %.3e, "
+          "p99 %.3e; largest displacement %.3e l0" % (abi.SOLVER_NAMES[solver], steps, int(bulk.sum()),
+                                                    err.max(), np.sqrt(np.mean(err ** 2)),
+                                                    np.percentile(err, 99), drift / l0))
+    assert bulk.sum() > 50000
+    assert np.all(np.isfinite(P["p"]))
+    assert err.max() <= 0.01
+
+
+def test_c2_dam_break_500_steps(gpu_lib):
+    s = scenes.config_c2()
+    dt = s.meta["dt"]
+    c = Computer(s.params(solver=abi.SOLVER_MIXED_MG, criterion=abi.CRIT_RHS, eps=1e-8))
+    c.add_scene(s)
+    its = []
+    for _ in range(s.meta["steps"]):
+        c.forward_time(dt)
+        st = c.stats()
+        assert st["cg_true_relres"] <= 1e-8 and st["fallback"] == 0, st
+        its.append(st["cg_iterations"])
+    P = c.particles()
+    fluid = P["type"] == abi.TYPE_FLUID
+    assert st["disabled"] == 0
+    for k in ("x", "z", "u", "w", "p"):
+        assert np.all(np.isfinite(P[k])), k
+    front = float(np.max(P["x"][fluid]))
+    print("C2: %d steps (t = %.4f s), PPE iterations per step mean %.1f max %d, surge front x = %.4f m "
+          "(column edge at %.4f m)" % (len(its), c.environment().t, np.mean(its), max(its), front,
+                                       s.meta["water_w"] - s.l0))
+    assert front > s.meta["water_w"] - s.l0  # the column has started to collapse
+
+
+def test_c3_batch_1000_steps(gpu_lib):
+    from test_gpu_batch import DT, batch_scenes, params
+
+    sc = batch_scenes(256)
+    b = Batch(params(sc[0]), sc)
+    worst, its = 0.0, []
+    for _ in range(1000):
+        b.forward(DT, 1)
+        for k in range(len(sc)):
+            st = b.scene_stats(k)
+            assert st["converged"] == 1 and st["fallback"] == 0, (k, st)
+            worst = max(worst, st["true_relres"])
+            its.append(st["iterations"])
+    assert worst <= 1e-8
+    for k in (0, 127, 255):
+        P = b.scene(k)
+        assert all(np.all(np.isfinite(P[f])) for f in ("x", "z", "u", "w", "p"))
+    print("C3: 256 scenes x 1000 steps, PPE iterations mean %.1f max %d, worst true relres %.2e"
+          % (np.mean(its), max(its), worst))
+
+
+def test_c0_plain_mps_diverges_like_the_oracle(gpu_lib, oracle_lib):
+    from oracle.oracle import Oracle, OracleError
+
+    s = scenes.config_c0_plain()
+    dt = s.meta["dt"]
+    prm = s.params()
+    assert prm.flags == abi.PRESET_PLAIN and prm.eps == 1e-10
+    gpu = Computer(prm)
+    gpu.add_scene(s)
+    cpu = Oracle(prm)
+    cpu.add_scene(s)
+    fail = {}
+    early = None
+    for k in range(1, s.meta["steps"] + 1):
+        for name, h, exc in (("gpu", gpu, ComputerError), ("oracle", cpu, OracleError)):
+            if name in fail:
+                continue
+            try:
+                h.forward_time(dt)
+            except exc as e:
+                fail[name] = (k, e.code)
+        if k == 200 and not fail:
+            G, Cp = gpu.particles(), cpu.particles()
+            early = max(rel_err(G["x"], Cp["x"], scale=s.l0), rel_err(G["z"], Cp["z"], scale=s.l0))
+        if len(fail) == 2:
+            break
+    print("C0 plain MPS: failures %s (step, status); positions after 200 steps agree to %.2e l0" % (fail, early))
+    assert set(fail) == {"gpu", "oracle"}
+    assert fail["gpu"][1] == fail["oracle"][1] == abi.MPS_ERR_CG_NOT_CONVERGED
+    assert abs(fail["gpu"][0] - fail["oracle"][0]) <= 50
+    assert early is not None and early < 1e-6

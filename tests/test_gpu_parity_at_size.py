@@ -107,7 +107,7 @@ def test_stage_chain_at_size(gpu_lib, warmed):
     for h in (gpu, cpu):
         h.stage("set_ppe")
     assert_same_ppe(gpu, cpu, name + " assembly")
-    nnz = gpu.stats()["ppe_nnz"]
+    nnz = gpu.ppe()[1].size
     print("%s: %d particles, %d PPE nonzeros bit-identical" % (name, s.count, nnz))
     for h in (gpu, cpu):
         h.stage("solve_ppe")
