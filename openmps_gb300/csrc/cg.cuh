@@ -50,6 +50,7 @@ struct CgOperands {
     int32_t nchunks;    // chunks of kSellRows rows
     int32_t grid_vec;   // blocks of the vector kernels (one thread per row)
     int32_t grid_spmv;  // blocks of the SpMV kernels (one warp per chunk)
+    int32_t grid_staged;  // blocks of the staged SpMV kernels (one per SM; 0: not used)
     const int32_t* len; // row lengths, kSellRows * nchunks (rows >= n have length 0)
     const int32_t* off; // chunk offsets, nchunks + 1
     const int32_t* col; // SELL-32 columns
@@ -163,6 +164,8 @@ void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, 
                          cudaStream_t s);
 // One launch of the solver's SpMV kernel (the CG iteration's dominant kernel) alone.
 void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s);
+// Shared-memory opt-in of the staged SpMV kernels (once per device, before they launch).
+cudaError_t cg_prepare_device();
 // Launch shapes of the solver kernels for n rows, and the partials they need.
 int cg_grid_vec(int64_t n);
 int cg_grid_spmv(int64_t n);

@@ -33,6 +33,7 @@ constexpr int kStatusCellOverflow = 1;
 constexpr int kStatusDeviceCheck = 2;
 constexpr int kStatusCgNotConverged = 4;
 constexpr int kStatusNonFinite = 8;
+constexpr int kStatusWaitTimeout = 16;  // a bounded device wait gave up (MPS_ERR_TIMEOUT)
 
 // Per-scene constants (Environment.hpp:129-216, Grid.hpp:137-150), passed by value.
 struct SceneConst {

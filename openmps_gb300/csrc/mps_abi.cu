@@ -60,6 +60,7 @@ struct mps_handle {
     CgScalars* S_fb = nullptr;  // scalars of the FP64 fallback after a preconditioned solve
     MgHierarchy mg;             // cell multigrid (MIXED_MG, LEARNED)
     bool mg_device_ready = false;
+    bool cg_device_ready = false;  // staged SpMV kernels' shared-memory opt-in done
     // learned warm start / preconditioner scale
     LearnedOps lrn;
     CgScalars* S_lrn = nullptr;
@@ -534,11 +535,16 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
 }
 
 CgOperands cg_operands(mps_handle* h) {
+    if (!h->cg_device_ready) {
+        check(cg_prepare_device(), "SpMV kernel attributes");
+        h->cg_device_ready = true;
+    }
     CgOperands o{};
     o.n = static_cast<int32_t>(h->n);
     o.nchunks = static_cast<int32_t>(sell_chunks(h->n));
     o.grid_vec = cg_grid_vec(h->n);
     o.grid_spmv = cg_grid_spmv(h->n);
+    o.grid_staged = h->sm_count;
     o.len = h->st.ppe_len;
     o.off = h->st.ppe_off;
     o.col = h->st.ppe_col;
@@ -650,6 +656,8 @@ void read_status(mps_handle* h, bool solve_done) {
     }
     const int f = h->h_status->flags;
     if (f & kStatusCellOverflow) throw StatusError{MPS_ERR_CELL_OVERFLOW, "Too many particle in a block"};
+    if (f & kStatusWaitTimeout)
+        throw StatusError{MPS_ERR_TIMEOUT, "a shared-memory stage of the SpMV stream timed out"};
     if (f & kStatusDeviceCheck) {
         char buf[96];
         std::snprintf(buf, sizeof(buf), "device bounds check fired at particle %d",

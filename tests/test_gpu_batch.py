@@ -105,3 +105,40 @@ def test_batch_rejects_single_scene_calls(gpu_lib):
         b.forward_time(DT)
     with pytest.raises(Exception):
         b.forward(-1.0, 1)
+
+
+def test_batch_matches_oracle(gpu_lib, oracle_lib):
+    # each scene of a batch against the oracle run as its own Computer: bit-identical
+    # neighbour lists after the first search, and after five steps the same pressure and
+    # motion as the oracle's FP64 CG to the same residual
+    from oracle.oracle import Oracle
+
+    sc = batch_scenes(4, seed=31)
+    b = Batch(params(sc[0]), sc)
+    cpus = []
+    for s in sc:
+        o = Oracle(s.params(criterion=abi.CRIT_RHS, eps=1e-8))
+        o.add_scene(s)
+        cpus.append(o)
+    b.forward(DT, 1)
+    bc, bl = b.neighbors()
+    row0 = 0
+    for k, (s, o) in enumerate(zip(sc, cpus)):
+        o.forward_time(DT)
+        cc, cl = o.neighbors()
+        start = int(np.sum(bc[:row0]))
+        got = bl[start:start + int(np.sum(bc[row0:row0 + s.count]))] - row0
+        np.testing.assert_array_equal(bc[row0:row0 + s.count], cc, err_msg="counts scene %d" % k)
+        np.testing.assert_array_equal(got, cl, err_msg="lists scene %d" % k)
+        row0 += (s.count + 31) // 32 * 32
+    for _ in range(4):
+        b.forward(DT, 1)
+        for o in cpus:
+            o.forward_time(DT)
+    for k, (s, o) in enumerate(zip(sc, cpus)):
+        P, Q = b.scene(k), o.particles()
+        np.testing.assert_array_equal(P["type"], Q["type"])
+        ep = rel_err(P["p"], Q["p"])
+        ex = max(rel_err(P["x"], Q["x"], scale=L0), rel_err(P["z"], Q["z"], scale=L0))
+        print("batch scene %d (%d particles) vs oracle after 5 steps: p %.2e, x %.2e l0" % (k, s.count, ep, ex))
+        assert ep < 1e-5 and ex < 1e-6, k

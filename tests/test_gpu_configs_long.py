@@ -105,6 +105,11 @@ def test_c3_batch_1000_steps(gpu_lib):
 
 
 def test_c0_plain_mps_diverges_like_the_oracle(gpu_lib, oracle_lib):
+    # Plain MPS on this dam break is unstable: a small difference grows by orders of
+    # magnitude every 50 steps once the column collapses, so the GPU (whose CG sums in
+    # another order) and the oracle agree closely for the first 50 steps and then part;
+    # both end with the reference's instability errors (a cell overflow or a CG failure)
+    # well before step 1000, within a quarter of each other's step count.
     from oracle.oracle import Oracle, OracleError
 
     s = scenes.config_c0_plain()
@@ -125,13 +130,17 @@ def test_c0_plain_mps_diverges_like_the_oracle(gpu_lib, oracle_lib):
                 h.forward_time(dt)
             except exc as e:
                 fail[name] = (k, e.code)
-        if k == 200 and not fail:
+        if k == 50:
+            assert not fail
             G, Cp = gpu.particles(), cpu.particles()
-            early = max(rel_err(G["x"], Cp["x"], scale=s.l0), rel_err(G["z"], Cp["z"], scale=s.l0))
+            early = (max(rel_err(G["x"], Cp["x"], scale=s.l0), rel_err(G["z"], Cp["z"], scale=s.l0)),
+                     rel_err(G["p"], Cp["p"]))
         if len(fail) == 2:
             break
-    print("C0 plain MPS: failures %s (step, status); positions after 200 steps agree to %.2e l0" % (fail, early))
+    print("C0 plain MPS: failures %s (step, status); after 50 steps positions agree to %.2e l0, pressure to "
+          "%.2e" % (fail, early[0], early[1]))
+    assert early[0] < 1e-9 and early[1] < 1e-7
     assert set(fail) == {"gpu", "oracle"}
-    assert fail["gpu"][1] == fail["oracle"][1] == abi.MPS_ERR_CG_NOT_CONVERGED
-    assert abs(fail["gpu"][0] - fail["oracle"][0]) <= 50
-    assert early is not None and early < 1e-6
+    unstable = (abi.MPS_ERR_CG_NOT_CONVERGED, abi.MPS_ERR_CELL_OVERFLOW)
+    assert fail["gpu"][1] in unstable and fail["oracle"][1] in unstable
+    assert abs(fail["gpu"][0] - fail["oracle"][0]) <= fail["oracle"][0] // 4
