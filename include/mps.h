@@ -82,7 +82,8 @@ extern "C" {
 
 /* ----------------------------------------------------------- PPE solver */
 #define MPS_SOLVER_CG64 0   /* FP64 CG, the reference algorithm (Computer.hpp:1359-1429) */
-#define MPS_SOLVER_MIXED 1  /* FP32 inner CG + FP64 true residual / iterative refinement */
+#define MPS_SOLVER_MIXED 1  /* FP32 inner CG + FP64 true residual / iterative refinement; the
+                               FP64 CG finishes the solve if the true residual stops halving */
 #define MPS_SOLVER_LEARNED 2 /* MIXED_MG with the learned initial guess + diagonal scale */
 /* MIXED preconditioned by a cell-aggregation multigrid (Jacobi on the particles plus a
  * V-cycle on the neighbour-search cells), FP64 CG fallback when it stalls.  Not in the
@@ -160,7 +161,8 @@ typedef struct mps_stats {
     int32_t cg_iterations;    /* inner iterations of the last solve (all passes) */
     int32_t cg_refinements;   /* FP64 outer passes of the last solve (1 for CG64) */
     int32_t disabled;         /* particles of type Disabled after the last search */
-    int32_t fallback;         /* 1 if the last learned solve fell back to plain CG64 */
+    int32_t fallback;         /* 1 if the last mixed-precision solve (MIXED, MIXED_MG, LEARNED)
+                                 stalled and the plain FP64 CG finished it */
     double cg_rr0;            /* r_0.r_0 of the last solve */
     double cg_rr;             /* final (recursive) r.r of the last solve */
     double cg_true_relres;    /* |b - A x| / |b| recomputed in FP64 after the last solve */
@@ -310,6 +312,13 @@ int mps_debug_get_aux3(mps_handle* h, double* n_without_spp, double* ecs, double
                        double* oz);
 int mps_debug_set_aux3(mps_handle* h, const double* n_without_spp, const double* ecs,
                        const double* ox, const double* oy, const double* oz);
+
+/* The stage kernels' FP64 division and square root (computed on the FP32 and integer
+ * pipes, rounded like IEEE division and square root) on host arrays of n values, run on
+ * `device`: quot[i] = a[i] / b[i], root[i] = sqrt(a[i]).  No counterpart in the
+ * reference; tests compare them with the host's IEEE arithmetic. */
+int mps_debug_exact_arith(int32_t device, int64_t n, const double* a, const double* b, double* quot,
+                          double* root);
 
 /* SolvePressurePoissonEquation on a caller-supplied CSR system (host arrays), the
  * entry the reference's CG tests drive (test_ComputerConjugateGradient.cpp).

@@ -57,6 +57,7 @@ PROTOTYPES = {
     "mps_forward_time": (C.c_int, [_P, C.c_double]),
     "mps_forward_steps": (C.c_int, [_P, C.c_double, C.c_int32]),
     "mps_determine_dt": (C.c_int, [_P, _D]),
+    "mps_debug_exact_arith": (C.c_int, [C.c_int32, C.c_int64, _D, _D, _D, _D]),
     "mps_get_environment": (C.c_int, [_P, C.POINTER(abi.MpsEnvironment)]),
     "mps_get_stats": (C.c_int, [_P, C.POINTER(abi.MpsStats)]),
     "mps_set_solver": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double]),
@@ -456,6 +457,18 @@ def _f32(a):
 def _status(rc: int, what: str):
     if rc != abi.MPS_OK:
         raise ComputerError(rc, what)
+
+
+def exact_arith(a, b, device: int = 0):
+    """(a / b, sqrt(a)) by the stage kernels' FP64 division and square root on the GPU."""
+    lib = load_library()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    q = np.empty_like(a)
+    r = np.empty_like(a)
+    _status(lib.mps_debug_exact_arith(device, a.size, _ptr(a), _ptr(b), _ptr(q), _ptr(r)),
+            "mps_debug_exact_arith")
+    return q, r
 
 
 def mlp_infer(blob, features, device: int = 0) -> np.ndarray:

@@ -525,7 +525,15 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                 S->rr = gam;
                 S->pAp = del;
             }
-            if (mode == 2) S->do_update = 0;
+            if (mode == 2) {
+                // after a reliable update: the true residual must at least halve in norm
+                // between updates, or the FP32 iteration has stalled (the FP64 CG takes over)
+                const int stalled = S->true_rr > 0.25 * S->prev_true_rr;
+                S->prev_true_rr = S->true_rr;
+                S->stalled = stalled;
+                S->do_update = 0;
+                if (use_cond && stalled) cudaGraphSetConditional(h, 0u);
+            }
         }
     }
 }
@@ -1488,7 +1496,9 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     cudaGraphConditionalHandle h, h_fb = 0;
     e = cudaGraphConditionalHandleCreate(&h, graph_, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return e;
-    if (is_pcg(solver)) {
+    // the mixed-precision solvers end with the plain FP64 CG when they stall
+    const bool with_fb = solver != MPS_SOLVER_CG64 && fb != nullptr;
+    if (with_fb) {
         e = cudaGraphConditionalHandleCreate(&h_fb, graph_, 0, cudaGraphCondAssignDefault);
         if (e != cudaSuccess) return e;
     }
@@ -1554,14 +1564,14 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     if (solver != MPS_SOLVER_CG64) k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
-    if (is_pcg(solver)) {
+    if (with_fb) {
         k_cg_init<<<gs, kBlock, 0, s>>>(*fb, h_fb, 1, ops.S);
     } else {
         k_true_residual<<<gs, kBlock, 0, s>>>(ops, solver != MPS_SOLVER_CG64 ? 1 : 0);
     }
     e = cudaStreamEndCapture(s, &captured);
     if (e != cudaSuccess) return e;
-    if (is_pcg(solver)) {
+    if (with_fb) {
         cudaGraphNode_t fb_init;
         e = sink_node(graph_, &fb_init);
         if (e != cudaSuccess) return e;
@@ -1718,7 +1728,7 @@ cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, 
         k_mx_finish<<<gv, kBlock, 0, s>>>(ops);
         k++;
     }
-    if (is_pcg(solver)) {
+    if (solver != MPS_SOLVER_CG64 && fb) {
         k_cg_init<<<gs, kBlock, 0, s>>>(*fb, none, 0, ops.S);
         k++;
         e = host_loop(MPS_SOLVER_CG64, *fb, nullptr, host_S, chunk, s, &k);

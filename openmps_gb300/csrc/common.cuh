@@ -128,6 +128,130 @@ struct DeviceState {
     float* y32;  // FP32 copy of y (range prefilter), rewritten with y
 };
 
+// ------------------------------- FP64 division and square root off the FP64 pipe
+// GB300 issues FP64 arithmetic at a small fraction of its FP32 rate, and a correctly
+// rounded FP64 division or square root costs about as much as eight FP64 fused
+// multiply-adds there.  The stage kernels need both for every pair in range, with the
+// IEEE result bit for bit.  ddiv_rn / dsqrt_rn below compute that result on the FP32
+// and integer pipes:
+//   1. the 53-bit significands are split into float-float pairs (hi: the top 24 bits,
+//      exact; lo: the next 29 bits, rounded), and the quotient ma / mb or the root of
+//      the significand is approximated as q1 + q2 in FP32 (one Newton correction with
+//      an error-free product for q1 * hi), to about 2^-44;
+//   2. the estimate, scaled to a 53-bit integer Q', gives the exact integer remainder
+//      R = N - Q' mb (or N - S'^2) in 64-bit modular arithmetic: |Q - Q'| < 2^9 by the
+//      error bound of step 1, so |R| < 2^62 and the low 64 bits hold it exactly;
+//   3. R's top bits give the correction d ~ R / mb (off by at most one), two compares
+//      each way bring 0 <= R < mb (0 <= R <= 2S for the root), and the quotient or root
+//      rounds up when 2R > mb (R > S); ties cannot occur for a quotient or a root of
+//      53-bit significands.
+// Operands that are zero, subnormal, infinite or NaN, and results outside the normal
+// range, take __ddiv_rn / __dsqrt_rn, so every input gives the IEEE result.
+namespace exact {
+
+constexpr unsigned long long kM52 = (1ull << 52) - 1ull, kH52 = 1ull << 52;
+
+// the float of a 24-bit integer in [2^23, 2^24) (exact)
+__device__ __forceinline__ float f24(unsigned int v) { return __int_as_float((150 << 23) | (v & 0x7FFFFFu)); }
+
+// f * 2^s as an integer for |f| 2^s < 2^63 (truncated below the float's last bit)
+__device__ __forceinline__ long long fscale(float f, int s) {
+    const unsigned int u = static_cast<unsigned int>(__float_as_int(f));
+    const int e = static_cast<int>((u >> 23) & 0xFFu) - 150 + s;
+    const long long m = static_cast<long long>((u & 0x7FFFFFu) | 0x800000u);
+    long long v = e >= 0 ? (m << min(e, 63)) : (m >> min(-e, 63));
+    if ((u & 0x7FFFFFFFu) == 0u) v = 0;
+    return (u >> 31) ? -v : v;
+}
+
+}  // namespace exact
+
+// a / b, rounded to nearest even (the IEEE quotient)
+__device__ __forceinline__ double ddiv_rn(double a, double b) {
+    using namespace exact;
+    const unsigned long long ua = static_cast<unsigned long long>(__double_as_longlong(a));
+    const unsigned long long ub = static_cast<unsigned long long>(__double_as_longlong(b));
+    const int ea = static_cast<int>((ua >> 52) & 0x7FFu), eb = static_cast<int>((ub >> 52) & 0x7FFu);
+    const unsigned long long ma = (ua & kM52) | kH52, mb = (ub & kM52) | kH52;
+    const int ge = ma >= mb;
+    int e = ea - eb + 1022 + ge;
+    const int s = ge ? 52 : 53;
+    const float ah = f24(static_cast<unsigned int>(ma >> 29)), bh = f24(static_cast<unsigned int>(mb >> 29));
+    const float al = __fmul_rn(__uint2float_rn(static_cast<unsigned int>(ma & 0x1FFFFFFFu)), 0x1p-29f);
+    const float bl = __fmul_rn(__uint2float_rn(static_cast<unsigned int>(mb & 0x1FFFFFFFu)), 0x1p-29f);
+    float y = __fdividef(1.0f, bh);
+    y = __fmaf_rn(y, __fmaf_rn(-bh, y, 1.0f), y);
+    const float q1 = __fmul_rn(ah, y);
+    const float p = __fmul_rn(q1, bh);
+    const float pe = __fmaf_rn(q1, bh, -p);
+    const float rho = __fadd_rn(__fsub_rn(__fsub_rn(ah, p), pe), __fmaf_rn(-q1, bl, al));
+    const float q2 = __fmul_rn(rho, y);
+    long long Q = fscale(q1, s) + fscale(q2, s);
+    const long long B = static_cast<long long>(mb);
+    long long R = static_cast<long long>((ma << s) - static_cast<unsigned long long>(Q) * mb);
+    const int d = __float2int_rd(__fmul_rn(__fmul_rn(__int2float_rn(static_cast<int>(R >> 32)), 8.0f), y));
+    Q += d;
+    R -= static_cast<long long>(d) * B;
+    if (R < 0) { Q--; R += B; }
+    if (R < 0) { Q--; R += B; }
+    if (R >= B) { Q++; R -= B; }
+    if (R >= B) { Q++; R -= B; }
+    const bool in_range = R >= 0 && R < B;
+    if (2ull * static_cast<unsigned long long>(R) > mb) Q++;
+    if (Q == (1ll << 53)) {
+        Q = static_cast<long long>(kH52);
+        e++;
+    }
+    const bool fast = ea != 0 && ea != 2047 && eb != 0 && eb != 2047 && e >= 1 && e <= 2046 && in_range;
+    if (!fast) return __ddiv_rn(a, b);
+    return __longlong_as_double(static_cast<long long>(((ua ^ ub) & (1ull << 63)) |
+                                                       (static_cast<unsigned long long>(e) << 52) |
+                                                       (static_cast<unsigned long long>(Q) & kM52)));
+}
+
+// sqrt(x), rounded to nearest even (the IEEE square root)
+__device__ __forceinline__ double dsqrt_rn(double x) {
+    using namespace exact;
+    const unsigned long long ux = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int ex = static_cast<int>(ux >> 52);  // >= 2048 for a set sign bit
+    const unsigned long long m = (ux & kM52) | kH52;
+    const int E = ex - 1023;
+    const int odd = E & 1;
+    int e = ((E - odd) >> 1) + 1023;
+    // X = m 2^t with S = floor(sqrt(X)) in [2^52, 2^53); v = X / 2^80 = (xh + xl) in
+    // float-float, sqrt(X) = sqrt(v) 2^40
+    const int t = odd ? 53 : 52;
+    const float f = odd ? 4.0f : 2.0f;
+    const float xh = __fmul_rn(f24(static_cast<unsigned int>(m >> 29)), f);
+    const float xl = __fmul_rn(__fmul_rn(__uint2float_rn(static_cast<unsigned int>(m & 0x1FFFFFFFu)), 0x1p-29f), f);
+    const float rs = rsqrtf(xh);
+    const float s1 = __fmul_rn(xh, rs);
+    const float p = __fmul_rn(s1, s1);
+    const float pe = __fmaf_rn(s1, s1, -p);
+    const float rho = __fadd_rn(__fsub_rn(__fsub_rn(xh, p), pe), xl);
+    const float h = __fmul_rn(0.5f, rs);
+    const float s2 = __fmul_rn(rho, h);
+    long long S = fscale(s1, 40) + fscale(s2, 40);
+    const unsigned long long X = m << t;
+    long long R = static_cast<long long>(X - static_cast<unsigned long long>(S) * static_cast<unsigned long long>(S));
+    // d ~ R / (2 S) with S ~ s1 2^40: (R >> 32) 2^-9 / s1 = (R >> 32) 2^-8 h
+    S += __float2int_rd(__fmul_rn(__fmul_rn(__int2float_rn(static_cast<int>(R >> 32)), 0x1p-8f), h));
+    R = static_cast<long long>(X - static_cast<unsigned long long>(S) * static_cast<unsigned long long>(S));
+    if (R < 0) { S--; R += 2 * S + 1; }
+    if (R < 0) { S--; R += 2 * S + 1; }
+    if (R > 2 * S) { R -= 2 * S + 1; S++; }
+    if (R > 2 * S) { R -= 2 * S + 1; S++; }
+    const bool fast = ex != 0 && ex < 2047 && R >= 0 && R <= 2 * S;
+    if (R > S) S++;
+    if (S == (1ll << 53)) {
+        S = static_cast<long long>(kH52);
+        e++;
+    }
+    if (!fast) return __dsqrt_rn(x);
+    return __longlong_as_double(static_cast<long long>((static_cast<unsigned long long>(e) << 52) |
+                                                       (static_cast<unsigned long long>(S) & kM52)));
+}
+
 // --------------------------------------------------------------- helpers
 // uBLAS inner_prod of 2-vectors: t = 0; t += a0*b0; t += a1*b1, each op rounded.
 __device__ __forceinline__ double dot2(double a0, double a1, double b0, double b1) {
@@ -155,7 +279,7 @@ __device__ __forceinline__ double dist2(double dx, double dz) {
 __device__ __forceinline__ double weight(double r, double re) {
     const unsigned long long br = static_cast<unsigned long long>(__double_as_longlong(r));
     const unsigned long long be = static_cast<unsigned long long>(__double_as_longlong(re));
-    return (br - 1ull < be - 1ull) ? __dadd_rn(__ddiv_rn(re, r), -1.0) : 0.0;
+    return (br - 1ull < be - 1ull) ? __dadd_rn(ddiv_rn(re, r), -1.0) : 0.0;
 }
 
 __device__ __forceinline__ bool has_flag(uint32_t flags, uint32_t f) { return (flags & f) != 0u; }

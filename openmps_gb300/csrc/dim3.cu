@@ -34,7 +34,7 @@ __device__ __forceinline__ double dist3(double dx, double dy, double dz) {
 }
 
 __device__ __forceinline__ bool is_surface3(const SceneConst& sc, double nd) {
-    return __ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
+    return ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
 }
 
 // FP32 copies of particle i's position (the range screen reads them).
@@ -57,9 +57,9 @@ __global__ void k3_bucket(SceneConst sc, DeviceState st) {
         atomicAdd(&st.status->disabled, 1);
         return;
     }
-    const double fx = floor(__ddiv_rn(__dadd_rn(st.x[i], -sc.min_x), sc.nl));
-    const double fy = floor(__ddiv_rn(__dadd_rn(st.y[i], -sc.min_y), sc.nl));
-    const double fz = floor(__ddiv_rn(__dadd_rn(st.z[i], -sc.min_z), sc.nl));
+    const double fx = floor(ddiv_rn(__dadd_rn(st.x[i], -sc.min_x), sc.nl));
+    const double fy = floor(ddiv_rn(__dadd_rn(st.y[i], -sc.min_y), sc.nl));
+    const double fz = floor(ddiv_rn(__dadd_rn(st.z[i], -sc.min_z), sc.nl));
     if (!(fx >= 0.0 && fx < static_cast<double>(sc.gnx) && fy >= 0.0 && fy < static_cast<double>(sc.gny) &&
           fz >= 0.0 && fz < static_cast<double>(sc.gnz))) {
         st.type[i] = MPS_TYPE_DISABLED;
@@ -86,9 +86,9 @@ __global__ void k3_neighbors(SceneConst sc, DeviceState st) {
         const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
         const float xi32 = st.x32[i], yi32 = st.y32[i], zi32 = st.z32[i];
         const float si32 = (fabsf(xi32) + fabsf(yi32)) + fabsf(zi32);
-        const int bx = static_cast<int>(floor(__ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
-        const int by = static_cast<int>(floor(__ddiv_rn(__dadd_rn(yi, -sc.min_y), sc.nl)));
-        const int bz = static_cast<int>(floor(__ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
+        const int bx = static_cast<int>(floor(ddiv_rn(__dadd_rn(xi, -sc.min_x), sc.nl)));
+        const int by = static_cast<int>(floor(ddiv_rn(__dadd_rn(yi, -sc.min_y), sc.nl)));
+        const int bz = static_cast<int>(floor(ddiv_rn(__dadd_rn(zi, -sc.min_z), sc.nl)));
         for (int di = -1; di <= 1; di++) {
             const int cx = bx + di;
             if (cx < 0 || cx >= sc.gnx) continue;
@@ -112,7 +112,7 @@ __global__ void k3_neighbors(SceneConst sc, DeviceState st) {
                             const double dy = __dadd_rn(yi, -st.y[j]);
                             const double dz = __dadd_rn(zi, -st.z[j]);
                             const double r2 = dist3(dx, dy, dz);
-                            inside = (r2 < sc.nl2_lo) ? true : (r2 > sc.nl2_hi) ? false : __dsqrt_rn(r2) < sc.nl;
+                            inside = (r2 < sc.nl2_lo) ? true : (r2 > sc.nl2_hi) ? false : dsqrt_rn(r2) < sc.nl;
                         }
                         if (inside) {
                             if (cnt < sc.nb_stride) {
@@ -140,15 +140,15 @@ __device__ __forceinline__ bool spp_particle3(const SceneConst& sc, const Device
                                               double gx, double gy, double gz, double& xs, double& ys,
                                               double& zs) {
     const double thisN = st.n_wo_spp[i];
-    gx = __ddiv_rn(gx, sc.n0);
-    gy = __ddiv_rn(gy, sc.n0);
-    gz = __ddiv_rn(gz, sc.n0);
+    gx = ddiv_rn(gx, sc.n0);
+    gy = ddiv_rn(gy, sc.n0);
+    gz = ddiv_rn(gz, sc.n0);
     if (thisN < sc.n0) {
-        const double r_g = __dsqrt_rn(dot3(gx, gy, gz, gx, gy, gz));
+        const double r_g = dsqrt_rn(dot3(gx, gy, gz, gx, gy, gz));
         if (r_g > 2.220446049250313080847e-16) {  // std::numeric_limits<double>::epsilon()
             const double w_spp = __dadd_rn(sc.n0, -thisN);
-            const double r_spp = __ddiv_rn(radius, __dadd_rn(w_spp, 1.0));
-            const double s = __ddiv_rn(r_spp, r_g);
+            const double r_spp = ddiv_rn(radius, __dadd_rn(w_spp, 1.0));
+            const double s = ddiv_rn(r_spp, r_g);
             xs = __dadd_rn(st.x[i], -__dmul_rn(s, gx));
             ys = __dadd_rn(st.y[i], -__dmul_rn(s, gy));
             zs = __dadd_rn(st.z[i], -__dmul_rn(s, gz));
@@ -173,11 +173,11 @@ __device__ __forceinline__ LapFactors3 lap_factors3(const SceneConst& sc) {
     return f;
 }
 __device__ __forceinline__ double viscosity_coefficient3(const SceneConst& sc, const LapFactors3& f, double r) {
-    if (f.hl) return f.visc / (r * r * r);  // Computer.hpp:963-970
+    if (f.hl) return ddiv_rn(f.visc, r * r * r);  // Computer.hpp:963-970
     return f.visc * weight(r, sc.re_lap);
 }
 __device__ __forceinline__ double ppe_coefficient3(const SceneConst& sc, const LapFactors3& f, double r) {
-    if (f.hl) return f.ppe / (r * r * r);  // Computer.hpp:1290-1297
+    if (f.hl) return ddiv_rn(f.ppe, r * r * r);  // Computer.hpp:1290-1297
     return f.ppe * weight(r, sc.re_lap);
 }
 
@@ -197,8 +197,8 @@ __device__ double density_variation3(const SceneConst& sc, const DeviceState& st
                 const double du = st.u[j] - ui;
                 const double dv = st.v[j] - vi;
                 const double dw = st.w[j] - wi;
-                const double r = __dsqrt_rn(r2);
-                sum += dot3(dx, dy, dz, du, dv, dw) / (r * r * r);
+                const double r = dsqrt_rn(r2);
+                sum += ddiv_rn(dot3(dx, dy, dz, du, dv, dw), r * r * r);
             }
         });
         return -sc.re * sum;
@@ -230,7 +230,7 @@ __global__ void k3_density(SceneConst sc, DeviceState st) {
     double thisN = 0.0;
     for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
         const double r2 = dist3(st.x[j] - xi, st.y[j] - yi, st.z[j] - zi);
-        if (below(r2, sc.re2)) thisN += weight(__dsqrt_rn(r2), sc.re);
+        if (below(r2, sc.re2)) thisN += weight(dsqrt_rn(r2), sc.re);
     });
     if (spp) {
         st.n_wo_spp[i] = thisN;
@@ -277,7 +277,7 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
         const double r2 = dist3(dx, dy, dz);
         if (!below(r2, sc.rl2)) return;
         if (st.type[j] != MPS_TYPE_DUMMY) {
-            const double c = viscosity_coefficient3(sc, lf, __dsqrt_rn(r2));
+            const double c = viscosity_coefficient3(sc, lf, dsqrt_rn(r2));
             ax += c * (st.u[j] - ui);
             ay += c * (st.v[j] - vi);
             az += c * (st.w[j] - wi);
@@ -287,7 +287,7 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
             az = __dadd_rn(az, 0.0);
         }
         if (spp) {
-            const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+            const double wg = weight(dsqrt_rn(r2), sc.re_lap);
             gx += wg * dx;
             gy += wg * dy;
             gz += wg * dz;
@@ -296,14 +296,14 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re_lap, gx, gy, gz, xs, ys, zs)) {
         const double ddx = xi - xs, ddy = yi - ys, ddz = zi - zs;
-        const double c = viscosity_coefficient3(sc, lf, __dsqrt_rn(dot3(ddx, ddy, ddz, ddx, ddy, ddz)));
+        const double c = viscosity_coefficient3(sc, lf, dsqrt_rn(dot3(ddx, ddy, ddz, ddx, ddy, ddz)));
         ax += c * (ui - ui);
         ay += c * (vi - vi);
         az += c * (wi - wi);
     }
     if (has_flag(sc.flags, MPS_FLAG_CENTRAL_GRAVITY)) {  // Computer.hpp:981-988
         const double g = -sc.g;
-        const double r = __dsqrt_rn(dot3(xi, yi, zi, xi, yi, zi));
+        const double r = dsqrt_rn(dot3(xi, yi, zi, xi, yi, zi));
         double cx = 0.0, cy = 0.0, cz = 0.0;
         if (!(r < sc.l0 * 0.01)) {
             cx = xi / r;
@@ -397,7 +397,7 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
         const double r2 = dist3(dx, dy, dz);
         if (!below(r2, sc.rl2)) return;
         if (st.type[j] != MPS_TYPE_DUMMY) {
-            const double a_ij = ppe_coefficient3(sc, lf, __dsqrt_rn(r2));
+            const double a_ij = ppe_coefficient3(sc, lf, dsqrt_rn(r2));
             if (spp || !is_surface3(sc, st.nd[j])) {
                 st.ppe_col_tmp[ell(m, n, i)] = j;
                 st.ppe_val_tmp[ell(m, n, i)] = a_ij;
@@ -408,7 +408,7 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
             a_ii = __dadd_rn(a_ii, 0.0);
         }
         if (spp) {
-            const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+            const double wg = weight(dsqrt_rn(r2), sc.re_lap);
             gx += wg * dx;
             gy += wg * dy;
             gz += wg * dz;
@@ -417,7 +417,7 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
     double xs, ys, zs;
     if (spp && spp_particle3(sc, st, i, sc.re_lap, gx, gy, gz, xs, ys, zs)) {
         const double ddx = xi - xs, ddy = yi - ys, ddz = zi - zs;
-        a_ii += -ppe_coefficient3(sc, lf, __dsqrt_rn(dot3(ddx, ddy, ddz, ddx, ddy, ddz)));
+        a_ii += -ppe_coefficient3(sc, lf, dsqrt_rn(dot3(ddx, ddy, ddz, ddx, ddy, ddz)));
     }
     st.ppe_col_tmp[ell(m, n, i)] = i;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
@@ -479,8 +479,8 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
             const double dz = st.z[j] - zi;
             const double r2 = dist3(dx, dy, dz);
             if (!below(r2, sc.re2)) return;
-            const double wg = weight(__dsqrt_rn(r2), sc.re);
-            const double t = wg / r2;
+            const double wg = weight(dsqrt_rn(r2), sc.re);
+            const double t = ddiv_rn(wg, r2);
             m00 += t * (dx * dx);
             m01 += t * (dx * dy);
             m02 += t * (dx * dz);
@@ -497,7 +497,7 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
         if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
             const double dx = xs - xi, dy = ys - yi, dz = zs - zi;
             const double r2 = dist3(dx, dy, dz);
-            const double t = weight(__dsqrt_rn(r2), sc.re) / r2;
+            const double t = ddiv_rn(weight(dsqrt_rn(r2), sc.re), r2);
             m00 += t * (dx * dx);
             m01 += t * (dx * dy);
             m02 += t * (dx * dz);
@@ -516,9 +516,9 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
         const double dz = st.z[j] - zi;
         const double r2 = dist3(dx, dy, dz);
         if (!below(r2, sc.re2)) return;
-        const double wg = weight(__dsqrt_rn(r2), sc.re);
+        const double wg = weight(dsqrt_rn(r2), sc.re);
         if (st.type[j] != MPS_TYPE_DUMMY) {
-            const double c = (st.p[j] + pi) / r2 * wg;
+            const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
             if (kGc) {
                 sx += c * row3(C, dx, dy, dz);
                 sy += c * row3(C + 3, dx, dy, dz);
@@ -543,7 +543,7 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
     if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
         const double dx = xs - xi, dy = ys - yi, dz = zs - zi;
         const double r2 = dist3(dx, dy, dz);
-        const double c = (0.0 + pi) / r2 * weight(__dsqrt_rn(r2), sc.re);
+        const double c = ddiv_rn(0.0 + pi, r2) * weight(dsqrt_rn(r2), sc.re);
         if (kGc) {
             sx += c * row3(C, dx, dy, dz);
             sy += c * row3(C + 3, dx, dy, dz);
@@ -585,14 +585,14 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
             const double dx0 = st.ox[j] - oxi;
             const double dy0 = st.oy[j] - oyi;
             const double dz0 = st.oz[j] - ozi;
-            const double nrm = __dsqrt_rn(dot3(dx0, dy0, dz0, dx0, dy0, dz0));
-            const double ex = dx0 / nrm, ey = dy0 / nrm, ez = dz0 / nrm;
+            const double nrm = dsqrt_rn(dot3(dx0, dy0, dz0, dx0, dy0, dz0));
+            const double ex = ddiv_rn(dx0, nrm), ey = ddiv_rn(dy0, nrm), ez = ddiv_rn(dz0, nrm);
             const double r_par = dot3(dx, dy, dz, ex, ey, ez);
             const double px = dx - r_par * ex;
             const double py = dy - r_par * ey;
             const double pz = dz - r_par * ez;
             const double r_perp2 = dot3(px, py, pz, px, py, pz);
-            const double mag = __dsqrt_rn(d2 - r_perp2) - r_par;
+            const double mag = dsqrt_rn(d2 - r_perp2) - r_par;
             sx += mag * ex;
             sy += mag * ey;
             sz += mag * ez;
@@ -602,7 +602,7 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
             sz = __dadd_rn(sz, 0.0);
         }
         if (spp) {
-            const double wg = weight(__dsqrt_rn(r2), sc.re);
+            const double wg = weight(dsqrt_rn(r2), sc.re);
             gx += wg * dx;
             gy += wg * dy;
             gz += wg * dz;

@@ -632,7 +632,7 @@ void read_status(mps_handle* h, bool solve_done) {
     if (solve_done) {
         const CgScalars& S = *h->h_S;
         h->stats.cg_iterations = S.iter;
-        h->stats.fallback = is_preconditioned(h->prm.solver) ? S.fallback : 0;
+        h->stats.fallback = h->prm.solver != MPS_SOLVER_CG64 ? S.fallback : 0;
         h->stats.cg_refinements = (h->prm.solver == MPS_SOLVER_CG64) ? 1 : S.updates + 1;
         h->stats.cg_rr0 = S.rr0;
         h->stats.cg_rr = S.rr_new;
@@ -650,7 +650,8 @@ void read_status(mps_handle* h, bool solve_done) {
                 launched(h, mg_setup_launches(h->mg) + 2 + mg_apply_launches(h->mg) + loop + 3 + 3 * S.fb_iter +
                                 (h->prm.solver == MPS_SOLVER_LEARNED ? 1 + learned_prep_launches(h->mg, true) : 0));
             } else {
-                launched(h, 4 + S.iter * kpi + S.updates * kpu);
+                const int own = S.iter - S.fb_iter;
+                launched(h, 4 + own * kpi + S.updates * kpu + (S.fallback ? 2 + 3 * S.fb_iter : 1));
             }
         }
     }
@@ -738,7 +739,8 @@ void do_solve(mps_handle* h) {
         after_launch("learned features");
         launched(h, 1 + mg_setup_launches(h->mg) + learned_prep_launches(h->mg, false));
     }
-    if (pcg) {
+    const bool with_fb = solver != MPS_SOLVER_CG64;  // the FP64 CG finishes a stalled mixed solve
+    if (with_fb) {
         launch_cg_configure(h->S_fb, h->prm.eps, h->prm.criterion,
                             default_max_iter(0, h->n, MPS_SOLVER_CG64), 0.01, s);
         after_launch("cg configure");
@@ -749,7 +751,7 @@ void do_solve(mps_handle* h) {
     if (h->prm.cg_launch == MPS_CG_LAUNCH_HOST) {
         int64_t k = 0;
         check(cg_run_direct(solver, cg_operands(h), h->h_S, 16, s, &k, pcg ? &mg : nullptr,
-                            pcg ? &fb : nullptr, learned ? &run : nullptr),
+                            with_fb ? &fb : nullptr, learned ? &run : nullptr),
               "CG host loop");
         h->direct_launches = k;
     } else {
@@ -771,7 +773,7 @@ void do_solve(mps_handle* h) {
                 }
             }
             if (!built)
-                check(h->cg.build(solver, cg_operands(h), s, pcg ? &mg : nullptr, pcg ? &fb : nullptr,
+                check(h->cg.build(solver, cg_operands(h), s, pcg ? &mg : nullptr, with_fb ? &fb : nullptr,
                                   learned ? &run : nullptr),
                       "CG graph build");
         }
@@ -1972,6 +1974,33 @@ int mps_learned_samples(mps_handle* h, float* samples, int32_t* active, int64_t 
             check(cudaMemcpyAsync(active, h->lrn.active, sizeof(int32_t) * h->n, cudaMemcpyDeviceToHost, s),
                   "samples");
         check(cudaStreamSynchronize(s), "samples");
+    });
+}
+
+namespace {
+// quot[i] = a[i] / b[i] and root[i] = sqrt(a[i]) with the stage kernels' exact routines
+__global__ void k_exact_arith(int64_t n, const double* a, const double* b, double* quot, double* root) {
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    quot[i] = ddiv_rn(a[i], b[i]);
+    root[i] = dsqrt_rn(a[i]);
+}
+}  // namespace
+
+int mps_debug_exact_arith(int32_t device, int64_t n, const double* a, const double* b, double* quot, double* root) {
+    if (n <= 0 || !a || !b || !quot || !root) return MPS_ERR_INVALID_ARGUMENT;
+    return on_device(device, [&] {
+        ScopedBuffers buf;
+        double* da = buf.get<double>(static_cast<size_t>(n));
+        double* db = buf.get<double>(static_cast<size_t>(n));
+        double* dq = buf.get<double>(static_cast<size_t>(n));
+        double* dr = buf.get<double>(static_cast<size_t>(n));
+        check(cudaMemcpy(da, a, sizeof(double) * n, cudaMemcpyHostToDevice), "copy");
+        check(cudaMemcpy(db, b, sizeof(double) * n, cudaMemcpyHostToDevice), "copy");
+        k_exact_arith<<<static_cast<unsigned>((n + 255) / 256), 256>>>(n, da, db, dq, dr);
+        check(cudaGetLastError(), "exact arithmetic");
+        check(cudaMemcpy(quot, dq, sizeof(double) * n, cudaMemcpyDeviceToHost), "copy");
+        check(cudaMemcpy(root, dr, sizeof(double) * n, cudaMemcpyDeviceToHost), "copy");
     });
 }
 

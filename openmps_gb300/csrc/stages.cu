@@ -18,7 +18,7 @@ namespace mpsgb {
 namespace {
 
 __device__ __forceinline__ bool is_surface(const SceneConst& sc, double nd) {
-    return __ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
+    return ddiv_rn(nd, sc.n0) < sc.surface_ratio;  // Computer.hpp:586-589
 }
 
 // The SPP virtual particle of AccumulateNeighbor (Computer.hpp:664-692).  (gx, gz)
@@ -27,14 +27,14 @@ __device__ __forceinline__ bool spp_particle(const SceneConst& sc, const DeviceS
                                              double radius, double gx, double gz, double& xs,
                                              double& zs) {
     const double thisN = st.n_wo_spp[i];
-    gx = __ddiv_rn(gx, sc.n0);
-    gz = __ddiv_rn(gz, sc.n0);
+    gx = ddiv_rn(gx, sc.n0);
+    gz = ddiv_rn(gz, sc.n0);
     if (thisN < sc.n0) {
-        const double r_g = __dsqrt_rn(dot2(gx, gz, gx, gz));
+        const double r_g = dsqrt_rn(dot2(gx, gz, gx, gz));
         if (r_g > 2.220446049250313080847e-16) {  // std::numeric_limits<double>::epsilon()
             const double w_spp = __dadd_rn(sc.n0, -thisN);
-            const double r_spp = __ddiv_rn(radius, __dadd_rn(w_spp, 1.0));
-            const double s = __ddiv_rn(r_spp, r_g);
+            const double r_spp = ddiv_rn(radius, __dadd_rn(w_spp, 1.0));
+            const double s = ddiv_rn(r_spp, r_g);
             xs = __dadd_rn(st.x[i], -__dmul_rn(s, gx));
             zs = __dadd_rn(st.z[i], -__dmul_rn(s, gz));
             return true;
@@ -49,7 +49,7 @@ __device__ __forceinline__ void add_gravity(const SceneConst& sc, double xi, dou
                                             double& ax, double& az) {
     if (has_flag(sc.flags, MPS_FLAG_CENTRAL_GRAVITY)) {
         const double g = -sc.g;
-        const double r = __dsqrt_rn(dot2(xi, zi, xi, zi));
+        const double r = dsqrt_rn(dot2(xi, zi, xi, zi));
         double cx = 0.0, cz = 0.0;
         if (!(r < sc.l0 * 0.01)) {
             cx = xi / r;
@@ -77,8 +77,8 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
             if (below(r2, sc.re2)) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
-                const double r = __dsqrt_rn(r2);
-                sum += dot2(dx, dz, du, dw) / (r * r * r);
+                const double r = dsqrt_rn(r2);
+                sum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
             }
         });
         return -sc.re * sum;
@@ -103,13 +103,13 @@ __device__ __forceinline__ LapFactors lap_factors(const SceneConst& sc) {
 
 // viscosity coefficient (Computer.hpp:963-970) at the Laplacian radius
 __device__ __forceinline__ double viscosity_coefficient(const SceneConst& sc, const LapFactors& f, double r) {
-    if (f.hl) return f.visc / (r * r * r);
+    if (f.hl) return ddiv_rn(f.visc, r * r * r);
     return f.visc * weight(r, sc.re_lap);
 }
 
 // PPE off-diagonal coefficient (Computer.hpp:1290-1297)
 __device__ __forceinline__ double ppe_coefficient(const SceneConst& sc, const LapFactors& f, double r) {
-    if (f.hl) return f.ppe / (r * r * r);
+    if (f.hl) return ddiv_rn(f.ppe, r * r * r);
     return f.ppe * weight(r, sc.re_lap);
 }
 
@@ -142,7 +142,7 @@ __global__ void k_max_speed(SceneConst sc, DeviceState st) {
 __global__ void k_cfl_dt(SceneConst sc, DeviceState st) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         const double u2 = __longlong_as_double(static_cast<long long>(st.step->max_u2_bits));
-        const double maxU = __dsqrt_rn(u2);
+        const double maxU = dsqrt_rn(u2);
         double dt;
         if (maxU == 0) {
             dt = sc.max_dt;
@@ -171,7 +171,7 @@ __global__ void k_density(SceneConst sc, DeviceState st) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dist2(dx, dz);
-        if (below(r2, sc.re2)) thisN += weight(__dsqrt_rn(r2), sc.re);
+        if (below(r2, sc.re2)) thisN += weight(dsqrt_rn(r2), sc.re);
     });
     if (spp) {
         st.n_wo_spp[i] = thisN;
@@ -205,7 +205,7 @@ __global__ void k_density_explicit_pressure(SceneConst sc, DeviceState st, int32
             const double dz = st.z[j] - zi;
             const double r2 = dist2(dx, dz);
             if (below(r2, sc.re2)) {
-                const double w = weight(__dsqrt_rn(r2), sc.re);
+                const double w = weight(dsqrt_rn(r2), sc.re);
                 thisN += w;
                 if (m_re < kReCache) st.w_re[static_cast<int64_t>(m_re) * n + i] = w;
                 m_re++;
@@ -262,7 +262,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(r2));
+                const double c = viscosity_coefficient(sc, lf, dsqrt_rn(r2));
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
             } else {
@@ -270,7 +270,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
                 vz = __dadd_rn(vz, 0.0);
             }
             if (spp) {
-                const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+                const double wg = weight(dsqrt_rn(r2), sc.re_lap);
                 gx += wg * dx;
                 gz += wg * dz;
             }
@@ -279,7 +279,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        const double c = viscosity_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
@@ -316,13 +316,13 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
         const bool in_re = below(r2, sc.re2);
         const bool in_rl = fluid && below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
-        const double r = __dsqrt_rn(r2);
+        const double r = dsqrt_rn(r2);
         if (in_re) {
             thisN += weight(r, sc.re);
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
-                hsum += dot2(dx, dz, du, dw) / (r * r * r);
+                hsum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
             }
         }
         if (in_rl) {
@@ -366,7 +366,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        const double c = viscosity_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
         vx += c * (ui - ui);
         vz += c * (wi - wi);
     }
@@ -451,7 +451,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double a_ij = ppe_coefficient(sc, lf, __dsqrt_rn(r2));
+                const double a_ij = ppe_coefficient(sc, lf, dsqrt_rn(r2));
                 if (spp || !is_surface(sc, st.nd[j])) {
                     st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
                     st.ppe_val_tmp[ell(m, n, i)] = a_ij;
@@ -462,7 +462,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
                 a_ii = __dadd_rn(a_ii, 0.0);
             }
             if (spp) {
-                const double wg = weight(__dsqrt_rn(r2), sc.re_lap);
+                const double wg = weight(dsqrt_rn(r2), sc.re_lap);
                 gx += wg * dx;
                 gz += wg * dz;
             }
@@ -471,7 +471,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        a_ii += -ppe_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        a_ii += -ppe_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
     st.ppe_col_tmp[ell(m, n, i)] = row;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
@@ -512,7 +512,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         const bool in_re = below(r2, sc.re2);
         const bool in_rl = below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
-        const double r = __dsqrt_rn(r2);
+        const double r = dsqrt_rn(r2);
         if (in_re) {
             const double w = weight(r, sc.re);
             thisN += w;
@@ -521,7 +521,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
-                hsum += dot2(dx, dz, du, dw) / (r * r * r);
+                hsum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
             }
         }
         if (in_rl) {
@@ -556,7 +556,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     double xs, zs;
     if (spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
-        a_ii += -ppe_coefficient(sc, lf, __dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
+        a_ii += -ppe_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
     st.ppe_col_tmp[ell(m, n, i)] = row;
     st.ppe_val_tmp[ell(m, n, i)] = a_ii;
@@ -654,10 +654,10 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.re2)) {
             const double wg = (kCached && m_re < kReCache) ? st.w_re[static_cast<int64_t>(m_re) * sc.n + i]
-                                                           : weight(__dsqrt_rn(r2), sc.re);
+                                                           : weight(dsqrt_rn(r2), sc.re);
             m_re++;
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double c = (st.p[j] + pi) / r2 * wg;
+                const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
                 sx += c * dx;
                 sz += c * dz;
             } else {
@@ -675,7 +675,7 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
         const double dx = xs - xi;
         const double dz = zs - zi;
         const double r2 = dist2(dx, dz);
-        const double c = (0.0 + pi) / r2 * weight(__dsqrt_rn(r2), sc.re);
+        const double c = ddiv_rn(0.0 + pi, r2) * weight(dsqrt_rn(r2), sc.re);
         sx += c * dx;
         sz += c * dz;
     }
@@ -734,7 +734,7 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
     const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
     auto w_of = [&](int m, double r2) {
         return (kCached && m < kReCache) ? st.w_re[static_cast<int64_t>(m) * sc.n + i]
-                                         : weight(__dsqrt_rn(r2), sc.re);
+                                         : weight(dsqrt_rn(r2), sc.re);
     };
     double m00 = 0.0, m01 = 0.0, m11 = 0.0, gx = 0.0, gz = 0.0;
     int m_re = 0;
@@ -745,7 +745,7 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
         if (below(r2, sc.re2)) {
             const double wg = w_of(m_re, r2);
             m_re++;
-            const double t = wg / r2;
+            const double t = ddiv_rn(wg, r2);
             m00 += t * (dx * dx);
             m01 += t * (dx * dz);
             m11 += t * (dz * dz);
@@ -762,8 +762,8 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
         sdx = xs - xi;
         sdz = zs - zi;
         sr2 = dist2(sdx, sdz);
-        sw = weight(__dsqrt_rn(sr2), sc.re);
-        const double t = sw / sr2;
+        sw = weight(dsqrt_rn(sr2), sc.re);
+        const double t = ddiv_rn(sw, sr2);
         m00 += t * (sdx * sdx);
         m01 += t * (sdx * sdz);
         m11 += t * (sdz * sdz);
@@ -780,7 +780,7 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
             const double wg = w_of(m_re, r2);
             m_re++;
             if (st.type[j] != MPS_TYPE_DUMMY) {
-                const double c = (st.p[j] + pi) / r2 * wg;
+                const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
                 sx += c * row_dot(C[0], C[1], dx, dz);
                 sz += c * row_dot(C[2], C[3], dx, dz);
             } else {
@@ -790,7 +790,7 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
         }
     });
     if (has_spp) {
-        const double c = (0.0 + pi) / sr2 * sw;
+        const double c = ddiv_rn(0.0 + pi, sr2) * sw;
         sx += c * row_dot(C[0], C[1], sdx, sdz);
         sz += c * row_dot(C[2], C[3], sdx, sdz);
     }
@@ -821,14 +821,14 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
             if (st.type[j] != MPS_TYPE_DUMMY && below(r2, d2)) {
                 const double dx0 = st.ox[j] - oxi;
                 const double dz0 = st.oz[j] - ozi;
-                const double nrm = __dsqrt_rn(dot2(dx0, dz0, dx0, dz0));
-                const double ex = dx0 / nrm;
-                const double ez = dz0 / nrm;
+                const double nrm = dsqrt_rn(dot2(dx0, dz0, dx0, dz0));
+                const double ex = ddiv_rn(dx0, nrm);
+                const double ez = ddiv_rn(dz0, nrm);
                 const double r_par = dot2(dx, dz, ex, ez);
                 const double px = dx - r_par * ex;
                 const double pz = dz - r_par * ez;
                 const double r_perp2 = dot2(px, pz, px, pz);
-                const double mag = __dsqrt_rn(d2 - r_perp2) - r_par;
+                const double mag = dsqrt_rn(d2 - r_perp2) - r_par;
                 sx += mag * ex;
                 sz += mag * ez;
             } else {
@@ -836,7 +836,7 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
                 sz = __dadd_rn(sz, 0.0);
             }
             if (spp) {
-                const double wg = weight(__dsqrt_rn(r2), sc.re);
+                const double wg = weight(dsqrt_rn(r2), sc.re);
                 gx += wg * dx;
                 gz += wg * dz;
             }

@@ -86,8 +86,14 @@ def plain_tank(l0=0.01, ds=False):
 
 
 def stock_tank():
-    """The l0 = 0.01 dam break with the stock method set and two radii (the workload physics)."""
+    """The l0 = 0.01 dam break with the stock method set at one radius (the workload physics)."""
     return scenes.config_c0()
+
+
+def stock_two_radii_tank():
+    """The same dam break with the stock method set and two radii: r_e = 2.1 l0 for the
+    density and gradient, 4.0 l0 for the Laplacian (the two-radius extension)."""
+    return scenes.config_c0(dict(scenes.STOCK_PHYSICS, re_by_l0=2.1, re_lap_by_l0=4.0))
 
 
 def jittered_tank(l0=0.01, jitter=0.05, seed=7, preset=abi.PRESET_PLAIN):
@@ -120,7 +126,7 @@ def threshold_rings(l0=0.01, seed=5):
     """A fluid particle with rings of neighbours at distances within a few ulps to 1e-5
     (relative) of r_e, the Laplacian radius and the neighbour length, on both sides:
     every range test of the step meets pairs that only the FP64 comparison decides."""
-    base = stock_tank()
+    base = stock_two_radii_tank()
     prm = dict(base.meta["params"])
     re = prm.get("re_by_l0", 2.1) * l0
     rl = prm.get("re_lap_by_l0", 4.0) * l0

@@ -12,7 +12,7 @@ import pytest
 
 from helpers import (assert_same_neighbors, assert_same_particles, assert_same_ppe, copy_state,
                      far_tank, jittered_tank, make_pair, plain_tank, reference_tank, stock_tank,
-                     threshold_rings)
+                     stock_two_radii_tank, threshold_rings)
 from openmps_gb300 import _abi as abi
 
 pytestmark = pytest.mark.gpu
@@ -23,7 +23,8 @@ CASES = {
     "plain_two_radii_ds": lambda: plain_tank(ds=True),
     "jittered_reference": lambda: jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
     "jittered_plain": lambda: jittered_tank(jitter=0.1),
-    "stock_two_radii": stock_tank,
+    "stock_one_radius": stock_tank,
+    "stock_two_radii": stock_two_radii_tank,
     "stock_far_from_origin": far_tank,
 }
 
@@ -158,7 +159,7 @@ def test_cfl_time_step(gpu_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("case", ["reference_preset", "plain_two_radii", "plain_two_radii_ds",
-                                  "stock_two_radii", "stock_far_from_origin"])
+                                  "stock_one_radius", "stock_two_radii", "stock_far_from_origin"])
 def test_step_equals_stage_chain(gpu_lib, oracle_lib, case):
     # mps_forward_time walks each neighbour row once for density, ECS and the explicit
     # accelerations together, and once for the second density and the PPE assembly

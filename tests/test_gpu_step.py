@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from helpers import (copy_state, jittered_tank, make_pair, plain_tank, reference_tank, rel_err,
-                     stock_tank)
+                     stock_tank, stock_two_radii_tank)
 from openmps_gb300 import _abi as abi
 from openmps_gb300 import scenes
 
@@ -24,7 +24,8 @@ CASES = {
     "plain_two_radii": plain_tank,
     "plain_two_radii_ds": lambda: plain_tank(ds=True),
     "jittered_reference": lambda: jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
-    "stock_two_radii": stock_tank,
+    "stock_one_radius": stock_tank,
+    "stock_two_radii": stock_two_radii_tank,
 }
 
 

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from helpers import (assert_same_particles, copy_state, jittered_tank, make_pair, plain_tank,
-                     reference_tank, rel_err, stock_tank)
+                     reference_tank, rel_err, stock_tank, stock_two_radii_tank)
 from openmps_gb300 import _abi as abi
 from openmps_gb300 import scenes
 
@@ -44,7 +44,8 @@ GC_CASES = {
     "jittered_reference": lambda: _with_flags(jittered_tank(jitter=0.1, preset=abi.PRESET_REFERENCE),
                                               abi.FLAG_GC),
     "jittered_plain": lambda: _with_flags(jittered_tank(jitter=0.1), abi.FLAG_GC),
-    "stock_two_radii": lambda: _with_flags(stock_tank(), abi.FLAG_GC),
+    "stock_one_radius": lambda: _with_flags(stock_tank(), abi.FLAG_GC),
+    "stock_two_radii": lambda: _with_flags(stock_two_radii_tank(), abi.FLAG_GC),
 }
 GIVEN_PRESSURE_CASES = dict(GC_CASES, singular_row=lambda: _with_flags(row_of_particles(), abi.FLAG_GC))
 

@@ -19,7 +19,8 @@ def test_dam_break_counts():
     c2 = scenes.config_c2()
     assert c2.counts()["fluid"] == 320000 and c2.count == 340050
     assert c2.params().flags == abi.PRESET_REFERENCE
-    assert c2.params().re_lap_by_l0 == 4.0
+    # one radius, 4.0 l0: the Laplacian radius of the workload (about 45 PPE nonzeros a row)
+    assert c2.params().re_by_l0 == 4.0 and c2.params().re_lap_by_l0 == 0.0
 
 
 def test_hydrostatic_jitter_is_seeded():
