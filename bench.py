@@ -87,6 +87,8 @@ def parse_args():
     ap.add_argument("--cg-launch", choices=("graph", "host", "persistent"), default="graph",
                     help="host: CG kernels launched one by one (profilers cannot see kernels "
                          "inside conditional CUDA graphs)")
+    ap.add_argument("--profile-scene", choices=("c2", "c1"), default="c2",
+                    help="with --profile-steps: the 320k dam break (c2) or the 80k hydrostatic tank (c1)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run --warmup + this many steps and exit (for ncu)")
     return ap.parse_args()
@@ -274,7 +276,7 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
     solver = SOLVERS[args.solver]
-    scene = scenes.config_c2()
+    scene = scenes.config_c1() if (args.profile_steps > 0 and args.profile_scene == "c1") else scenes.config_c2()
     dt = scene.meta["dt"]
     launch = {"graph": abi.CG_LAUNCH_GRAPH, "host": abi.CG_LAUNCH_HOST,
               "persistent": abi.CG_LAUNCH_PERSISTENT}[args.cg_launch]
@@ -481,7 +483,7 @@ def compare_solvers(comp, scene, dt, device, steps=3):
         c.add_particles(P["type"], P["x"], P["z"], P["u"], P["w"], P["p"], P["n"])
         c.set_aux(A["n_without_spp"], A["ecs"], A["ox"], A["oz"])
         c.set_stage_timing(True)
-        step_ms, solve_ms, its = [], [], []
+        step_ms, solve_ms, its, fbs = [], [], [], 0
         for _ in range(steps):
             c.flush_l2(FLUSH_BYTES)
             c.event_record(0)
@@ -491,17 +493,18 @@ def compare_solvers(comp, scene, dt, device, steps=3):
             st = c.stats()
             solve_ms.append(st["stage_ms"]["solve"])
             its.append(st["cg_iterations"])
+            fbs += st["fallback"]
             assert st["cg_true_relres"] <= 1e-8
         c.close()
         out[name] = {"step_ms": round(statistics.mean(step_ms), 3), "ppe_ms": round(statistics.mean(solve_ms), 3),
-                     "iterations": round(statistics.mean(its), 1)}
+                     "iterations": round(statistics.mean(its), 1), "fp64_fallbacks": fbs}
     base = out["cg64"]
     for name, v in list(out.items()):
         v["step_x_vs_cg64"] = round(base["step_ms"] / v["step_ms"], 2)
         v["ppe_x_vs_cg64"] = round(base["ppe_ms"] / v["ppe_ms"], 2)
     out["note"] = ("one snapshot, %d steps per solver, L2 flushed before each step, PPE to 1e-8 |b|: cg64 = FP64 CG "
-                   "(reference algorithm), mixed = FP32 CG + FP64 reliable updates, mg = mixed preconditioned by "
-                   "the cell multigrid, learned = mg started from the network's guess and Jacobi scale" % steps)
+                   "(reference algorithm), mixed = FP32 CG + FP64 reliable updates (the FP64 CG finishes it when it "
+                   "stalls), mg = mixed preconditioned by the cell multigrid, learned = mg started from the network's guess and Jacobi scale" % steps)
     return out
 
 

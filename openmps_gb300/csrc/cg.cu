@@ -227,6 +227,7 @@ __device__ void init_scalars(CgScalars* S, double rr, double bb, cudaGraphCondit
     S->aborted = 0;
     S->stalled = 0;
     S->prev_true_rr = rr;
+    S->iter_upd = 0;
     if (use_cond) cudaGraphSetConditional(h, (!conv && S->max_iter > 0) ? 1u : 0u);
 }
 
@@ -470,6 +471,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_axpy(CgOperands o) {
 // w = A r (FP32); gamma = r.r and delta = w.r in FP64; the next Chronopoulos-Gear step
 // sizes; decides a reliable update.  mode 0: after init (beta = 0); mode 1: an
 // iteration; mode 2: after a reliable update (also clears d, folded into x).
+// Iterations the plain mixed solver may run without a reliable update (a tenfold drop of
+// its recursive residual norm takes a few hundred iterations on the PPEs of the
+// workloads when the FP32 recursion makes progress).
+constexpr int kMixedStallIter = 2000;
+
 __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                                                    cudaGraphConditionalHandle h,
                                                    cudaGraphConditionalHandle h_true, int use_cond) {
@@ -520,7 +526,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                     S->beta = beta;
                     S->alpha = gam / (del - beta * gam / S->alpha);
                     S->iter += 1;
-                    if (use_cond) cudaGraphSetConditional(h, (S->iter < S->max_iter) ? 1u : 0u);
+                    // no tenfold drop of the recursive residual for kMixedStallIter
+                    // iterations: the FP32 iteration has stalled (the FP64 CG takes over)
+                    const int stuck = S->iter - S->iter_upd > kMixedStallIter;
+                    if (stuck) S->stalled = 1;
+                    if (use_cond) cudaGraphSetConditional(h, (!stuck && S->iter < S->max_iter) ? 1u : 0u);
                 }
                 S->rr = gam;
                 S->pAp = del;
@@ -574,6 +584,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
             S->rr_upd = rr;
             S->rr_new = rr;
             S->updates += 1;
+            S->iter_upd = S->iter;
             const int conv = rr < S->thr;
             S->converged = conv;
             if (conv) {

@@ -41,7 +41,7 @@ struct CgScalars {
     int32_t stalled;      // breakdown or a reliable update that did not halve |r|
     int32_t fallback;     // the plain FP64 CG ran after the preconditioned solve
     int32_t fb_iter;      // iterations of that fallback
-    int32_t pad0;
+    int32_t iter_upd;     // MIXED: iteration of the last reliable update
     double prev_true_rr;  // true r.r at the previous reliable update
 };
 
