@@ -265,7 +265,8 @@ int mps_synchronize(mps_handle* h);
 int mps_event_record(mps_handle* h, int32_t slot);
 /* Milliseconds between two recorded events (synchronizes on `end`). */
 int mps_event_elapsed(mps_handle* h, int32_t begin, int32_t end, float* ms);
-/* Writes `bytes` of scratch on the handle's stream (evicts L2 between timed runs). */
+/* Writes `bytes` of scratch on the handle's stream, then reads it back: evicts L2 between
+ * timed runs and leaves it holding clean lines, so the timed work writes nothing back. */
 int mps_flush_l2(mps_handle* h, int64_t bytes);
 /* Times the PPE solver's SpMV kernel alone on the last assembled matrix: `reps`
  * back-to-back launches (FP64 values for MPS_SOLVER_CG64, FP32 for MPS_SOLVER_MIXED);

@@ -11,11 +11,13 @@
 //                memory, symmetrised).
 // Cycle, once per iteration (FP32, reads L2-resident planes):
 //   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
-//   and after a reliable update k_mg_restrict0), k_mg_down (levels above the bottom),
-//   k_mg_bottom (the coarsest levels in one block, all in shared memory, __syncthreads
-//   between levels), k_mg_up, k_mg_up_prolong_rows (level-1 post-smoothing + prolongation
-//   to the particles, one thread per row; k_mg_prolong0 when the bottom block covers
-//   level 1).
+//   and after a reliable update k_mg_restrict0), k_mg_down_fused (the coarse residuals of
+//   levels 2 .. bottom, tiles with halos in shared memory), k_mg_bottom (the coarsest
+//   levels in one block, all in shared memory, __syncthreads between levels),
+//   k_mg_up_fused (post-smoothing of levels bottom-1 .. 1 and the prolongation to the
+//   particles, tiles again; k_mg_prolong0 when the bottom block covers level 1).
+//   Hierarchies deeper than kMgFuseLevels levels above the bottom run the extra levels
+//   with k_mg_down / k_mg_up, one kernel per level.
 // A 16-block cluster kernel for levels 2 .. coarsest (cluster barriers between levels)
 // was measured slower: about 4 us per level against well under 1 us per level for one
 // block with __syncthreads, and the grid-wide kernels for the larger levels.
@@ -301,30 +303,6 @@ __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const Cg
     }
 }
 
-// Level-1 post-smoothing fused with the prolongation, one thread per row: the rows of a
-// cell are contiguous, so the threads of a warp mostly share one cell and its stencil
-// loads hit in L1 (the correction is a pure function of the cell: every row of the cell
-// gets the same value).  Rows outside every cell and identity rows get u = 0.
-__global__ void __launch_bounds__(kBlock) k_mg_up_prolong_rows(MgLevel f, MgLevel c, int n, const int32_t* row_cell,
-                                                               const float* dinv0, const float* scale,
-                                                               const float* r, float* u, const CgScalars* S,
-                                                               int mode) {
-    pdl_begin();
-    if (pcg_skip(S, mode)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float d = dinv0[i];
-    const int code = row_cell[i];
-    float v = 0.0f;
-    if (d != 0.0f && code >= 0) {
-        const int ch = (code >> 16) * f.nz + (code & 0xffff);
-        const float e = smoothed_correction(f.nx, f.nz, f.cells, f.k32, f.dinv, f.r, c.nz, c.e, ch);
-        const float sc = scale ? scale[i] : 1.0f;
-        v = sc * d * r[i] + e;
-    }
-    u[i] = v;
-}
-
 struct MgBottom {
     int32_t first, last;
     MgLevel lv[kMgMaxLevels + 1];
@@ -431,6 +409,200 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* ce
     }
 }
 
+// ------------------------------------------------------------- fused sweeps
+// The levels between the particles and the bottom block as two kernels instead of one
+// per level.  A block owns a tile of one level and computes, level by level in shared
+// memory, every cell of the other levels that its tile depends on: the tile's children
+// or parents plus a ring of one cell per level.  So no grid-wide dependency separates
+// the levels.  A ring cell is computed by every block that needs it, with the arithmetic
+// of its owner, so all blocks see the same value; only owned cells are written.
+//
+// Down sweep over levels 0 .. depth of a chain (level 0 is read, levels 1 .. depth are
+// written): a block owns kMgDownTile x kMgDownTile cells of level depth.  Its region at
+// level d starts at o_d = 2 o_{d+1} - 1 and spans n_d = 2 n_{d+1} + 2 cells per side
+// (the children of level d+1's region and their stencil ring).
+constexpr int kMgDownTile = 2;
+constexpr int kMgUpTile = 8;  // level-1 cells per side of an up-sweep tile (one warp per column)
+static_assert(kMgUpTile * 32 == kBlock, "one warp per tile column");
+
+constexpr int down_side(int steps) { return steps == 0 ? kMgDownTile : 2 * down_side(steps - 1) + 2; }
+constexpr int kDownSide0 = down_side(kMgFuseLevels);      // level-0 region side
+constexpr int kDownSide1 = down_side(kMgFuseLevels - 1);  // level-1 region side
+
+struct MgChain {
+    int32_t depth;                   // 1 .. kMgFuseLevels
+    MgLevel lv[kMgFuseLevels + 1];   // lv[0]: finest
+};
+
+__global__ void __launch_bounds__(kBlock) k_mg_down_fused(MgChain C, const CgScalars* S, int mode) {
+    // ping-pong planes: even levels in A, odd levels in B (each level's r, then x = dinv r)
+    __shared__ float A[2 * kDownSide0 * kDownSide0];
+    __shared__ float B[2 * kDownSide1 * kDownSide1];
+    pdl_begin();
+    if (pcg_skip(S, mode)) return;
+    const int D = C.depth;
+    const int X0 = blockIdx.x * kMgDownTile, Z0 = blockIdx.y * kMgDownTile;
+    // level-0 region: r and the pre-smoothed x = dinv r; cells outside the grid are never
+    // read by the stencil of a cell inside it (neighbours are clamped into the grid)
+    {
+        const MgLevel& F = C.lv[0];
+        const int n = (kMgDownTile << D) + (2 << D) - 2;
+        const int ox = (X0 << D) - ((1 << D) - 1), oz = (Z0 << D) - ((1 << D) - 1);
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t - (t / n) * n;
+            const int gx = ox + i, gz = oz + j;
+            float r = 0.0f, x = 0.0f;
+            if (gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz) {
+                const int c = gx * F.nz + gz;
+                r = F.r[c];
+                x = F.dinv[c] * r;
+            }
+            A[t] = r;
+            A[n * n + t] = x;
+        }
+    }
+    __syncthreads();
+    for (int d = 1; d <= D; d++) {
+        const MgLevel& F = C.lv[d - 1];
+        const MgLevel& L = C.lv[d];
+        const int sh = D - d;
+        const int nf = (kMgDownTile << (sh + 1)) + (2 << (sh + 1)) - 2;
+        const int fox = (X0 << (sh + 1)) - ((1 << (sh + 1)) - 1), foz = (Z0 << (sh + 1)) - ((1 << (sh + 1)) - 1);
+        const int n = (kMgDownTile << sh) + (2 << sh) - 2;
+        const int ox = (X0 << sh) - ((1 << sh) - 1), oz = (Z0 << sh) - ((1 << sh) - 1);
+        const float* fr = (d & 1) ? A : B;
+        const float* fx = fr + nf * nf;
+        float* cr = (d & 1) ? B : A;
+        const int own_x0 = X0 << sh, own_x1 = (X0 + kMgDownTile) << sh;
+        const int own_z0 = Z0 << sh, own_z1 = (Z0 + kMgDownTile) << sh;
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t - (t / n) * n;
+            const int gx = ox + i, gz = oz + j;
+            const bool in = gx >= 0 && gx < L.nx && gz >= 0 && gz < L.nz;
+            float v = 0.0f;
+            if (in) {
+                float part[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int cx = 2 * gx + (q >> 1), cz = 2 * gz + (q & 1);
+                    const bool valid = cx < F.nx && cz < F.nz;
+                    const int ccx = min(cx, F.nx - 1), ccz = min(cz, F.nz - 1);
+                    const int ch = ccx * F.nz + ccz;
+                    float res = fr[(ccx - fox) * nf + (ccz - foz)];
+#pragma unroll
+                    for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+                        for (int dz = -1; dz <= 1; dz++) {
+                            const int lx = clampi(ccx + dx, F.nx - 1) - fox, lz = clampi(ccz + dz, F.nz - 1) - foz;
+                            res -= F.k32[((dx + 1) * 3 + dz + 1) * F.cells + ch] * fx[lx * nf + lz];
+                        }
+                    }
+                    part[q] = valid ? res : 0.0f;
+                }
+                // the order of the four-thread kernel's shuffles: (00 + 01) + (10 + 11)
+                v = (part[0] + part[1]) + (part[2] + part[3]);
+                if (gx >= own_x0 && gx < own_x1 && gz >= own_z0 && gz < own_z1) L.r[gx * L.nz + gz] = v;
+            }
+            if (d < D) {
+                cr[t] = v;
+                cr[n * n + t] = in ? L.dinv[gx * L.nz + gz] * v : 0.0f;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Up sweep: post-smoothed corrections of chain levels depth-1 .. 0 (the coarse correction
+// of level depth is read from memory) and the prolongation to the rows of level 0, which
+// is level 1 of the hierarchy.  A block owns kMgUpTile x kMgUpTile level-1 cells and
+// writes u for their rows; the region of level d+1 is the parents of level d's region
+// widened by one cell.
+struct MgUpChain {
+    int32_t depth;                   // 1 .. kMgFuseLevels
+    int32_t n;                       // rows
+    MgLevel lv[kMgFuseLevels + 1];
+    const int32_t* cell_start;
+    const int32_t* row_cell;
+    const float* dinv0;
+    const float* scale;
+    const float* r;
+    float* u;
+};
+
+__global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgScalars* S, int mode) {
+    constexpr int kSide = kMgUpTile;  // every coarser region is at most this wide
+    __shared__ float E[kMgFuseLevels][kSide * kSide];
+    pdl_begin();
+    if (pcg_skip(S, mode)) return;
+    const int D = C.depth;
+    const MgLevel& L0 = C.lv[0];
+    const int x0 = blockIdx.x * kMgUpTile, z0 = blockIdx.y * kMgUpTile;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // the rows of tile column `warp` (cells x0 + warp, z0 .. z0 + 7 are contiguous rows)
+    const int gxw = x0 + warp;
+    int rb = 0, re = 0;
+    if (gxw < L0.nx) {
+        rb = C.cell_start[gxw * L0.nz + z0];
+        re = C.cell_start[gxw * L0.nz + min(z0 + kMgUpTile, L0.nz)];
+    }
+    // rows without a cell (after every cell's rows) are identity rows: u = 0
+    {
+        const int tail = C.cell_start[L0.cells];
+        const int stride = gridDim.x * gridDim.y * blockDim.x;
+        for (int i = tail + (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; i < C.n; i += stride)
+            C.u[i] = 0.0f;
+    }
+    if (!__syncthreads_or(re > rb)) return;
+    // region bounds per level (inclusive), from level 0 (the tile) upwards
+    int lox[kMgFuseLevels + 1], loz[kMgFuseLevels + 1], hix[kMgFuseLevels + 1], hiz[kMgFuseLevels + 1];
+    lox[0] = x0;
+    loz[0] = z0;
+    hix[0] = x0 + kMgUpTile - 1;
+    hiz[0] = z0 + kMgUpTile - 1;
+#pragma unroll
+    for (int d = 1; d <= kMgFuseLevels; d++) {
+        lox[d] = (lox[d - 1] - 1) >> 1;
+        loz[d] = (loz[d - 1] - 1) >> 1;
+        hix[d] = (hix[d - 1] + 1) >> 1;
+        hiz[d] = (hiz[d - 1] + 1) >> 1;
+    }
+#pragma unroll
+    for (int d = kMgFuseLevels - 1; d >= 0; d--) {
+        if (d >= D) continue;
+        const MgLevel& F = C.lv[d];
+        const MgLevel& Cl = C.lv[d + 1];
+        const int wx = hix[d] - lox[d] + 1, wz = hiz[d] - loz[d] + 1;
+        const int cwz = hiz[d + 1] - loz[d + 1] + 1;
+        const int clx = lox[d + 1], clz = loz[d + 1];
+        const float* ce = d + 1 < D ? E[d + 1] : nullptr;
+        for (int t = threadIdx.x; t < wx * wz; t += blockDim.x) {
+            const int gx = lox[d] + t / wz, gz = loz[d] + (t - (t / wz) * wz);
+            float e = 0.0f;
+            if (gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz) {
+                if (ce)
+                    e = smoothed_correction_at(F.nx, F.nz, F.cells, F.k32, F.dinv, F.r, gx, gz,
+                                               [&](int px, int pz) { return ce[(px - clx) * cwz + (pz - clz)]; });
+                else
+                    e = smoothed_correction_at(F.nx, F.nz, F.cells, F.k32, F.dinv, F.r, gx, gz,
+                                               [&](int px, int pz) { return Cl.e[px * Cl.nz + pz]; });
+            }
+            E[d][t] = e;
+        }
+        __syncthreads();
+    }
+    // u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows
+    for (int i = rb + lane; i < re; i += 32) {
+        const float d = C.dinv0[i];
+        float v = 0.0f;
+        if (d != 0.0f) {
+            const int lz = (C.row_cell[i] & 0xffff) - z0;
+            const float sc = C.scale ? C.scale[i] : 1.0f;
+            v = sc * d * C.r[i] + E[0][warp * kMgUpTile + lz];
+        }
+        C.u[i] = v;
+    }
+}
+
 size_t bottom_bytes(const MgLevel* lv, int first, int last) {
     size_t floats = 0;
     for (int l = first; l <= last; l++) floats += 12 * static_cast<size_t>(lv[l].cells);
@@ -508,26 +680,51 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
         launch_pdl(k_mg_axpy_restrict, g1, kBlock, 0, s, *fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
     else
         launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
-    for (int l = 1; l < mg.bottom; l++)
-        launch_pdl(k_mg_down, grid_for(4 * static_cast<int64_t>(mg.lv[l + 1].cells)), kBlock, 0, s, mg.lv[l],
-                   mg.lv[l + 1], S, mode);
     MgBottom B{};
     B.first = mg.bottom;
     B.last = mg.levels;
     for (int l = 1; l <= mg.levels; l++) B.lv[l] = mg.lv[l];
     B.dense = mg.dense;
-    launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_bytes(mg.lv, mg.bottom, mg.levels), s, B, S, mode);
-    for (int l = mg.bottom - 1; l >= 2; l--)
-        launch_pdl(k_mg_up, grid_for(4 * static_cast<int64_t>(mg.lv[l].cells)), kBlock, 0, s, mg.lv[l], mg.lv[l + 1],
-                   S, mode);
-    if (mg.bottom > 1)
-        launch_pdl(k_mg_up_prolong_rows, grid_for(mg.n), kBlock, 0, s, L1, mg.lv[2], mg.n, mg.cell_xz, mg.dinv0,
-                   mg.scale, r, u, S, mode);
-    else
+    const size_t bottom_smem = bottom_bytes(mg.lv, mg.bottom, mg.levels);
+    if (mg.bottom == 1) {
+        launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_smem, s, B, S, mode);
         launch_pdl(k_mg_prolong0, grid_for(mg.n), kBlock, 0, s, mg.n, mg.cell_xz, L1.nz, mg.dinv0, mg.scale,
                    r, L1.e, u, S, mode);
+        return;
+    }
+    // down: levels 1 .. bottom, the last kMgFuseLevels steps in one kernel
+    const int fuse = std::min(mg.bottom - 1, kMgFuseLevels);
+    for (int l = 1; l < mg.bottom - fuse; l++)
+        launch_pdl(k_mg_down, grid_for(4 * static_cast<int64_t>(mg.lv[l + 1].cells)), kBlock, 0, s, mg.lv[l],
+                   mg.lv[l + 1], S, mode);
+    MgChain dc{};
+    dc.depth = fuse;
+    for (int d = 0; d <= fuse; d++) dc.lv[d] = mg.lv[mg.bottom - fuse + d];
+    const MgLevel& Lb = mg.lv[mg.bottom];
+    launch_pdl(k_mg_down_fused, dim3((Lb.nx + kMgDownTile - 1) / kMgDownTile, (Lb.nz + kMgDownTile - 1) / kMgDownTile),
+               kBlock, 0, s, dc, S, mode);
+    launch_pdl(k_mg_bottom, 1, kMgBottomThreads, bottom_smem, s, B, S, mode);
+    // up: levels bottom - 1 .. 1, the last kMgFuseLevels with the prolongation in one kernel
+    for (int l = mg.bottom - 1; l > fuse; l--)
+        launch_pdl(k_mg_up, grid_for(4 * static_cast<int64_t>(mg.lv[l].cells)), kBlock, 0, s, mg.lv[l], mg.lv[l + 1],
+                   S, mode);
+    MgUpChain uc{};
+    uc.depth = fuse;
+    uc.n = mg.n;
+    for (int d = 0; d <= fuse; d++) uc.lv[d] = mg.lv[1 + d];
+    uc.cell_start = mg.cell_start;
+    uc.row_cell = mg.cell_xz;
+    uc.dinv0 = mg.dinv0;
+    uc.scale = mg.scale;
+    uc.r = r;
+    uc.u = u;
+    launch_pdl(k_mg_up_fused, dim3((L1.nx + kMgUpTile - 1) / kMgUpTile, (L1.nz + kMgUpTile - 1) / kMgUpTile), kBlock,
+               0, s, uc, S, mode);
 }
 
-int mg_apply_launches(const MgHierarchy& mg) { return mg.bottom > 1 ? 2 * mg.bottom : 3; }
+int mg_apply_launches(const MgHierarchy& mg) {
+    if (mg.bottom == 1) return 3;
+    return 4 + 2 * (mg.bottom - 1 - std::min(mg.bottom - 1, kMgFuseLevels));
+}
 
 }  // namespace mpsgb

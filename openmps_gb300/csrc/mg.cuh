@@ -26,6 +26,9 @@ constexpr int kMgDenseCells = 128;     // the coarsest level, solved with its de
 // inverse fit this much shared memory.
 constexpr size_t kMgBottomBytes = 200 * 1024;
 constexpr int kMgBottomThreads = 1024;
+// Cycle levels between the particles and the bottom block that one down-sweep or one
+// up-sweep kernel covers (deeper hierarchies run the remaining levels one kernel each).
+constexpr int kMgFuseLevels = 3;
 constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
 constexpr float kMgOmegaCoarse = 0.9f; // Jacobi weight of the cell levels (best of 0.6-0.9 measured)
 
@@ -135,13 +138,15 @@ __device__ __forceinline__ float child_residual(int nx, int nz, int cells, const
     return valid ? res : 0.0f;
 }
 
-// Post-smoothed correction of fine cell ch: x = dinv r + e_parent, then one Jacobi step.
-__device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
-                                                     const float* dinv, const float* r, int cnz,
-                                                     const float* ce, int ch) {
-    const int cx = ch / nz, cz = ch - (ch / nz) * nz;
+// Post-smoothed correction of fine cell (cx, cz): x = dinv r + e_parent, then one Jacobi
+// step; ce(px, pz) returns the coarse correction of parent cell (px, pz).
+template <class CoarseE>
+__device__ __forceinline__ float smoothed_correction_at(int nx, int nz, int cells, const float* k,
+                                                        const float* dinv, const float* r, int cx, int cz,
+                                                        CoarseE ce) {
+    const int ch = cx * nz + cz;
     const float rc = r[ch];
-    const float xc = dinv[ch] * rc + ce[(cx >> 1) * cnz + (cz >> 1)];
+    const float xc = dinv[ch] * rc + ce(cx >> 1, cz >> 1);
     float res = rc;
 #pragma unroll
     for (int dx = -1; dx <= 1; dx++) {
@@ -149,11 +154,20 @@ __device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, 
         for (int dz = -1; dz <= 1; dz++) {
             const int nx_ = clampi(cx + dx, nx - 1), nz_ = clampi(cz + dz, nz - 1);
             const int nb = nx_ * nz + nz_;
-            const float xn = dinv[nb] * r[nb] + ce[(nx_ >> 1) * cnz + (nz_ >> 1)];
+            const float xn = dinv[nb] * r[nb] + ce(nx_ >> 1, nz_ >> 1);
             res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * xn;
         }
     }
     return xc + dinv[ch] * res;
+}
+
+// The same with the coarse corrections in a plane of row length cnz.
+__device__ __forceinline__ float smoothed_correction(int nx, int nz, int cells, const float* k,
+                                                     const float* dinv, const float* r, int cnz,
+                                                     const float* ce, int ch) {
+    const int cx = ch / nz, cz = ch - (ch / nz) * nz;
+    return smoothed_correction_at(nx, nz, cells, k, dinv, r, cx, cz,
+                                  [&](int px, int pz) { return ce[px * cnz + pz]; });
 }
 
 // Gate of a preconditioned-solve kernel: mode 0 after init, 1 an iteration, 2 after a
