@@ -447,6 +447,11 @@ __host__ __device__ __forceinline__ int64_t sell_chunks(int64_t n) {
     return (n + kSellRows - 1) / kSellRows;
 }
 
+// Block size of the neighbour walks (a thread per particle, 60-90 registers): small blocks
+// fill an SM's register file in finer steps and leave a shorter tail of partly idle SMs
+// than 256-thread blocks, whose launch of a few hundred blocks is barely over one wave.
+constexpr int kWalkBlock = 64;
+
 inline int grid_for(int64_t n, int block = kBlock) {
     return static_cast<int>((n + block - 1) / block);
 }

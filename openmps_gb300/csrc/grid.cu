@@ -208,7 +208,7 @@ void launch_cell_sort(const SceneConst& sc, const DeviceState& st, cudaStream_t 
 }
 
 void launch_neighbors(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_neighbors<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_neighbors<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
 }
 
 int launch_rows(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {

@@ -416,6 +416,10 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong0(int n, const int32_t* ce
 // or parents plus a ring of one cell per level.  So no grid-wide dependency separates
 // the levels.  A ring cell is computed by every block that needs it, with the arithmetic
 // of its owner, so all blocks see the same value; only owned cells are written.
+// Each thread of a block owns one cell of one level and issues every global load its
+// cell needs (stencil coefficients, residuals, the coarse correction) when the kernel
+// starts, so a sweep waits for one round trip to L2, not one per level; the levels then
+// run from registers and shared memory with a block barrier between them.
 //
 // Down sweep over levels 0 .. depth of a chain (level 0 is read, levels 1 .. depth are
 // written): a block owns kMgDownTile x kMgDownTile cells of level depth.  Its region at
@@ -425,9 +429,17 @@ constexpr int kMgDownTile = 2;
 constexpr int kMgUpTile = 8;  // level-1 cells per side of an up-sweep tile (one warp per column)
 static_assert(kMgUpTile * 32 == kBlock, "one warp per tile column");
 
-constexpr int down_side(int steps) { return steps == 0 ? kMgDownTile : 2 * down_side(steps - 1) + 2; }
-constexpr int kDownSide0 = down_side(kMgFuseLevels);      // level-0 region side
-constexpr int kDownSide1 = down_side(kMgFuseLevels - 1);  // level-1 region side
+// region side at the level `steps` levels below the tile's level
+__host__ __device__ constexpr int down_side(int steps) {
+    return steps == 0 ? kMgDownTile : 2 * down_side(steps - 1) + 2;
+}
+constexpr int kDownSide0 = down_side(kMgFuseLevels);      // level 0 at the deepest chain
+constexpr int kDownSide1 = down_side(kMgFuseLevels - 1);
+constexpr int kDownSide2 = down_side(kMgFuseLevels - 2);
+static_assert(kMgFuseLevels == 3, "the down sweep keeps three region planes");
+static_assert(down_side(2) * down_side(2) + down_side(1) * down_side(1) + down_side(0) * down_side(0) <= kBlock,
+              "one thread per computed cell");
+constexpr int kDownPer0 = (kDownSide0 * kDownSide0 + kBlock - 1) / kBlock;  // level-0 cells per thread
 
 struct MgChain {
     int32_t depth;                   // 1 .. kMgFuseLevels
@@ -435,50 +447,90 @@ struct MgChain {
 };
 
 __global__ void __launch_bounds__(kBlock) k_mg_down_fused(MgChain C, const CgScalars* S, int mode) {
-    // ping-pong planes: even levels in A, odd levels in B (each level's r, then x = dinv r)
-    __shared__ float A[2 * kDownSide0 * kDownSide0];
-    __shared__ float B[2 * kDownSide1 * kDownSide1];
+    __shared__ float R0[kDownSide0 * kDownSide0], X0[kDownSide0 * kDownSide0];
+    __shared__ float R1[kDownSide1 * kDownSide1], X1[kDownSide1 * kDownSide1];
+    __shared__ float R2[kDownSide2 * kDownSide2], X2[kDownSide2 * kDownSide2];
     pdl_begin();
     if (pcg_skip(S, mode)) return;
     const int D = C.depth;
-    const int X0 = blockIdx.x * kMgDownTile, Z0 = blockIdx.y * kMgDownTile;
-    // level-0 region: r and the pre-smoothed x = dinv r; cells outside the grid are never
-    // read by the stencil of a cell inside it (neighbours are clamped into the grid)
-    {
-        const MgLevel& F = C.lv[0];
-        const int n = (kMgDownTile << D) + (2 << D) - 2;
-        const int ox = (X0 << D) - ((1 << D) - 1), oz = (Z0 << D) - ((1 << D) - 1);
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-            const int i = t / n, j = t - (t / n) * n;
-            const int gx = ox + i, gz = oz + j;
-            float r = 0.0f, x = 0.0f;
-            if (gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz) {
-                const int c = gx * F.nz + gz;
-                r = F.r[c];
-                x = F.dinv[c] * r;
+    const int TX = blockIdx.x * kMgDownTile, TZ = blockIdx.y * kMgDownTile;
+    const int tid = threadIdx.x;
+    // level-0 region: r and dinv (cells outside the grid are never read by the stencil
+    // of a cell inside it: neighbours are clamped into the grid)
+    const MgLevel& F0 = C.lv[0];
+    const int n0 = (kMgDownTile << D) + (2 << D) - 2;
+    const int o0x = (TX << D) - ((1 << D) - 1), o0z = (TZ << D) - ((1 << D) - 1);
+    float r0[kDownPer0], d0[kDownPer0];
+#pragma unroll
+    for (int k = 0; k < kDownPer0; k++) {
+        const int t = tid + k * kBlock;
+        r0[k] = 0.0f;
+        d0[k] = 0.0f;
+        if (t < n0 * n0) {
+            const int gx = o0x + t / n0, gz = o0z + (t - (t / n0) * n0);
+            if (gx >= 0 && gx < F0.nx && gz >= 0 && gz < F0.nz) {
+                const int c = gx * F0.nz + gz;
+                r0[k] = F0.r[c];
+                d0[k] = F0.dinv[c];
             }
-            A[t] = r;
-            A[n * n + t] = x;
+        }
+    }
+    // this thread's cell: threads [0, n_1^2) take level 1, the next n_2^2 level 2, ...
+    int my_d = 0, my_t = 0;
+    {
+        int t = tid;
+        for (int d = 1; d <= D; d++) {
+            const int sh = D - d;
+            const int n = (kMgDownTile << sh) + (2 << sh) - 2;
+            if (t < n * n) {
+                my_d = d;
+                my_t = t;
+                break;
+            }
+            t -= n * n;
+        }
+    }
+    int gx = 0, gz = 0, n = 0, fn = 1, fox = 0, foz = 0;
+    bool in = false;
+    float kk[4][9];
+    float my_dinv = 0.0f;
+    if (my_d > 0) {
+        const MgLevel& L = C.lv[my_d];
+        const MgLevel& F = C.lv[my_d - 1];
+        const int sh = D - my_d;
+        n = (kMgDownTile << sh) + (2 << sh) - 2;
+        fn = (kMgDownTile << (sh + 1)) + (2 << (sh + 1)) - 2;
+        fox = (TX << (sh + 1)) - ((1 << (sh + 1)) - 1);
+        foz = (TZ << (sh + 1)) - ((1 << (sh + 1)) - 1);
+        gx = (TX << sh) - ((1 << sh) - 1) + my_t / n;
+        gz = (TZ << sh) - ((1 << sh) - 1) + (my_t - (my_t / n) * n);
+        in = gx >= 0 && gx < L.nx && gz >= 0 && gz < L.nz;
+        if (in) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int ccx = min(2 * gx + (q >> 1), F.nx - 1), ccz = min(2 * gz + (q & 1), F.nz - 1);
+                const int ch = ccx * F.nz + ccz;
+#pragma unroll
+                for (int k = 0; k < 9; k++) kk[q][k] = F.k32[k * F.cells + ch];
+            }
+            if (my_d < D) my_dinv = L.dinv[gx * L.nz + gz];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kDownPer0; k++) {
+        const int t = tid + k * kBlock;
+        if (t < n0 * n0) {
+            R0[t] = r0[k];
+            X0[t] = d0[k] * r0[k];
         }
     }
     __syncthreads();
     for (int d = 1; d <= D; d++) {
-        const MgLevel& F = C.lv[d - 1];
-        const MgLevel& L = C.lv[d];
-        const int sh = D - d;
-        const int nf = (kMgDownTile << (sh + 1)) + (2 << (sh + 1)) - 2;
-        const int fox = (X0 << (sh + 1)) - ((1 << (sh + 1)) - 1), foz = (Z0 << (sh + 1)) - ((1 << (sh + 1)) - 1);
-        const int n = (kMgDownTile << sh) + (2 << sh) - 2;
-        const int ox = (X0 << sh) - ((1 << sh) - 1), oz = (Z0 << sh) - ((1 << sh) - 1);
-        const float* fr = (d & 1) ? A : B;
-        const float* fx = fr + nf * nf;
-        float* cr = (d & 1) ? B : A;
-        const int own_x0 = X0 << sh, own_x1 = (X0 + kMgDownTile) << sh;
-        const int own_z0 = Z0 << sh, own_z1 = (Z0 + kMgDownTile) << sh;
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-            const int i = t / n, j = t - (t / n) * n;
-            const int gx = ox + i, gz = oz + j;
-            const bool in = gx >= 0 && gx < L.nx && gz >= 0 && gz < L.nz;
+        if (my_d == d) {
+            const MgLevel& F = C.lv[d - 1];
+            const MgLevel& L = C.lv[d];
+            const float* fr = d == 1 ? R0 : (d == 2 ? R1 : R2);
+            const float* fx = d == 1 ? X0 : (d == 2 ? X1 : X2);
             float v = 0.0f;
             if (in) {
                 float part[4];
@@ -487,25 +539,29 @@ __global__ void __launch_bounds__(kBlock) k_mg_down_fused(MgChain C, const CgSca
                     const int cx = 2 * gx + (q >> 1), cz = 2 * gz + (q & 1);
                     const bool valid = cx < F.nx && cz < F.nz;
                     const int ccx = min(cx, F.nx - 1), ccz = min(cz, F.nz - 1);
-                    const int ch = ccx * F.nz + ccz;
-                    float res = fr[(ccx - fox) * nf + (ccz - foz)];
+                    float res = fr[(ccx - fox) * fn + (ccz - foz)];
 #pragma unroll
                     for (int dx = -1; dx <= 1; dx++) {
 #pragma unroll
                         for (int dz = -1; dz <= 1; dz++) {
                             const int lx = clampi(ccx + dx, F.nx - 1) - fox, lz = clampi(ccz + dz, F.nz - 1) - foz;
-                            res -= F.k32[((dx + 1) * 3 + dz + 1) * F.cells + ch] * fx[lx * nf + lz];
+                            res -= kk[q][(dx + 1) * 3 + dz + 1] * fx[lx * fn + lz];
                         }
                     }
                     part[q] = valid ? res : 0.0f;
                 }
                 // the order of the four-thread kernel's shuffles: (00 + 01) + (10 + 11)
                 v = (part[0] + part[1]) + (part[2] + part[3]);
-                if (gx >= own_x0 && gx < own_x1 && gz >= own_z0 && gz < own_z1) L.r[gx * L.nz + gz] = v;
+                const int sh = D - d;
+                if (gx >= (TX << sh) && gx < ((TX + kMgDownTile) << sh) && gz >= (TZ << sh) &&
+                    gz < ((TZ + kMgDownTile) << sh))
+                    L.r[gx * L.nz + gz] = v;
             }
             if (d < D) {
-                cr[t] = v;
-                cr[n * n + t] = in ? L.dinv[gx * L.nz + gz] * v : 0.0f;
+                float* cr = d == 1 ? R1 : R2;
+                float* cx_ = d == 1 ? X1 : X2;
+                cr[my_t] = v;
+                cx_[my_t] = my_dinv * v;
             }
         }
         __syncthreads();
@@ -529,6 +585,10 @@ struct MgUpChain {
     float* u;
 };
 
+// rows of a tile column a lane prefetches (a column of eight cells holds about 130 rows
+// in the dam break, so longer columns take a second pass)
+constexpr int kUpRowsPre = 4;
+
 __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgScalars* S, int mode) {
     constexpr int kSide = kMgUpTile;  // every coarser region is at most this wide
     __shared__ float E[kMgFuseLevels][kSide * kSide];
@@ -537,7 +597,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
     const int D = C.depth;
     const MgLevel& L0 = C.lv[0];
     const int x0 = blockIdx.x * kMgUpTile, z0 = blockIdx.y * kMgUpTile;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // the rows of tile column `warp` (cells x0 + warp, z0 .. z0 + 7 are contiguous rows)
     const int gxw = x0 + warp;
     int rb = 0, re = 0;
@@ -549,7 +609,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
     {
         const int tail = C.cell_start[L0.cells];
         const int stride = gridDim.x * gridDim.y * blockDim.x;
-        for (int i = tail + (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; i < C.n; i += stride)
+        for (int i = tail + (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + tid; i < C.n; i += stride)
             C.u[i] = 0.0f;
     }
     if (!__syncthreads_or(re > rb)) return;
@@ -566,38 +626,124 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
         hix[d] = (hix[d - 1] + 1) >> 1;
         hiz[d] = (hiz[d - 1] + 1) >> 1;
     }
+    // this thread's cell: threads take the cells of level depth-1 first, then depth-2, ...
+    int my_d = -1, my_t = 0;
+    {
+        int t = tid;
+#pragma unroll
+        for (int d = kMgFuseLevels - 1; d >= 0; d--) {
+            if (d >= D || my_d >= 0) continue;
+            const int cnt = (hix[d] - lox[d] + 1) * (hiz[d] - loz[d] + 1);
+            if (t < cnt) {
+                my_d = d;
+                my_t = t;
+            } else {
+                t -= cnt;
+            }
+        }
+    }
+    // the stencil of this thread's cell: r, dinv and K of the nine neighbours, and the
+    // coarse corrections of their parents when the coarse level is read from memory
+    float rn[9], dn[9], kn[9], cn[9];
+    int gx = 0, gz = 0;
+    bool in = false;
+    if (my_d >= 0) {
+        const MgLevel& F = C.lv[my_d];
+        const MgLevel& Cl = C.lv[my_d + 1];
+        int lx = 0, lz = 0, w = 1;
+#pragma unroll
+        for (int d = 0; d < kMgFuseLevels; d++)
+            if (d == my_d) {
+                lx = lox[d];
+                lz = loz[d];
+                w = hiz[d] - loz[d] + 1;
+            }
+        gx = lx + my_t / w;
+        gz = lz + (my_t - (my_t / w) * w);
+        in = gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz;
+        if (in) {
+            const int ch = gx * F.nz + gz;
+            const bool top = my_d + 1 == D;
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+                for (int dz = -1; dz <= 1; dz++) {
+                    const int k = (dx + 1) * 3 + dz + 1;
+                    const int ax = clampi(gx + dx, F.nx - 1), az = clampi(gz + dz, F.nz - 1);
+                    const int nb = ax * F.nz + az;
+                    rn[k] = F.r[nb];
+                    dn[k] = F.dinv[nb];
+                    kn[k] = F.k32[k * F.cells + ch];
+                    cn[k] = top ? Cl.e[(ax >> 1) * Cl.nz + (az >> 1)] : 0.0f;
+                }
+            }
+        }
+    }
+    // the rows of this lane: dinv0, scale, r and the cell of up to kUpRowsPre rows
+    float rd[kUpRowsPre], rs[kUpRowsPre], rr[kUpRowsPre];
+    int rc[kUpRowsPre];
+#pragma unroll
+    for (int k = 0; k < kUpRowsPre; k++) {
+        const int i = rb + lane + 32 * k;
+        rd[k] = 0.0f;
+        rs[k] = 1.0f;
+        rr[k] = 0.0f;
+        rc[k] = 0;
+        if (i < re) {
+            rd[k] = C.dinv0[i];
+            if (C.scale) rs[k] = C.scale[i];
+            rr[k] = C.r[i];
+            rc[k] = C.row_cell[i];
+        }
+    }
 #pragma unroll
     for (int d = kMgFuseLevels - 1; d >= 0; d--) {
         if (d >= D) continue;
-        const MgLevel& F = C.lv[d];
-        const MgLevel& Cl = C.lv[d + 1];
-        const int wx = hix[d] - lox[d] + 1, wz = hiz[d] - loz[d] + 1;
-        const int cwz = hiz[d + 1] - loz[d + 1] + 1;
-        const int clx = lox[d + 1], clz = loz[d + 1];
-        const float* ce = d + 1 < D ? E[d + 1] : nullptr;
-        for (int t = threadIdx.x; t < wx * wz; t += blockDim.x) {
-            const int gx = lox[d] + t / wz, gz = loz[d] + (t - (t / wz) * wz);
+        if (my_d == d) {
             float e = 0.0f;
-            if (gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz) {
-                if (ce)
-                    e = smoothed_correction_at(F.nx, F.nz, F.cells, F.k32, F.dinv, F.r, gx, gz,
-                                               [&](int px, int pz) { return ce[(px - clx) * cwz + (pz - clz)]; });
-                else
-                    e = smoothed_correction_at(F.nx, F.nz, F.cells, F.k32, F.dinv, F.r, gx, gz,
-                                               [&](int px, int pz) { return Cl.e[px * Cl.nz + pz]; });
+            if (in) {
+                const int cwz = hiz[d + 1] - loz[d + 1] + 1;
+                const int clx = lox[d + 1], clz = loz[d + 1];
+                const bool top = d + 1 == D;
+                const MgLevel& F = C.lv[d];
+                const float* ce = top ? nullptr : E[d + 1];
+                // smoothed_correction_at with the stencil's values from registers
+                float cen[9];
+#pragma unroll
+                for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int k = (dx + 1) * 3 + dz + 1;
+                        const int ax = clampi(gx + dx, F.nx - 1), az = clampi(gz + dz, F.nz - 1);
+                        cen[k] = top ? cn[k] : ce[((ax >> 1) - clx) * cwz + ((az >> 1) - clz)];
+                    }
+                }
+                const float rc0 = rn[4];
+                const float xc = dn[4] * rc0 + cen[4];
+                float res = rc0;
+#pragma unroll
+                for (int k = 0; k < 9; k++) res -= kn[k] * (dn[k] * rn[k] + cen[k]);
+                e = xc + dn[4] * res;
             }
-            E[d][t] = e;
+            E[d][my_t] = e;
         }
         __syncthreads();
     }
     // u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows
-    for (int i = rb + lane; i < re; i += 32) {
+#pragma unroll
+    for (int k = 0; k < kUpRowsPre; k++) {
+        const int i = rb + lane + 32 * k;
+        if (i < re) {
+            const float d = rd[k];
+            C.u[i] = d != 0.0f ? rs[k] * d * rr[k] + E[0][warp * kMgUpTile + ((rc[k] & 0xffff) - z0)] : 0.0f;
+        }
+    }
+    for (int i = rb + lane + 32 * kUpRowsPre; i < re; i += 32) {
         const float d = C.dinv0[i];
         float v = 0.0f;
         if (d != 0.0f) {
-            const int lz = (C.row_cell[i] & 0xffff) - z0;
             const float sc = C.scale ? C.scale[i] : 1.0f;
-            v = sc * d * C.r[i] + E[0][warp * kMgUpTile + lz];
+            v = sc * d * C.r[i] + E[0][warp * kMgUpTile + ((C.row_cell[i] & 0xffff) - z0)];
         }
         C.u[i] = v;
     }

@@ -886,11 +886,11 @@ void launch_cfl_dt_finish(const SceneConst& sc, const DeviceState& st, cudaStrea
 }
 
 void launch_density(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_density<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_density<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
 }
 
 void launch_error_correction(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_error_correction<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_error_correction<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
 }
 
 void launch_density_variation(const SceneConst& sc, const DeviceState& st, double* out,
@@ -900,9 +900,9 @@ void launch_density_variation(const SceneConst& sc, const DeviceState& st, doubl
 
 void launch_pre_pressure(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     if ((sc.flags & MPS_FLAG_ECS) != 0u)
-        k_pre_pressure<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pre_pressure<true><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     else
-        k_pre_pressure<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pre_pressure<false><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
 }
 
 void launch_explicit_update(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
@@ -910,7 +910,7 @@ void launch_explicit_update(const SceneConst& sc, const DeviceState& st, cudaStr
 }
 
 void launch_explicit(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_explicit_accel<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_explicit_accel<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     k_explicit_update<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
@@ -925,7 +925,7 @@ void launch_ppe_layout(const SceneConst& sc, const DeviceState& st, bool want_fp
 }
 
 void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
-    k_ppe_build<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_ppe_build<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     launch_ppe_layout(sc, st, want_fp32, s);
 }
 
@@ -934,7 +934,7 @@ bool density_ppe_fusable(const SceneConst& sc) {
 }
 
 void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
-    k_density_ppe<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_density_ppe<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     launch_ppe_layout(sc, st, want_fp32, s);
 }
 
@@ -943,32 +943,32 @@ void launch_assign_pressure(const SceneConst& sc, const DeviceState& st, cudaStr
 }
 
 void launch_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok, cudaStream_t s) {
-    k_explicit_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, ok);
+    k_explicit_pressure<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st, ok);
 }
 
 void launch_density_explicit_pressure(const SceneConst& sc, const DeviceState& st, int32_t* ok,
                                       cudaStream_t s) {
-    k_density_explicit_pressure<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, ok);
+    k_density_explicit_pressure<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st, ok);
 }
 
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     if (sc.flags & MPS_FLAG_GC)
-        k_pressure_gradient_gc<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pressure_gradient_gc<false><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     else
-        k_pressure_gradient<false><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pressure_gradient<false><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     if (sc.flags & MPS_FLAG_GC)
-        k_pressure_gradient_gc<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pressure_gradient_gc<true><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     else
-        k_pressure_gradient<true><<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+        k_pressure_gradient<true><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    k_dynamic_stabilize<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
+    k_dynamic_stabilize<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
