@@ -387,20 +387,19 @@ def run_ours(args, rank, world, local_rank):
     n = comp.count
     spmv_solver = abi.SOLVER_MIXED_MG if solver == abi.SOLVER_LEARNED else solver
     spmv_ms = comp.bench_spmv(spmv_solver, reps=20, flush_bytes=FLUSH_BYTES)
+    # algorithmic bytes of one launch, from the library (it knows the FP32 layout)
+    alg_bytes = comp.spmv_bytes(spmv_solver)
     if solver == abi.SOLVER_CG64:
-        alg_bytes = 12 * nnz + 4 * (n + 1) + 16 * n
         key, kernel = "cg64", "k_cg_spmv_dot"
     elif solver == abi.SOLVER_MIXED:
-        alg_bytes = 8 * nnz + 4 * (n + 1) + 8 * n
         key, kernel = "mixed", "k_mx_spmv"
     else:  # preconditioned: also reads u (own row) next to r
-        alg_bytes = 8 * nnz + 4 * (n + 1) + 12 * n
         key, kernel = "mg", "k_pmx_spmv"
     spmv64_ms = comp.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
     peak, peak_kind = load_peak()
     achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
     traffic = load_traffic(key, alg_bytes)
-    alg64 = 12 * nnz + 4 * (n + 1) + 16 * n
+    alg64 = comp.spmv_bytes(abi.SOLVER_CG64)
     achieved64 = alg64 / (spmv64_ms * 1e-3) / 1e9
 
     # ---- reduce over ranks (max time)
@@ -593,8 +592,8 @@ def config_sweep(device, peak, warmup=3, steps=5):
             its.append(c.stats()["cg_iterations"])
         st = c.stats()
         n, nnz = sc.count, st["ppe_nnz"]
-        b32 = 8 * nnz + 4 * (n + 1) + 12 * n
-        b64 = 12 * nnz + 4 * (n + 1) + 16 * n
+        b32 = c.spmv_bytes(abi.SOLVER_MIXED)
+        b64 = c.spmv_bytes(abi.SOLVER_CG64)
         t32 = c.bench_spmv(abi.SOLVER_MIXED, reps=20, flush_bytes=FLUSH_BYTES)
         t64 = c.bench_spmv(abi.SOLVER_CG64, reps=20, flush_bytes=FLUSH_BYTES)
         c.close()

@@ -274,6 +274,12 @@ int mps_flush_l2(mps_handle* h, int64_t bytes);
  * > 0, L2 is flushed before every launch and only the launch is timed. */
 int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_bytes,
                    float* ms_per_launch);
+/* Algorithmic bytes of one launch of that SpMV on the last assembled matrix (nnz entries,
+ * n rows): every matrix entry and row length read once, each vector read or written once
+ * per row.  FP64 CG: 12 nnz + 4 (n + 1) + 16 n; MIXED: e nnz + 4 (n + 1) + 8 n; MIXED_MG:
+ * e nnz + 4 (n + 1) + 12 n, where e = 8 bytes per FP32 entry ({column, value}) or 6 where
+ * the handle stores 16-bit column offsets (2D scenes whose offsets fit). */
+int mps_spmv_bytes(mps_handle* h, int32_t solver, int64_t* bytes);
 
 /* ------------------------------------------------------------------------
  * Stage hooks.  They mirror the reference's friend-class test access to the

@@ -68,6 +68,7 @@ PROTOTYPES = {
     "mps_event_elapsed": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "mps_flush_l2": (C.c_int, [_P, C.c_int64]),
     "mps_bench_spmv": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_float)]),
+    "mps_spmv_bytes": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int64)]),
     "mps_stage_search_neighbor": (C.c_int, [_P]),
     "mps_stage_density": (C.c_int, [_P]),
     "mps_stage_error_correction": (C.c_int, [_P]),
@@ -308,6 +309,12 @@ class Computer:
         ms = C.c_float()
         self._check(self.lib.mps_event_elapsed(self.h, begin, end, C.byref(ms)))
         return float(ms.value)
+
+    def spmv_bytes(self, solver: int) -> int:
+        """Algorithmic bytes of one launch of the solver's SpMV on the last matrix."""
+        b = C.c_int64()
+        self._check(self.lib.mps_spmv_bytes(self.h, solver, C.byref(b)))
+        return int(b.value)
 
     def flush_l2(self, nbytes: int = 512 << 20):
         self._check(self.lib.mps_flush_l2(self.h, nbytes))

@@ -113,9 +113,13 @@ __global__ void k_mg_cells(MgLevel L1, const int32_t* cell_start, const double* 
 
 // The list of level-1 cells holding particles, in ascending cell order (neighbouring
 // warps of the cycle kernels then work on neighbouring cells).
-__global__ void k_mg_active(int cells, const int32_t* flag, const int32_t* pos, int32_t* active) {
+__global__ void k_mg_active(int cells, const int32_t* flag, const int32_t* pos, const int32_t* cell_start,
+                            int32_t* active, int2* active_rows) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < cells && flag[c]) active[pos[c]] = c;
+    if (c < cells && flag[c]) {
+        active[pos[c]] = c;
+        active_rows[pos[c]] = make_int2(cell_start[c], cell_start[c + 1]);
+    }
 }
 
 // Galerkin product of the 2 x 2 aggregation of level f into level c (FP64).
@@ -205,55 +209,73 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
 }
 
 // --------------------------------------------------------------------- cycle
-// Level-1 residual: per search cell, the sum of its rows' residuals (one warp per
-// cell, lanes over the rows, fixed-order shuffle sum).
-__global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int32_t* cell_start,
+// The level-1 kernels walk the active cells with half a warp per cell (a cell holds at
+// most max_per_cell rows, 25 in 2D at r_e = 4 l0): a warp takes two cells, their row
+// ranges come from the per-solve list, and the sixteen lanes of a cell sum their rows
+// with a fixed shuffle tree.
+__device__ __forceinline__ float half_warp_sum(float v) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Level-1 residual: per search cell, the sum of its rows' residuals.
+__global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int2* active_rows,
                                                          const float* r, const CgScalars* S, int mode,
                                                          const int32_t* active, const int32_t* n_active) {
     pdl_begin();
     if (pcg_skip(S, mode)) return;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
     const int nact = *n_active;
     const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
-        const int c = active[a];
-        const int e = cell_start[c + 1];
+    for (int base = 2 * static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); base < nact;
+         base += 2 * nwarps) {
+        const int a = base + half;
         float sum = 0.0f;
-        for (int i = cell_start[c] + lane; i < e; i += 32) sum += r[i];
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-        if (lane == 0) L1.r[c] = sum;
+        int c = -1;
+        if (a < nact) {
+            const int2 rr = active_rows[a];
+            c = active[a];
+            for (int i = rr.x + hl; i < rr.y; i += 16) sum += r[i];
+        }
+        sum = half_warp_sum(sum);
+        if (hl == 0 && c >= 0) L1.r[c] = sum;
     }
 }
 
 // An iteration's vector updates fused with the level-1 restriction of the new residual:
 // s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s for the particles of each
 // cell (particles outside every cell are identity rows whose vectors stay zero).
-__global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1,
-                                                             const int32_t* cell_start, const int32_t* active,
-                                                             const int32_t* n_active) {
+__global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1, const int2* active_rows,
+                                                             const int32_t* active, const int32_t* n_active) {
     pdl_begin();
     if (pcg_skip(o.S, 1)) return;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
     const float alpha = __double2float_rn(o.S->alpha);
     const float beta = __double2float_rn(o.S->beta);
     const int nact = *n_active;
     const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-    for (int a = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < nact; a += nwarps) {
-        const int c = active[a];
-        const int e = cell_start[c + 1];
+    for (int base = 2 * static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); base < nact;
+         base += 2 * nwarps) {
+        const int a = base + half;
         float sum = 0.0f;
-        for (int i = cell_start[c] + lane; i < e; i += 32) {
-            const float si = fmaf(beta, o.s32[i], o.w32[i]);
-            const float pi = fmaf(beta, o.p32[i], o.u32[i]);
-            const float ri = fmaf(-alpha, si, o.r32[i]);
-            o.s32[i] = si;
-            o.p32[i] = pi;
-            o.d32[i] = fmaf(alpha, pi, o.d32[i]);
-            o.r32[i] = ri;
-            sum += ri;
+        int c = -1;
+        if (a < nact) {
+            const int2 rr = active_rows[a];
+            c = active[a];
+            for (int i = rr.x + hl; i < rr.y; i += 16) {
+                const float si = fmaf(beta, o.s32[i], o.w32[i]);
+                const float pi = fmaf(beta, o.p32[i], o.u32[i]);
+                const float ri = fmaf(-alpha, si, o.r32[i]);
+                o.s32[i] = si;
+                o.p32[i] = pi;
+                o.d32[i] = fmaf(alpha, pi, o.d32[i]);
+                o.r32[i] = ri;
+                sum += ri;
+            }
         }
-        for (int k = 16; k > 0; k >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, k);
-        if (lane == 0) L1.r[c] = sum;
+        sum = half_warp_sum(sum);
+        if (hl == 0 && c >= 0) L1.r[c] = sum;
     }
 }
 
@@ -291,14 +313,14 @@ __global__ void __launch_bounds__(kBlock) k_mg_up(MgLevel f, MgLevel c, const Cg
         const int dx = k / 3 - 1, dz = k - (k / 3) * 3 - 1;
         const int nx_ = clampi(cx + dx, f.nx - 1), nz_ = clampi(cz + dz, f.nz - 1);
         const int nb = nx_ * f.nz + nz_;
-        const float xn = f.dinv[nb] * f.r[nb] + c.e[(nx_ >> 1) * c.nz + (nz_ >> 1)];
+        const float xn = f.dinv[nb] * f.r[nb] + kMgCoarseWeight * c.e[(nx_ >> 1) * c.nz + (nz_ >> 1)];
         part += f.k32[k * f.cells + ch] * xn;
     }
     part += __shfl_xor_sync(0xffffffffu, part, 1);
     part += __shfl_xor_sync(0xffffffffu, part, 2);
     if (q == 0 && ch0 < f.cells) {
         const float rc = f.r[ch];
-        const float xc = f.dinv[ch] * rc + c.e[(cx >> 1) * c.nz + (cz >> 1)];
+        const float xc = f.dinv[ch] * rc + kMgCoarseWeight * c.e[(cx >> 1) * c.nz + (cz >> 1)];
         f.e[ch] = xc + f.dinv[ch] * (rc - part);
     }
 }
@@ -309,56 +331,82 @@ struct MgBottom {
     const float* dense;
 };
 
-// n floats from global memory to shared memory, four independent 16-byte loads in flight
-// per thread where both sides are 16-byte aligned.
-__device__ __forceinline__ void stage_floats(float* dst, const float* __restrict__ src, int n, int tid, int nt) {
-    int done = 0;
-    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
-        const int n4 = n >> 2;
-        const float4* s4 = reinterpret_cast<const float4*>(src);
-        float4* d4 = reinterpret_cast<float4*>(dst);
-        int i = tid;
-        for (; i + 3 * nt < n4; i += 4 * nt) {
-            const float4 a = __ldg(s4 + i), b = __ldg(s4 + i + nt), c = __ldg(s4 + i + 2 * nt),
-                         d = __ldg(s4 + i + 3 * nt);
-            d4[i] = a;
-            d4[i + nt] = b;
-            d4[i + 2 * nt] = c;
-            d4[i + 3 * nt] = d;
+// The bottom kernel's shared-memory copies: every array it stages, as one list.  Each
+// thread issues eight independent 16-byte loads before it stores any of them, so the
+// whole stage takes about one round trip to L2 rather than one per array (arrays and
+// shared-memory segments both start on 16 bytes and hold a multiple of four floats).
+struct StageSeg {
+    float* dst;
+    const float* src;
+    int32_t n4;  // float4s
+};
+constexpr int kMaxStageSegs = 2 * kMgMaxLevels + 2;
+
+__device__ __forceinline__ void stage_segments(const StageSeg* segs, const int* pre4, int nseg, int tid, int nt) {
+    constexpr int kU = 8;
+    const int tot4 = pre4[nseg];
+    for (int base = 0; base < tot4; base += kU * nt) {
+        float4 v[kU];
+        float4* d[kU];
+        int s = 0;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int g = base + u * nt + tid;
+            d[u] = nullptr;
+            if (g < tot4) {
+                while (pre4[s + 1] <= g) s++;
+                const int o = g - pre4[s];
+                v[u] = __ldg(reinterpret_cast<const float4*>(segs[s].src) + o);
+                d[u] = reinterpret_cast<float4*>(segs[s].dst) + o;
+            }
         }
-        for (; i < n4; i += nt) d4[i] = __ldg(s4 + i);
-        done = 4 * n4;
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+            if (d[u]) *d[u] = v[u];
     }
-    for (int k = done + tid; k < n; k += nt) dst[k] = __ldg(src + k);
 }
 
 // Levels first..last in one block, everything in shared memory: per level the nine
 // coefficient planes, dinv, r and e, then the dense inverse of the last level.
 __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, const CgScalars* S,
                                                                 int mode) {
+    __shared__ StageSeg segs[kMaxStageSegs];
+    __shared__ int pre4[kMaxStageSegs + 1];
     pdl_begin();
     if (pcg_skip(S, mode)) return;
-    extern __shared__ float sm[];
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
     const int tid = threadIdx.x, nt = blockDim.x;
     float* ks[kMgMaxLevels + 1];
     float* ds[kMgMaxLevels + 1];
     float* rs[kMgMaxLevels + 1];
     float* es[kMgMaxLevels + 1];
     float* at = sm;
+    int nseg = 0;
     for (int l = B.first; l <= B.last; l++) {
         const int cells = B.lv[l].cells;
+        const int c4 = static_cast<int>(mg_round4(cells));
         ks[l] = at;
-        ds[l] = at + 9 * cells;
-        rs[l] = ds[l] + cells;
-        es[l] = rs[l] + cells;
-        at = es[l] + cells;
-        stage_floats(ks[l], B.lv[l].k32, 9 * cells, tid, nt);
-        stage_floats(ds[l], B.lv[l].dinv, cells, tid, nt);
+        ds[l] = at + mg_round4(9 * cells);
+        rs[l] = ds[l] + c4;
+        es[l] = rs[l] + c4;
+        at = es[l] + c4;
+        if (tid == 0) {
+            segs[nseg++] = StageSeg{ks[l], B.lv[l].k32, static_cast<int32_t>(mg_round4(9 * cells) / 4)};
+            segs[nseg++] = StageSeg{ds[l], B.lv[l].dinv, c4 / 4};
+        }
     }
     const int m = B.lv[B.last].cells;
     float* dn = at;
-    stage_floats(dn, B.dense, m * m, tid, nt);
-    stage_floats(rs[B.first], B.lv[B.first].r, B.lv[B.first].cells, tid, nt);
+    if (tid == 0) {
+        segs[nseg++] = StageSeg{dn, B.dense, static_cast<int32_t>(mg_round4(static_cast<int64_t>(m) * m) / 4)};
+        segs[nseg++] = StageSeg{rs[B.first], B.lv[B.first].r, static_cast<int32_t>(mg_round4(B.lv[B.first].cells) / 4)};
+        pre4[0] = 0;
+        for (int k = 0; k < nseg; k++) pre4[k + 1] = pre4[k] + segs[k].n4;
+    }
+    nseg = 2 * (B.last - B.first + 1) + 2;
+    __syncthreads();
+    stage_segments(segs, pre4, nseg, tid, nt);
     __syncthreads();
     for (int l = B.first; l < B.last; l++) {
         const MgLevel& f = B.lv[l];
@@ -715,7 +763,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
                     for (int dz = -1; dz <= 1; dz++) {
                         const int k = (dx + 1) * 3 + dz + 1;
                         const int ax = clampi(gx + dx, F.nx - 1), az = clampi(gz + dz, F.nz - 1);
-                        cen[k] = top ? cn[k] : ce[((ax >> 1) - clx) * cwz + ((az >> 1) - clz)];
+                        cen[k] = kMgCoarseWeight * (top ? cn[k] : ce[((ax >> 1) - clx) * cwz + ((az >> 1) - clz)]);
                     }
                 }
                 const float rc0 = rn[4];
@@ -750,10 +798,10 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
 }
 
 size_t bottom_bytes(const MgLevel* lv, int first, int last) {
-    size_t floats = 0;
-    for (int l = first; l <= last; l++) floats += 12 * static_cast<size_t>(lv[l].cells);
-    const size_t m = static_cast<size_t>(lv[last].cells);
-    return (floats + m * m) * sizeof(float);
+    int64_t floats = 0;
+    for (int l = first; l <= last; l++) floats += mg_round4(9 * static_cast<int64_t>(lv[l].cells)) + 3 * mg_round4(lv[l].cells);
+    const int64_t m = lv[last].cells;
+    return static_cast<size_t>(floats + mg_round4(m * m)) * sizeof(float);
 }
 
 size_t dense_smem(const MgHierarchy& mg) {
@@ -801,7 +849,7 @@ void mg_setup_level1(const MgHierarchy& mg, const CgOperands& o, cudaStream_t s)
                                                           kMgOmegaCoarse, mg.status, mg.active_flag);
     launch_exclusive_scan(mg.active_flag, mg.active_pos, mg.lv[1].cells, mg.scan_scratch, s);
     k_mg_active<<<grid_for(mg.lv[1].cells), kBlock, 0, s>>>(mg.lv[1].cells, mg.active_flag, mg.active_pos,
-                                                           mg.active);
+                                                           mg.cell_start, mg.active, mg.active_rows);
 }
 
 void mg_setup_coarse(const MgHierarchy& mg, cudaStream_t s) {
@@ -823,9 +871,9 @@ void mg_apply(const MgHierarchy& mg, const CgScalars* S, int mode, const float* 
     const MgLevel& L1 = mg.lv[1];
     const int g1 = active_grid(L1.cells);
     if (fuse_axpy)
-        launch_pdl(k_mg_axpy_restrict, g1, kBlock, 0, s, *fuse_axpy, L1, mg.cell_start, mg.active, mg.n_active);
+        launch_pdl(k_mg_axpy_restrict, g1, kBlock, 0, s, *fuse_axpy, L1, mg.active_rows, mg.active, mg.n_active);
     else
-        launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.cell_start, r, S, mode, mg.active, mg.n_active);
+        launch_pdl(k_mg_restrict0, g1, kBlock, 0, s, L1, mg.active_rows, r, S, mode, mg.active, mg.n_active);
     MgBottom B{};
     B.first = mg.bottom;
     B.last = mg.levels;

@@ -31,6 +31,16 @@ constexpr int kMgBottomThreads = 1024;
 constexpr int kMgFuseLevels = 3;
 constexpr float kMgOmegaFine = 0.5f;   // Jacobi weight of the particle level
 constexpr float kMgOmegaCoarse = 0.9f; // Jacobi weight of the cell levels (best of 0.6-0.9 measured)
+// Weight of the coarse-grid correction at every cell level: piecewise-constant aggregation
+// underestimates the smooth error components, and over-weighting their correction is the
+// usual remedy for unsmoothed aggregation.  A CPU model of this cycle on the 320k
+// dam break's PPE system gave 62 PCG iterations to 1e-8 at weight 1, 41-42 at 1.5-1.7 and
+// 48 at 1.9 (84k tank: 41 -> 39).  The cycle stays symmetric, so CG applies.
+constexpr float kMgCoarseWeight = 1.6f;
+
+// Floats a cycle array of n values is allocated with (a multiple of four), so the bottom
+// kernel can stage every array with 16-byte loads.
+__host__ __device__ constexpr int64_t mg_round4(int64_t n) { return (n + 3) & ~static_cast<int64_t>(3); }
 
 // One cell level: nine coefficient planes K[d * cells + c], d = 3 (dx + 1) + (dz + 1).
 struct MgLevel {
@@ -56,6 +66,7 @@ struct MgHierarchy {
     const float* scale = nullptr;       // per-row scale of the Jacobi term (null: 1)
     double* bins = nullptr;             // 9 * n FP64 scratch of the level-1 product
     int32_t* active = nullptr;          // level-1 cells holding particles, ascending (per solve)
+    int2* active_rows = nullptr;        // their row ranges [cell_start[c], cell_start[c + 1])
     int32_t* n_active = nullptr;        // their count (the total of the flag scan)
     int32_t* active_flag = nullptr;     // per level-1 cell: 1 with particles
     int32_t* active_pos = nullptr;      // exclusive prefix sum of active_flag (cells + 1)
@@ -138,15 +149,16 @@ __device__ __forceinline__ float child_residual(int nx, int nz, int cells, const
     return valid ? res : 0.0f;
 }
 
-// Post-smoothed correction of fine cell (cx, cz): x = dinv r + e_parent, then one Jacobi
-// step; ce(px, pz) returns the coarse correction of parent cell (px, pz).
+// Post-smoothed correction of fine cell (cx, cz): x = dinv r + w e_parent (w the coarse
+// weight), then one Jacobi step; ce(px, pz) returns the coarse correction of parent cell
+// (px, pz).
 template <class CoarseE>
 __device__ __forceinline__ float smoothed_correction_at(int nx, int nz, int cells, const float* k,
                                                         const float* dinv, const float* r, int cx, int cz,
                                                         CoarseE ce) {
     const int ch = cx * nz + cz;
     const float rc = r[ch];
-    const float xc = dinv[ch] * rc + ce(cx >> 1, cz >> 1);
+    const float xc = dinv[ch] * rc + kMgCoarseWeight * ce(cx >> 1, cz >> 1);
     float res = rc;
 #pragma unroll
     for (int dx = -1; dx <= 1; dx++) {
@@ -154,7 +166,7 @@ __device__ __forceinline__ float smoothed_correction_at(int nx, int nz, int cell
         for (int dz = -1; dz <= 1; dz++) {
             const int nx_ = clampi(cx + dx, nx - 1), nz_ = clampi(cz + dz, nz - 1);
             const int nb = nx_ * nz + nz_;
-            const float xn = dinv[nb] * r[nb] + ce(nx_ >> 1, nz_ >> 1);
+            const float xn = dinv[nb] * r[nb] + kMgCoarseWeight * ce(nx_ >> 1, nz_ >> 1);
             res -= k[((dx + 1) * 3 + dz + 1) * cells + ch] * xn;
         }
     }

@@ -378,6 +378,8 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.ppe_col = dalloc<int32_t>(h, sell_cap);
     st.ppe_val = dalloc<double>(h, sell_cap);
     st.ppe_cv32 = dalloc<uint2>(h, sell_cap);
+    st.ppe_v32 = nullptr;
+    st.ppe_d16 = nullptr;
     st.ppe_b = dalloc<double>(h, n);
     st.ppe_x = dalloc<double>(h, n);
     st.step = dalloc<StepScalars>(h, 1);
@@ -413,6 +415,11 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         st.unplaced = dalloc<int32_t>(h, n);
         st.unplaced_pos = dalloc<int32_t>(h, n + 1);
         st.row_scratch = dalloc<int32_t>(h, scan_scratch_ints(static_cast<int>(std::max<int64_t>(cells, n))));
+        // cell-ordered rows: a column is within (gnz + 2) max_per_cell rows of its row
+        if ((static_cast<int64_t>(sc.gnz) + 2) * sc.max_per_cell < 32768) {
+            st.ppe_v32 = dalloc<float>(h, sell_cap);
+            st.ppe_d16 = dalloc<int16_t>(h, sell_cap);
+        }
     }
     // multigrid hierarchy over the search cells (level sizes fixed by the domain)
     MgHierarchy& mg = h->mg;
@@ -424,15 +431,16 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         for (int l = 1; l <= mg.levels; l++) {
             MgLevel& L = mg.lv[l];
             L.k64 = dalloc<double>(h, 9 * static_cast<int64_t>(L.cells));
-            L.k32 = dalloc<float>(h, 9 * static_cast<int64_t>(L.cells));
-            L.dinv = dalloc<float>(h, L.cells);
-            L.r = dalloc<float>(h, L.cells);
-            L.e = dalloc<float>(h, L.cells);
+            L.k32 = dalloc<float>(h, mg_round4(9 * static_cast<int64_t>(L.cells)));
+            L.dinv = dalloc<float>(h, mg_round4(L.cells));
+            L.r = dalloc<float>(h, mg_round4(L.cells));
+            L.e = dalloc<float>(h, mg_round4(L.cells));
         }
         const int64_t m = mg.lv[mg.levels].cells;
-        mg.dense = dalloc<float>(h, m * m);
+        mg.dense = dalloc<float>(h, mg_round4(m * m));
         mg.bins = dalloc<double>(h, 9 * n);
         mg.active = dalloc<int32_t>(h, mg.lv[1].cells);
+        mg.active_rows = dalloc<int2>(h, mg.lv[1].cells);
         mg.active_flag = dalloc<int32_t>(h, mg.lv[1].cells);
         mg.active_pos = dalloc<int32_t>(h, mg.lv[1].cells + 1);
         mg.n_active = mg.active_pos + mg.lv[1].cells;
@@ -550,6 +558,8 @@ CgOperands cg_operands(mps_handle* h) {
     o.col = h->st.ppe_col;
     o.val = h->st.ppe_val;
     o.cv32 = h->st.ppe_cv32;
+    o.v32 = h->st.ppe_v32;
+    o.d16 = h->st.ppe_d16;
     o.b = h->st.ppe_b;
     o.x = h->st.ppe_x;
     o.r = h->r;
@@ -1614,6 +1624,21 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
         h->stats.kernel_launches += reps + 1;
         *ms_per_launch = total / static_cast<float>(reps);
     });
+}
+
+int mps_spmv_bytes(mps_handle* h, int32_t solver, int64_t* bytes) {
+    if (!h || !bytes) return MPS_ERR_INVALID_ARGUMENT;
+    if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED && solver != MPS_SOLVER_MIXED_MG)
+        return MPS_ERR_NOT_SUPPORTED;
+    const int64_t nnz = h->stats.ppe_nnz, n = h->n;
+    const int64_t e = h->st.ppe_d16 ? 6 : 8;
+    if (solver == MPS_SOLVER_CG64)
+        *bytes = 12 * nnz + 4 * (n + 1) + 16 * n;
+    else if (solver == MPS_SOLVER_MIXED)
+        *bytes = e * nnz + 4 * (n + 1) + 8 * n;
+    else
+        *bytes = e * nnz + 4 * (n + 1) + 12 * n;
+    return MPS_OK;
 }
 
 // ---------------------------------------------------------------- stages
