@@ -276,9 +276,8 @@ int mps_bench_spmv(mps_handle* h, int32_t solver, int32_t reps, int64_t flush_by
                    float* ms_per_launch);
 /* Algorithmic bytes of one launch of that SpMV on the last assembled matrix (nnz entries,
  * n rows): every matrix entry and row length read once, each vector read or written once
- * per row.  FP64 CG: 12 nnz + 4 (n + 1) + 16 n; MIXED: e nnz + 4 (n + 1) + 8 n; MIXED_MG:
- * e nnz + 4 (n + 1) + 12 n, where e = 8 bytes per FP32 entry ({column, value}) or 6 where
- * the handle stores 16-bit column offsets (2D scenes whose offsets fit). */
+ * per row.  FP64 CG: 12 nnz + 4 (n + 1) + 16 n; MIXED: 8 nnz + 4 (n + 1) + 8 n; MIXED_MG:
+ * 8 nnz + 4 (n + 1) + 12 n (an FP32 entry is {column, value}). */
 int mps_spmv_bytes(mps_handle* h, int32_t solver, int64_t* bytes);
 
 /* ------------------------------------------------------------------------

@@ -423,51 +423,6 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
     return acc;
 }
 
-// The same row from the 6-byte streams (FP32 value, 16-bit column offset from `row`):
-// the same products summed in the same order, so the same result as row32 with a quarter
-// fewer bytes of matrix.
-template <int D = 8>
-__device__ __forceinline__ float row16(const CgOperands& o, int64_t at, int L, int row,
-                                       const float* __restrict__ v) {
-    float acc = 0.0f;
-    const int nb = L / D;
-    float a[D];
-    int c[D];
-    if (nb > 0) {
-#pragma unroll
-        for (int u = 0; u < D; u++) {
-            a[u] = ld_sell_f32(o.v32 + at + u * kSellRows);
-            c[u] = ld_sell_s16(o.d16 + at + u * kSellRows);
-        }
-    }
-    for (int bt = 0; bt < nb; bt++) {
-        float xv[D];
-#pragma unroll
-        for (int u = 0; u < D; u++) xv[u] = v[row + c[u]];
-        float a2[D];
-        int c2[D];
-        if (bt + 1 < nb) {
-            const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
-#pragma unroll
-            for (int u = 0; u < D; u++) {
-                a2[u] = ld_sell_f32(o.v32 + nx + u * kSellRows);
-                c2[u] = ld_sell_s16(o.d16 + nx + u * kSellRows);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < D; u++) acc = fmaf(a[u], xv[u], acc);
-#pragma unroll
-        for (int u = 0; u < D; u++) {
-            a[u] = a2[u];
-            c[u] = c2[u];
-        }
-    }
-    at += static_cast<int64_t>(nb) * D * kSellRows;
-    for (int k = nb * D; k < L; k++, at += kSellRows)
-        acc = fmaf(ld_sell_f32(o.v32 + at), v[row + ld_sell_s16(o.d16 + at)], acc);
-    return acc;
-}
-
 // init: r_0 = b - A x (FP64); r32 = r_0; d = 0; p = 0; s = 0; rr, bb
 __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
@@ -521,7 +476,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_axpy(CgOperands o) {
 // workloads when the FP32 recursion makes progress).
 constexpr int kMixedStallIter = 2000;
 
-template <bool kOff16>
 __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
                                                    cudaGraphConditionalHandle h,
                                                    cudaGraphConditionalHandle h_true, int use_cond) {
@@ -541,8 +495,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
     for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
         const int L = o.len[i];
-        const int64_t at = sell_index(o.off[c], cl.lane, 0);
-        const float wi = kOff16 ? row16(o, at, L, i, r) : row32(o, at, L, r);
+        const float wi = row32(o, sell_index(o.off[c], cl.lane, 0), L, r);
         if (i < o.n) {
             const double ri = static_cast<double>(r[i]);
             o.w32[i] = wi;
@@ -595,12 +548,25 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv(CgOperands o, int mode,
     }
 }
 
-// the plain mixed SpMV for the handle's FP32 layout
-using MxSpmvKernel = void (*)(CgOperands, int, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int);
-MxSpmvKernel mx_spmv(const CgOperands& o) { return o.d16 ? k_mx_spmv<true> : k_mx_spmv<false>; }
-
 // Reliable update, part 1: x' = x + d and r = b - A x' in FP64 (FP64 matrix), written
 // over the r the iteration produced; convergence on this true residual.
+// The scalars after a reliable update's true residual r.r: the new reference for the
+// next update, and convergence (which ends the loop).
+__device__ __forceinline__ void true_residual_done(CgScalars* S, double rr, cudaGraphConditionalHandle h,
+                                                   int use_cond) {
+    S->true_rr = rr;
+    S->rr_upd = rr;
+    S->rr_new = rr;
+    S->updates += 1;
+    S->iter_upd = S->iter;
+    const int conv = rr < S->thr;
+    S->converged = conv;
+    if (conv) {
+        S->iter += 1;
+        if (use_cond) cudaGraphSetConditional(h, 0u);
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphConditionalHandle h,
                                                    int use_cond) {
     __shared__ BlockTicket tk;
@@ -627,22 +593,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_true(CgOperands o, cudaGraphCondi
     }
     double tot[3];
     if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
-        const double rr = tot[0];
-        {
-            CgScalars* S = o.S;
-            S->counter = 0;
-            S->true_rr = rr;
-            S->rr_upd = rr;
-            S->rr_new = rr;
-            S->updates += 1;
-            S->iter_upd = S->iter;
-            const int conv = rr < S->thr;
-            S->converged = conv;
-            if (conv) {
-                S->iter += 1;
-                if (use_cond) cudaGraphSetConditional(h, 0u);
-            }
-        }
+        o.S->counter = 0;
+        true_residual_done(o.S, tot[0], h, use_cond);
     }
 }
 
@@ -669,7 +621,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 // (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
 // Four entries per pipeline step and at most 48 registers: five blocks per SM hide the
 // gather latency better than eight-deep steps at four blocks (measured 53 -> 51 us).
-template <bool kOff16>
 __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
@@ -684,8 +635,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
     for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
         const int L = o.len[i];
-        const int64_t at = sell_index(o.off[c], cl.lane, 0);
-        const float wi = kOff16 ? row16<4>(o, at, L, i, u) : row32<4>(o, at, L, u);
+        const float wi = row32<4>(o, sell_index(o.off[c], cl.lane, 0), L, u);
         if (i < o.n) {
             const double ri = static_cast<double>(o.r32[i]);
             const double ui = static_cast<double>(u[i]);
@@ -884,12 +834,22 @@ __device__ __forceinline__ double stage_row64(const int32_t* __restrict__ sc, co
     return acc;
 }
 
-// k_cg_spmv_dot with the staged stream: Ap = A p and p.Ap, alpha = rr / p.Ap.
-template <int SLICE, int STAGES, int MINB>
-__global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOperands o) {
+// What a staged FP64 SpMV computes: the CG's A p (with p.Ap and the step size alpha =
+// rr / p.Ap, as k_cg_spmv_dot), or the mixed solves' true residual r = b - A x' after a
+// reliable update folded the FP32 correction into x' (with r.r and the update's decisions).
+enum StagedKind { kStagedCgAp = 0, kStagedTrueResidual = 1 };
+
+// k_cg_spmv_dot with the staged stream.
+template <int SLICE, int STAGES, int MINB, int KIND>
+__global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOperands o, cudaGraphConditionalHandle h,
+                                                                          int use_cond) {
     extern __shared__ __align__(128) unsigned char stg_sm[];
     __shared__ BlockTicket tk;
-    if (cg_done(o.S)) return;
+    if (KIND == kStagedCgAp) {
+        if (cg_done(o.S)) return;
+    } else if (o.S->converged || o.S->aborted || o.S->stalled || !o.S->do_update) {
+        return;
+    }
     ticket_init(tk);
     using Ring = StageRing<SLICE, STAGES, 2>;
     constexpr int kStageBytes = Ring::kEntries * 12;
@@ -904,7 +864,8 @@ __global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOper
            reinterpret_cast<uint64_t*>(stg_sm + static_cast<size_t>(kStgWarps) * STAGES * kStageBytes) + w * STAGES,
            gw);
     for (int k = 0; k < STAGES; k++) R.issue(o, nw);
-    const double* __restrict__ p = o.p;
+    // the gathered vector: p, or the folded solution x' (the buffer the update writes)
+    const double* __restrict__ p = KIND == kStagedCgAp ? o.p : ((o.S->updates & 1) != 0 ? o.x : o.x2);
     double v = 0.0;
     int item = 0;
     bool ok = true;
@@ -931,17 +892,39 @@ __global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOper
         }
         if (!ok) break;
         if (i < o.n) {
-            o.Ap[i] = acc;
-            v += p[i] * acc;
+            if (KIND == kStagedCgAp) {
+                o.Ap[i] = acc;
+                v += p[i] * acc;
+            } else {
+                const double ri = o.b[i] - acc;
+                o.r32[i] = __double2float_rn(ri);
+                v += ri * ri;
+            }
         }
     }
     double tot[3];
     if (grid_sum(v, 0.0, 0.0, o.partials, o.tickets, &o.S->counter, tk, tot)) {
-        o.S->counter = 0;
-        o.S->pAp = tot[0];
-        o.S->alpha = o.S->rr / tot[0];
-        if (o.status && (o.status->flags & kStatusWaitTimeout)) o.S->aborted = 1;
+        CgScalars* S = o.S;
+        S->counter = 0;
+        if (KIND == kStagedCgAp) {
+            S->pAp = tot[0];
+            S->alpha = S->rr / tot[0];
+        } else {
+            true_residual_done(S, tot[0], h, use_cond);
+        }
+        if (o.status && (o.status->flags & kStatusWaitTimeout)) S->aborted = 1;
     }
+}
+
+// The reliable update's first half: x' = x + d in FP64, into the other solution buffer
+// (the staged true-residual SpMV then gathers x').
+__global__ void __launch_bounds__(kBlock) k_mx_fold(CgOperands o) {
+    if (o.S->converged || o.S->aborted || o.S->stalled || !o.S->do_update) return;
+    const bool odd = (o.S->updates & 1) != 0;
+    const double* __restrict__ xc = odd ? o.x2 : o.x;
+    double* __restrict__ xn = odd ? o.x : o.x2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x)
+        xn[i] = xc[i] + static_cast<double>(o.d32[i]);
 }
 
 // The staged FP64 SpMV: 8-entry slices, two stages per warp, three blocks of eight warps
@@ -961,20 +944,38 @@ void launch_cg_spmv(const CgOperands& o, cudaStream_t s) {
         const int cap = o.grid_staged * g_stg_per_sm64;
         const int need = (o.nchunks + kStgWarps - 1) / kStgWarps;
         const int g = need < cap ? (need > 0 ? need : 1) : cap;
-        k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64><<<g, kStgThreads, kStgSmem64, s>>>(o);
+        k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64, kStagedCgAp>
+            <<<g, kStgThreads, kStgSmem64, s>>>(o, 0, 0);
         return;
     }
     k_cg_spmv_dot<<<o.grid_spmv, kBlock, 0, s>>>(o);
 }
 
+// A reliable update's true residual: the fold x' = x + d and the staged FP64 SpMV
+// r = b - A x' (about 50 us at 340k), or, without an SM count, one per-chunk kernel that
+// gathers x + d on the fly.
+void launch_mx_true(const CgOperands& o, cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+    if (o.grid_staged > 0) {
+        const int cap = o.grid_staged * g_stg_per_sm64;
+        const int need = (o.nchunks + kStgWarps - 1) / kStgWarps;
+        const int g = need < cap ? (need > 0 ? need : 1) : cap;
+        k_mx_fold<<<o.grid_vec, kBlock, 0, s>>>(o);
+        k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64, kStagedTrueResidual>
+            <<<g, kStgThreads, kStgSmem64, s>>>(o, h, use_cond);
+        return;
+    }
+    k_mx_true<<<o.grid_spmv, kBlock, 0, s>>>(o, h, use_cond);
+}
+
+int mx_true_launches(const CgOperands& o) { return o.grid_staged > 0 ? 2 : 1; }
+
 // the preconditioned FP32 SpMV (w = A u, three dot products)
 void launch_pmx_spmv(const CgOperands& o, int mode, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_true,
                      int use_cond, cudaStream_t s, bool pdl) {
     if (pdl)
-        launch_pdl(o.d16 ? k_pmx_spmv<true> : k_pmx_spmv<false>, o.grid_spmv, kBlock, 0, s, o, mode, h, h_true,
-                   use_cond);
+        launch_pdl(k_pmx_spmv, o.grid_spmv, kBlock, 0, s, o, mode, h, h_true, use_cond);
     else
-        (o.d16 ? k_pmx_spmv<true> : k_pmx_spmv<false>)<<<o.grid_spmv, kBlock, 0, s>>>(o, mode, h, h_true, use_cond);
+        k_pmx_spmv<<<o.grid_spmv, kBlock, 0, s>>>(o, mode, h, h_true, use_cond);
 }
 
 // After the fallback: report it in the primary scalars.
@@ -1318,12 +1319,12 @@ void cg64_body(const CgOperands& ops, cudaGraphConditionalHandle h, int use_cond
 
 void reliable_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
                       cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
-    k_mx_true<<<ops.grid_spmv, kBlock, 0, s>>>(ops, h, use_cond);
+    launch_mx_true(ops, h, use_cond, s);
     if (is_pcg(solver)) {
         mg_apply(*mg, ops.S, 2, ops.r32, ops.u32, s);
         launch_pmx_spmv(ops, 2, h, 0, use_cond, s, false);
     } else {
-        mx_spmv(ops)<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
+        k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 2, h, 0, use_cond);
     }
 }
 
@@ -1340,7 +1341,7 @@ void body_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
         launch_pmx_spmv(ops, 1, h, h_true, use_cond, s, true);
     } else {
         k_mx_axpy<<<gv, kBlock, 0, s>>>(ops);
-        mx_spmv(ops)<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 1, h, h_true, use_cond);
     }
     if (with_true) reliable_kernels(solver, ops, mg, h, use_cond, s);
 }
@@ -1408,7 +1409,7 @@ void init_kernels(int solver, const CgOperands& ops, const MgHierarchy* mg,
         mg_apply(*mg, ops.S, 0, ops.r32, ops.u32, s);
         launch_pmx_spmv(ops, 0, h, 0, use_cond, s, false);
     } else {
-        mx_spmv(ops)<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, use_cond);
+        k_mx_spmv<<<gs, kBlock, 0, s>>>(ops, 0, h, 0, use_cond);
     }
 }
 
@@ -1418,8 +1419,11 @@ int cg_grid_vec(int64_t n) { return grid_for(n); }
 int cg_grid_spmv(int64_t n) { return grid_for(sell_chunks(n) * 32); }
 
 cudaError_t cg_prepare_device() {
-    auto k = k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64>;
+    auto k = k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64, kStagedCgAp>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStgSmem64));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_cg_spmv_dot_staged<kStgSlice64, kStgStages64, kStgBlocks64, kStagedTrueResidual>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStgSmem64));
     if (e != cudaSuccess) return e;
     int b = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kStgThreads, kStgSmem64);
@@ -1450,7 +1454,7 @@ void launch_spmv_only(int solver, const CgOperands& ops, cudaStream_t s) {
     else if (is_pcg(solver))
         launch_pmx_spmv(ops, 1, 0, 0, 0, s, false);
     else
-        mx_spmv(ops)<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
+        k_mx_spmv<<<ops.grid_spmv, kBlock, 0, s>>>(ops, 1, 0, 0, 0);
 }
 
 void learned_prep(const LearnedOps& L, const CgOperands& o, const MgHierarchy& mg, CgScalars* S,
@@ -1468,9 +1472,10 @@ int cg_kernels_per_iteration(int solver, const MgHierarchy* mg) {
     return is_pcg(solver) && mg ? 1 + mg_apply_launches(*mg) : 2;
 }
 
-int cg_kernels_per_update(int solver, const MgHierarchy* mg) {
+int cg_kernels_per_update(int solver, const MgHierarchy* mg, const CgOperands& ops) {
     if (solver == MPS_SOLVER_CG64) return 0;
-    return is_pcg(solver) && mg ? 2 + mg_apply_launches(*mg) : 2;
+    const int t = mx_true_launches(ops);
+    return is_pcg(solver) && mg ? t + 1 + mg_apply_launches(*mg) : t + 1;
 }
 
 CgGraph::~CgGraph() {
@@ -1554,7 +1559,7 @@ cudaError_t CgGraph::build_impl(int solver, const CgOperands& ops, cudaStream_t 
     solver_ = solver;
     nested_ = nested;
     kpi_ = cg_kernels_per_iteration(solver, mg);
-    kri_ = cg_kernels_per_update(solver, mg);
+    kri_ = cg_kernels_per_update(solver, mg, ops);
     const int gv = ops.grid_vec, gs = ops.grid_spmv;
     cudaError_t e = cudaGraphCreate(&graph_, 0);
     if (e != cudaSuccess) return e;
@@ -1768,7 +1773,7 @@ cudaError_t host_loop(int solver, const CgOperands& ops, const MgHierarchy* mg, 
         for (int c = 0; c < chunk; c++) {
             body_kernels(solver, ops, mg, none, none, 0, true, s);
             // every kernel of the iteration and of the reliable update is launched
-            *k += cg_kernels_per_iteration(solver, mg) + cg_kernels_per_update(solver, mg);
+            *k += cg_kernels_per_iteration(solver, mg) + cg_kernels_per_update(solver, mg, ops);
         }
         e = cudaGetLastError();
     }

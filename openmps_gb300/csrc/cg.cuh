@@ -15,18 +15,6 @@ __device__ __forceinline__ uint2 ld_sell_pair(const uint2* p) {
     return e;
 }
 
-// The two streams of the 6-byte FP32 layout, loaded the same way.
-__device__ __forceinline__ float ld_sell_f32(const float* p) {
-    float v;
-    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ int ld_sell_s16(const int16_t* p) {
-    short d;
-    asm("ld.global.nc.L1::no_allocate.s16 %0, [%1];" : "=h"(d) : "l"(p));
-    return d;
-}
-
 // Scalars of one solve, in device memory (read back once per step).
 struct CgScalars {
     double rr;        // r.r of the current direction update
@@ -68,8 +56,6 @@ struct CgOperands {
     const int32_t* col; // SELL-32 columns
     const double* val;  // SELL-32 FP64 values
     const uint2* cv32;  // SELL-32 {column, FP32 value}
-    const float* v32;   // SELL-32 FP32 values and column offsets (column - row), 6 bytes
-    const int16_t* d16; // per entry; null: the SpMVs read cv32
     const double* b;
     double* x;          // initial guess in, solution out
     // CG64
@@ -171,7 +157,7 @@ cudaError_t cg_run_direct(int solver, const CgOperands& ops, CgScalars* host_S, 
 int persistent_blocks();
 // Kernels of one iteration of the solver, and of one reliable update.
 int cg_kernels_per_iteration(int solver, const MgHierarchy* mg);
-int cg_kernels_per_update(int solver, const MgHierarchy* mg);
+int cg_kernels_per_update(int solver, const MgHierarchy* mg, const CgOperands& ops);
 
 // Sets eps / criterion / max_iter / delta for the next solve (stream-ordered).
 void launch_cg_configure(CgScalars* S, double eps, int criterion, int max_iter, double delta2,

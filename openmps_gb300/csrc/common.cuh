@@ -119,11 +119,6 @@ struct DeviceState {
     int32_t* ppe_col;                              // SELL-32 columns
     double* ppe_val;                               // SELL-32 FP64 values
     uint2* ppe_cv32;                               // SELL-32 {column, FP32 value}
-    // The same FP32 matrix as two streams, values and 16-bit column offsets (column - row),
-    // 6 bytes per entry; null where an offset may not fit in 16 bits (rows are in cell
-    // order, so |column - row| < (gnz + 2) max_per_cell, checked when the handle is made).
-    float* ppe_v32;
-    int16_t* ppe_d16;
     StepScalars* step;
     DevStatus* status;
     const int32_t* solve_ok;  // converged flag of the last PPE solve

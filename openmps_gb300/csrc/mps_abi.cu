@@ -378,8 +378,6 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.ppe_col = dalloc<int32_t>(h, sell_cap);
     st.ppe_val = dalloc<double>(h, sell_cap);
     st.ppe_cv32 = dalloc<uint2>(h, sell_cap);
-    st.ppe_v32 = nullptr;
-    st.ppe_d16 = nullptr;
     st.ppe_b = dalloc<double>(h, n);
     st.ppe_x = dalloc<double>(h, n);
     st.step = dalloc<StepScalars>(h, 1);
@@ -415,11 +413,6 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         st.unplaced = dalloc<int32_t>(h, n);
         st.unplaced_pos = dalloc<int32_t>(h, n + 1);
         st.row_scratch = dalloc<int32_t>(h, scan_scratch_ints(static_cast<int>(std::max<int64_t>(cells, n))));
-        // cell-ordered rows: a column is within (gnz + 2) max_per_cell rows of its row
-        if ((static_cast<int64_t>(sc.gnz) + 2) * sc.max_per_cell < 32768) {
-            st.ppe_v32 = dalloc<float>(h, sell_cap);
-            st.ppe_d16 = dalloc<int16_t>(h, sell_cap);
-        }
     }
     // multigrid hierarchy over the search cells (level sizes fixed by the domain)
     MgHierarchy& mg = h->mg;
@@ -558,8 +551,6 @@ CgOperands cg_operands(mps_handle* h) {
     o.col = h->st.ppe_col;
     o.val = h->st.ppe_val;
     o.cv32 = h->st.ppe_cv32;
-    o.v32 = h->st.ppe_v32;
-    o.d16 = h->st.ppe_d16;
     o.b = h->st.ppe_b;
     o.x = h->st.ppe_x;
     o.r = h->r;
@@ -1631,13 +1622,12 @@ int mps_spmv_bytes(mps_handle* h, int32_t solver, int64_t* bytes) {
     if (solver != MPS_SOLVER_CG64 && solver != MPS_SOLVER_MIXED && solver != MPS_SOLVER_MIXED_MG)
         return MPS_ERR_NOT_SUPPORTED;
     const int64_t nnz = h->stats.ppe_nnz, n = h->n;
-    const int64_t e = h->st.ppe_d16 ? 6 : 8;
     if (solver == MPS_SOLVER_CG64)
         *bytes = 12 * nnz + 4 * (n + 1) + 16 * n;
     else if (solver == MPS_SOLVER_MIXED)
-        *bytes = e * nnz + 4 * (n + 1) + 8 * n;
+        *bytes = 8 * nnz + 4 * (n + 1) + 8 * n;
     else
-        *bytes = e * nnz + 4 * (n + 1) + 12 * n;
+        *bytes = 8 * nnz + 4 * (n + 1) + 12 * n;
     return MPS_OK;
 }
 

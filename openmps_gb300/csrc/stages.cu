@@ -593,19 +593,8 @@ __global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
         const int64_t at = sell_index(base, r, rank);
         st.ppe_col[at] = ce;
         st.ppe_val[at] = v;
-        if (want_fp32) {
-            const float v32 = __double2float_rn(v);
-            st.ppe_cv32[at] = make_uint2(static_cast<unsigned>(ce), __float_as_uint(v32));
-            if (st.ppe_d16) {
-                const int d = ce - row;
-                if (d < -32768 || d > 32767) {  // cannot happen for cell-ordered rows: fail the step
-                    atomicOr(&st.status->flags, kStatusDeviceCheck);
-                    st.status->check_index = i;
-                }
-                st.ppe_v32[at] = v32;
-                st.ppe_d16[at] = static_cast<int16_t>(d);
-            }
-        }
+        if (want_fp32) st.ppe_cv32[at] = make_uint2(static_cast<unsigned>(ce),
+                                                     __float_as_uint(__double2float_rn(v)));
     };
     // Rows in search-cell order: a neighbour list walks the cells in ascending cell index
     // and each cell in slot (= row) order, so the off-diagonal columns arrive ascending and
