@@ -617,6 +617,47 @@ __global__ void __launch_bounds__(kBlock) k_mx_finish(CgOperands o) {
 // one reduction.  A and M are both negative definite on the rows the solve acts on, so
 // this is CG on the SPD pair (-A, -M).
 
+// The last block's step of the preconditioned SpMV: the dot products gamma = r.u,
+// delta = w.u, rho = r.r decide the next step sizes, a reliable update (mode 1) or a
+// stall (mode 2), and the loop's condition.
+__device__ __forceinline__ void pmx_finish(CgScalars* S, int mode, const double* tot, cudaGraphConditionalHandle h,
+                                           cudaGraphConditionalHandle h_true, int use_cond) {
+    const double gam = tot[0];
+    const double del = tot[1];
+    const double rho = tot[2];
+    S->counter = 0;
+    S->rr_new = rho;
+    int reliable = 0;
+    int stalled = 0;
+    if (mode == 1) {
+        reliable = (rho < S->delta2 * S->rr_upd) || (rho < S->thr);
+        S->do_update = reliable;
+        if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
+    } else if (mode == 2) {
+        stalled = S->true_rr > 0.25 * S->prev_true_rr;
+        S->prev_true_rr = S->true_rr;
+    }
+    if (!reliable && !stalled) {
+        double alpha, beta = 0.0;
+        if (mode == 0) {
+            alpha = gam / del;
+        } else {
+            beta = gam / S->rr;
+            alpha = gam / (del - beta * gam / S->alpha);
+            S->iter += 1;
+        }
+        stalled = !(std::isfinite(alpha) && std::isfinite(beta) && alpha != 0.0);
+        S->alpha = alpha;
+        S->beta = beta;
+        S->rr = gam;
+        S->pAp = del;
+    }
+    if (mode == 2) S->do_update = 0;
+    S->stalled = stalled;
+    if (use_cond && (mode != 1 || !reliable))
+        cudaGraphSetConditional(h, (!stalled && S->iter < S->max_iter) ? 1u : 0u);
+}
+
 // w = A u (FP32); gamma, delta, rho in FP64; next step sizes; reliable-update decision
 // (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
 // Four entries per pipeline step and at most 48 registers: five blocks per SM hide the
@@ -647,44 +688,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
         }
     }
     double tot[3];
-    if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) {
-        const double gam = tot[0];
-        const double del = tot[1];
-        const double rho = tot[2];
-        {
-            S->counter = 0;
-            S->rr_new = rho;
-            int reliable = 0;
-            int stalled = 0;
-            if (mode == 1) {
-                reliable = (rho < S->delta2 * S->rr_upd) || (rho < S->thr);
-                S->do_update = reliable;
-                if (use_cond && h_true) cudaGraphSetConditional(h_true, reliable ? 1u : 0u);
-            } else if (mode == 2) {
-                stalled = S->true_rr > 0.25 * S->prev_true_rr;
-                S->prev_true_rr = S->true_rr;
-            }
-            if (!reliable && !stalled) {
-                double alpha, beta = 0.0;
-                if (mode == 0) {
-                    alpha = gam / del;
-                } else {
-                    beta = gam / S->rr;
-                    alpha = gam / (del - beta * gam / S->alpha);
-                    S->iter += 1;
-                }
-                stalled = !(std::isfinite(alpha) && std::isfinite(beta) && alpha != 0.0);
-                S->alpha = alpha;
-                S->beta = beta;
-                S->rr = gam;
-                S->pAp = del;
-            }
-            if (mode == 2) S->do_update = 0;
-            S->stalled = stalled;
-            if (use_cond && (mode != 1 || !reliable))
-                cudaGraphSetConditional(h, (!stalled && S->iter < S->max_iter) ? 1u : 0u);
-        }
-    }
+    if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) pmx_finish(S, mode, tot, h, h_true, use_cond);
 }
 
 // ------------------------------------------------ staged SELL stream
@@ -783,7 +787,7 @@ struct StageRing {
     __device__ void issue(const CgOperands& o, int nw) {
         while (pc < o.nchunks) {
             const int off = o.off[pc];
-            const int width = (o.off[pc + 1] - off) / kSellRows;
+            const int width = o.chunk[pc] / kSellRows;
             if (ps * SLICE < width) {
                 const int m = min(SLICE, width - ps * SLICE);
                 if ((threadIdx.x & 31) == 0) {
@@ -810,36 +814,14 @@ struct StageRing {
     }
 };
 
-// Sums the lane's FP64 row from the stage (columns and values apart), ascending k, one
-// accumulator (the order of row64).
-__device__ __forceinline__ double stage_row64(const int32_t* __restrict__ sc, const double* __restrict__ sv, int m,
-                                              const double* __restrict__ v, double acc) {
-    constexpr int D = 8;
-    const int lane = threadIdx.x & 31;
-    int k = 0;
-    for (; k + D <= m; k += D) {
-        int c[D];
-        double a[D], xv[D];
-#pragma unroll
-        for (int t = 0; t < D; t++) {
-            c[t] = sc[(k + t) * kSellRows + lane];
-            a[t] = sv[(k + t) * kSellRows + lane];
-        }
-#pragma unroll
-        for (int t = 0; t < D; t++) xv[t] = __ldg(v + c[t]);
-#pragma unroll
-        for (int t = 0; t < D; t++) acc = fma(a[t], xv[t], acc);
-    }
-    for (; k < m; k++) acc = fma(sv[k * kSellRows + lane], __ldg(v + sc[k * kSellRows + lane]), acc);
-    return acc;
-}
-
 // What a staged FP64 SpMV computes: the CG's A p (with p.Ap and the step size alpha =
 // rr / p.Ap, as k_cg_spmv_dot), or the mixed solves' true residual r = b - A x' after a
 // reliable update folded the FP32 correction into x' (with r.r and the update's decisions).
 enum StagedKind { kStagedCgAp = 0, kStagedTrueResidual = 1 };
 
-// k_cg_spmv_dot with the staged stream.
+// k_cg_spmv_dot with the staged stream.  A lane sums its row from the stages in
+// ascending column order with one accumulator (the order of row64), so the row sums are
+// those of the per-chunk kernel.
 template <int SLICE, int STAGES, int MINB, int KIND>
 __global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOperands o, cudaGraphConditionalHandle h,
                                                                           int use_cond) {
@@ -872,7 +854,7 @@ __global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOper
     for (int c = gw; c < o.nchunks && ok; c += nw) {
         const int i = kSellRows * c + lane;
         const int L = o.len[i];
-        const int width = (o.off[c + 1] - o.off[c]) / kSellRows;
+        const int width = o.chunk[c] / kSellRows;
         double acc = 0.0;
         for (int k0 = 0; k0 < width; k0 += SLICE, item++) {
             if (!stg_wait(R.bar + item % STAGES, (item / STAGES) & 1)) {
@@ -881,14 +863,31 @@ __global__ void __launch_bounds__(kStgThreads, MINB) k_cg_spmv_dot_staged(CgOper
                 ok = false;
                 break;
             }
+            // the lane's entries of this slice into registers, then the stage is refilled
+            // at once: the copy then overlaps this slice's gathers and multiply-adds
             const int m = min(SLICE, L - k0);
-            if (m > 0)
-                acc = stage_row64(reinterpret_cast<const int32_t*>(R.stage(item, 1)),
-                                  reinterpret_cast<const double*>(R.stage(item, 0)), m, p, acc);
+            const int32_t* sc = reinterpret_cast<const int32_t*>(R.stage(item, 1));
+            const double* sv = reinterpret_cast<const double*>(R.stage(item, 0));
+            int cc[SLICE];
+            double av[SLICE];
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) {
+                cc[t] = t < m ? sc[t * kSellRows + lane] : 0;
+                av[t] = t < m ? sv[t * kSellRows + lane] : 0.0;
+            }
+            // the values must have arrived before the copy may overwrite the stage
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) asm volatile("" ::"r"(cc[t]), "d"(av[t]));
             __syncwarp();
             if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             R.issue(o, nw);
+            double xv[SLICE];
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) xv[t] = t < m ? __ldg(p + cc[t]) : 0.0;
+#pragma unroll
+            for (int t = 0; t < SLICE; t++)
+                if (t < m) acc = fma(av[t], xv[t], acc);
         }
         if (!ok) break;
         if (i < o.n) {
@@ -926,6 +925,93 @@ __global__ void __launch_bounds__(kBlock) k_mx_fold(CgOperands o) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < o.n; i += gridDim.x * blockDim.x)
         xn[i] = xc[i] + static_cast<double>(o.d32[i]);
 }
+
+// k_pmx_spmv with the staged stream: the {column, FP32 value} pairs of each warp's chunk
+// come through a ring of shared-memory stages, each refilled as soon as the lanes have
+// read it, so the copies overlap the gathers of u and the FP32 multiply-adds.  A lane
+// sums its row in ascending column order, as row32 does.
+template <int SLICE, int STAGES, int MINB>
+__global__ void __launch_bounds__(kStgThreads, MINB) k_pmx_spmv_staged(CgOperands o, int mode,
+                                                                       cudaGraphConditionalHandle h,
+                                                                       cudaGraphConditionalHandle h_true,
+                                                                       int use_cond) {
+    extern __shared__ __align__(128) unsigned char stg_sm[];
+    __shared__ BlockTicket tk;
+    pdl_begin();
+    CgScalars* S = o.S;
+    if (pcg_skip(S, mode)) return;
+    ticket_init(tk);
+    using Ring = StageRing<SLICE, STAGES, 1>;
+    constexpr int kStageBytes = Ring::kEntries * 8;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kStgWarps + w, nw = gridDim.x * kStgWarps;
+    Ring R;
+    R.src[0] = o.cv32;
+    R.esize[0] = 8;
+    R.init(stg_sm + static_cast<size_t>(w) * STAGES * kStageBytes,
+           reinterpret_cast<uint64_t*>(stg_sm + static_cast<size_t>(kStgWarps) * STAGES * kStageBytes) + w * STAGES,
+           gw);
+    for (int k = 0; k < STAGES; k++) R.issue(o, nw);
+    const float* __restrict__ u = o.u32;
+    double vg = 0.0, vd = 0.0, vr = 0.0;
+    int item = 0;
+    bool ok = true;
+    for (int c = gw; c < o.nchunks && ok; c += nw) {
+        const int i = kSellRows * c + lane;
+        const int L = o.len[i];
+        const int width = o.chunk[c] / kSellRows;
+        float acc = 0.0f;
+        for (int k0 = 0; k0 < width; k0 += SLICE, item++) {
+            if (!stg_wait(R.bar + item % STAGES, (item / STAGES) & 1)) {
+                if (lane == 0 && o.status) atomicOr(&const_cast<DevStatus*>(o.status)->flags, kStatusWaitTimeout);
+                R.drain(item);
+                ok = false;
+                break;
+            }
+            const int m = min(SLICE, L - k0);
+            const uint2* se = reinterpret_cast<const uint2*>(R.stage(item, 0));
+            uint2 e[SLICE];
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) e[t] = t < m ? se[t * kSellRows + lane] : make_uint2(0u, 0u);
+            // the values must have arrived before the copy may overwrite the stage
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) asm volatile("" ::"r"(e[t].x), "r"(e[t].y));
+            __syncwarp();
+            if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            R.issue(o, nw);
+            float xv[SLICE];
+#pragma unroll
+            for (int t = 0; t < SLICE; t++) xv[t] = t < m ? u[e[t].x] : 0.0f;
+#pragma unroll
+            for (int t = 0; t < SLICE; t++)
+                if (t < m) acc = fmaf(__uint_as_float(e[t].y), xv[t], acc);
+        }
+        if (!ok) break;
+        if (i < o.n) {
+            const double ri = static_cast<double>(o.r32[i]);
+            const double ui = static_cast<double>(u[i]);
+            o.w32[i] = acc;
+            if (mode == 2) o.d32[i] = 0.0f;
+            vg += ri * ui;
+            vd += static_cast<double>(acc) * ui;
+            vr += ri * ri;
+        }
+    }
+    double tot[3];
+    if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) {
+        pmx_finish(S, mode, tot, h, h_true, use_cond);
+        if (o.status && (o.status->flags & kStatusWaitTimeout)) S->aborted = 1;
+    }
+}
+
+// The staged FP32 SpMV: 8-entry slices, three stages per warp, four blocks per SM (48 KB of
+// stages per block).
+constexpr int kStgSlice32 = 8, kStgStages32 = 3, kStgBlocks32 = 4;
+constexpr size_t kStgSmem32 = static_cast<size_t>(kStgWarps) * kStgStages32 * (kStgSlice32 * kSellRows * 8 + 8);
+// the preconditioned solve's SpMV is staged (set false to time the register-pipelined one)
+constexpr bool kPmxStaged = false;
+int g_stg_per_sm32 = 1;
 
 // The staged FP64 SpMV: 8-entry slices, two stages per warp, three blocks of eight warps
 // per SM (a sweep over slices of 4-32 entries, 2-4 stages and 1-6 blocks per SM measured
@@ -972,6 +1058,17 @@ int mx_true_launches(const CgOperands& o) { return o.grid_staged > 0 ? 2 : 1; }
 // the preconditioned FP32 SpMV (w = A u, three dot products)
 void launch_pmx_spmv(const CgOperands& o, int mode, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_true,
                      int use_cond, cudaStream_t s, bool pdl) {
+    if (kPmxStaged && o.grid_staged > 0) {
+        const int cap = o.grid_staged * g_stg_per_sm32;
+        const int need = (o.nchunks + kStgWarps - 1) / kStgWarps;
+        const int g = need < cap ? (need > 0 ? need : 1) : cap;
+        auto k = k_pmx_spmv_staged<kStgSlice32, kStgStages32, kStgBlocks32>;
+        if (pdl)
+            launch_pdl(k, g, kStgThreads, kStgSmem32, s, o, mode, h, h_true, use_cond);
+        else
+            k<<<g, kStgThreads, kStgSmem32, s>>>(o, mode, h, h_true, use_cond);
+        return;
+    }
     if (pdl)
         launch_pdl(k_pmx_spmv, o.grid_spmv, kBlock, 0, s, o, mode, h, h_true, use_cond);
     else
@@ -1429,6 +1526,12 @@ cudaError_t cg_prepare_device() {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kStgThreads, kStgSmem64);
     if (e != cudaSuccess) return e;
     g_stg_per_sm64 = b > 0 ? b : 1;
+    auto k32 = k_pmx_spmv_staged<kStgSlice32, kStgStages32, kStgBlocks32>;
+    e = cudaFuncSetAttribute(k32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStgSmem32));
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k32, kStgThreads, kStgSmem32);
+    if (e != cudaSuccess) return e;
+    g_stg_per_sm32 = b > 0 ? b : 1;
     return cudaSuccess;
 }
 

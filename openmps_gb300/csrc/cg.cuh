@@ -53,6 +53,8 @@ struct CgOperands {
     int32_t grid_staged;  // blocks of the staged SpMV kernels (one per SM; 0: not used)
     const int32_t* len; // row lengths, kSellRows * nchunks (rows >= n have length 0)
     const int32_t* off; // chunk offsets, nchunks + 1
+    const int32_t* chunk;  // entries of each chunk (32 x its widest row): chunks may sit
+                           // farther apart than their width (rows assembled in place)
     const int32_t* col; // SELL-32 columns
     const double* val;  // SELL-32 FP64 values
     const uint2* cv32;  // SELL-32 {column, FP32 value}

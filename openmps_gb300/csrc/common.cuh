@@ -119,6 +119,11 @@ struct DeviceState {
     int32_t* ppe_col;                              // SELL-32 columns
     double* ppe_val;                               // SELL-32 FP64 values
     uint2* ppe_cv32;                               // SELL-32 {column, FP32 value}
+    // 1: PPE rows in cell order, SELL chunks at a fixed stride of ppe_stride entries per
+    // row, written in place by the assembly walk; 0: rows through the ELL scratch and
+    // k_ppe_sort into the compact layout
+    int32_t ppe_direct;
+    int32_t ppe_fp32;  // the assembly also writes ppe_cv32 (set per launch)
     StepScalars* step;
     DevStatus* status;
     const int32_t* solve_ok;  // converged flag of the last PPE solve
@@ -542,6 +547,8 @@ void launch_pressure_gradient3(const SceneConst& sc, const DeviceState& st, cuda
 void launch_dynamic_stabilize3(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // the PPE layout kernels (stages.cu) after a row assembly: chunk sizes, offsets, SELL sort
 void launch_ppe_layout(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s);
+// kernels the PPE assembly's layout step launches (direct rows skip the scan and the sort)
+int set_ppe_launches(const DeviceState& st);
 constexpr int kLaunchesSearch3 = 3;
 // scan.cu
 int scan_scratch_ints(int m);

@@ -367,74 +367,82 @@ __device__ __forceinline__ void stage_segments(const StageSeg* segs, const int* 
 }
 
 // Levels first..last in one block, everything in shared memory: per level the nine
-// coefficient planes, dinv, r and e, then the dense inverse of the last level.
+// coefficient planes, dinv, r and e, then the dense inverse of the last level.  The
+// places of the arrays in shared memory are one table in shared memory (thread 0 lays
+// them out): per-thread pointer arrays indexed by level would live in local memory,
+// which a 1024-thread block with 130 KB of shared memory cannot keep in L1.
 __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, const CgScalars* S,
                                                                 int mode) {
     __shared__ StageSeg segs[kMaxStageSegs];
     __shared__ int pre4[kMaxStageSegs + 1];
+    __shared__ int place[4][kMgMaxLevels + 2];  // float offsets of K, dinv, r, e; [0][last + 1]: dense
     pdl_begin();
     if (pcg_skip(S, mode)) return;
     extern __shared__ float4 sm4[];
     float* sm = reinterpret_cast<float*>(sm4);
     const int tid = threadIdx.x, nt = blockDim.x;
-    float* ks[kMgMaxLevels + 1];
-    float* ds[kMgMaxLevels + 1];
-    float* rs[kMgMaxLevels + 1];
-    float* es[kMgMaxLevels + 1];
-    float* at = sm;
-    int nseg = 0;
-    for (int l = B.first; l <= B.last; l++) {
-        const int cells = B.lv[l].cells;
-        const int c4 = static_cast<int>(mg_round4(cells));
-        ks[l] = at;
-        ds[l] = at + mg_round4(9 * cells);
-        rs[l] = ds[l] + c4;
-        es[l] = rs[l] + c4;
-        at = es[l] + c4;
-        if (tid == 0) {
-            segs[nseg++] = StageSeg{ks[l], B.lv[l].k32, static_cast<int32_t>(mg_round4(9 * cells) / 4)};
-            segs[nseg++] = StageSeg{ds[l], B.lv[l].dinv, c4 / 4};
-        }
-    }
     const int m = B.lv[B.last].cells;
-    float* dn = at;
     if (tid == 0) {
-        segs[nseg++] = StageSeg{dn, B.dense, static_cast<int32_t>(mg_round4(static_cast<int64_t>(m) * m) / 4)};
-        segs[nseg++] = StageSeg{rs[B.first], B.lv[B.first].r, static_cast<int32_t>(mg_round4(B.lv[B.first].cells) / 4)};
+        int at = 0, nseg = 0;
+        for (int l = B.first; l <= B.last; l++) {
+            const int cells = B.lv[l].cells;
+            const int c4 = static_cast<int>(mg_round4(cells));
+            const int k4 = static_cast<int>(mg_round4(9 * static_cast<int64_t>(cells)));
+            place[0][l] = at;
+            place[1][l] = at + k4;
+            place[2][l] = place[1][l] + c4;
+            place[3][l] = place[2][l] + c4;
+            at = place[3][l] + c4;
+            segs[nseg++] = StageSeg{sm + place[0][l], B.lv[l].k32, k4 / 4};
+            segs[nseg++] = StageSeg{sm + place[1][l], B.lv[l].dinv, c4 / 4};
+        }
+        place[0][B.last + 1] = at;
+        segs[nseg++] = StageSeg{sm + at, B.dense, static_cast<int32_t>(mg_round4(static_cast<int64_t>(m) * m) / 4)};
+        segs[nseg++] = StageSeg{sm + place[2][B.first], B.lv[B.first].r,
+                                static_cast<int32_t>(mg_round4(B.lv[B.first].cells) / 4)};
         pre4[0] = 0;
         for (int k = 0; k < nseg; k++) pre4[k + 1] = pre4[k] + segs[k].n4;
     }
-    nseg = 2 * (B.last - B.first + 1) + 2;
     __syncthreads();
-    stage_segments(segs, pre4, nseg, tid, nt);
+    stage_segments(segs, pre4, 2 * (B.last - B.first + 1) + 2, tid, nt);
     __syncthreads();
     for (int l = B.first; l < B.last; l++) {
         const MgLevel& f = B.lv[l];
         const MgLevel& c = B.lv[l + 1];
+        const float* k = sm + place[0][l];
+        const float* d = sm + place[1][l];
+        const float* r = sm + place[2][l];
+        float* rc = sm + place[2][l + 1];
         for (int I = tid; I < c.cells; I += nt)
-            rs[l + 1][I] = child_residuals(f.nx, f.nz, f.cells, ks[l], ds[l], rs[l], I / c.nz,
-                                           I - (I / c.nz) * c.nz);
+            rc[I] = child_residuals(f.nx, f.nz, f.cells, k, d, r, I / c.nz, I - (I / c.nz) * c.nz);
         __syncthreads();
     }
     {
         const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-        const float* rl = rs[B.last];
+        const float* dn = sm + place[0][B.last + 1];
+        const float* rl = sm + place[2][B.last];
+        float* el = sm + place[3][B.last];
         for (int row = warp; row < m; row += nwarps) {
             float v = 0.0f;
             for (int k = lane; k < m; k += 32) v += dn[row * m + k] * rl[k];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) es[B.last][row] = v;
+            if (lane == 0) el[row] = v;
         }
         __syncthreads();
     }
     for (int l = B.last - 1; l >= B.first; l--) {
         const MgLevel& f = B.lv[l];
         const int cnz = B.lv[l + 1].nz;
-        for (int ch = tid; ch < f.cells; ch += nt)
-            es[l][ch] = smoothed_correction(f.nx, f.nz, f.cells, ks[l], ds[l], rs[l], cnz, es[l + 1], ch);
+        const float* k = sm + place[0][l];
+        const float* d = sm + place[1][l];
+        const float* r = sm + place[2][l];
+        float* e = sm + place[3][l];
+        const float* ec = sm + place[3][l + 1];
+        for (int ch = tid; ch < f.cells; ch += nt) e[ch] = smoothed_correction(f.nx, f.nz, f.cells, k, d, r, cnz, ec, ch);
         __syncthreads();
     }
-    for (int c = tid; c < B.lv[B.first].cells; c += nt) B.lv[B.first].e[c] = es[B.first][c];
+    const float* e1 = sm + place[3][B.first];
+    for (int c = tid; c < B.lv[B.first].cells; c += nt) B.lv[B.first].e[c] = e1[c];
 }
 
 // u = s_i dinv0_i r_i + e_1[cell(i)] on active rows, 0 on identity rows (used when the

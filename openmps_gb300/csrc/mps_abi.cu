@@ -414,6 +414,18 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
         st.unplaced_pos = dalloc<int32_t>(h, n + 1);
         st.row_scratch = dalloc<int32_t>(h, scan_scratch_ints(static_cast<int>(std::max<int64_t>(cells, n))));
     }
+    // Cell-ordered rows are assembled in place: SELL chunks at the fixed stride the
+    // layout is allocated with (ppe_stride entries per row), so the chunk offsets are set
+    // once here and no per-step scan or sort runs.  They must fit in 32 bits.
+    st.ppe_direct = 0;
+    st.ppe_fp32 = 0;
+    if (st.row_of && sell_cap < (static_cast<int64_t>(1) << 31)) {
+        std::vector<int32_t> off(static_cast<size_t>(nchunks + 1));
+        for (int64_t c = 0; c <= nchunks; c++)
+            off[static_cast<size_t>(c)] = static_cast<int32_t>(c * sc.ppe_stride * kSellRows);
+        check(cudaMemcpy(st.ppe_off, off.data(), sizeof(int32_t) * (nchunks + 1), cudaMemcpyHostToDevice), "copy");
+        st.ppe_direct = 1;
+    }
     // multigrid hierarchy over the search cells (level sizes fixed by the domain)
     MgHierarchy& mg = h->mg;
     mg = MgHierarchy{};
@@ -548,6 +560,7 @@ CgOperands cg_operands(mps_handle* h) {
     o.grid_staged = h->sm_count;
     o.len = h->st.ppe_len;
     o.off = h->st.ppe_off;
+    o.chunk = h->st.ppe_chunk;
     o.col = h->st.ppe_col;
     o.val = h->st.ppe_val;
     o.cv32 = h->st.ppe_cv32;
@@ -591,8 +604,15 @@ bool is_preconditioned(int32_t solver) {
 constexpr int kPcgMaxIter = 400;
 // Reliable-update thresholds on the squared residual norm: the FP32 recurrence is folded
 // into FP64 after a 10x drop in norm (plain FP32 CG, 1000+ iterations per solve) or a
-// ~30x drop (multigrid-preconditioned, ~70 iterations: less drift between updates).
-constexpr double kReliableDelta2 = 1e-2, kReliableDelta2Pcg = 1e-3;
+// 100x drop (multigrid-preconditioned, ~45 iterations: little drift between updates).
+// At 340k: 30x / 100x / 300x measured 43.8 / 44.2 / 44.5 iterations and solves of
+// 4.11 / 3.88 / 3.75 ms (each update costs an FP64 SpMV, a cycle and an FP32 SpMV), but
+// at 300x the FP32 recursion of the dam break's first step (from p = 0) drifted until a
+// reliable update no longer halved the true residual, and the FP64 CG had to finish.
+constexpr double kReliableDelta2 = 1e-2, kReliableDelta2Pcg = 1e-4;
+// The batched scenes' multigrid solve: a 100x drop (35 iterations per scene, the same as
+// with 10x, in 5 % less time at 256 scenes).
+constexpr double kReliableDelta2Batch = 1e-4;
 
 // Iteration limit: the reference stops after as many iterations as unknowns
 // (Computer.hpp:1392).  The mixed solver restarts its FP32 recursion at every reliable
@@ -827,7 +847,7 @@ void forward3(mps_handle* h, double dt) {
     if (implicit) {
         launch_set_ppe3(sc, h->st, wants_fp32(h), s);
         h->ppe_fp32 = wants_fp32(h);
-        launched(h, kLaunchesSetPpe);
+        launched(h, set_ppe_launches(h->st));
         after_launch("stages");
     }
     stage_mark(h, kSolve);
@@ -917,7 +937,7 @@ void forward(mps_handle* h, double dt) {
         else
             launch_set_ppe(sc, h->st, wants_fp32(h), s);
         h->ppe_fp32 = wants_fp32(h);
-        launched(h, kLaunchesSetPpe);
+        launched(h, set_ppe_launches(h->st));
         after_launch("stages");
     }
     stage_mark(h, kSolve);
@@ -1029,7 +1049,7 @@ BatchOps batch_ops(mps_handle* h) {
     B.all_ok = h->d_all_ok;
     B.status = h->st.status;
     B.eps = h->prm.eps;
-    B.delta2 = 0.01;
+    B.delta2 = kReliableDelta2Batch;
     B.criterion = h->prm.criterion;
     B.max_iter = h->prm.max_cg_iters > 0 ? h->prm.max_cg_iters : kPcgMaxIter;
     return B;
@@ -1063,7 +1083,7 @@ void batch_stages_pre(mps_handle* h, double dt) {
     h->ppe_fp32 = true;
     after_launch("batch stages");
     launched(h, kLaunchesDt + kLaunchesSearch + kLaunchesPrePressure + kLaunchesExplicitUpdate +
-                    (fused ? 0 : kLaunchesDensity) + (implicit ? kLaunchesSetPpe : 0) +
+                    (fused ? 0 : kLaunchesDensity) + (implicit ? set_ppe_launches(h->st) : 0) +
                     ((h->prm.flags & MPS_FLAG_DS) ? kLaunchesSaveX : 0));
 }
 
@@ -1904,6 +1924,10 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         o.grid_spmv = cg_grid_spmv(n);
         int32_t* dlen = loc.get<int32_t>(len.size());
         int32_t* doff = loc.get<int32_t>(off.size());
+        std::vector<int32_t> chunk(static_cast<size_t>(nchunks));
+        for (int64_t c = 0; c < nchunks; c++)
+            chunk[static_cast<size_t>(c)] = off[static_cast<size_t>(c + 1)] - off[static_cast<size_t>(c)];
+        int32_t* dchunk = loc.get<int32_t>(std::max<size_t>(chunk.size(), 1));
         int32_t* dcol = loc.get<int32_t>(total);
         double* dval = loc.get<double>(total);
         uint2* dcv = loc.get<uint2>(total);
@@ -1911,6 +1935,7 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         double* dx = loc.get<double>(nn);
         o.len = dlen;
         o.off = doff;
+        o.chunk = dchunk;
         o.col = dcol;
         o.val = dval;
         o.cv32 = dcv;
@@ -1935,6 +1960,7 @@ int mps_cg_solve_csr(mps_handle* h, int64_t n, const int64_t* row_ptr, const int
         };
         up(dlen, len.data(), sizeof(int32_t) * len.size());
         up(doff, off.data(), sizeof(int32_t) * off.size());
+        if (nchunks > 0) up(dchunk, chunk.data(), sizeof(int32_t) * chunk.size());
         up(dcol, ecol.data(), sizeof(int32_t) * total);
         up(dval, eval.data(), sizeof(double) * total);
         up(dcv, ecv.data(), sizeof(uint2) * total);

@@ -412,6 +412,52 @@ __global__ void k_save_x(SceneConst sc, DeviceState st) {
     st.oz[i] = st.z[i];
 }
 
+// One PPE row as the assembly walk produces it: its off-diagonal entries in neighbour
+// order, then the diagonal.  With the ELL scratch, entry m of particle i goes to
+// [m n + i] and k_ppe_sort orders the row later.  In direct mode (rows in cell order)
+// the columns arrive ascending: the neighbour list walks the cells in ascending index and
+// each cell in row order.  So entry m goes straight to its rank among the row's SELL
+// slots (m before the diagonal, m + 1 after it) and the diagonal to the count of columns
+// below it: the ascending-column layout of the reference's compressed matrix
+// (Computer.hpp:1330-1350).  A column out of order fails the step (it cannot happen for
+// cell-ordered rows).
+struct PpeRow {
+    int i, row, m, below, prev;
+    __device__ PpeRow(int i_, int row_) : i(i_), row(row_), m(0), below(0), prev(-1) {}
+    __device__ __forceinline__ void store(const SceneConst& sc, const DeviceState& st, int rank, int col,
+                                          double v) const {
+        const int64_t base = static_cast<int64_t>(row / kSellRows) * sc.ppe_stride * kSellRows;
+        const int64_t at = sell_index(base, row % kSellRows, rank);
+        st.ppe_col[at] = col;
+        st.ppe_val[at] = v;
+        if (st.ppe_fp32) st.ppe_cv32[at] = make_uint2(static_cast<unsigned>(col), __float_as_uint(__double2float_rn(v)));
+    }
+    __device__ __forceinline__ void put(const SceneConst& sc, const DeviceState& st, int col, double v) {
+        if (st.ppe_direct) {
+            if (col <= prev) {
+                atomicOr(&st.status->flags, kStatusDeviceCheck);
+                st.status->check_index = i;
+            }
+            prev = col;
+            below += col < row ? 1 : 0;
+            store(sc, st, m + (col > row ? 1 : 0), col, v);
+        } else {
+            st.ppe_col_tmp[ell(m, sc.n, i)] = col;
+            st.ppe_val_tmp[ell(m, sc.n, i)] = v;
+        }
+        m++;
+    }
+    __device__ __forceinline__ void diag(const SceneConst& sc, const DeviceState& st, double a_ii) {
+        if (st.ppe_direct) {
+            store(sc, st, below, row, a_ii);
+        } else {
+            st.ppe_col_tmp[ell(m, sc.n, i)] = row;
+            st.ppe_val_tmp[ell(m, sc.n, i)] = a_ii;
+        }
+        st.ppe_len[row] = m + 1;
+    }
+};
+
 // SetPressurePoissonEquation (Computer.hpp:1145-1328): right-hand side, initial guess
 // and one matrix row per particle in neighbour order (diagonal last) into the
 // scratch ELL arrays (column k of particle i at [k n + i]).  Rows and columns are PPE
@@ -426,9 +472,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     if (!ppe_alive(sc, st, i)) {
         st.ppe_b[row] = 0;
         st.ppe_x[row] = 0;
-        st.ppe_col_tmp[ell(0, n, i)] = row;
-        st.ppe_val_tmp[ell(0, n, i)] = 1.0;
-        st.ppe_len[row] = 1;
+        PpeRow(i, row).diag(sc, st, 1.0);
         return;
     }
     const double dt = st.step->dt;
@@ -444,7 +488,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
 
     const double xi = st.x[i], zi = st.z[i];
     double a_ii = 0.0, gx = 0.0, gz = 0.0;
-    int m = 0;
+    PpeRow pr(i, row);
     for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
@@ -452,11 +496,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
         if (below(r2, sc.rl2)) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double a_ij = ppe_coefficient(sc, lf, dsqrt_rn(r2));
-                if (spp || !is_surface(sc, st.nd[j])) {
-                    st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
-                    st.ppe_val_tmp[ell(m, n, i)] = a_ij;
-                    m++;
-                }
+                if (spp || !is_surface(sc, st.nd[j])) pr.put(sc, st, ppe_row(st, j), a_ij);
                 a_ii += -a_ij;
             } else {
                 a_ii = __dadd_rn(a_ii, 0.0);
@@ -473,9 +513,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
         const double ddx = xi - xs, ddz = zi - zs;
         a_ii += -ppe_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
-    st.ppe_col_tmp[ell(m, n, i)] = row;
-    st.ppe_val_tmp[ell(m, n, i)] = a_ii;
-    st.ppe_len[row] = m + 1;
+    pr.diag(sc, st, a_ii);
 }
 
 // Number density after the move (the second ComputeNeighborDensities) and the PPE
@@ -496,15 +534,14 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
     if (t == MPS_TYPE_DUMMY || t == MPS_TYPE_DISABLED) {
         st.ppe_b[row] = 0;
         st.ppe_x[row] = 0;
-        st.ppe_col_tmp[ell(0, n, i)] = row;
-        st.ppe_val_tmp[ell(0, n, i)] = 1.0;
-        st.ppe_len[row] = 1;
+        PpeRow(i, row).diag(sc, st, 1.0);
         return;
     }
     const bool hs = has_flag(sc.flags, MPS_FLAG_HS);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
     double thisN = 0.0, hsum = 0.0, a_ii = 0.0, gx = 0.0, gz = 0.0;
-    int m = 0, m_re = 0;
+    int m_re = 0;
+    PpeRow pr(i, row);
     for_near(sc, st, i, fmaxf(sc.f32_out_re, sc.f32_out_rl), [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
@@ -527,9 +564,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         if (in_rl) {
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double a_ij = ppe_coefficient(sc, lf, r);
-                st.ppe_col_tmp[ell(m, n, i)] = ppe_row(st, j);
-                st.ppe_val_tmp[ell(m, n, i)] = a_ij;
-                m++;
+                pr.put(sc, st, ppe_row(st, j), a_ij);
                 a_ii += -a_ij;
             } else {
                 a_ii = __dadd_rn(a_ii, 0.0);
@@ -558,9 +593,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         const double ddx = xi - xs, ddz = zi - zs;
         a_ii += -ppe_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
     }
-    st.ppe_col_tmp[ell(m, n, i)] = row;
-    st.ppe_val_tmp[ell(m, n, i)] = a_ii;
-    st.ppe_len[row] = m + 1;
+    pr.diag(sc, st, a_ii);
 }
 
 // Chunk sizes of the SELL-32 layout: one warp per chunk of 32 rows.
@@ -570,6 +603,7 @@ __global__ void k_ppe_chunks(SceneConst sc, DeviceState st) {
     if (step_failed(sc, st)) return;
     const int lane = threadIdx.x & 31;
     const int len = st.ppe_len[c * kSellRows + lane];
+    warp_add_u64(&st.status->ppe_nnz, static_cast<unsigned long long>(len));
     const int m = __reduce_max_sync(0xffffffffu, len);
     if (lane == 0) st.ppe_chunk[c] = static_cast<int>(sell_chunk_size(m));
 }
@@ -581,10 +615,9 @@ __global__ void k_ppe_sort(SceneConst sc, DeviceState st, int want_fp32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (step_failed(sc, st)) return;
     const int n = sc.n;
-    const int row = (i < n) ? ppe_row(st, i) : 0;
-    const int len = (i < n) ? st.ppe_len[row] : 0;
-    warp_add_u64(&st.status->ppe_nnz, static_cast<unsigned long long>(len));
     if (i >= n) return;
+    const int row = ppe_row(st, i);
+    const int len = st.ppe_len[row];
     const int64_t base = st.ppe_off[row / kSellRows];
     const int r = row % kSellRows;
     auto put = [&](int e, int rank) {
@@ -918,14 +951,26 @@ void launch_save_x(const SceneConst& sc, const DeviceState& st, cudaStream_t s) 
     k_save_x<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
+// Chunk widths (and the nonzero count); with the ELL scratch also the chunk offsets and
+// the sorted rows.  Direct-mode rows are already in place, at fixed chunk offsets.
 void launch_ppe_layout(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
     k_ppe_chunks<<<grid_for(static_cast<int64_t>(sc.nchunks) * 32), kBlock, 0, s>>>(sc, st);
+    if (st.ppe_direct) return;
     launch_exclusive_scan(st.ppe_chunk, st.ppe_off, sc.nchunks, st.scan_scratch, s);
     k_ppe_sort<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st, want_fp32 ? 1 : 0);
 }
 
+int set_ppe_launches(const DeviceState& st) { return st.ppe_direct ? 2 : kLaunchesSetPpe; }
+
+// the state the assembly walk writes with: the FP32 copy of the matrix only when asked
+DeviceState assembly_state(const DeviceState& st, bool want_fp32) {
+    DeviceState a = st;
+    a.ppe_fp32 = want_fp32 ? 1 : 0;
+    return a;
+}
+
 void launch_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
-    k_ppe_build<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
+    k_ppe_build<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, assembly_state(st, want_fp32));
     launch_ppe_layout(sc, st, want_fp32, s);
 }
 
@@ -934,7 +979,7 @@ bool density_ppe_fusable(const SceneConst& sc) {
 }
 
 void launch_density_set_ppe(const SceneConst& sc, const DeviceState& st, bool want_fp32, cudaStream_t s) {
-    k_density_ppe<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
+    k_density_ppe<<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, assembly_state(st, want_fp32));
     launch_ppe_layout(sc, st, want_fp32, s);
 }
 
