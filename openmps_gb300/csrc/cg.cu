@@ -926,93 +926,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_fold(CgOperands o) {
         xn[i] = xc[i] + static_cast<double>(o.d32[i]);
 }
 
-// k_pmx_spmv with the staged stream: the {column, FP32 value} pairs of each warp's chunk
-// come through a ring of shared-memory stages, each refilled as soon as the lanes have
-// read it, so the copies overlap the gathers of u and the FP32 multiply-adds.  A lane
-// sums its row in ascending column order, as row32 does.
-template <int SLICE, int STAGES, int MINB>
-__global__ void __launch_bounds__(kStgThreads, MINB) k_pmx_spmv_staged(CgOperands o, int mode,
-                                                                       cudaGraphConditionalHandle h,
-                                                                       cudaGraphConditionalHandle h_true,
-                                                                       int use_cond) {
-    extern __shared__ __align__(128) unsigned char stg_sm[];
-    __shared__ BlockTicket tk;
-    pdl_begin();
-    CgScalars* S = o.S;
-    if (pcg_skip(S, mode)) return;
-    ticket_init(tk);
-    using Ring = StageRing<SLICE, STAGES, 1>;
-    constexpr int kStageBytes = Ring::kEntries * 8;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kStgWarps + w, nw = gridDim.x * kStgWarps;
-    Ring R;
-    R.src[0] = o.cv32;
-    R.esize[0] = 8;
-    R.init(stg_sm + static_cast<size_t>(w) * STAGES * kStageBytes,
-           reinterpret_cast<uint64_t*>(stg_sm + static_cast<size_t>(kStgWarps) * STAGES * kStageBytes) + w * STAGES,
-           gw);
-    for (int k = 0; k < STAGES; k++) R.issue(o, nw);
-    const float* __restrict__ u = o.u32;
-    double vg = 0.0, vd = 0.0, vr = 0.0;
-    int item = 0;
-    bool ok = true;
-    for (int c = gw; c < o.nchunks && ok; c += nw) {
-        const int i = kSellRows * c + lane;
-        const int L = o.len[i];
-        const int width = o.chunk[c] / kSellRows;
-        float acc = 0.0f;
-        for (int k0 = 0; k0 < width; k0 += SLICE, item++) {
-            if (!stg_wait(R.bar + item % STAGES, (item / STAGES) & 1)) {
-                if (lane == 0 && o.status) atomicOr(&const_cast<DevStatus*>(o.status)->flags, kStatusWaitTimeout);
-                R.drain(item);
-                ok = false;
-                break;
-            }
-            const int m = min(SLICE, L - k0);
-            const uint2* se = reinterpret_cast<const uint2*>(R.stage(item, 0));
-            uint2 e[SLICE];
-#pragma unroll
-            for (int t = 0; t < SLICE; t++) e[t] = t < m ? se[t * kSellRows + lane] : make_uint2(0u, 0u);
-            // the values must have arrived before the copy may overwrite the stage
-#pragma unroll
-            for (int t = 0; t < SLICE; t++) asm volatile("" ::"r"(e[t].x), "r"(e[t].y));
-            __syncwarp();
-            if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncwarp();
-            R.issue(o, nw);
-            float xv[SLICE];
-#pragma unroll
-            for (int t = 0; t < SLICE; t++) xv[t] = t < m ? u[e[t].x] : 0.0f;
-#pragma unroll
-            for (int t = 0; t < SLICE; t++)
-                if (t < m) acc = fmaf(__uint_as_float(e[t].y), xv[t], acc);
-        }
-        if (!ok) break;
-        if (i < o.n) {
-            const double ri = static_cast<double>(o.r32[i]);
-            const double ui = static_cast<double>(u[i]);
-            o.w32[i] = acc;
-            if (mode == 2) o.d32[i] = 0.0f;
-            vg += ri * ui;
-            vd += static_cast<double>(acc) * ui;
-            vr += ri * ri;
-        }
-    }
-    double tot[3];
-    if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) {
-        pmx_finish(S, mode, tot, h, h_true, use_cond);
-        if (o.status && (o.status->flags & kStatusWaitTimeout)) S->aborted = 1;
-    }
-}
-
-// The staged FP32 SpMV: 8-entry slices, three stages per warp, four blocks per SM (48 KB of
-// stages per block).
-constexpr int kStgSlice32 = 8, kStgStages32 = 3, kStgBlocks32 = 4;
-constexpr size_t kStgSmem32 = static_cast<size_t>(kStgWarps) * kStgStages32 * (kStgSlice32 * kSellRows * 8 + 8);
-// the preconditioned solve's SpMV is staged (set false to time the register-pipelined one)
-constexpr bool kPmxStaged = false;
-int g_stg_per_sm32 = 1;
-
 // The staged FP64 SpMV: 8-entry slices, two stages per warp, three blocks of eight warps
 // per SM (a sweep over slices of 4-32 entries, 2-4 stages and 1-6 blocks per SM measured
 // 57 us at 340k particles against 63 us for the per-chunk kernel; the staged FP32 SpMV
@@ -1058,17 +971,6 @@ int mx_true_launches(const CgOperands& o) { return o.grid_staged > 0 ? 2 : 1; }
 // the preconditioned FP32 SpMV (w = A u, three dot products)
 void launch_pmx_spmv(const CgOperands& o, int mode, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_true,
                      int use_cond, cudaStream_t s, bool pdl) {
-    if (kPmxStaged && o.grid_staged > 0) {
-        const int cap = o.grid_staged * g_stg_per_sm32;
-        const int need = (o.nchunks + kStgWarps - 1) / kStgWarps;
-        const int g = need < cap ? (need > 0 ? need : 1) : cap;
-        auto k = k_pmx_spmv_staged<kStgSlice32, kStgStages32, kStgBlocks32>;
-        if (pdl)
-            launch_pdl(k, g, kStgThreads, kStgSmem32, s, o, mode, h, h_true, use_cond);
-        else
-            k<<<g, kStgThreads, kStgSmem32, s>>>(o, mode, h, h_true, use_cond);
-        return;
-    }
     if (pdl)
         launch_pdl(k_pmx_spmv, o.grid_spmv, kBlock, 0, s, o, mode, h, h_true, use_cond);
     else
@@ -1526,12 +1428,6 @@ cudaError_t cg_prepare_device() {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kStgThreads, kStgSmem64);
     if (e != cudaSuccess) return e;
     g_stg_per_sm64 = b > 0 ? b : 1;
-    auto k32 = k_pmx_spmv_staged<kStgSlice32, kStgStages32, kStgBlocks32>;
-    e = cudaFuncSetAttribute(k32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStgSmem32));
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k32, kStgThreads, kStgSmem32);
-    if (e != cudaSuccess) return e;
-    g_stg_per_sm32 = b > 0 ? b : 1;
     return cudaSuccess;
 }
 
