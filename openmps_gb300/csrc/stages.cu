@@ -317,8 +317,10 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
         const bool in_rl = fluid && below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
         const double r = dsqrt_rn(r2);
+        // W(r, r_e), reused for W(r, r_e^lap) when the two radii are one
+        const double w_re = in_re ? weight(r, sc.re) : 0.0;
         if (in_re) {
-            thisN += weight(r, sc.re);
+            thisN += w_re;
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
@@ -335,7 +337,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
                 vz = __dadd_rn(vz, 0.0);
             }
             if (spp) {
-                const double wg = weight(r, sc.re_lap);
+                const double wg = (in_re && sc.re_lap == sc.re) ? w_re : weight(r, sc.re_lap);
                 gx += wg * dx;
                 gz += wg * dz;
             }
@@ -550,8 +552,9 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         const bool in_rl = below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
         const double r = dsqrt_rn(r2);
+        // W(r, r_e), reused for W(r, r_e^lap) when the two radii are one
+        const double w = in_re ? weight(r, sc.re) : 0.0;
         if (in_re) {
-            const double w = weight(r, sc.re);
             thisN += w;
             if (m_re < kReCache) st.w_re[static_cast<int64_t>(m_re) * n + i] = w;
             m_re++;
@@ -569,7 +572,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
             } else {
                 a_ii = __dadd_rn(a_ii, 0.0);
             }
-            const double wg = weight(r, sc.re_lap);
+            const double wg = (in_re && sc.re_lap == sc.re) ? w : weight(r, sc.re_lap);
             gx += wg * dx;
             gz += wg * dz;
         }
