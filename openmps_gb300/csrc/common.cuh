@@ -472,6 +472,11 @@ __device__ __forceinline__ void pdl_begin() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+// A kernel may read, before pdl_begin(), what no kernel still running can write: data
+// fixed for the whole solve (matrix, cycle planes, row ranges) and what kernels two or
+// more launches back wrote (every kernel of a chain waits for its predecessor before it
+// lets its own successor launch, so those have completed and flushed).  Such loads then
+// overlap the predecessor's tail instead of following it.
 
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,

@@ -248,21 +248,28 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict0(MgLevel L1, const int2*
 // cell (particles outside every cell are identity rows whose vectors stay zero).
 __global__ void __launch_bounds__(kBlock) k_mg_axpy_restrict(CgOperands o, MgLevel L1, const int2* active_rows,
                                                              const int32_t* active, const int32_t* n_active) {
-    pdl_begin();
-    if (pcg_skip(o.S, 1)) return;
     const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    const int base0 = 2 * static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    // the first cell's row range (the active list is fixed for the solve)
+    const int nact = *n_active;
+    int2 rr0 = make_int2(0, 0);
+    int c0 = -1;
+    if (base0 + half < nact) {
+        rr0 = active_rows[base0 + half];
+        c0 = active[base0 + half];
+    }
+    pdl_begin();  // the step sizes and the vectors come from the SpMV just before
+    if (pcg_skip(o.S, 1)) return;
     const float alpha = __double2float_rn(o.S->alpha);
     const float beta = __double2float_rn(o.S->beta);
-    const int nact = *n_active;
-    const int nwarps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-    for (int base = 2 * static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); base < nact;
-         base += 2 * nwarps) {
+    for (int base = base0; base < nact; base += 2 * nwarps) {
         const int a = base + half;
         float sum = 0.0f;
         int c = -1;
         if (a < nact) {
-            const int2 rr = active_rows[a];
-            c = active[a];
+            const int2 rr = base == base0 ? rr0 : active_rows[a];
+            c = base == base0 ? c0 : active[a];
             for (int i = rr.x + hl; i < rr.y; i += 16) {
                 const float si = fmaf(beta, o.s32[i], o.w32[i]);
                 const float pi = fmaf(beta, o.p32[i], o.u32[i]);
@@ -376,8 +383,7 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, cons
     __shared__ StageSeg segs[kMaxStageSegs];
     __shared__ int pre4[kMaxStageSegs + 1];
     __shared__ int place[4][kMgMaxLevels + 2];  // float offsets of K, dinv, r, e; [0][last + 1]: dense
-    pdl_begin();
-    if (pcg_skip(S, mode)) return;
+    if (pcg_skip(S, mode)) return;  // no kernel of the cycle writes the scalars
     extern __shared__ float4 sm4[];
     float* sm = reinterpret_cast<float*>(sm4);
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -404,7 +410,16 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_bottom(MgBottom B, cons
         for (int k = 0; k < nseg; k++) pre4[k + 1] = pre4[k] + segs[k].n4;
     }
     __syncthreads();
-    stage_segments(segs, pre4, 2 * (B.last - B.first + 1) + 2, tid, nt);
+    // the planes and the dense inverse are fixed for the solve: staged while the down
+    // sweep still runs; the residuals of the first level (the last segment) after it
+    const int nconst = 2 * (B.last - B.first + 1) + 1;
+    stage_segments(segs, pre4, nconst, tid, nt);
+    pdl_begin();
+    {
+        const float4* src = reinterpret_cast<const float4*>(segs[nconst].src);
+        float4* dst = reinterpret_cast<float4*>(segs[nconst].dst);
+        for (int k = tid; k < segs[nconst].n4; k += nt) dst[k] = __ldg(src + k);
+    }
     __syncthreads();
     for (int l = B.first; l < B.last; l++) {
         const MgLevel& f = B.lv[l];
@@ -506,31 +521,10 @@ __global__ void __launch_bounds__(kBlock) k_mg_down_fused(MgChain C, const CgSca
     __shared__ float R0[kDownSide0 * kDownSide0], X0[kDownSide0 * kDownSide0];
     __shared__ float R1[kDownSide1 * kDownSide1], X1[kDownSide1 * kDownSide1];
     __shared__ float R2[kDownSide2 * kDownSide2], X2[kDownSide2 * kDownSide2];
-    pdl_begin();
-    if (pcg_skip(S, mode)) return;
+    if (pcg_skip(S, mode)) return;  // no kernel of the cycle writes the scalars
     const int D = C.depth;
     const int TX = blockIdx.x * kMgDownTile, TZ = blockIdx.y * kMgDownTile;
     const int tid = threadIdx.x;
-    // level-0 region: r and dinv (cells outside the grid are never read by the stencil
-    // of a cell inside it: neighbours are clamped into the grid)
-    const MgLevel& F0 = C.lv[0];
-    const int n0 = (kMgDownTile << D) + (2 << D) - 2;
-    const int o0x = (TX << D) - ((1 << D) - 1), o0z = (TZ << D) - ((1 << D) - 1);
-    float r0[kDownPer0], d0[kDownPer0];
-#pragma unroll
-    for (int k = 0; k < kDownPer0; k++) {
-        const int t = tid + k * kBlock;
-        r0[k] = 0.0f;
-        d0[k] = 0.0f;
-        if (t < n0 * n0) {
-            const int gx = o0x + t / n0, gz = o0z + (t - (t / n0) * n0);
-            if (gx >= 0 && gx < F0.nx && gz >= 0 && gz < F0.nz) {
-                const int c = gx * F0.nz + gz;
-                r0[k] = F0.r[c];
-                d0[k] = F0.dinv[c];
-            }
-        }
-    }
     // this thread's cell: threads [0, n_1^2) take level 1, the next n_2^2 level 2, ...
     int my_d = 0, my_t = 0;
     {
@@ -570,6 +564,27 @@ __global__ void __launch_bounds__(kBlock) k_mg_down_fused(MgChain C, const CgSca
                 for (int k = 0; k < 9; k++) kk[q][k] = F.k32[k * F.cells + ch];
             }
             if (my_d < D) my_dinv = L.dinv[gx * L.nz + gz];
+        }
+    }
+    pdl_begin();  // the level-0 residuals come from the kernel just before
+    // level-0 region: r (written by the kernel just before) and dinv (cells outside the
+    // grid are never read by the stencil of a cell inside it: neighbours are clamped)
+    const MgLevel& F0 = C.lv[0];
+    const int n0 = (kMgDownTile << D) + (2 << D) - 2;
+    const int o0x = (TX << D) - ((1 << D) - 1), o0z = (TZ << D) - ((1 << D) - 1);
+    float r0[kDownPer0], d0[kDownPer0];
+#pragma unroll
+    for (int k = 0; k < kDownPer0; k++) {
+        const int t = tid + k * kBlock;
+        r0[k] = 0.0f;
+        d0[k] = 0.0f;
+        if (t < n0 * n0) {
+            const int gx = o0x + t / n0, gz = o0z + (t - (t / n0) * n0);
+            if (gx >= 0 && gx < F0.nx && gz >= 0 && gz < F0.nz) {
+                const int c = gx * F0.nz + gz;
+                r0[k] = F0.r[c];
+                d0[k] = F0.dinv[c];
+            }
         }
     }
 #pragma unroll
@@ -648,8 +663,7 @@ constexpr int kUpRowsPre = 4;
 __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgScalars* S, int mode) {
     constexpr int kSide = kMgUpTile;  // every coarser region is at most this wide
     __shared__ float E[kMgFuseLevels][kSide * kSide];
-    pdl_begin();
-    if (pcg_skip(S, mode)) return;
+    if (pcg_skip(S, mode)) return;  // no kernel of the cycle writes the scalars
     const int D = C.depth;
     const MgLevel& L0 = C.lv[0];
     const int x0 = blockIdx.x * kMgUpTile, z0 = blockIdx.y * kMgUpTile;
@@ -698,14 +712,14 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
             }
         }
     }
-    // the stencil of this thread's cell: r, dinv and K of the nine neighbours, and the
-    // coarse corrections of their parents when the coarse level is read from memory
+    // the stencil of this thread's cell: r, dinv and K of the nine neighbours (all final
+    // before the kernel just before this one), and the coarse corrections of their parents
+    // when the coarse level is read from memory (written by the kernel just before)
     float rn[9], dn[9], kn[9], cn[9];
     int gx = 0, gz = 0;
     bool in = false;
     if (my_d >= 0) {
         const MgLevel& F = C.lv[my_d];
-        const MgLevel& Cl = C.lv[my_d + 1];
         int lx = 0, lz = 0, w = 1;
 #pragma unroll
         for (int d = 0; d < kMgFuseLevels; d++)
@@ -719,7 +733,6 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
         in = gx >= 0 && gx < F.nx && gz >= 0 && gz < F.nz;
         if (in) {
             const int ch = gx * F.nz + gz;
-            const bool top = my_d + 1 == D;
 #pragma unroll
             for (int dx = -1; dx <= 1; dx++) {
 #pragma unroll
@@ -730,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
                     rn[k] = F.r[nb];
                     dn[k] = F.dinv[nb];
                     kn[k] = F.k32[k * F.cells + ch];
-                    cn[k] = top ? Cl.e[(ax >> 1) * Cl.nz + (az >> 1)] : 0.0f;
+                    cn[k] = 0.0f;
                 }
             }
         }
@@ -750,6 +763,19 @@ __global__ void __launch_bounds__(kBlock) k_mg_up_fused(MgUpChain C, const CgSca
             if (C.scale) rs[k] = C.scale[i];
             rr[k] = C.r[i];
             rc[k] = C.row_cell[i];
+        }
+    }
+    pdl_begin();  // the coarse corrections of level `depth`
+    if (in && my_d + 1 == D) {
+        const MgLevel& F = C.lv[my_d];
+        const MgLevel& Cl = C.lv[my_d + 1];
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) {
+#pragma unroll
+            for (int dz = -1; dz <= 1; dz++) {
+                const int ax = clampi(gx + dx, F.nx - 1), az = clampi(gz + dz, F.nz - 1);
+                cn[(dx + 1) * 3 + dz + 1] = Cl.e[(ax >> 1) * Cl.nz + (az >> 1)];
+            }
         }
     }
 #pragma unroll
