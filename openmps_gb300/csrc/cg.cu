@@ -389,17 +389,21 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o, int afte
 // followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
 
 // Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
-// Software-pipelined like row64.
-template <int D = 8>
-__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
-                                       const float* __restrict__ v) {
-    float acc = 0.0f;
-    const int nb = L / D;
-    uint2 e[D];
-    if (nb > 0) {
+// Software-pipelined like row64: row32_first loads the first D entries (they may be
+// loaded before the vector v is ready), row32_rest gathers and sums the row.
+template <int D>
+__device__ __forceinline__ void row32_first(const CgOperands& o, int64_t at, int L, uint2 (&e)[D]) {
+    if (L >= D) {
 #pragma unroll
         for (int u = 0; u < D; u++) e[u] = ld_sell_pair(o.cv32 + at + u * kSellRows);
     }
+}
+
+template <int D>
+__device__ __forceinline__ float row32_rest(const CgOperands& o, int64_t at, int L, const float* __restrict__ v,
+                                            uint2 (&e)[D]) {
+    float acc = 0.0f;
+    const int nb = L / D;
     for (int bt = 0; bt < nb; bt++) {
         float xv[D];
 #pragma unroll
@@ -421,6 +425,13 @@ __device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L,
         acc = fmaf(__uint_as_float(t.y), v[t.x], acc);
     }
     return acc;
+}
+
+template <int D = 8>
+__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L, const float* __restrict__ v) {
+    uint2 e[D];
+    row32_first(o, at, L, e);
+    return row32_rest(o, at, L, v, e);
 }
 
 // init: r_0 = b - A x (FP64); r32 = r_0; d = 0; p = 0; s = 0; rr, bb
@@ -665,20 +676,29 @@ __device__ __forceinline__ void pmx_finish(CgScalars* S, int mode, const double*
 __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
-    pdl_begin();
     __shared__ BlockTicket tk;
     CgScalars* S = o.S;
+    const ChunkLoop cl;
+    // Before the wait for u: the first chunk's row length and first stream entries (the
+    // matrix is fixed for the solve) and the row's residual (written by the vector
+    // updates or the reliable update, three or more kernels back).
+    int L0 = 0;
+    uint2 e0[4];
+    float r0 = 0.0f;
+    if (cl.warp < o.nchunks) {
+        const int i = kSellRows * cl.warp + cl.lane;
+        L0 = o.len[i];
+        row32_first(o, sell_index(o.off[cl.warp], cl.lane, 0), L0, e0);
+        if (i < o.n) r0 = o.r32[i];
+    }
+    pdl_begin();
     if (pcg_skip(S, mode)) return;
     ticket_init(tk);
-    const ChunkLoop cl;
     const float* __restrict__ u = o.u32;
     double vg = 0.0, vd = 0.0, vr = 0.0;
-    for (int c = cl.warp; c < o.nchunks; c += cl.nwarps) {
-        const int i = kSellRows * c + cl.lane;
-        const int L = o.len[i];
-        const float wi = row32<4>(o, sell_index(o.off[c], cl.lane, 0), L, u);
+    auto row_done = [&](int i, float wi, float rf) {
         if (i < o.n) {
-            const double ri = static_cast<double>(o.r32[i]);
+            const double ri = static_cast<double>(rf);
             const double ui = static_cast<double>(u[i]);
             o.w32[i] = wi;
             if (mode == 2) o.d32[i] = 0.0f;
@@ -686,6 +706,16 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
             vd += static_cast<double>(wi) * ui;
             vr += ri * ri;
         }
+    };
+    if (cl.warp < o.nchunks) {
+        const int i = kSellRows * cl.warp + cl.lane;
+        row_done(i, row32_rest(o, sell_index(o.off[cl.warp], cl.lane, 0), L0, u, e0), r0);
+    }
+    // further chunks (the launch gives every warp one chunk; kept for other grids)
+    for (int c = cl.warp + cl.nwarps; c < o.nchunks; c += cl.nwarps) {
+        const int i = kSellRows * c + cl.lane;
+        const float wi = row32<4>(o, sell_index(o.off[c], cl.lane, 0), o.len[i], u);
+        row_done(i, wi, i < o.n ? o.r32[i] : 0.0f);
     }
     double tot[3];
     if (grid_sum(vg, vd, vr, o.partials, o.tickets, &o.S->counter, tk, tot)) pmx_finish(S, mode, tot, h, h_true, use_cond);
