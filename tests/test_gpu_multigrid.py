@@ -118,3 +118,25 @@ def test_iterations_on_larger_dam_break(gpu_lib):
     # l0; the pressures differ by a few 1e-5 of max |p| (measured 2.5e-5 at r_e = 4.0 l0)
     assert rel_err(Pmg["x"], P64["x"], scale=2e-3) < 1e-6
     assert rel_err(Pmg["p"], P64["p"]) < 1e-4
+
+
+def test_deep_hierarchy_matches_fp64_cg(gpu_lib, oracle_lib):
+    # The l0 = 0.01 dam break in a 40 m x 40 m domain: an 837 x 837 search grid (cells of
+    # 4.8 l0), so 8 cell levels with the single-block bottom at level 5.  The cycle then
+    # runs one level each way with the per-level kernels and three each way with the
+    # fused sweeps (the workload's 320k dam break uses the fused sweeps alone).
+    def deep():
+        s = stock_tank()
+        s.max_x = 40.0
+        s.max_z = 40.0
+        return s
+
+    mg, cpu = _one_step(deep)
+    st = mg.stats()
+    assert mg.environment().grid_nx == 837 and mg.environment().grid_nz == 837
+    assert st["fallback"] == 0
+    assert st["cg_true_relres"] <= 1e-10
+    err = rel_err(mg.particles()["p"], cpu.particles()["p"])
+    print("deep hierarchy: %d iterations (FP64 CG %d), pressure rel err %.2e"
+          % (st["cg_iterations"], cpu.stats()["cg_iterations"], err))
+    assert err < 1e-7, err
