@@ -150,50 +150,6 @@ __device__ __forceinline__ bool cg_done(const CgScalars* S) {
     return S->converged || S->aborted || S->iter >= S->max_iter;
 }
 
-// Row i (lane of a chunk at `at`) times v in FP64, ascending columns.  The FP64 matrix
-// streams with evict-first hints: on big scenes it exceeds L2 and the solver's vectors
-// should stay resident instead.  Software-pipelined: the next D entries are loaded
-// before this batch's gathers, so a lane keeps both kinds of loads in flight.
-template <int D = 8, class V>
-__device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, V v) {
-    double acc = 0.0;
-    const int nb = L / D;
-    int c[D];
-    double a[D];
-    if (nb > 0) {
-#pragma unroll
-        for (int u = 0; u < D; u++) {
-            c[u] = __ldcs(o.col + at + u * kSellRows);
-            a[u] = __ldcs(o.val + at + u * kSellRows);
-        }
-    }
-    for (int bt = 0; bt < nb; bt++) {
-        double xv[D];
-#pragma unroll
-        for (int u = 0; u < D; u++) xv[u] = v(c[u]);
-        int cn[D];
-        double an[D];
-        if (bt + 1 < nb) {
-            const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
-#pragma unroll
-            for (int u = 0; u < D; u++) {
-                cn[u] = __ldcs(o.col + nx + u * kSellRows);
-                an[u] = __ldcs(o.val + nx + u * kSellRows);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < D; u++) acc = fma(a[u], xv[u], acc);
-#pragma unroll
-        for (int u = 0; u < D; u++) {
-            c[u] = cn[u];
-            a[u] = an[u];
-        }
-    }
-    at += static_cast<int64_t>(nb) * D * kSellRows;
-    for (int k = nb * D; k < L; k++, at += kSellRows) acc = fma(__ldcs(o.val + at), v(__ldcs(o.col + at)), acc);
-    return acc;
-}
-
 // One warp per chunk of kSellRows rows (lane = row within the chunk).  The SpMV kernels
 // launch as many warps as chunks so the block scheduler balances uneven chunks.
 struct ChunkLoop {
@@ -387,52 +343,6 @@ __global__ void __launch_bounds__(kBlock) k_true_residual(CgOperands o, int afte
 // vectors, both dot products of an iteration (gamma = r.r, delta = w.r) come out of one
 // reduction.  An iteration is an elementwise kernel (s, p, d, r updates, no reduction)
 // followed by the SpMV w = A r that also forms gamma and delta and the next step sizes.
-
-// Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
-// Software-pipelined like row64: row32_first loads the first D entries (they may be
-// loaded before the vector v is ready), row32_rest gathers and sums the row.
-template <int D>
-__device__ __forceinline__ void row32_first(const CgOperands& o, int64_t at, int L, uint2 (&e)[D]) {
-    if (L >= D) {
-#pragma unroll
-        for (int u = 0; u < D; u++) e[u] = ld_sell_pair(o.cv32 + at + u * kSellRows);
-    }
-}
-
-template <int D>
-__device__ __forceinline__ float row32_rest(const CgOperands& o, int64_t at, int L, const float* __restrict__ v,
-                                            uint2 (&e)[D]) {
-    float acc = 0.0f;
-    const int nb = L / D;
-    for (int bt = 0; bt < nb; bt++) {
-        float xv[D];
-#pragma unroll
-        for (int u = 0; u < D; u++) xv[u] = v[e[u].x];
-        uint2 f[D];
-        if (bt + 1 < nb) {
-            const int64_t nx = at + static_cast<int64_t>(bt + 1) * D * kSellRows;
-#pragma unroll
-            for (int u = 0; u < D; u++) f[u] = ld_sell_pair(o.cv32 + nx + u * kSellRows);
-        }
-#pragma unroll
-        for (int u = 0; u < D; u++) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
-#pragma unroll
-        for (int u = 0; u < D; u++) e[u] = f[u];
-    }
-    at += static_cast<int64_t>(nb) * D * kSellRows;
-    for (int k = nb * D; k < L; k++, at += kSellRows) {
-        const uint2 t = ld_sell_pair(o.cv32 + at);
-        acc = fmaf(__uint_as_float(t.y), v[t.x], acc);
-    }
-    return acc;
-}
-
-template <int D = 8>
-__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L, const float* __restrict__ v) {
-    uint2 e[D];
-    row32_first(o, at, L, e);
-    return row32_rest(o, at, L, v, e);
-}
 
 // init: r_0 = b - A x (FP64); r32 = r_0; d = 0; p = 0; s = 0; rr, bb
 __global__ void __launch_bounds__(kBlock) k_mx_init(CgOperands o, cudaGraphConditionalHandle h,
@@ -671,8 +581,11 @@ __device__ __forceinline__ void pmx_finish(CgScalars* S, int mode, const double*
 
 // w = A u (FP32); gamma, delta, rho in FP64; next step sizes; reliable-update decision
 // (mode 1) or stall check (mode 2: the true residual must at least halve between updates).
-// Four entries per pipeline step and at most 48 registers: five blocks per SM hide the
-// gather latency better than eight-deep steps at four blocks (measured 53 -> 51 us).
+// Five entries per pipeline step at 48 registers and five blocks per SM (measured on the
+// 340k PPE, alone after an L2 flush: 37.7 us against 39.0 for four entries, 38.8 for six,
+// 42-43 for eight at three or four blocks, 39.6-41.0 at six blocks and 40 registers).
+constexpr int kPmxDepth = 5;
+
 __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
                                                     cudaGraphConditionalHandle h,
                                                     cudaGraphConditionalHandle h_true, int use_cond) {
@@ -683,7 +596,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
     // matrix is fixed for the solve) and the row's residual (written by the vector
     // updates or the reliable update, three or more kernels back).
     int L0 = 0;
-    uint2 e0[4];
+    uint2 e0[kPmxDepth];
     float r0 = 0.0f;
     if (cl.warp < o.nchunks) {
         const int i = kSellRows * cl.warp + cl.lane;
@@ -714,7 +627,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
     // further chunks (the launch gives every warp one chunk; kept for other grids)
     for (int c = cl.warp + cl.nwarps; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
-        const float wi = row32<4>(o, sell_index(o.off[c], cl.lane, 0), o.len[i], u);
+        const float wi = row32<kPmxDepth>(o, sell_index(o.off[c], cl.lane, 0), o.len[i], u);
         row_done(i, wi, i < o.n ? o.r32[i] : 0.0f);
     }
     double tot[3];

@@ -72,6 +72,90 @@ struct CgOperands {
     const DevStatus* status;  // step status (may be null): a failed search aborts the solve
 };
 
+// Row i (lane of a chunk at `at`) times v in FP64, ascending columns.  The FP64 matrix
+// streams with evict-first hints: on big scenes it exceeds L2 and the solver's vectors
+// should stay resident instead.  Software-pipelined: the next D entries are loaded
+// before this batch's gathers, so a lane keeps both kinds of loads in flight.  The
+// row's last step is predicated (slots past L load nothing and add nothing): a row costs
+// ceil(L / D) dependent round trips, and the sum is the same sequence of fma as one
+// entry at a time.
+template <int D = 8, class V>
+__device__ __forceinline__ double row64(const CgOperands& o, int64_t at, int L, V v) {
+    double acc = 0.0;
+    int c[D];
+    double a[D];
+#pragma unroll
+    for (int u = 0; u < D; u++) {
+        c[u] = u < L ? __ldcs(o.col + at + u * kSellRows) : 0;
+        a[u] = u < L ? __ldcs(o.val + at + u * kSellRows) : 0.0;
+    }
+    for (int k0 = 0; k0 < L; k0 += D) {
+        double xv[D];
+#pragma unroll
+        for (int u = 0; u < D; u++) xv[u] = k0 + u < L ? v(c[u]) : 0.0;
+        int cn[D];
+        double an[D];
+        const int64_t nx = at + static_cast<int64_t>(k0 + D) * kSellRows;
+#pragma unroll
+        for (int u = 0; u < D; u++) {
+            const bool in = k0 + D + u < L;
+            cn[u] = in ? __ldcs(o.col + nx + u * kSellRows) : 0;
+            an[u] = in ? __ldcs(o.val + nx + u * kSellRows) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < D; u++)
+            if (k0 + u < L) acc = fma(a[u], xv[u], acc);
+#pragma unroll
+        for (int u = 0; u < D; u++) {
+            c[u] = cn[u];
+            a[u] = an[u];
+        }
+    }
+    return acc;
+}
+
+// Lane's row of the FP32 matrix times v, FP32 accumulation, ascending columns.
+// Software-pipelined: row32_first loads the first D entries (they may be loaded before
+// the vector v is ready), row32_rest gathers and sums the row D entries per step while
+// the next step's entries load.  The row's last step is predicated (slots past L load
+// nothing and add nothing), so a row costs ceil(L / D) dependent round trips and the
+// sum is the same sequence of fmaf as one entry at a time.
+template <int D>
+__device__ __forceinline__ void row32_first(const CgOperands& o, int64_t at, int L, uint2 (&e)[D]) {
+#pragma unroll
+    for (int u = 0; u < D; u++)
+        e[u] = u < L ? ld_sell_pair(o.cv32 + at + u * kSellRows) : make_uint2(0u, 0u);
+}
+
+template <int D>
+__device__ __forceinline__ float row32_rest(const CgOperands& o, int64_t at, int L, const float* __restrict__ v,
+                                            uint2 (&e)[D]) {
+    float acc = 0.0f;
+    for (int k0 = 0; k0 < L; k0 += D) {
+        float xv[D];
+#pragma unroll
+        for (int u = 0; u < D; u++) xv[u] = k0 + u < L ? v[e[u].x] : 0.0f;
+        uint2 f[D];
+        const int64_t nx = at + static_cast<int64_t>(k0 + D) * kSellRows;
+#pragma unroll
+        for (int u = 0; u < D; u++)
+            f[u] = k0 + D + u < L ? ld_sell_pair(o.cv32 + nx + u * kSellRows) : make_uint2(0u, 0u);
+#pragma unroll
+        for (int u = 0; u < D; u++)
+            if (k0 + u < L) acc = fmaf(__uint_as_float(e[u].y), xv[u], acc);
+#pragma unroll
+        for (int u = 0; u < D; u++) e[u] = f[u];
+    }
+    return acc;
+}
+
+template <int D = 8>
+__device__ __forceinline__ float row32(const CgOperands& o, int64_t at, int L, const float* __restrict__ v) {
+    uint2 e[D];
+    row32_first(o, at, L, e);
+    return row32_rest(o, at, L, v, e);
+}
+
 struct MgHierarchy;
 struct LearnedOps;
 
