@@ -627,7 +627,11 @@ __global__ void __launch_bounds__(kBlock, 5) k_pmx_spmv(CgOperands o, int mode,
     // further chunks (the launch gives every warp one chunk; kept for other grids)
     for (int c = cl.warp + cl.nwarps; c < o.nchunks; c += cl.nwarps) {
         const int i = kSellRows * c + cl.lane;
-        const float wi = row32<kPmxDepth>(o, sell_index(o.off[c], cl.lane, 0), o.len[i], u);
+        const int L = o.len[i];
+        const int64_t at = sell_index(o.off[c], cl.lane, 0);
+        uint2 e[kPmxDepth];
+        row32_first(o, at, L, e);
+        const float wi = row32_rest(o, at, L, u, e);
         row_done(i, wi, i < o.n ? o.r32[i] : 0.0f);
     }
     double tot[3];
