@@ -273,6 +273,13 @@ __device__ __forceinline__ bool below(double a, double b) {
            static_cast<unsigned long long>(__double_as_longlong(b));
 }
 
+// sums_from_zero: where the reference adds a zero term to an accumulator of a neighbour
+// walk (a dummy neighbour's zero vector, a pair outside the collision distance), the
+// stage kernels add nothing.  Each such accumulator starts at +0, and a round-to-nearest
+// sum that starts at +0 never holds -0 (x + y is -0 only when both are -0), so x + 0 is
+// x bit for bit; only the payload of a NaN could differ (it stays a NaN).  On GB300 that
+// saves two FP64 additions per pair in range of the dynamic stabilisation walk.
+
 // Squared distance: the reference's inner_prod(r, r) = (0 + dx dx) + dz dz.  The 0 + is
 // the identity here (a square is never -0), so it is left out.
 __device__ __forceinline__ double dist2(double dx, double dz) {

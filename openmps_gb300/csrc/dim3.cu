@@ -281,11 +281,7 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
             ax += c * (st.u[j] - ui);
             ay += c * (st.v[j] - vi);
             az += c * (st.w[j] - wi);
-        } else {
-            ax = __dadd_rn(ax, 0.0);
-            ay = __dadd_rn(ay, 0.0);
-            az = __dadd_rn(az, 0.0);
-        }
+        }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
         if (spp) {
             const double wg = weight(dsqrt_rn(r2), sc.re_lap);
             gx += wg * dx;
@@ -404,9 +400,7 @@ __global__ void k3_ppe_build(SceneConst sc, DeviceState st) {
                 m++;
             }
             a_ii += -a_ij;
-        } else {
-            a_ii = __dadd_rn(a_ii, 0.0);
-        }
+        }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
         if (spp) {
             const double wg = weight(dsqrt_rn(r2), sc.re_lap);
             gx += wg * dx;
@@ -528,11 +522,7 @@ __global__ void k3_pressure_gradient(SceneConst sc, DeviceState st) {
                 sy += c * dy;
                 sz += c * dz;
             }
-        } else {
-            sx = __dadd_rn(sx, 0.0);
-            sy = __dadd_rn(sy, 0.0);
-            sz = __dadd_rn(sz, 0.0);
-        }
+        }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
         if (spp) {
             gx += wg * dx;
             gy += wg * dy;
@@ -596,11 +586,7 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
             sx += mag * ex;
             sy += mag * ey;
             sz += mag * ez;
-        } else {
-            sx = __dadd_rn(sx, 0.0);
-            sy = __dadd_rn(sy, 0.0);
-            sz = __dadd_rn(sz, 0.0);
-        }
+        }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
         if (spp) {
             const double wg = weight(dsqrt_rn(r2), sc.re);
             gx += wg * dx;

@@ -265,10 +265,7 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
                 const double c = viscosity_coefficient(sc, lf, dsqrt_rn(r2));
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
-            } else {
-                vx = __dadd_rn(vx, 0.0);
-                vz = __dadd_rn(vz, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             if (spp) {
                 const double wg = weight(dsqrt_rn(r2), sc.re_lap);
                 gx += wg * dx;
@@ -332,10 +329,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
                 const double c = viscosity_coefficient(sc, lf, r);
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
-            } else {
-                vx = __dadd_rn(vx, 0.0);
-                vz = __dadd_rn(vz, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             if (spp) {
                 const double wg = (in_re && sc.re_lap == sc.re) ? w_re : weight(r, sc.re_lap);
                 gx += wg * dx;
@@ -500,9 +494,7 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
                 const double a_ij = ppe_coefficient(sc, lf, dsqrt_rn(r2));
                 if (spp || !is_surface(sc, st.nd[j])) pr.put(sc, st, ppe_row(st, j), a_ij);
                 a_ii += -a_ij;
-            } else {
-                a_ii = __dadd_rn(a_ii, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             if (spp) {
                 const double wg = weight(dsqrt_rn(r2), sc.re_lap);
                 gx += wg * dx;
@@ -569,9 +561,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
                 const double a_ij = ppe_coefficient(sc, lf, r);
                 pr.put(sc, st, ppe_row(st, j), a_ij);
                 a_ii += -a_ij;
-            } else {
-                a_ii = __dadd_rn(a_ii, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             const double wg = (in_re && sc.re_lap == sc.re) ? w : weight(r, sc.re_lap);
             gx += wg * dx;
             gz += wg * dz;
@@ -696,10 +686,7 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
                 const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
                 sx += c * dx;
                 sz += c * dz;
-            } else {
-                sx = __dadd_rn(sx, 0.0);
-                sz = __dadd_rn(sz, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             if (spp) {
                 gx += wg * dx;
                 gz += wg * dz;
@@ -819,10 +806,7 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
                 const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
                 sx += c * row_dot(C[0], C[1], dx, dz);
                 sz += c * row_dot(C[2], C[3], dx, dz);
-            } else {
-                sx = __dadd_rn(sx, 0.0);
-                sz = __dadd_rn(sz, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
         }
     });
     if (has_spp) {
@@ -867,10 +851,7 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
                 const double mag = dsqrt_rn(d2 - r_perp2) - r_par;
                 sx += mag * ex;
                 sz += mag * ez;
-            } else {
-                sx = __dadd_rn(sx, 0.0);
-                sz = __dadd_rn(sz, 0.0);
-            }
+            }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
             if (spp) {
                 const double wg = weight(dsqrt_rn(r2), sc.re);
                 gx += wg * dx;
