@@ -266,10 +266,9 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
     if (step_failed(sc, st)) return;
     if (st.type[i] != MPS_TYPE_FLUID) return;
     const LapFactors3 lf = lap_factors3(sc);
-    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     const double ui = st.u[i], vi = st.v[i], wi = st.w[i];
-    double ax = 0.0, ay = 0.0, az = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0;
     for_near3(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
@@ -282,21 +281,10 @@ __global__ void k3_explicit_accel(SceneConst sc, DeviceState st) {
             ay += c * (st.v[j] - vi);
             az += c * (st.w[j] - wi);
         }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-        if (spp) {
-            const double wg = weight(dsqrt_rn(r2), sc.re_lap);
-            gx += wg * dx;
-            gy += wg * dy;
-            gz += wg * dz;
-        }
     });
-    double xs, ys, zs;
-    if (spp && spp_particle3(sc, st, i, sc.re_lap, gx, gy, gz, xs, ys, zs)) {
-        const double ddx = xi - xs, ddy = yi - ys, ddz = zi - zs;
-        const double c = viscosity_coefficient3(sc, lf, dsqrt_rn(dot3(ddx, ddy, ddz, ddx, ddy, ddz)));
-        ax += c * (ui - ui);
-        ay += c * (vi - vi);
-        az += c * (wi - wi);
-    }
+    // With SPP the reference adds the virtual particle's viscosity term c (u_i - u_i),
+    // which is +0 for finite velocities: the virtual particle is not built here
+    // (sums_from_zero, common.cuh).
     if (has_flag(sc.flags, MPS_FLAG_CENTRAL_GRAVITY)) {  // Computer.hpp:981-988
         const double g = -sc.g;
         const double r = dsqrt_rn(dot3(xi, yi, zi, xi, yi, zi));
@@ -564,7 +552,7 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const double factor = -1.0 / (2 * dt * sc.n0);
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     const double oxi = st.ox[i], oyi = st.oy[i], ozi = st.oz[i];
-    double sx = 0.0, sy = 0.0, sz = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
     for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
@@ -587,19 +575,9 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
             sy += mag * ey;
             sz += mag * ez;
         }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-        if (spp) {
-            const double wg = weight(dsqrt_rn(r2), sc.re);
-            gx += wg * dx;
-            gy += wg * dy;
-            gz += wg * dz;
-        }
     });
-    double xs, ys, zs;
-    if (spp && spp_particle3(sc, st, i, sc.re, gx, gy, gz, xs, ys, zs)) {
-        sx = __dadd_rn(sx, 0.0);  // the SPP particle is excluded (Computer.hpp:1597-1598)
-        sy = __dadd_rn(sy, 0.0);
-        sz = __dadd_rn(sz, 0.0);
-    }
+    // With SPP the reference places the virtual particle too but leaves it out of the sum
+    // (Computer.hpp:1597-1598): a zero vector, so it is not built here.
     st.dux[i] = factor * sx;
     st.duy[i] = factor * sy;
     st.duz[i] = factor * sz;

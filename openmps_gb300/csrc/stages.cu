@@ -253,9 +253,8 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
     if (step_failed(sc, st)) return;
     const LapFactors lf = lap_factors(sc);
     if (st.type[i] != MPS_TYPE_FLUID) return;
-    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
-    double vx = 0.0, vz = 0.0, gx = 0.0, gz = 0.0;
+    double vx = 0.0, vz = 0.0;
     for_near(sc, st, i, sc.f32_out_rl, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
@@ -266,20 +265,11 @@ __global__ void k_explicit_accel(SceneConst sc, DeviceState st) {
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
             }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-            if (spp) {
-                const double wg = weight(dsqrt_rn(r2), sc.re_lap);
-                gx += wg * dx;
-                gz += wg * dz;
-            }
         }
     });
-    double xs, zs;
-    if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
-        const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
-        vx += c * (ui - ui);
-        vz += c * (wi - wi);
-    }
+    // With SPP the reference adds the virtual particle's viscosity term c (u_i - u_i),
+    // which is +0 for finite velocities: the virtual particle is not built here
+    // (sums_from_zero, common.cuh).
     add_gravity(sc, xi, zi, vx, vz, st.dux[i], st.duz[i]);  // a += G (Environment.hpp:149)
 }
 
@@ -304,7 +294,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     const bool hs = kEcs && has_flag(sc.flags, MPS_FLAG_HS);
     const double xi = st.x[i], zi = st.z[i], ui = st.u[i], wi = st.w[i];
     double thisN = 0.0, hsum = 0.0;
-    double vx = 0.0, vz = 0.0, gx = 0.0, gz = 0.0;
+    double vx = 0.0, vz = 0.0;
     const float out_thr = fluid ? fmaxf(sc.f32_out_re, sc.f32_out_rl) : sc.f32_out_re;
     for_near(sc, st, i, out_thr, [&](int j) {
         const double dx = st.x[j] - xi;
@@ -314,10 +304,8 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
         const bool in_rl = fluid && below(r2, sc.rl2);
         if (!in_re && !in_rl) return;
         const double r = dsqrt_rn(r2);
-        // W(r, r_e), reused for W(r, r_e^lap) when the two radii are one
-        const double w_re = in_re ? weight(r, sc.re) : 0.0;
         if (in_re) {
-            thisN += w_re;
+            thisN += weight(r, sc.re);
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
@@ -330,11 +318,6 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
                 vx += c * (st.u[j] - ui);
                 vz += c * (st.w[j] - wi);
             }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-            if (spp) {
-                const double wg = (in_re && sc.re_lap == sc.re) ? w_re : weight(r, sc.re_lap);
-                gx += wg * dx;
-                gz += wg * dz;
-            }
         }
     });
     // ComputeNeighborDensities
@@ -359,13 +342,9 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
     }
     if (!fluid) return;
     // ComputeExplicitForces, first loop
-    double xs, zs;
-    if (spp && spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
-        const double ddx = xi - xs, ddz = zi - zs;
-        const double c = viscosity_coefficient(sc, lf, dsqrt_rn(dot2(ddx, ddz, ddx, ddz)));
-        vx += c * (ui - ui);
-        vz += c * (wi - wi);
-    }
+    // With SPP the reference adds the virtual particle's viscosity term c (u_i - u_i),
+    // which is +0 for finite velocities: the virtual particle is not built here
+    // (sums_from_zero, common.cuh).
     add_gravity(sc, xi, zi, vx, vz, st.dux[i], st.duz[i]);
 }
 
@@ -463,7 +442,6 @@ __global__ void k_ppe_build(SceneConst sc, DeviceState st) {
     if (i >= sc.n) return;
     if (step_failed(sc, st)) return;
     const LapFactors lf = lap_factors(sc);
-    const int n = sc.n;
     const int row = ppe_row(st, i);
     if (!ppe_alive(sc, st, i)) {
         st.ppe_b[row] = 0;
@@ -826,13 +804,12 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
     if (i >= sc.n) return;
     if (solve_failed(sc, st)) return;
     if (st.type[i] != MPS_TYPE_FLUID) return;
-    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double dt = st.step->dt;
     const double d = sc.l0 - sc.max_dx;
     const double d2 = d * d;
     const double factor = -1.0 / (2 * dt * sc.n0);
     const double xi = st.x[i], zi = st.z[i], oxi = st.ox[i], ozi = st.oz[i];
-    double sx = 0.0, sz = 0.0, gx = 0.0, gz = 0.0;
+    double sx = 0.0, sz = 0.0;
     for_near(sc, st, i, sc.f32_out_re, [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
@@ -852,18 +829,10 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
                 sx += mag * ex;
                 sz += mag * ez;
             }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-            if (spp) {
-                const double wg = weight(dsqrt_rn(r2), sc.re);
-                gx += wg * dx;
-                gz += wg * dz;
-            }
         }
     });
-    double xs, zs;
-    if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
-        sx = __dadd_rn(sx, 0.0);  // the virtual particle is excluded (Computer.hpp:1597-1598)
-        sz = __dadd_rn(sz, 0.0);
-    }
+    // With SPP the reference places the virtual particle too but leaves it out of the sum
+    // (Computer.hpp:1597-1598): a zero vector, so it is not built here.
     st.dux[i] = factor * sx;
     st.duz[i] = factor * sz;
 }
