@@ -47,9 +47,10 @@ struct SceneConst {
     int32_t cells_per_scene;  // gnx * gnz: cells of one scene
     int32_t nscenes;          // scenes of a batch (1 for a single scene)
     // FP32 bounds of the FP64 range tests (range_class below): r^2 surely below nl2_lo
-    // under f32_in_nl, surely above nl2_hi / re^2 / re_lap^2 over the f32_out_* values
+    // under f32_in_nl, surely above nl2_hi / re^2 / re_lap^2 / d^2 over the f32_out_*
+    // values (d = l0 - max_dx, the collision distance of DynamicStabilize)
     float f32_in_nl;
-    float f32_out_nl, f32_out_re, f32_out_rl, pad1;
+    float f32_out_nl, f32_out_re, f32_out_rl, f32_out_ds;
     double l0, re, re2, re_lap, rl2;
     double nl, nl2_lo, nl2_hi;  // neighbour length and a guard band around nl^2
     double n0, lambda, n0_lap, lambda_lap;

@@ -545,7 +545,6 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
     if (i >= sc.n) return;
     if (solve_failed(sc, st)) return;
     if (st.type[i] != MPS_TYPE_FLUID) return;
-    const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double dt = st.step->dt;
     const double d = sc.l0 - sc.max_dx;
     const double d2 = d * d;
@@ -553,7 +552,7 @@ __global__ void k3_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const double xi = st.x[i], yi = st.y[i], zi = st.z[i];
     const double oxi = st.ox[i], oyi = st.oy[i], ozi = st.oz[i];
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for_near3(sc, st, i, sc.f32_out_re, [&](int j) {
+    for_near3(sc, st, i, fminf(sc.f32_out_re, sc.f32_out_ds), [&](int j) {
         const double dx = st.x[j] - xi;
         const double dy = st.y[j] - yi;
         const double dz = st.z[j] - zi;

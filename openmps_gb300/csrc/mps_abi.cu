@@ -270,7 +270,6 @@ void setup_constants(mps_handle* h) {
     sc.f32_out_nl = f32_bound(sc.nl2_hi, true);
     sc.f32_out_re = f32_bound(sc.re2, true);
     sc.f32_out_rl = f32_bound(sc.rl2, true);
-    sc.pad1 = 0.0f;
     sc.dim = (p.dim == 3) ? 3 : 2;
     const bool d3 = sc.dim == 3;
     if (d3) {
@@ -290,6 +289,10 @@ void setup_constants(mps_handle* h) {
     else
         sc.max_dt = std::min(p.max_dt, std::sqrt(2 * (p.courant * p.l0) / p.g));  // :138
     sc.max_dx = p.courant * p.l0;                                             // :143
+    {
+        const double d = sc.l0 - sc.max_dx;  // the collision distance, as k_dynamic_stabilize forms it
+        sc.f32_out_ds = f32_bound(d * d, true);
+    }
     sc.min_x = p.min_x;
     sc.min_z = p.min_z;
     sc.min_y = d3 ? p.min_y : 0.0;

@@ -810,7 +810,7 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
     const double factor = -1.0 / (2 * dt * sc.n0);
     const double xi = st.x[i], zi = st.z[i], oxi = st.ox[i], ozi = st.oz[i];
     double sx = 0.0, sz = 0.0;
-    for_near(sc, st, i, sc.f32_out_re, [&](int j) {
+    for_near(sc, st, i, fminf(sc.f32_out_re, sc.f32_out_ds), [&](int j) {
         const double dx = st.x[j] - xi;
         const double dz = st.z[j] - zi;
         const double r2 = dist2(dx, dz);
@@ -832,7 +832,9 @@ __global__ void k_dynamic_stabilize(SceneConst sc, DeviceState st) {
         }
     });
     // With SPP the reference places the virtual particle too but leaves it out of the sum
-    // (Computer.hpp:1597-1598): a zero vector, so it is not built here.
+    // (Computer.hpp:1597-1598): a zero vector, so it is not built here, and only pairs
+    // within the collision distance d add anything: the FP32 screen uses the smaller of
+    // d and r_e.
     st.dux[i] = factor * sx;
     st.duz[i] = factor * sz;
 }
