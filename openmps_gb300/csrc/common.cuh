@@ -111,6 +111,10 @@ struct DeviceState {
     // order ([m n + i]), written by the fused density + assembly walk and read by the
     // pressure gradient on the same positions
     double* w_re;
+    // the SPP sums sum W(r, r_e^lap) dx and dz of the fused density + assembly walk
+    // ([i], [n + i]), read by the pressure gradient on the same positions when r_e^lap =
+    // r_e (the same pairs in the same order: the sums are the gradient's own)
+    double* spp_g;
     const int32_t* scene_of;  // batch: scene of each particle (its cells start at
                               // scene * cells_per_scene); null for a single scene
     int32_t *nb_count, *nb;
@@ -543,7 +547,7 @@ void launch_density_explicit_pressure(const SceneConst& sc, const DeviceState& s
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // the same reading the weights launch_density_set_ppe or launch_density_explicit_pressure
 // cached (positions unchanged since)
-void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
+void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, bool spp_sums, cudaStream_t s);
 void launch_dynamic_stabilize(const SceneConst& sc, const DeviceState& st, cudaStream_t s);
 // part 2 of the CFL step (dt from the max |u|^2 a launch before it gathered)
 void launch_cfl_dt_finish(const SceneConst& sc, const DeviceState& st, cudaStream_t s);

@@ -405,6 +405,7 @@ void allocate(mps_handle* h, int64_t n, int64_t keep) {
     st.z32 = dalloc<float>(h, n);
     st.y32 = d3 ? dalloc<float>(h, n) : nullptr;
     st.w_re = dalloc<double>(h, n * kReCache);
+    st.spp_g = dalloc<double>(h, 2 * n);
     st.row_of = st.particle_of = st.row_cell = st.cell_fill = st.cell_start = nullptr;
     st.unplaced = st.unplaced_pos = st.row_scratch = nullptr;
     if (h->nscenes == 0 && !d3) {  // single 2D scene: PPE rows in cell order
@@ -951,8 +952,8 @@ void forward(mps_handle* h, double dt) {
         launched(h, kLaunchesAssign);
     }
     stage_mark(h, kGradient);
-    if (fused || !implicit)  // the density walk cached W(r, r_e) on these positions
-        launch_pressure_gradient_cached(sc, h->st, s);
+    if (fused || !implicit)  // the density walk cached W(r, r_e) (and the SPP sums) on these positions
+        launch_pressure_gradient_cached(sc, h->st, implicit && sc.re_lap == sc.re, s);
     else
         launch_pressure_gradient(sc, h->st, s);
     launched(h, kLaunchesGradient);
@@ -1097,7 +1098,7 @@ void batch_stages_post(mps_handle* h) {
     const bool implicit = batch_implicit(h);
     if (implicit) launch_assign_pressure(sc, h->st, s);
     if (density_ppe_fusable(sc) || !implicit)  // batch_stages_pre's density walk cached W
-        launch_pressure_gradient_cached(sc, h->st, s);
+        launch_pressure_gradient_cached(sc, h->st, implicit && sc.re_lap == sc.re, s);
     else
         launch_pressure_gradient(sc, h->st, s);
     if (h->prm.flags & MPS_FLAG_DS) launch_dynamic_stabilize(sc, h->st, s);

@@ -559,6 +559,8 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
         st.ppe_b[row] = -sc.rho / (sc.n0 * dt) * speed;
     }
     st.ppe_x[row] = st.p[i];
+    st.spp_g[i] = gx;
+    st.spp_g[n + i] = gz;
     double xs, zs;
     if (spp_particle(sc, st, i, sc.re_lap, gx, gz, xs, zs)) {
         const double ddx = xi - xs, ddz = zi - zs;
@@ -638,9 +640,9 @@ __global__ void k_assign_pressure(SceneConst sc, DeviceState st) {
 }
 
 // ModifyByPressureGradient, midpoint branch (Computer.hpp:1501-1521): du only.
-// kCached: W of the entries within r_e comes from st.w_re (the fused density + assembly
-// walk wrote it on the same positions, in the same list order).
-template <bool kCached>
+// kCache >= 1: W of the entries within r_e comes from st.w_re (the density walk wrote it
+// on the same positions, in the same list order); 2: the SPP sums come from st.spp_g too.
+template <int kCache>
 __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
@@ -657,20 +659,24 @@ __global__ void k_pressure_gradient(SceneConst sc, DeviceState st) {
         const double dz = st.z[j] - zi;
         const double r2 = dist2(dx, dz);
         if (below(r2, sc.re2)) {
-            const double wg = (kCached && m_re < kReCache) ? st.w_re[static_cast<int64_t>(m_re) * sc.n + i]
-                                                           : weight(dsqrt_rn(r2), sc.re);
+            const double wg = (kCache >= 1 && m_re < kReCache) ? st.w_re[static_cast<int64_t>(m_re) * sc.n + i]
+                                                               : weight(dsqrt_rn(r2), sc.re);
             m_re++;
             if (st.type[j] != MPS_TYPE_DUMMY) {
                 const double c = ddiv_rn(st.p[j] + pi, r2) * wg;
                 sx += c * dx;
                 sz += c * dz;
             }  // the reference adds zero here: the identity on this sum (sums_from_zero, common.cuh)
-            if (spp) {
+            if (kCache < 2 && spp) {
                 gx += wg * dx;
                 gz += wg * dz;
             }
         }
     });
+    if (kCache == 2 && spp) {
+        gx = st.spp_g[i];
+        gz = st.spp_g[sc.n + i];
+    }
     double xs, zs;
     if (spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs)) {
         const double dx = xs - xi;
@@ -725,7 +731,7 @@ __device__ __forceinline__ double row_dot(double c0, double c1, double dx, doubl
 // particle; the second sums (p_ij / r^2 W) C dx over the non-dummy ones in the same
 // order.  The two off-diagonal sums of C^-1 add the same products (dx dz = dz dx
 // exactly), so one accumulator holds both.
-template <bool kCached>
+template <int kCache>
 __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.n) return;
@@ -734,8 +740,8 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
     const bool spp = has_flag(sc.flags, MPS_FLAG_SPP);
     const double xi = st.x[i], zi = st.z[i], pi = st.p[i];
     auto w_of = [&](int m, double r2) {
-        return (kCached && m < kReCache) ? st.w_re[static_cast<int64_t>(m) * sc.n + i]
-                                         : weight(dsqrt_rn(r2), sc.re);
+        return (kCache >= 1 && m < kReCache) ? st.w_re[static_cast<int64_t>(m) * sc.n + i]
+                                             : weight(dsqrt_rn(r2), sc.re);
     };
     double m00 = 0.0, m01 = 0.0, m11 = 0.0, gx = 0.0, gz = 0.0;
     int m_re = 0;
@@ -750,12 +756,16 @@ __global__ void k_pressure_gradient_gc(SceneConst sc, DeviceState st) {
             m00 += t * (dx * dx);
             m01 += t * (dx * dz);
             m11 += t * (dz * dz);
-            if (spp) {
+            if (kCache < 2 && spp) {
                 gx += wg * dx;
                 gz += wg * dz;
             }
         }
     });
+    if (kCache == 2 && spp) {  // the SPP sums of the density walk (see k_pressure_gradient)
+        gx = st.spp_g[i];
+        gz = st.spp_g[sc.n + i];
+    }
     double xs = 0.0, zs = 0.0;
     const bool has_spp = spp && spp_particle(sc, st, i, sc.re, gx, gz, xs, zs);
     double sdx = 0.0, sdz = 0.0, sr2 = 0.0, sw = 0.0;
@@ -953,17 +963,26 @@ void launch_density_explicit_pressure(const SceneConst& sc, const DeviceState& s
 
 void launch_pressure_gradient(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
     if (sc.flags & MPS_FLAG_GC)
-        k_pressure_gradient_gc<false><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
+        k_pressure_gradient_gc<0><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     else
-        k_pressure_gradient<false><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
+        k_pressure_gradient<0><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
-void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, cudaStream_t s) {
-    if (sc.flags & MPS_FLAG_GC)
-        k_pressure_gradient_gc<true><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
-    else
-        k_pressure_gradient<true><<<grid_for(sc.n, kWalkBlock), kWalkBlock, 0, s>>>(sc, st);
+// spp_sums: the fused density + assembly walk (k_density_ppe) ran on these positions with
+// r_e^lap = r_e, so its SPP sums are the gradient's
+void launch_pressure_gradient_cached(const SceneConst& sc, const DeviceState& st, bool spp_sums, cudaStream_t s) {
+    const dim3 g(grid_for(sc.n, kWalkBlock));
+    if (sc.flags & MPS_FLAG_GC) {
+        if (spp_sums)
+            k_pressure_gradient_gc<2><<<g, kWalkBlock, 0, s>>>(sc, st);
+        else
+            k_pressure_gradient_gc<1><<<g, kWalkBlock, 0, s>>>(sc, st);
+    } else if (spp_sums) {
+        k_pressure_gradient<2><<<g, kWalkBlock, 0, s>>>(sc, st);
+    } else {
+        k_pressure_gradient<1><<<g, kWalkBlock, 0, s>>>(sc, st);
+    }
     k_apply_du<<<grid_for(sc.n), kBlock, 0, s>>>(sc, st);
 }
 
