@@ -285,6 +285,13 @@ __device__ __forceinline__ bool below(double a, double b) {
 // x bit for bit; only the payload of a NaN could differ (it stays a NaN).  On GB300 that
 // saves two FP64 additions per pair in range of the dynamic stabilisation walk.
 
+// dot2 without its leading 0 +: the two differ only in the sign of a zero result, so
+// dot2_term serves where that sign cannot reach the result: the HS term dot / r^3 (r > 0)
+// added to a sum that starts at +0 (sums_from_zero above).
+__device__ __forceinline__ double dot2_term(double a0, double a1, double b0, double b1) {
+    return __dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1));
+}
+
 // Squared distance: the reference's inner_prod(r, r) = (0 + dx dx) + dz dz.  The 0 + is
 // the identity here (a square is never -0), so it is left out.
 __device__ __forceinline__ double dist2(double dx, double dz) {

@@ -28,6 +28,11 @@ __device__ __forceinline__ double dot3(double a0, double a1, double a2, double b
     return __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(a0, b0)), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
 }
 
+// dot3 without its leading 0 + (see dot2_term in common.cuh)
+__device__ __forceinline__ double dot3_term(double a0, double a1, double a2, double b0, double b1, double b2) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a0, b0), __dmul_rn(a1, b1)), __dmul_rn(a2, b2));
+}
+
 // inner_prod(d, d) without the 0 + (a square is never -0)
 __device__ __forceinline__ double dist3(double dx, double dy, double dz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
@@ -198,7 +203,7 @@ __device__ double density_variation3(const SceneConst& sc, const DeviceState& st
                 const double dv = st.v[j] - vi;
                 const double dw = st.w[j] - wi;
                 const double r = dsqrt_rn(r2);
-                sum += ddiv_rn(dot3(dx, dy, dz, du, dv, dw), r * r * r);
+                sum += ddiv_rn(dot3_term(dx, dy, dz, du, dv, dw), r * r * r);
             }
         });
         return -sc.re * sum;

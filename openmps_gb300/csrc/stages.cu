@@ -78,7 +78,7 @@ __device__ double density_variation(const SceneConst& sc, const DeviceState& st,
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
                 const double r = dsqrt_rn(r2);
-                sum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
+                sum += ddiv_rn(dot2_term(dx, dz, du, dw), r * r * r);
             }
         });
         return -sc.re * sum;
@@ -309,7 +309,7 @@ __global__ void k_pre_pressure(SceneConst sc, DeviceState st) {
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
-                hsum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
+                hsum += ddiv_rn(dot2_term(dx, dz, du, dw), r * r * r);
             }
         }
         if (in_rl) {
@@ -531,7 +531,7 @@ __global__ void k_density_ppe(SceneConst sc, DeviceState st) {
             if (hs) {
                 const double du = st.u[j] - ui;
                 const double dw = st.w[j] - wi;
-                hsum += ddiv_rn(dot2(dx, dz, du, dw), r * r * r);
+                hsum += ddiv_rn(dot2_term(dx, dz, du, dw), r * r * r);
             }
         }
         if (in_rl) {
