@@ -7,8 +7,8 @@
 //   k_mg_cells   level-1 operator: per cell, the bins of its particles in slot order
 //                (deterministic, no atomics);
 //   k_mg_coarsen Galerkin product of a 2 x 2 aggregation, FP64;
-//   k_mg_dense   dense inverse of the coarsest level (Gauss-Jordan in FP32 in shared
-//                memory, symmetrised).
+//   k_mg_dense   dense inverse of the coarsest level (banded L U and one substitution
+//                per column, FP32 in shared memory, symmetrised).
 // Cycle, once per iteration (FP32, reads L2-resident planes):
 //   k_mg_axpy_restrict (the iteration's vector updates + level-1 restriction; after init
 //   and after a reliable update k_mg_restrict0), k_mg_down_fused (the coarse residuals of
@@ -154,16 +154,21 @@ __global__ void k_mg_coarsen(MgLevel f, MgLevel c, float omega, const DevStatus*
     store_level(c, I, k, omega);
 }
 
-// Dense inverse of the coarsest level: Gauss-Jordan without pivoting (the operator is
-// negative definite on its non-empty cells; empty cells get a unit diagonal and a zero
-// row and column in the inverse), FP32 in shared memory, symmetrised on output.
+// Dense inverse of the coarsest level, FP32 in shared memory, symmetrised on output.  The
+// 9-point operator is banded in the level's cell order c = X nz + Z (a row couples cells
+// at most nz + 1 apart), so one warp factors it as L U inside the band without pivoting
+// (the operator is negative definite on its non-empty cells; empty cells get a unit
+// diagonal and a zero row and column in the inverse), and then thread c solves
+// L U x = e_c for column c.  The substitutions need no barrier, and all threads run them
+// in step: their reads of L and U are broadcasts, their columns sit in distinct banks.
 __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float* dense,
                                                                const DevStatus* status) {
     if (setup_failed(status)) return;
-    extern __shared__ float A[];  // m * m, then m (column) + 1 (pivot)
+    extern __shared__ float A[];  // m * m operator, then its L U factors in place
     const int m = L.cells;
-    float* colp = A + m * m;
-    float* piv = colp + m;
+    float* W = A + m * m;         // m * m: column c of the inverse in W[i m + c]
+    float* rd = W + m * m;        // m: 1 / U_ii
+    const int b = min(L.nz + 1, m - 1);
     for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) A[idx] = 0.0f;
     __syncthreads();
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
@@ -182,29 +187,43 @@ __global__ void __launch_bounds__(kMgBottomThreads) k_mg_dense(MgLevel L, float*
             }
         }
     }
-    // elimination: G threads per row, each over the columns g, g + G, ... (no division
-    // in the pivot loop); the block has at least m threads
-    const int G = max(1, static_cast<int>(blockDim.x) / m);
-    const int my_i = threadIdx.x / G, my_g = threadIdx.x - (threadIdx.x / G) * G;
-    for (int p = 0; p < m; p++) {
-        __syncthreads();
-        if (threadIdx.x == 0) piv[0] = 1.0f / A[p * m + p];
-        for (int i = threadIdx.x; i < m; i += blockDim.x) colp[i] = A[i * m + p];
-        __syncthreads();
-        const float ip = piv[0];
-        for (int j = threadIdx.x; j < m; j += blockDim.x) A[p * m + j] = (j == p ? 1.0f : A[p * m + j]) * ip;
-        __syncthreads();
-        if (my_i < m && my_i != p) {
-            const float cp = colp[my_i];
-            float* row = A + my_i * m;
-            for (int j = my_g; j < m; j += G) row[j] = (j == p ? 0.0f : row[j]) - cp * A[p * m + j];
+    __syncthreads();
+    if (threadIdx.x < 32) {  // banded L U (Doolittle), one warp
+        const int lane = threadIdx.x;
+        for (int p = 0; p < m; p++) {
+            const int last = min(m - 1, p + b);
+            const float ip = 1.0f / A[p * m + p];
+            for (int i = p + 1 + lane; i <= last; i += 32) A[i * m + p] *= ip;
+            __syncwarp();
+            const int w = last - p;  // rows and columns p + 1 .. last
+            for (int t = lane; t < w * w; t += 32) {
+                const int i = p + 1 + t / w, j = p + 1 + (t - (t / w) * w);
+                A[i * m + j] -= A[i * m + p] * A[p * m + j];
+            }
+            __syncwarp();
+        }
+        for (int i = lane; i < m; i += 32) rd[i] = 1.0f / A[i * m + i];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        // forward: L y = e_c (unit lower), rows in order
+        for (int i = 0; i < m; i++) {
+            float y = (i == c) ? 1.0f : 0.0f;
+            for (int k = max(0, i - b); k < i; k++) y -= A[i * m + k] * W[k * m + c];
+            W[i * m + c] = y;
+        }
+        // backward: U x = y
+        for (int i = m - 1; i >= 0; i--) {
+            float x = W[i * m + c];
+            for (int k = i + 1; k <= min(m - 1, i + b); k++) x -= A[i * m + k] * W[k * m + c];
+            W[i * m + c] = x * rd[i];
         }
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
         const int i = idx / m, j = idx - (idx / m) * m;
         const bool live = L.k64[4 * m + i] != 0.0 && L.k64[4 * m + j] != 0.0;
-        dense[idx] = live ? 0.5f * (A[i * m + j] + A[j * m + i]) : 0.0f;
+        dense[idx] = live ? 0.5f * (W[i * m + j] + W[j * m + i]) : 0.0f;
     }
 }
 
@@ -840,7 +859,7 @@ size_t bottom_bytes(const MgLevel* lv, int first, int last) {
 
 size_t dense_smem(const MgHierarchy& mg) {
     const size_t m = static_cast<size_t>(mg.lv[mg.levels].cells);
-    return (m * m + m + 1) * sizeof(float);
+    return (2 * m * m + m) * sizeof(float);
 }
 
 int warp_grid(int cells) { return grid_for(static_cast<int64_t>(cells) * 32); }
@@ -868,7 +887,7 @@ int mg_plan(int gnx, int gnz, MgLevel* lv, int* bottom) {
 }
 
 cudaError_t mg_prepare_device() {
-    const int dense_max = (kMgDenseCells * kMgDenseCells + kMgDenseCells + 1) * static_cast<int>(sizeof(float));
+    const int dense_max = (2 * kMgDenseCells * kMgDenseCells + kMgDenseCells) * static_cast<int>(sizeof(float));
     cudaError_t e = cudaFuncSetAttribute(k_mg_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, dense_max);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_mg_bottom, cudaFuncAttributeMaxDynamicSharedMemorySize,
