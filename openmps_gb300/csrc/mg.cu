@@ -57,20 +57,34 @@ __global__ void __launch_bounds__(kBlock) k_mg_bins(CgOperands o, const int32_t*
         double aii = 0.0;
         bool bad = false;
         if (ci >= 0) {
+            // four entries per step: their columns and values, then their cells, load
+            // together; the bins then take them in row order (the same sums)
+            constexpr int D = 4;
             const int L = o.len[i];
             int64_t at = sell_index(o.off[c], lane, 0);
-            for (int k = 0; k < L; k++, at += kSellRows) {
-                const int j = o.col[at];
-                const double a = o.val[at];
-                if (j == i) aii = a;
-                const int cj = cell_xz[j];
-                const int dx = (cj >> 16) - (ci >> 16);
-                const int dz = (cj & 0xffff) - (ci & 0xffff);
-                if (cj < 0 || dx < -1 || dx > 1 || dz < -1 || dz > 1) {
-                    bad = true;
-                    continue;
+            for (int k0 = 0; k0 < L; k0 += D, at += D * kSellRows) {
+                int jj[D], cc[D];
+                double aa[D];
+#pragma unroll
+                for (int u = 0; u < D; u++) {
+                    jj[u] = k0 + u < L ? o.col[at + u * kSellRows] : 0;
+                    aa[u] = k0 + u < L ? o.val[at + u * kSellRows] : 0.0;
                 }
-                acc[((dx + 1) * 3 + dz + 1) * kBlock + t] += a;
+#pragma unroll
+                for (int u = 0; u < D; u++) cc[u] = k0 + u < L ? cell_xz[jj[u]] : -1;
+#pragma unroll
+                for (int u = 0; u < D; u++) {
+                    if (k0 + u >= L) continue;
+                    if (jj[u] == i) aii = aa[u];
+                    const int cj = cc[u];
+                    const int dx = (cj >> 16) - (ci >> 16);
+                    const int dz = (cj & 0xffff) - (ci & 0xffff);
+                    if (cj < 0 || dx < -1 || dx > 1 || dz < -1 || dz > 1) {
+                        bad = true;
+                        continue;
+                    }
+                    acc[((dx + 1) * 3 + dz + 1) * kBlock + t] += aa[u];
+                }
             }
         }
         if (bad) {
